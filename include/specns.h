@@ -1,0 +1,178 @@
+/*
+ * specns.h -- C ABI of the GB300-native pseudo-spectral Navier-Stokes step.
+ *
+ * Drop-in boundary for the hot path of yili-shef/SpecCodeLib: the right-hand
+ * side of the incompressible Navier-Stokes equations in rotational form
+ * (Lamb vector, forcing, symmetrize, projection, optional Smagorinsky /
+ * dynamic-Smagorinsky stress) and its integrating-factor time steps, on one
+ * GPU.  Arrays crossing this boundary use the reference's FFTW r2c
+ * half-complex layout: a Fortran complex(sp) array c(nx/2+1, ny, nz),
+ * kx fastest, spectral coefficients normalised as
+ * u^ = (1/(nx ny nz)) sum_x u e^{-ik.x}.
+ *
+ * Every function returns an int status: SC_OK or one of SC_ERR_*; the text of
+ * the last error on the calling thread is returned by sc_last_error().
+ * A handle is used by one host thread at a time.  Host pointers may be
+ * pageable or pinned; device pointers must be CUDA device memory.
+ * Precision of element data follows sc_params.precision: SC_FP32 arrays are
+ * complex(4) (two floats per element), SC_FP64 arrays complex(8).
+ */
+#ifndef SPECNS_H
+#define SPECNS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SC_OK 0
+#define SC_ERR_INVALID 1     /* bad argument or unsupported size */
+#define SC_ERR_CUDA 2        /* a CUDA call failed */
+#define SC_ERR_NONFINITE 3   /* NaN/Inf found in the state */
+#define SC_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+#define SC_ERR_NOMEM 5       /* device allocation failed */
+
+#define SC_FP32 0            /* FP32 bulk (twiddles rounded from FP64, FP64 reductions) */
+#define SC_FP64 1            /* plain FP64 */
+
+#define SC_SGS_NONE 0
+#define SC_SGS_SMAG 1        /* smag.f90 */
+#define SC_SGS_DYNSMAG 2     /* dynsmag.f90 */
+
+#define SC_MASK_AFTER_STEP 0   /* 2/3 truncation of the state after each step (dns-deform.f90:233-237) */
+#define SC_MASK_RHS_AND_STEP 1 /* also truncate every right-hand side */
+
+typedef struct sc_params {
+  int nx, ny, nz;        /* grid; each a power of two in [8, 1024] */
+  int precision;         /* SC_FP32 | SC_FP64 */
+  double nu;             /* kinematic viscosity */
+  double dt;             /* time step */
+  int forced;            /* constant-power forcing on/off (force.f90) */
+  double eps;            /* injected power */
+  double fkmax;          /* forcing band k2 < fkmax^2 */
+  double kcut;           /* 2/3 cutoff; 0 -> 2*(nx/2)/3 (dns-deform.f90:75) */
+  int sgs;               /* SC_SGS_* */
+  double c1;             /* Smagorinsky c1 = Cs^2 (smag.f90:7 hard-codes 0.026) */
+  double delta;          /* filter width; 0 -> pi/kcut (spectral_les.f90:87) */
+  double delta_ratio;    /* test-filter width ratio; 0 -> 2 (spectral_les.f90:16) */
+  int dyn_every;         /* dynamic coefficient refresh interval; 0 -> 10 */
+  int mask_mode;         /* SC_MASK_* */
+} sc_params;
+
+typedef struct sc_diag {
+  double energy;         /* sum of 1/2-weighted |v|^2 (specdns-forced-omp-ft.f90:142-144) */
+  double enstrophy;      /* sum k^2 q(k) */
+  double dissipation;    /* 2 nu sum k^2 q(k) (meaneps.f90:37-44, per mode) */
+  double max_div;        /* max |k . v^| */
+  double max_u;          /* max |u| over grid points (CFL) */
+  double nonfinite;      /* count of non-finite values seen */
+  double cs2;            /* current Smagorinsky coefficient (c1 or dynamic cs2) */
+  double mm, lm;         /* last dynamic-procedure sums (dynsmag.f90:176,184) */
+} sc_diag;
+
+typedef struct sc_handle sc_handle;
+
+/* defaults for an n^3 grid: the forced-DNS configuration nu=0.01, dt=2e-3,
+ * eps=0.1, fkmax=2.5 (shells k<=2), 2/3 rule, no SGS. */
+int sc_default_params(sc_params* p, int n, int precision);
+
+/* Create / destroy a solver instance; allocates its device state.
+ * Replaces fftwplan3d / destroyplan3d (fftwplan.f90:7-30) and the
+ * program-level allocations (specdns-forced-omp-ft.f90:81-86). */
+int sc_create(const sc_params* p, sc_handle** out);
+int sc_destroy(sc_handle* h);
+
+/* Launch on this CUDA stream (cudaStream_t passed as void*; NULL = the
+ * handle's own stream). */
+int sc_set_stream(sc_handle* h, void* stream);
+/* Change dt (recomputes the integrating-factor tables). */
+int sc_set_dt(sc_handle* h, double dt);
+
+/* State upload / download in the reference layout (host pointers).
+ * Replaces input / output of input.f90:106-136, output.f90:103-132. */
+int sc_set_state(sc_handle* h, const void* vx, const void* vy, const void* vz);
+int sc_get_state(sc_handle* h, void* vx, void* vy, void* vz);
+/* Same with device pointers (reference layout, pitch nx/2+1). */
+int sc_set_state_device(sc_handle* h, const void* vx, const void* vy, const void* vz);
+int sc_get_state_device(sc_handle* h, void* vx, void* vy, void* vz);
+
+/* Seeded initial field: initialize3dvelhighmemdealiased (initialize.f90:
+ * 284-371) with Numerical Recipes ran1/gasdev (initialize.f90:507-548) in the
+ * reference's draw order.  kind 0: amplitude ~ k exp(-k^2/akp^2) (E(k) ~
+ * k^4 exp(-2 (k/akp)^2)); kind 1: E(k) ~ k^(-5/3) on kmin <= |k| <= kmax.
+ * Rescaled to energy 3/2 u0^2. */
+int sc_init_field(sc_handle* h, int seed, int kind, double akp, double u0, double kmin,
+                  double kmax);
+
+/* Right-hand side of the current state: dns-deform.f90:259-288 (ratesdudt)
+ * plus the SGS divergence of spectral_les.f90:232-234 when sgs != NONE.
+ * Outputs are host arrays in the reference layout. */
+int sc_rhs(sc_handle* h, void* wx, void* wy, void* wz);
+
+/* nsteps integrating-factor RK4 steps of dns-deform.f90:160-237 (computed in
+ * the equivalent division-free form). */
+int sc_rk4_steps(sc_handle* h, int nsteps);
+/* npasses passes of the IF-AB2 loop of specdns-forced-omp-ft.f90:224-287
+ * (pass 0: Euler half step; pass 1: midpoint restart; then AB2).  Its RHS is
+ * the AB2 solver's own: no symmetrize (specdns-forced-omp-ft.f90:180-221). */
+int sc_ab2_steps(sc_handle* h, int npasses);
+
+/* FP64 diagnostics of the current state; eks (may be NULL) receives the
+ * shell spectrum E(k), k = 1..nx/2 (specdns-forced-omp-ft.f90:159-176). */
+int sc_diagnostics(sc_handle* h, sc_diag* d, double* eks);
+
+/* Per-kernel timing with CUDA events on the launching stream.
+ * sc_profile_enable(h, 1) starts recording; sc_profile_read returns, for
+ * kernel family `name` ("zinv","ypass_inv","xpass","ypass_fwd","zfwd",
+ * "fixup", ...), the launch count and summed milliseconds since enabling. */
+int sc_profile_enable(sc_handle* h, int on);
+int sc_profile_read(sc_handle* h, const char* name, long long* launches, double* ms);
+
+/* Algorithmic bytes (field-pass model) of one RK4 step for this handle. */
+int sc_step_bytes(sc_handle* h, double* bytes_per_step);
+
+const char* sc_last_error(void);
+
+/* ---------------------------------------------------------------------
+ * Reference-signature operators (one call = one reference subroutine).
+ * Arrays are host memory in the reference layout; integer sizes are passed
+ * by value.  `precision` selects complex(4) or complex(8) element data.
+ * ------------------------------------------------------------------- */
+
+/* convec_dns(vx,vy,vz,wx,wy,wz,lx1,ly,lz,nx,ny,nz), convec_dns.f90:1:
+ * w <- spectral Lamb vector u x w (inputs v^, w^ = vorticity). */
+int sc_convec_dns(int precision, const void* vx, const void* vy, const void* vz, void* wx,
+                  void* wy, void* wz, int lx1, int ly, int lz, int nx, int ny, int nz);
+
+/* projection(vx,vy,vz,kx,ky,kz,lx1,ly,lz), projection.f90:2 (kx, ky, kz are
+ * implied by the FFTW ordering and not passed). */
+int sc_projection(int precision, void* vx, void* vy, void* vz, int lx1, int ly, int lz);
+
+/* force(wx,wy,wz,vx,vy,vz,k2,lx1,ly,lz,fkmax,eps), force.f90:3 (k2 implied). */
+int sc_force(int precision, void* wx, void* wy, void* wz, const void* vx, const void* vy,
+             const void* vz, int lx1, int ly, int lz, double fkmax, double eps);
+
+/* symmetrize(c,lx1,ly,lz), symmetrize.f90:32 (3D). */
+int sc_symmetrize(int precision, void* c, int lx1, int ly, int lz);
+
+/* dealiasing(c,k2,lx1,ly,lz), dealiasing.f90:2. */
+int sc_dealiasing(int precision, void* c, int lx1, int ly, int lz);
+
+/* smag(vx,vy,vz,t11,t12,t13,t22,t23,t33,kx,ky,kz,lx1,ly,lz,nx,ny,nz,delta),
+ * smag.f90:1, with c1 an argument (the reference fixes 0.026). */
+int sc_smag(int precision, const void* vx, const void* vy, const void* vz, void* t11, void* t12,
+            void* t13, void* t22, void* t23, void* t33, int lx1, int ly, int lz, int nx, int ny,
+            int nz, double delta, double c1);
+
+/* dynsmag(ux,uy,uz,t11..t33,kx,ky,kz,g_test,lx1,ly,lz,nx,ny,nz,lx,delta,
+ * delta_test,mm,lm,cs2,update), dynsmag.f90:1.  g_test is the sharp filter
+ * k2 <= k_test^2 (spectral_les.f90:105-109), passed as k_test.  cs2 is read
+ * when update == 0 and written otherwise, with mm and lm. */
+int sc_dynsmag(int precision, const void* ux, const void* uy, const void* uz, void* t11,
+               void* t12, void* t13, void* t22, void* t23, void* t33, int lx1, int ly, int lz,
+               int nx, int ny, int nz, double k_test, double delta, double delta_test,
+               double* mm, double* lm, double* cs2, int update);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPECNS_H */

@@ -1,0 +1,745 @@
+"""FP64 CPU oracle for the pseudo-spectral Navier-Stokes step.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline / reference leg of ``bench.py`` may import this module, and only
+as the checker or as the timed CPU baseline.  The product path (the CUDA
+library under ``speccodelib_gb300/``) never calls it.
+
+What it restates
+----------------
+A line-by-line restatement, in NumPy/SciPy double precision, of the reference
+(yili-shef/SpecCodeLib, Fortran 90 + FFTW) routines on the hot path.  Every
+function cites the reference file:line it follows.
+
+Layout
+------
+A spectral field is a complex128 array of shape ``(nz, ny, nx//2 + 1)`` in C
+order: the same memory as the reference's Fortran array ``c(lx1, ly, lz)``
+(kx fastest).  Fortran ``c(ii, jj, kk)`` is ``c[kk-1, jj-1, ii-1]`` here.  A
+physical field is a float64 array of shape ``(nz, ny, nx)``.  Transforms are
+unnormalised both ways exactly like FFTW's ``rfftwnd_f77_one_*``:
+``c2r`` = sum_k c e^{+ik.x}; ``r2c`` = sum_x u e^{-ik.x}; callers multiply by
+1/(nx ny nz) once in physical space (convec_dns.f90:15,40-42).
+
+Parity status
+-------------
+The reference cannot be built here (no Fortran compiler, no FFTW; the FFTW
+version it links is not pinned anywhere), so this oracle is NOT pinned to
+reference binaries.  It is pinned instead to the known answers the reference's
+own files imply (tests/test_oracle_pins.py): the Roberts/Beltrami flow of
+robertsflow.f90:23-25 (zero Lamb vector, exact e^{-2 nu t} decay under the
+integrating factor), single-mode transform identities in FFTW's sign and
+normalisation convention, the energy normalisation 3/2 u0^2 of
+initialize.f90:362-368, the Hermitian/Nyquist rules of symmetrize.f90:32-64 and
+the divergence-free output of projection.f90.  Golden fixtures under
+tests/golden/ are generated from this oracle by tests/golden/make_golden.py.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+try:  # scipy.fft is multi-threaded; numpy.fft is the fallback.
+    import scipy.fft as _sfft
+
+    def _irfftn(c, s, workers):
+        return _sfft.irfftn(c, s=s, axes=tuple(range(c.ndim - len(s), c.ndim)),
+                            norm="forward", workers=workers)
+
+    def _rfftn(r, workers):
+        return _sfft.rfftn(r, axes=tuple(range(r.ndim)), norm="backward",
+                           workers=workers)
+except ImportError:  # pragma: no cover
+    def _irfftn(c, s, workers):
+        return np.fft.irfftn(c, s=s, axes=tuple(range(c.ndim - len(s), c.ndim)),
+                             norm="forward")
+
+    def _rfftn(r, workers):
+        return np.fft.rfftn(r, norm="backward")
+
+WORKERS = int(os.environ.get("SC_ORACLE_WORKERS", "1"))
+
+# constant_sp.f90 / constant.f90 (the "-dp" build is followed: sp = double)
+PI_REF = 3.1415926536                      # constant.f90:40 (truncated pi)
+MYTINY_DP = float(np.finfo(np.float64).tiny)   # constant.f90:34 tiny(1.0_dp)
+MYTINY_SP = float(np.finfo(np.float32).tiny)   # constant.f90:36 tiny(1.0_sp)
+
+
+# --------------------------------------------------------------------------
+# grid
+# --------------------------------------------------------------------------
+def wavenumber(nx, ny, nz):
+    """kx, ky, kz (1D) and k2 (3D) -- wavenumber.f90:89-129 (low-mem 3D).
+
+    kx = 0..nx/2; ky, kz = 0..n/2-1, -n/2..-1 (wavenumber.f90:109,115);
+    k2(1,1,1) = tiny(1.0_sp) (wavenumber.f90:125).
+    """
+    kx = np.arange(nx // 2 + 1, dtype=np.float64)
+    ky = (np.mod(np.arange(ny) + ny // 2, ny) - ny // 2).astype(np.float64)
+    kz = (np.mod(np.arange(nz) + nz // 2, nz) - nz // 2).astype(np.float64)
+    k2 = kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2
+    k2[0, 0, 0] = MYTINY_SP
+    return kx, ky, kz, k2
+
+
+def wavenumber2d(nx, ny):
+    """2D counterpart (wavenumber.f90:187-266): k2(1,1) = tiny."""
+    kx = np.arange(nx // 2 + 1, dtype=np.float64)
+    ky = (np.mod(np.arange(ny) + ny // 2, ny) - ny // 2).astype(np.float64)
+    k2 = ky[:, None] ** 2 + kx[None, :] ** 2
+    k2[0, 0] = MYTINY_SP
+    return kx, ky, k2
+
+
+def c2r(c, nx, workers=None):
+    """FFTW c2r, unnormalised (rfftwnd_f77_one_complex_to_real)."""
+    s = c.shape[:-1] + (nx,)
+    return _irfftn(c, s, WORKERS if workers is None else workers)
+
+
+def r2c(r, workers=None):
+    """FFTW r2c, unnormalised (rfftwnd_f77_one_real_to_complex)."""
+    return _rfftn(r, WORKERS if workers is None else workers)
+
+
+def packed_to_physical(c):
+    """Reference packed-real view: real(c(i)) = x-point 2i-2, aimag = 2i-1
+    (robertsflow.f90:33-35); the last complex column is padding."""
+    nxh = c.shape[-1]
+    out = np.empty(c.shape[:-1] + (2 * (nxh - 1),), dtype=np.float64)
+    out[..., 0::2] = c[..., : nxh - 1].real
+    out[..., 1::2] = c[..., : nxh - 1].imag
+    return out
+
+
+# --------------------------------------------------------------------------
+# L3 operators
+# --------------------------------------------------------------------------
+def symmetrize3d(c):
+    """symmetrize.f90:32-64 (returns a new array)."""
+    c = np.array(c, dtype=np.complex128, copy=True)
+    nz, ny, nxh = c.shape
+    c[:, ny // 2, :] = 0.0            # :43 zero ky = -ly/2
+    c[nz // 2, :, :] = 0.0            # :45 zero kz = -lz/2
+    c[:, :, nxh - 1] = 0.0            # :47 zero kx = lx
+    c[0, 0, 0] = 0.0                  # :49 mean mode
+    # :52-57 kx = 0 plane, iz = lz/2+2..lz, all iy: c(1,iy,iz) =
+    #        conj(c(1, mod(ly+1-iy,ly)+1, lz+2-iz))
+    jz = np.arange(nz // 2 + 1, nz)
+    jy = np.arange(ny)
+    src_y = np.mod(ny - jy, ny)
+    src_z = nz - jz
+    c[jz[:, None], jy[None, :], 0] = np.conj(c[src_z[:, None], src_y[None, :], 0])
+    # :60-62 line kx = kz = 0, iy = ly/2+2..ly
+    jy2 = np.arange(ny // 2 + 1, ny)
+    c[0, jy2, 0] = np.conj(c[0, ny - jy2, 0])
+    return c
+
+
+def symmetrize2d(c):
+    """symmetrize.f90:8-30 (returns a new array); c shape (ny, nxh)."""
+    c = np.array(c, dtype=np.complex128, copy=True)
+    ny, nxh = c.shape
+    c[ny // 2, :] = 0.0
+    c[:, nxh - 1] = 0.0
+    c[0, 0] = 0.0
+    jy = np.arange(ny // 2 + 1, ny)
+    c[jy, 0] = np.conj(c[ny - jy, 0])
+    return c
+
+
+def dealiasing(c, k2):
+    """dealiasing.f90:2-37: symmetrize, then zero k2 >= ly^2/9 (:35)."""
+    ny = c.shape[1]
+    c = symmetrize3d(c)
+    c[k2 >= (ny * ny) / 9.0] = 0.0
+    return c
+
+
+def projection(vx, vy, vz, kx, ky, kz):
+    """projection.f90:2-31: v <- v - k (k.v)/(k^2 + tiny)."""
+    KX = kx[None, None, :]
+    KY = ky[None, :, None]
+    KZ = kz[:, None, None]
+    tmp = KX * vx + KY * vy + KZ * vz
+    tmp = tmp / (KX * KX + KY * KY + KZ * KZ + MYTINY_DP)
+    return vx - KX * tmp, vy - KY * tmp, vz - KZ * tmp
+
+
+def forcing_energy(vx, vy, vz, k2, fkmax):
+    """K_f of force.f90:16-22: sum over k2 < fkmax^2 of |v|^2, x1/2 at kx=0."""
+    tmp = np.where(k2 < fkmax * fkmax,
+                   (vx * np.conj(vx) + vy * np.conj(vy) + vz * np.conj(vz)).real,
+                   0.0)
+    tmp[:, :, 0] *= 0.5
+    return float(np.sum(tmp))
+
+
+def force(wx, wy, wz, vx, vy, vz, k2, fkmax, eps):
+    """force.f90:3-31: w += eps/(2 K_f) v on k2 < fkmax^2."""
+    kinet = forcing_energy(vx, vy, vz, k2, fkmax)
+    a = eps / (2.0 * kinet)
+    m = k2 < fkmax * fkmax
+    return (np.where(m, wx + a * vx, wx), np.where(m, wy + a * vy, wy),
+            np.where(m, wz + a * vz, wz))
+
+
+def vorticity(vx, vy, vz, kx, ky, kz):
+    """w = i k x v (dns-deform.f90:265-273)."""
+    KX = kx[None, None, :]
+    KY = ky[None, :, None]
+    KZ = kz[:, None, None]
+    wx = 1j * KY * vz - 1j * KZ * vy
+    wy = 1j * KZ * vx - 1j * KX * vz
+    wz = 1j * KX * vy - 1j * KY * vx
+    return wx, wy, wz
+
+
+def convec_dns(vx, vy, vz, wx, wy, wz, nx):
+    """convec_dns.f90:1-55: Lamb vector u x w, spectral in and out."""
+    ny, nz = vx.shape[1], vx.shape[0]
+    const = 1.0 / float(nx * ny * nz)
+    ux, uy, uz = (c2r(a, nx) for a in (vx, vy, vz))
+    ox, oy, oz = (c2r(a, nx) for a in (wx, wy, wz))
+    lx = uy * oz - uz * oy      # :30-32
+    ly = uz * ox - ux * oz      # :33-35
+    lz = ux * oy - uy * ox      # :36-38
+    return r2c(lx * const), r2c(ly * const), r2c(lz * const)
+
+
+# --------------------------------------------------------------------------
+# SGS models
+# --------------------------------------------------------------------------
+def strain_spectral(vx, vy, vz, kx, ky, kz):
+    """S_ij in spectral space, order (11, 12, 13, 22, 23, 33) (smag.f90:21-32)."""
+    KX = kx[None, None, :]
+    KY = ky[None, :, None]
+    KZ = kz[:, None, None]
+    t11 = 1j * KX * vx
+    t22 = 1j * KY * vy
+    t33 = 1j * KZ * vz
+    t12 = 1j * (KX * vy + KY * vx) * 0.5
+    t13 = 1j * (KX * vz + KZ * vx) * 0.5
+    t23 = 1j * (KY * vz + KZ * vy) * 0.5
+    return [t11, t12, t13, t22, t23, t33]
+
+
+def _smag_abs(s):
+    """|S| = sqrt(2 S_ij S_ij) on physical fields (11,12,13,22,23,33)."""
+    s11, s12, s13, s22, s23, s33 = s
+    return np.sqrt(2.0 * (s11 * s11 + s22 * s22 + s33 * s33
+                          + 2.0 * (s12 * s12 + s13 * s13 + s23 * s23)))
+
+
+def smag(vx, vy, vz, kx, ky, kz, nx, delta, c1=0.026):
+    """smag.f90:1-78: tau_ij = -2 c1 delta^2 |S| S_ij (spectral).
+
+    c1 is hard-coded to 0.026 in the reference (smag.f90:7); here it is an
+    argument with that default.
+    """
+    ny, nz = vx.shape[1], vx.shape[0]
+    const = 1.0 / float(nx * ny * nz)
+    s = [c2r(t, nx) for t in strain_spectral(vx, vy, vz, kx, ky, kz)]
+    sa = _smag_abs(s)
+    return [r2c(-2.0 * c1 * delta * delta * (sa * t) * const) for t in s]
+
+
+def test_filter(k2, k_test):
+    """Sharp spectral test filter g_test = [k2 <= k_test^2]
+    (spectral_les.f90:105-109)."""
+    return np.where(k2 <= k_test * k_test, 1.0, 0.0)
+
+
+def dynsmag(vx, vy, vz, kx, ky, kz, g, nx, delta, delta_test, update, cs2):
+    """dynsmag.f90:1-236 (Germano-Lilly, box-averaged least squares).
+
+    Returns (tau, mm, lm, cs2).  In the non-update branch mm, lm are None and
+    the passed-in cs2 is used (dynsmag.f90:196-232).
+    """
+    ny, nz = vx.shape[1], vx.shape[0]
+    const = 1.0 / float(nx * ny * nz)
+    d2 = delta * delta
+    dt2 = delta_test * delta_test
+    sspec = strain_spectral(vx, vy, vz, kx, ky, kz)
+    s = [c2r(t, nx) for t in sspec]
+    sa = _smag_abs(s)
+    if update:
+        # L_ij (:28-77)
+        u = [c2r(a, nx) for a in (vx, vy, vz)]
+        gu = [c2r(g * a, nx) for a in (vx, vy, vz)]
+        pairs = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+        L = []
+        for (i, j) in pairs:
+            f = c2r(g * r2c(u[i] * u[j]) * const, nx)
+            L.append(f - gu[i] * gu[j])
+        # M_ij (:79-168)
+        s2 = [r2c(2.0 * d2 * (sa * t) * const) for t in s]       # :110-122
+        gs = [c2r(g * t, nx) for t in sspec]                        # :88-130
+        gsa = _smag_abs(gs)
+        tpart = [-2.0 * dt2 * (gsa * t) for t in gs]                 # :140-145
+        M = [c2r(g * s2[n], nx) + tpart[n] for n in range(6)]       # :148-168
+        w = [1.0, 2.0, 2.0, 1.0, 2.0, 1.0]
+        mm = float(sum(w[n] * np.sum(M[n] * M[n]) for n in range(6)))   # :170-176
+        lm = float(sum(w[n] * np.sum(L[n] * M[n]) for n in range(6)))   # :178-184
+        cs2 = lm / mm                                                    # :186
+        tau = [-cs2 * t for t in s2]                                     # :188-193
+        return tau, mm, lm, cs2
+    tau = [r2c(-cs2 * 2.0 * d2 * (sa * t) * const) for t in s]          # :220-232
+    return tau, None, None, cs2
+
+
+def sgs_divergence(tau, kx, ky, kz):
+    """-i k_j tau_ij (spectral_les.f90:232-234)."""
+    t11, t12, t13, t22, t23, t33 = tau
+    KX = kx[None, None, :]
+    KY = ky[None, :, None]
+    KZ = kz[:, None, None]
+    return (-1j * (KX * t11 + KY * t12 + KZ * t13),
+            -1j * (KX * t12 + KY * t22 + KZ * t23),
+            -1j * (KX * t13 + KY * t23 + KZ * t33))
+
+
+# --------------------------------------------------------------------------
+# parameters and right-hand sides
+# --------------------------------------------------------------------------
+@dataclasses.dataclass
+class Params:
+    nx: int
+    ny: int = 0
+    nz: int = 0
+    nu: float = 0.01
+    dt: float = 2e-3
+    forced: bool = True
+    eps: float = 0.1
+    fkmax: float = 2.5
+    kcut: float = 0.0          # 0 -> 2*(nx/2)/3 (dns-deform.f90:75)
+    sgs: str = "none"          # "none" | "smag" | "dynsmag"
+    c1: float = 0.026          # smag.f90:7
+    delta: float = 0.0         # 0 -> pi/kcut (spectral_les.f90:87)
+    delta_ratio: float = 2.0   # spectral_les.f90:16
+    dyn_every: int = 10        # spectral_les.f90:17
+    mask: str = "after_step"   # "after_step" (dns-deform.f90:233-237) | "rhs_and_step"
+
+    def __post_init__(self):
+        self.ny = self.ny or self.nx
+        self.nz = self.nz or self.nx
+        if self.kcut == 0.0:
+            self.kcut = 2.0 * (self.nx // 2) / 3.0
+        if self.delta == 0.0:
+            self.delta = PI_REF / self.kcut
+
+    @property
+    def k_test(self):
+        return self.kcut / self.delta_ratio          # spectral_les.f90:89
+
+    @property
+    def delta_test(self):
+        return self.delta_ratio * self.delta         # spectral_les.f90:90
+
+
+class Grid:
+    def __init__(self, p: Params):
+        self.p = p
+        self.kx, self.ky, self.kz, self.k2 = wavenumber(p.nx, p.ny, p.nz)
+        self.g = test_filter(self.k2, p.k_test)
+
+
+def ratesdudt(v, grid: Grid, sgs_state=None):
+    """Right-hand side of dns-deform.f90:259-288 (plus the optional SGS term
+    of spectral_les.f90:204-234, applied before symmetrize/projection).
+
+    v: tuple of three spectral fields.  sgs_state: dict with keys 'cs2',
+    'update' for dynsmag; receives 'mm', 'lm', 'cs2' back.
+    """
+    p = grid.p
+    kx, ky, kz, k2 = grid.kx, grid.ky, grid.kz, grid.k2
+    vx, vy, vz = v
+    wx, wy, wz = vorticity(vx, vy, vz, kx, ky, kz)                     # :265-273
+    wx, wy, wz = convec_dns(vx, vy, vz, wx, wy, wz, p.nx)              # :276
+    if p.forced:
+        wx, wy, wz = force(wx, wy, wz, vx, vy, vz, k2, p.fkmax, p.eps)  # :279
+    if p.sgs != "none":
+        if p.sgs == "smag":
+            tau = smag(vx, vy, vz, kx, ky, kz, p.nx, p.delta, p.c1)
+        else:
+            st = sgs_state if sgs_state is not None else {"cs2": 0.0, "update": True}
+            tau, mm, lm, cs2 = dynsmag(vx, vy, vz, kx, ky, kz, grid.g, p.nx,
+                                        p.delta, p.delta_test, st["update"], st["cs2"])
+            st["cs2"] = cs2
+            if mm is not None:
+                st["mm"], st["lm"] = mm, lm
+        dx, dy, dz = sgs_divergence(tau, kx, ky, kz)
+        wx, wy, wz = wx + dx, wy + dy, wz + dz
+    wx, wy, wz = symmetrize3d(wx), symmetrize3d(wy), symmetrize3d(wz)  # :281-283
+    wx, wy, wz = projection(wx, wy, wz, kx, ky, kz)                    # :286
+    if p.mask == "rhs_and_step":
+        m = k2 >= p.kcut * p.kcut
+        wx, wy, wz = (np.where(m, 0.0, a) for a in (wx, wy, wz))
+    return wx, wy, wz
+
+
+def mask_state(v, grid: Grid):
+    """2/3 truncation of the state after the step (dns-deform.f90:233-237)."""
+    m = grid.k2 >= grid.p.kcut * grid.p.kcut
+    return tuple(np.where(m, 0.0, a) for a in v)
+
+
+def rk4_step(v, grid: Grid, sgs_state=None, dyn_update=None):
+    """One integrating-factor RK4 step, literally dns-deform.f90:160-237.
+
+    k2e = exp(-nu k2 dt/2) (dns-deform.f90:90).  For dynsmag, the dynamic
+    coefficient is recomputed only on the first stage when dyn_update is True.
+    """
+    p = grid.p
+    dt = p.dt
+    k2e = np.exp(-p.nu * grid.k2 * dt / 2)
+
+    def rhs(s, first):
+        if sgs_state is not None:
+            sgs_state["update"] = bool(dyn_update) and first
+        return ratesdudt(s, grid, sgs_state)
+
+    vx, vy, vz = v
+    w = rhs((vx, vy, vz), True)                                        # :164
+    ku = [dt * a for a in w]                                           # :165-167
+    du = list(ku)
+    s = [k2e * (a + b / 2) for a, b in zip((vx, vy, vz), ku)]          # :177-179
+    w = rhs(s, False)
+    ku = [dt * a / k2e for a in w]                                     # :182-184
+    du = [a + 2 * b for a, b in zip(du, ku)]
+    s = [k2e * (a + b / 2) for a, b in zip((vx, vy, vz), ku)]          # :194-196
+    w = rhs(s, False)
+    ku = [dt * a / k2e for a in w]                                     # :199-201
+    du = [a + 2 * b for a, b in zip(du, ku)]
+    s = [k2e * k2e * (a + b) for a, b in zip((vx, vy, vz), ku)]        # :211-213
+    w = rhs(s, False)
+    ku = [dt * a / k2e / k2e for a in w]                               # :216-218
+    du = [a + b for a, b in zip(du, ku)]
+    vn = [k2e * k2e * (a + b / 6) for a, b in zip((vx, vy, vz), du)]   # :226-228
+    return mask_state(vn, grid)
+
+
+def rk4_run(v, grid: Grid, nsteps, sgs_state=None):
+    """nsteps RK4 steps; dynsmag coefficient refreshed on steps that are
+    multiples of dyn_every (counted from 0)."""
+    for n in range(nsteps):
+        v = rk4_step(v, grid, sgs_state, dyn_update=(n % grid.p.dyn_every == 0))
+    return v
+
+
+def ab2_rhs(v, grid: Grid):
+    """RHS of the production IF-AB2 solver, specdns-forced-omp-ft.f90:180-221:
+    vorticity, Lamb vector, forcing, projection with /k2 (no symmetrize)."""
+    p = grid.p
+    kx, ky, kz, k2 = grid.kx, grid.ky, grid.kz, grid.k2
+    vx, vy, vz = v
+    wx, wy, wz = vorticity(vx, vy, vz, kx, ky, kz)
+    wx, wy, wz = convec_dns(vx, vy, vz, wx, wy, wz, p.nx)
+    if p.forced:
+        wx, wy, wz = force(wx, wy, wz, vx, vy, vz, k2, p.fkmax, p.eps)
+    KX, KY, KZ = kx[None, None, :], ky[None, :, None], kz[:, None, None]
+    t = (KX * wx.real + KY * wy.real + KZ * wz.real) / k2             # :211-214
+    wx = wx - KX * t
+    wy = wy - KY * t
+    wz = wz - KZ * t
+    t = (KX * wx.imag + KY * wy.imag + KZ * wz.imag) / k2             # :216-219
+    wx = wx - 1j * KX * t
+    wy = wy - 1j * KY * t
+    wz = wz - 1j * KZ * t
+    return wx, wy, wz
+
+
+def ab2_run(v, grid: Grid, nhalf_steps):
+    """IF-AB2 of specdns-forced-omp-ft.f90:224-287 for `nhalf_steps` passes of
+    its loop (pass 0 = Euler half step, pass 1 = midpoint restart from the
+    initial field, then AB2).  Returns (v, time)."""
+    p = grid.p
+    dt = p.dt
+    dt_h = 0.5 * dt
+    expk2 = np.exp(-grid.k2 * p.nu * dt)                             # :92
+    expk2[0, 0, 0] = 1.0                                             # :93
+    sq = np.sqrt(expk2)
+    o = list(v)
+    o0 = None
+    v = list(v)
+    t = 0.0
+    for istep in range(nhalf_steps):
+        w = ab2_rhs(v, grid)
+        if istep == 0:                                               # :225-234
+            v = [(a + dt_h * b) * sq for a, b in zip(v, w)]
+            t += dt_h
+            o0 = w
+        elif istep == 1:                                             # :236-251
+            v = [a * expk2 + dt * b * sq for a, b in zip(o, w)]
+            t += dt_h
+            o = o0
+        else:                                                        # :255-270
+            v = [(a + (3.0 * b - expk2 * c) * dt_h) * expk2 for a, b, c in zip(v, w, o)]
+            o = w
+            t += dt
+        v = [a.copy() for a in v]
+        for a in v:
+            a[0, 0, 0] = 0.0                                         # :277-279
+        m = grid.k2 >= (2.0 * (p.nx // 2) / 3.0) ** 2
+        v = [np.where(m, 0.0, a) for a in v]                         # :283-287
+    return tuple(v), t
+
+
+# --------------------------------------------------------------------------
+# diagnostics (FP64)
+# --------------------------------------------------------------------------
+def _q(v):
+    q = sum((a * np.conj(a)).real for a in v)
+    q[:, :, 0] *= 0.5
+    return q
+
+
+def energy(v):
+    """E = sum of 1/2-weighted |v|^2 (specdns-forced-omp-ft.f90:142-144)."""
+    return float(np.sum(_q(v)))
+
+
+def spectrum(v, k2, nx):
+    """Shell spectrum, ll = floor(sqrt(k2)+.5), 1 <= ll <= lx
+    (specdns-forced-omp-ft.f90:159-176).  Returns array eks[0..lx-1]."""
+    lx = nx // 2
+    q = _q(v)
+    ll = np.floor(np.sqrt(k2) + 0.5).astype(np.int64)
+    m = (ll >= 1) & (ll <= lx)
+    return np.bincount(ll[m] - 1, weights=q[m], minlength=lx)[:lx]
+
+
+def dissipation(v, k2, nu):
+    """eps = 2 nu sum k^2 q(k) over modes (the per-mode form of
+    meaneps.f90:37-44)."""
+    kk = k2.copy()
+    kk[0, 0, 0] = 0.0
+    return float(2.0 * nu * np.sum(kk * _q(v)))
+
+
+def enstrophy(v, k2):
+    kk = k2.copy()
+    kk[0, 0, 0] = 0.0
+    return float(np.sum(kk * _q(v)))
+
+
+def max_divergence(v, kx, ky, kz):
+    """max |k . v| over all modes."""
+    vx, vy, vz = v
+    d = kx[None, None, :] * vx + ky[None, :, None] * vy + kz[:, None, None] * vz
+    return float(np.max(np.abs(d)))
+
+
+def max_velocity(v, nx):
+    """max over grid points of |u| (CFL diagnostic)."""
+    u = [c2r(a, nx) for a in v]
+    return float(np.sqrt(np.max(u[0] ** 2 + u[1] ** 2 + u[2] ** 2)))
+
+
+# --------------------------------------------------------------------------
+# seeded initial fields (initialize.f90)
+# --------------------------------------------------------------------------
+_LIB = None
+
+
+def _ran1_lib():
+    """Compile oracle/ran1.c on first use (gcc), or load the prebuilt copy."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = os.path.join(here, "_build", "liboracle_ran1.so")
+    src = os.path.join(here, "ran1.c")
+    if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+        build_c(here)
+    lib = ctypes.CDLL(so)
+    lib.oracle_gauss_fields.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int32,
+                                        ctypes.c_void_p]
+    lib.oracle_ran1_sequence.argtypes = [ctypes.c_int32, ctypes.c_int64,
+                                         ctypes.c_void_p]
+    _LIB = lib
+    return lib
+
+
+def build_c(here=None):
+    """Compile the oracle's C helper into oracle/_build/."""
+    here = here or os.path.dirname(os.path.abspath(__file__))
+    os.makedirs(os.path.join(here, "_build"), exist_ok=True)
+    so = os.path.join(here, "_build", "liboracle_ran1.so")
+    tmp = so + ".%d.tmp" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", tmp,
+                           os.path.join(here, "ran1.c"), "-lm"])
+    os.replace(tmp, so)
+    return so
+
+
+def ran1_sequence(seed, count):
+    out = np.empty(count, dtype=np.float64)
+    _ran1_lib().oracle_ran1_sequence(seed, count, out.ctypes.data)
+    return out
+
+
+def ran1_sequence_py(seed, count):
+    """Pure-Python NR ran1 (initialize.f90:516-548), for cross-checking the C
+    helper on short sequences."""
+    ia, im, iq, ir, ntab = 16807, 2147483647, 127773, 2836, 32
+    ndiv = 1 + (im - 1) // ntab
+    am = 1.0 / im
+    rnmx = 1.0 - 1.2e-7
+    iv = [0] * ntab
+    idum = max(-seed, 1)                       # initialize.f90:530
+    for j in range(ntab + 8, 0, -1):
+        k = idum // iq
+        idum = ia * (idum - k * iq) - ir * k
+        if idum < 0:
+            idum += im
+        if j <= ntab:
+            iv[j - 1] = idum
+    iy = iv[0]
+    out = []
+    for _ in range(count):
+        k = idum // iq
+        idum = ia * (idum - k * iq) - ir * k
+        if idum < 0:
+            idum += im
+        j = iy // ndiv
+        iy = iv[j]
+        iv[j] = idum
+        out.append(min(am * iy, rnmx))
+    return np.array(out)
+
+
+def gauss_fields(nx, ny, nz, ncomp, seed):
+    """ncomp complex Gaussian fields drawn in the reference's loop order
+    (initialize.f90:305-326)."""
+    nxh = nx // 2 + 1
+    out = np.empty((ncomp, nz, ny, nxh), dtype=np.complex128)
+    _ran1_lib().oracle_gauss_fields(nxh, ny, nz, ncomp, seed, out.ctypes.data)
+    return out
+
+
+def initialize_dealiased(nx, ny, nz, seed, akp, u0, kcut, spectrum_kind="akp",
+                         kmin=0.0, kmax=0.0):
+    """initialize3dvelhighmemdealiased, initialize.f90:284-371.
+
+    spectrum_kind "akp": amplitude u0 sqrt(8 sqrt(2/pi)/(3 pi akp^5)) k
+    exp(-k^2/akp^2) (:349).  "kolmogorov": |v| ~ k^(-11/6) on kmin <= k <= kmax
+    (E(k) ~ k^(-5/3)), a new initializer that reuses the same draws; both are
+    rescaled to E = 3/2 u0^2 (:362-368).
+    """
+    kx, ky, kz, k2 = wavenumber(nx, ny, nz)
+    g = gauss_fields(nx, ny, nz, 3, seed)
+    vx, vy, vz = g[0], g[1], g[2]
+    KX = np.broadcast_to(kx[None, None, :], k2.shape)
+    KY = np.broadcast_to(ky[None, :, None], k2.shape)
+    KZ = np.broadcast_to(kz[:, None, None], k2.shape)
+    tmpz = KX * vx + KY * vy + KZ * vz                                  # :328-332
+    tmpz = tmpz / (KX * KX + KY * KY + KZ * KZ + MYTINY_DP)
+    vx = vx - KX * tmpz
+    vy = vy - KY * tmpz
+    vz = vz - KZ * tmpz
+    vx, vy, vz = symmetrize3d(vx), symmetrize3d(vy), symmetrize3d(vz)  # :337-339
+    m = k2 >= kcut * kcut                                               # :341-345
+    vx, vy, vz = (np.where(m, 0.0, a) for a in (vx, vy, vz))
+    if spectrum_kind == "akp":
+        tmp = (u0 * np.sqrt(8.0 * np.sqrt(2.0 / PI_REF) / (3.0 * PI_REF * akp ** 5))
+               * np.sqrt(k2) * np.exp(-k2 / (akp * akp)))               # :349
+    else:
+        k = np.sqrt(k2)
+        tmp = np.where((k >= kmin) & (k <= kmax), k ** (-11.0 / 6.0), 0.0)
+    vx, vy, vz = vx * tmp, vy * tmp, vz * tmp                          # :358-360
+    tmp1 = energy((vx, vy, vz))                                        # :362-364
+    tmp2 = 1.5 * u0 * u0
+    f = np.sqrt(tmp2 / tmp1)
+    return f * vx, f * vy, f * vz
+
+
+# --------------------------------------------------------------------------
+# 2D vorticity ensemble member (physics of turb_2d.f90:288-403 and
+# spectral_dns_2d.f90:94,160-188, restated; the reference 2D solver itself
+# does not run, see spectral_dns_2d.f90:166-168)
+# --------------------------------------------------------------------------
+@dataclasses.dataclass
+class Params2D:
+    n: int
+    alpha: float = 0.01
+    nu8: float = 0.0
+    dt: float = 1e-3
+
+
+def rhs2d(wz, p: Params2D):
+    """d(w)/dt nonlinear part: -(i kx (u w)^ + i ky (v w)^), with
+    u^ = i ky w^/k2, v^ = -i kx w^/k2 (spectral_dns_2d.f90:161-178), then
+    symmetrize2d and the 2/3 mask (:188)."""
+    n = p.n
+    kx, ky, k2 = wavenumber2d(n, n)
+    KX, KY = kx[None, :], ky[:, None]
+    const = 1.0 / (n * n)
+    u = c2r2(1j * KY * wz / k2, n)
+    v = c2r2(-1j * KX * wz / k2, n)
+    w = c2r2(wz, n)
+    a = r2c(u * w) * const
+    b = r2c(v * w) * const
+    nl = -(1j * KX * a + 1j * KY * b)
+    nl = symmetrize2d(nl)
+    nl[k2 >= (2.0 * (n // 2) / 3.0) ** 2] = 0.0
+    return nl
+
+
+def c2r2(c, n):
+    return _irfftn(c, (c.shape[0], n), WORKERS)
+
+
+def if_factor2d(p: Params2D, half=True):
+    """E = exp(-(alpha + nu8 k^8) dt/2) (linear damping + hyperviscosity)."""
+    _, _, k2 = wavenumber2d(p.n, p.n)
+    kk = k2.copy()
+    kk[0, 0] = 0.0
+    f = 0.5 if half else 1.0
+    return np.exp(-(p.alpha + p.nu8 * kk ** 4) * p.dt * f)
+
+
+def rk4_step2d(wz, p: Params2D):
+    """Division-free Lawson IF-RK4 (algebraically dns-deform.f90:160-230)."""
+    E = if_factor2d(p)
+    dt = p.dt
+    k1 = rhs2d(wz, p)
+    k2_ = rhs2d(E * (wz + 0.5 * dt * k1), p)
+    k3 = rhs2d(E * wz + 0.5 * dt * k2_, p)
+    k4 = rhs2d(E * E * wz + E * dt * k3, p)
+    return E * E * wz + dt * (E * E * k1 + 2 * E * k2_ + 2 * E * k3 + k4) / 6.0
+
+
+def initialize2d(n, seed, kpeak=6.0, enstrophy_target=None, energy_target=0.5):
+    """Seeded random vorticity with E(k) ~ k exp(-(k/kpeak)^2)
+    (draw order of initialize.f90:485-492, then symmetrize2d and the 2/3 mask
+    of :494-496); normalised to the given energy."""
+    kx, ky, k2 = wavenumber2d(n, n)
+    g = gauss_fields(n, n, 1, 1, seed)[0, 0]
+    w = symmetrize2d(g)
+    w[k2 >= (2.0 * (n // 2) / 3.0) ** 2] = 0.0
+    k = np.sqrt(k2)
+    # E(k) = pi k |u^|^2 per shell -> |w^| = k |u^| ~ k exp(-(k/kp)^2/2)
+    amp = k * np.exp(-0.5 * (k / kpeak) ** 2)
+    w = w * amp
+    q = (w * np.conj(w)).real / k2
+    q[0, 0] = 0.0
+    q[:, 0] *= 0.5
+    e = float(np.sum(q))
+    return w * np.sqrt(energy_target / e)
+
+
+def energy2d(wz):
+    """E = sum |w|^2/k2, 1/2 at kx = 0 (spectral_dns_2d.f90:127-129)."""
+    n = wz.shape[0]
+    _, _, k2 = wavenumber2d(n, n)
+    q = (wz * np.conj(wz)).real / k2
+    q[0, 0] = 0.0
+    q[:, 0] *= 0.5
+    return float(np.sum(q))

@@ -1,0 +1,72 @@
+"""Loader for the in-tree CUDA library ``lib/libspecns.so`` (ctypes).
+
+The library is built in place by ``speccodelib_gb300.build``.  Loading it
+needs no GPU; calling a compute entry point does.  There is no fallback: if
+the library is missing, `load()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libspecns.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "specns.h")
+
+_LIB = None
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+
+# argument types of every function declared in include/specns.h
+SIGNATURES = {
+    "sc_last_error": ([], C.c_char_p),
+    "sc_default_params": ([_P, _I, _I], _I),
+    "sc_create": ([_P, _P], _I),
+    "sc_destroy": ([_P], _I),
+    "sc_set_stream": ([_P, _P], _I),
+    "sc_set_dt": ([_P, _D], _I),
+    "sc_set_state": ([_P, _P, _P, _P], _I),
+    "sc_get_state": ([_P, _P, _P, _P], _I),
+    "sc_set_state_device": ([_P, _P, _P, _P], _I),
+    "sc_get_state_device": ([_P, _P, _P, _P], _I),
+    "sc_init_field": ([_P, _I, _I, _D, _D, _D, _D], _I),
+    "sc_rhs": ([_P, _P, _P, _P], _I),
+    "sc_rk4_steps": ([_P, _I], _I),
+    "sc_ab2_steps": ([_P, _I], _I),
+    "sc_diagnostics": ([_P, _P, _P], _I),
+    "sc_profile_enable": ([_P, _I], _I),
+    "sc_profile_read": ([_P, C.c_char_p, _P, _P], _I),
+    "sc_step_bytes": ([_P, _P], _I),
+    "sc_convec_dns": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
+    "sc_projection": ([_I, _P, _P, _P, _I, _I, _I], _I),
+    "sc_force": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _D], _I),
+    "sc_symmetrize": ([_I, _P, _I, _I, _I], _I),
+    "sc_dealiasing": ([_I, _P, _I, _I, _I], _I),
+    "sc_smag": ([_I, _P, _P, _P] + [_P] * 6 + [_I] * 6 + [_D, _D], _I),
+    "sc_dynsmag": ([_I, _P, _P, _P] + [_P] * 6 + [_I] * 6 + [_D, _D, _D, _P, _P, _P, _I], _I),
+}
+
+
+def declared_symbols(header=HEADER):
+    """Names of the functions declared in a C header of include/."""
+    src = open(header).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(sc_[a-z0-9_]+)\s*\(", src)))
+
+
+def load():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise OSError("libspecns.so is not built (%s); run speccodelib_gb300.build.build()" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = lib
+    return lib

@@ -1,0 +1,61 @@
+// Common device types and helpers for the spectral Navier-Stokes kernels.
+//
+// Field layout in HBM (internal, all kernels): a half-complex field is
+// (nz, ny, nxp) complex in C order, row pitch nxp >= nx/2+1 a multiple of the
+// pencil tile width, so every row starts on a 128-byte boundary.  Element
+// (kz|z, ky|y, kx) lives at (z*ny + y)*nxp + kx.  Columns kx >= nx/2+1 are
+// padding: zero-filled at allocation, never read by a transform and never
+// written with non-zero data.  The reference's Fortran array c(lx1,ly,lz) is
+// the same ordering with pitch lx1 = nx/2+1; host<->device copies repack
+// between the two pitches with a 2D memcpy.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sc {
+
+template <typename T> struct V2;
+template <> struct V2<float> { using t = float2; };
+template <> struct V2<double> { using t = double2; };
+
+template <typename T> using C2 = typename V2<T>::t;
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) {
+  C r; r.x = a; r.y = b; return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  return mk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
+// i * a
+template <typename C> __device__ __forceinline__ C cmuli(C a) { return mk<C>(-a.y, a.x); }
+// -i * a
+template <typename C> __device__ __forceinline__ C cmulmi(C a) { return mk<C>(a.y, -a.x); }
+template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) { return mk<C>(a.x * s, a.y * s); }
+template <typename C> __device__ __forceinline__ C czero() { return mk<C>(0, 0); }
+
+// Signed wavenumber of index i on an axis of length n: 0..n/2-1, -n/2..-1
+// (the FFTW ordering, wavenumber.f90:109,115).
+__device__ __forceinline__ int wavenum(int i, int n) { return i < n / 2 ? i : i - n; }
+
+// Grid geometry shared by all passes.
+struct Geom {
+  int nx, ny, nz;      // physical grid
+  int nxh;             // nx/2 + 1 complex columns
+  int nxp;             // padded row pitch (complex elements)
+  long long field;     // elements per field = nz*ny*nxp
+};
+
+constexpr int kMaxFields = 18;
+
+template <typename T> struct FieldList {
+  C2<T>* f[kMaxFields];
+};
+
+}  // namespace sc

@@ -1,0 +1,193 @@
+// Runtime-length dispatch of the pass kernels (compiled per precision and per
+// kernel family in separate translation units so the build runs in parallel).
+#pragma once
+#include "sc_launch.h"
+#include "sc_ops.cuh"
+
+namespace sc {
+
+// Raise the dynamic shared-memory limit once per kernel instance.
+template <typename K> inline cudaError_t smem_attr(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+#define SC_LOGN_CASES(X) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10)
+#define SC_LOGM_CASES(X) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9)
+
+template <typename T, int LOGN, bool INV>
+cudaError_t launch_plain(const FieldList<T>& fl, const PlainArgs<T>& pa, const Geom& g, int nouter,
+                         const C2<T>* tw, cudaStream_t s) {
+  using Cfg = PencilCfg<T, LOGN>;
+  auto k = pencil_plain_kernel<T, LOGN, INV>;
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, nouter);
+  k<<<grid, Cfg::NT, Cfg::SMEM, s>>>(fl, pa, g, tw);
+  return cudaGetLastError();
+}
+
+template <typename T, int LOGN, int MODE>
+cudaError_t launch_zinv(const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g,
+                        const C2<T>* tw, cudaStream_t s) {
+  using Cfg = PencilCfg<T, LOGN>;
+  auto k = zinv_vel_kernel<T, LOGN, MODE>;
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
+  k<<<grid, Cfg::NT, Cfg::SMEM, s>>>(za, out, g, tw);
+  return cudaGetLastError();
+}
+
+template <typename T, int LOGN, int NIN>
+cudaError_t launch_zfwd(const FieldList<T>& fin, const StageArgs<T>& st, const Geom& g,
+                        const C2<T>* tw, cudaStream_t s) {
+  using Cfg = PencilCfg<T, LOGN>;
+  auto k = zfwd_stage_kernel<T, LOGN, NIN>;
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
+  k<<<grid, Cfg::NT, Cfg::SMEM, s>>>(fin, st, g, tw);
+  return cudaGetLastError();
+}
+
+template <typename T, int LOGM, int MODE>
+cudaError_t launch_xpass(const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g,
+                         const C2<T>* twM, const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s) {
+  using Cfg = XpCfg<T, LOGM, MODE>;
+  auto k = xpass_kernel<T, LOGM, MODE>;
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  if (attr != cudaSuccess) return attr;
+  const long long nb = (xa.rows + Cfg::RB - 1) / Cfg::RB;
+  k<<<(unsigned)nb, Cfg::NT, Cfg::SMEM, s>>>(fin, fout, g, twM, twN, xa);
+  return cudaGetLastError();
+}
+
+}  // namespace sc
+
+#define SC_DEFINE_TILE(T) \
+  template <> int sc::Launch<T>::tile() { return sc::Tile<T>::P; }
+
+#define SC_DEFINE_PLAIN(T)                                                                       \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::plain(int logn, bool inv, const FieldList<T>& fl,                   \
+                                   const PlainArgs<T>& pa, const Geom& g, int nouter,            \
+                                   const C2<T>* tw, cudaStream_t s) {                            \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_PLAIN_CASE_##T)                                                           \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }
+
+#define SC_DEFINE_ZINV(T)                                                                        \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zinv_vel(int logn, int mode, const ZvArgs<T>& za,                   \
+                                      const FieldList<T>& out, const Geom& g, const C2<T>* tw,   \
+                                      cudaStream_t s) {                                          \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZINV_CASE_##T)                                                            \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }
+
+#define SC_DEFINE_ZFWD(T)                                                                        \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zfwd_stage(int logn, int nin, const FieldList<T>& fin,              \
+                                        const StageArgs<T>& st, const Geom& g, const C2<T>* tw,  \
+                                        cudaStream_t s) {                                        \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZFWD_CASE_##T)                                                            \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::fixup(const StageArgs<T>& st, const Geom& g, cudaStream_t s) {      \
+    long long n = (long long)g.ny * g.nz;                                                        \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 4096) nb = 4096;                                                                    \
+    sc::fixup_kx0_kernel<T><<<nb, 256, 0, s>>>(st, g);                                           \
+    return cudaGetLastError();                                                                   \
+  }
+
+#define SC_DEFINE_XPASS(T)                                                                       \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::xpass(int logm, int mode, const FieldList<T>& fin,                  \
+                                   const FieldList<T>& fout, const Geom& g, const C2<T>* twM,    \
+                                   const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s) {       \
+    switch (logm) {                                                                              \
+      SC_LOGM_CASES(SC_XPASS_CASE_##T)                                                           \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }
+
+#define SC_DEFINE_OPS(T)                                                                         \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::diag(const DiagArgs<T>& da, const Geom& g, cudaStream_t s) {        \
+    size_t sm = sizeof(double) * (size_t)da.nshell;                                              \
+    sc::diag_partial_kernel<T><<<da.nblocks, 256, sm, s>>>(da, g);                               \
+    cudaError_t e = cudaGetLastError();                                                          \
+    if (e != cudaSuccess) return e;                                                              \
+    sc::diag_final_kernel<<<1, 256, 0, s>>>(da.partial, da.nblocks, sc::DQ_N + da.nshell,        \
+                                            da.out);                                             \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::specop(const SpecOpArgs<T>& oa, const Geom& g, cudaStream_t s) {    \
+    long long n = (long long)g.ny * g.nz * g.nxh;                                                \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 152 * 16) nb = 152 * 16;                                                            \
+    sc::specop_kernel<T><<<nb, 256, 0, s>>>(oa, g);                                              \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::strain(const StrainArgs<T>& sa, const Geom& g, cudaStream_t s) {    \
+    long long n = (long long)g.ny * g.nz * g.nxh;                                                \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 152 * 16) nb = 152 * 16;                                                            \
+    sc::strain_kernel<T><<<nb, 256, 0, s>>>(sa, g);                                              \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::phys(const PhysArgs<T>& pa, int nblocks, const Geom& g,             \
+                                  double* c1_out, double* lm_mm, cudaStream_t s) {               \
+    sc::phys_kernel<T><<<nblocks, 256, 0, s>>>(pa, g);                                           \
+    cudaError_t e = cudaGetLastError();                                                          \
+    if (e != cudaSuccess || pa.op != sc::PH_DYN2) return e;                                      \
+    sc::dyn_final_kernel<<<1, 32, 0, s>>>(pa.partial, nblocks, c1_out, lm_mm);                   \
+    return cudaGetLastError();                                                                   \
+  }
+
+// per-type case bodies (token-pasted above)
+#define SC_PLAIN_CASE_float(L) \
+  case L: return inv ? sc::launch_plain<float, L, true>(fl, pa, g, nouter, tw, s) \
+                     : sc::launch_plain<float, L, false>(fl, pa, g, nouter, tw, s);
+#define SC_PLAIN_CASE_double(L) \
+  case L: return inv ? sc::launch_plain<double, L, true>(fl, pa, g, nouter, tw, s) \
+                     : sc::launch_plain<double, L, false>(fl, pa, g, nouter, tw, s);
+#define SC_ZINV_BODY(T, L)                                                      \
+  case L:                                                                       \
+    switch (mode) {                                                             \
+      case sc::ZV_DNS: return sc::launch_zinv<T, L, sc::ZV_DNS>(za, out, g, tw, s);   \
+      case sc::ZV_SMAG: return sc::launch_zinv<T, L, sc::ZV_SMAG>(za, out, g, tw, s); \
+      case sc::ZV_DYN: return sc::launch_zinv<T, L, sc::ZV_DYN>(za, out, g, tw, s);   \
+      default: return cudaErrorInvalidValue;                                    \
+    }
+#define SC_ZINV_CASE_float(L) SC_ZINV_BODY(float, L)
+#define SC_ZINV_CASE_double(L) SC_ZINV_BODY(double, L)
+#define SC_ZFWD_BODY(T, L)                                                      \
+  case L:                                                                       \
+    return nin == 9 ? sc::launch_zfwd<T, L, 9>(fin, st, g, tw, s)               \
+                    : sc::launch_zfwd<T, L, 3>(fin, st, g, tw, s);
+#define SC_ZFWD_CASE_float(L) SC_ZFWD_BODY(float, L)
+#define SC_ZFWD_CASE_double(L) SC_ZFWD_BODY(double, L)
+#define SC_XPASS_BODY(T, L)                                                           \
+  case L:                                                                             \
+    switch (mode) {                                                                   \
+      case sc::XP_DNS: return sc::launch_xpass<T, L, sc::XP_DNS>(fin, fout, g, twM, twN, xa, s);   \
+      case sc::XP_SMAG: return sc::launch_xpass<T, L, sc::XP_SMAG>(fin, fout, g, twM, twN, xa, s); \
+      case sc::XP_C2R3: return sc::launch_xpass<T, L, sc::XP_C2R3>(fin, fout, g, twM, twN, xa, s); \
+      case sc::XP_R2C3: return sc::launch_xpass<T, L, sc::XP_R2C3>(fin, fout, g, twM, twN, xa, s); \
+      default: return cudaErrorInvalidValue;                                          \
+    }
+#define SC_XPASS_CASE_float(L) SC_XPASS_BODY(float, L)
+#define SC_XPASS_CASE_double(L) SC_XPASS_BODY(double, L)

@@ -1,0 +1,239 @@
+// Block-level batched FFT engine for sm_103a.
+//
+// A thread block transforms P independent pencils of length N = 2^LOGN held
+// in shared memory as sm[n*PS + p] (pencil p, point n).  The transform is a
+// Stockham autosort FFT (radix-8 stages, then radix-4/2 to finish), so the
+// output comes out in natural order without a bit-reversal pass.
+//
+// The first stage takes its inputs straight from registers and the last stage
+// leaves its outputs in registers, so a pass that loads from HBM, transforms
+// and stores back touches shared memory only for the exchanges between
+// stages.  Input element (p, n) for register slot in[a][r] is
+//     job = threadIdx.x + a*NT, (p, j) = decode(job), n = j + r*(N/R1)
+// and output slot out[a][r] holds element n = j + r*(N/RL) of pencil p, with
+// decode giving p fastest (PFAST: consecutive threads walk consecutive
+// pencils, the layout of strided-axis passes whose pencils are contiguous in
+// HBM) or j fastest (consecutive threads walk one pencil, the layout of the
+// x-axis pass whose pencils are HBM rows).
+//
+// Twiddles W_N^m = exp(-2 pi i m/N) come from a table computed in double on
+// the host and rounded once to T.  Forward = exp(-i..), inverse = exp(+i..),
+// both unnormalised (FFTW's convention).
+#pragma once
+#include "sc_common.cuh"
+
+namespace sc {
+
+// Radix plan: as many radix-8 stages as possible, finished by one radix-4
+// (LOGN % 3 == 2), two radix-4 (LOGN % 3 == 1) or a lone radix-2 (N = 2).
+__host__ __device__ constexpr int fft_nstages(int logn) {
+  return logn <= 3 ? 1 : (logn % 3 == 0 ? logn / 3 : logn / 3 + 1);
+}
+__host__ __device__ constexpr int fft_radix(int logn, int s) {
+  return logn == 1 ? 2
+       : logn == 2 ? 4
+       : logn % 3 == 0 ? 8
+       : logn % 3 == 2 ? (s < logn / 3 ? 8 : 4)
+       : (s < logn / 3 - 1 ? 8 : 4);
+}
+__host__ __device__ constexpr int fft_ns(int logn, int s) {
+  return s == 0 ? 1 : fft_ns(logn, s - 1) * fft_radix(logn, s - 1);
+}
+
+template <typename T> struct Consts;
+template <> struct Consts<float> { static constexpr float rsqrt2 = 0.70710678118654752440f; };
+template <> struct Consts<double> { static constexpr double rsqrt2 = 0.70710678118654752440; };
+
+template <bool INV, typename C> __device__ __forceinline__ void dft2(C* v) {
+  C t = v[0];
+  v[0] = cadd(t, v[1]);
+  v[1] = csub(t, v[1]);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft4(C* v) {
+  C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  C t2 = cadd(v[1], v[3]), t3 = csub(v[1], v[3]);
+  t3 = INV ? cmuli(t3) : cmulmi(t3);
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[3] = csub(t1, t3);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft8(C* v) {
+  using R = decltype(C::x);
+  const R h = Consts<R>::rsqrt2;
+  C e[4] = {v[0], v[2], v[4], v[6]};
+  C o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<INV>(e);
+  dft4<INV>(o);
+  // o[k] *= W_8^{+-k}
+  if (INV) {
+    o[1] = mk<C>((o[1].x - o[1].y) * h, (o[1].x + o[1].y) * h);
+    o[2] = cmuli(o[2]);
+    o[3] = mk<C>((-o[3].x - o[3].y) * h, (o[3].x - o[3].y) * h);
+  } else {
+    o[1] = mk<C>((o[1].x + o[1].y) * h, (o[1].y - o[1].x) * h);
+    o[2] = cmulmi(o[2]);
+    o[3] = mk<C>((o[3].y - o[3].x) * h, (-o[3].x - o[3].y) * h);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 4] = csub(e[k], o[k]);
+  }
+}
+
+template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C* v) {
+  if constexpr (R == 2) dft2<INV>(v);
+  else if constexpr (R == 4) dft4<INV>(v);
+  else dft8<INV>(v);
+}
+
+template <typename T, int LOGN, int P, int PS, int NT, bool PFAST>
+struct FFTEngine {
+  using C = C2<T>;
+  static constexpr int N = 1 << LOGN;
+  static constexpr int NS = fft_nstages(LOGN);
+  static constexpr int R1 = fft_radix(LOGN, 0);
+  static constexpr int RL = fft_radix(LOGN, NS - 1);
+  static constexpr int TOT1 = P * (N / R1);
+  static constexpr int TOTL = P * (N / RL);
+  static constexpr int J1 = (TOT1 + NT - 1) / NT;
+  static constexpr int JL = (TOTL + NT - 1) / NT;
+  static constexpr int SMEM_ELEMS = N * PS;
+
+  template <int R>
+  __device__ static __forceinline__ void decode(int job, int& p, int& j) {
+    constexpr int NR = N / R;
+    if constexpr (PFAST) {
+      p = job % P;
+      j = job / P;
+    } else {
+      j = job % NR;
+      p = job / NR;
+    }
+  }
+  // Position of in[a][r]; returns false for padding jobs.
+  __device__ static __forceinline__ bool in_pos(int a, int r, int& p, int& n) {
+    int job = threadIdx.x + a * NT, j;
+    decode<R1>(job, p, j);
+    n = j + r * (N / R1);
+    return (TOT1 % NT == 0) || job < TOT1;
+  }
+  // Position of out[a][r]; returns false for padding jobs.
+  __device__ static __forceinline__ bool out_pos(int a, int r, int& p, int& n) {
+    int job = threadIdx.x + a * NT, j;
+    decode<RL>(job, p, j);
+    n = j + r * (N / RL);
+    return (TOTL % NT == 0) || job < TOTL;
+  }
+
+  template <int R, int NSV, bool INV>
+  __device__ static __forceinline__ void twiddle(C* v, int k, const C* __restrict__ tw) {
+    if constexpr (NSV > 1) {
+      constexpr int STRIDE = N / (NSV * R);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = __ldg(&tw[k * r * STRIDE]);
+        v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
+      }
+    }
+  }
+
+  // Stage S (0 < S < NS-1): shared -> shared.
+  template <int S, bool INV>
+  __device__ static __forceinline__ void mid_stage(C* sm, const C* __restrict__ tw) {
+    constexpr int R = fft_radix(LOGN, S);
+    constexpr int NR = N / R;
+    constexpr int NSV = fft_ns(LOGN, S);
+    constexpr int TOT = P * NR;
+    constexpr int J = (TOT + NT - 1) / NT;
+    C v[J][R];
+#pragma unroll
+    for (int a = 0; a < J; ++a) {
+      int job = threadIdx.x + a * NT, p, j;
+      decode<R>(job, p, j);
+      if ((TOT % NT == 0) || job < TOT) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[a][r] = sm[(j + r * NR) * PS + p];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < J; ++a) {
+      int job = threadIdx.x + a * NT, p, j;
+      decode<R>(job, p, j);
+      if ((TOT % NT == 0) || job < TOT) {
+        const int k = j % NSV;
+        twiddle<R, NSV, INV>(v[a], k, tw);
+        dft<R, INV>(v[a]);
+        const int d = (j / NSV) * NSV * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm[(d + r * NSV) * PS + p] = v[a][r];
+      }
+    }
+    __syncthreads();
+  }
+
+  template <int S, bool INV>
+  __device__ static __forceinline__ void mid_stages(C* sm, const C* __restrict__ tw) {
+    if constexpr (S < NS - 1) {
+      mid_stage<S, INV>(sm, tw);
+      mid_stages<S + 1, INV>(sm, tw);
+    }
+  }
+
+  // Full transform: registers (first-stage layout) -> registers (last-stage
+  // layout).  Ends with a barrier, so the caller may reuse `sm` at once.
+  template <bool INV>
+  __device__ static void run(C (&in)[J1][R1], C (&out)[JL][RL], C* sm, const C* __restrict__ tw) {
+    if constexpr (NS == 1) {
+#pragma unroll
+      for (int a = 0; a < J1; ++a) {
+#pragma unroll
+        for (int r = 0; r < R1; ++r) out[a][r] = in[a][r];
+        dft<R1, INV>(out[a]);
+      }
+    } else {
+      // stage 0: registers -> shared (Ns = 1, no twiddles)
+#pragma unroll
+      for (int a = 0; a < J1; ++a) {
+        int job = threadIdx.x + a * NT, p, j;
+        decode<R1>(job, p, j);
+        if ((TOT1 % NT == 0) || job < TOT1) {
+          dft<R1, INV>(in[a]);
+#pragma unroll
+          for (int r = 0; r < R1; ++r) sm[(j * R1 + r) * PS + p] = in[a][r];
+        }
+      }
+      __syncthreads();
+      mid_stages<1, INV>(sm, tw);
+      // last stage: shared -> registers
+      constexpr int NR = N / RL;
+      constexpr int NSV = fft_ns(LOGN, NS - 1);
+      static_assert(NSV == NR, "last stage spans the pencil");
+#pragma unroll
+      for (int a = 0; a < JL; ++a) {
+        int job = threadIdx.x + a * NT, p, j;
+        decode<RL>(job, p, j);
+        if ((TOTL % NT == 0) || job < TOTL) {
+#pragma unroll
+          for (int r = 0; r < RL; ++r) out[a][r] = sm[(j + r * NR) * PS + p];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int a = 0; a < JL; ++a) {
+        int job = threadIdx.x + a * NT, p, j;
+        decode<RL>(job, p, j);
+        if ((TOTL % NT == 0) || job < TOTL) {
+          twiddle<RL, NSV, INV>(out[a], j, tw);
+          dft<RL, INV>(out[a]);
+        }
+      }
+    }
+  }
+};
+
+}  // namespace sc

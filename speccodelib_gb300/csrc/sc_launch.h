@@ -1,0 +1,41 @@
+// Host-side launch interface of the pass kernels, one specialisation per
+// arithmetic type (float: FP32-bulk mode, double: plain FP64 mode).  Each
+// launcher dispatches the runtime axis length to a compiled template
+// instance; lengths outside 8..1024 return cudaErrorInvalidValue.
+#pragma once
+#include "sc_common.cuh"
+
+namespace sc {
+
+template <typename T> struct PlainArgs;
+template <typename T> struct ZvArgs;
+template <typename T> struct StageArgs;
+template <typename T> struct XArgs;
+template <typename T> struct DiagArgs;
+template <typename T> struct SpecOpArgs;
+template <typename T> struct StrainArgs;
+template <typename T> struct PhysArgs;
+
+template <typename T> struct Launch {
+  static int tile();                                   // pencil tile width P
+  // strided-axis pass: grid = (ceil(nxh/P), nouter)
+  static cudaError_t plain(int logn, bool inverse, const FieldList<T>& fl, const PlainArgs<T>& pa,
+                           const Geom& g, int nouter, const C2<T>* tw, cudaStream_t s);
+  static cudaError_t zinv_vel(int logn, int mode, const ZvArgs<T>& za, const FieldList<T>& out,
+                              const Geom& g, const C2<T>* tw, cudaStream_t s);
+  static cudaError_t zfwd_stage(int logn, int nin, const FieldList<T>& fin, const StageArgs<T>& st,
+                                const Geom& g, const C2<T>* tw, cudaStream_t s);
+  static cudaError_t fixup(const StageArgs<T>& st, const Geom& g, cudaStream_t s);
+  static cudaError_t xpass(int logm, int mode, const FieldList<T>& fin, const FieldList<T>& fout,
+                           const Geom& g, const C2<T>* twM, const C2<T>* twN, const XArgs<T>& xa,
+                           cudaStream_t s);
+  // spectral-space elementwise operators and reductions (sc_ops.cuh)
+  static cudaError_t diag(const DiagArgs<T>& da, const Geom& g, cudaStream_t s);
+  static cudaError_t specop(const SpecOpArgs<T>& oa, const Geom& g, cudaStream_t s);
+  static cudaError_t strain(const StrainArgs<T>& sa, const Geom& g, cudaStream_t s);
+  // physical-space pointwise op; PH_DYN2 also finishes cs2 into *c1_out
+  static cudaError_t phys(const PhysArgs<T>& pa, int nblocks, const Geom& g, double* c1_out,
+                          double* lm_mm, cudaStream_t s);
+};
+
+}  // namespace sc

@@ -1,0 +1,357 @@
+// Elementwise spectral operators and FP64 reductions.
+//
+// These are the pieces of the reference's L3 layer that are not fused into
+// the transform passes: the standalone operators behind the reference-
+// signature entry points (projection.f90, symmetrize.f90, dealiasing.f90,
+// force.f90), the seeded initial field's post-processing
+// (initialize.f90:328-368) and the in-loop diagnostics
+// (specdns-forced-omp-ft.f90:142-176).  All sums are accumulated in double.
+#pragma once
+#include "sc_passes.cuh"
+
+namespace sc {
+
+// ---------------------------------------------------------------------------
+// reductions over spectral (or packed physical) fields
+// ---------------------------------------------------------------------------
+enum DiagQ { DQ_ENERGY = 0, DQ_K2Q = 1, DQ_MAXDIV = 2, DQ_NONFINITE = 3, DQ_MAXU2 = 4, DQ_N = 5 };
+
+template <typename T> struct DiagArgs {
+  const C2<T>* v[3];
+  int physical;           // 0: spectral fields (energy etc.); 1: packed physical rows (max |u|^2)
+  double kmax2;           // < 0: every mode; else only modes with k2 < kmax2 (forcing band)
+  int rows_per_block;
+  int nshell;             // 0: no spectrum; else nx/2 shells
+  double* partial;        // [gridDim.x][DQ_N + nshell]
+  double* out;            // [DQ_N + nshell]
+  int nblocks;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) diag_partial_kernel(DiagArgs<T> da, Geom g) {
+  using C = C2<T>;
+  extern __shared__ double shells[];
+  __shared__ double red[8 + 1];
+  const int ns = da.nshell;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) shells[i] = 0.0;
+  __syncthreads();
+  double e = 0.0, k2q = 0.0, mdiv = 0.0, nf = 0.0, mu2 = 0.0;
+  const long long rows = (long long)g.ny * g.nz;
+  const long long r0 = (long long)blockIdx.x * da.rows_per_block;
+  const int ncol = da.physical ? g.nx / 2 : g.nxh;
+  const long long tot = (long long)da.rows_per_block * ncol;
+  for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
+    const long long row = r0 + t / ncol;
+    const int ix = (int)(t % ncol);
+    if (row >= rows) break;
+    const long long idx = row * g.nxp + ix;
+    const C a = da.v[0][idx], b = da.v[1][idx], c = da.v[2][idx];
+    if (da.physical) {
+      const double ue = (double)a.x * a.x + (double)b.x * b.x + (double)c.x * c.x;
+      const double uo = (double)a.y * a.y + (double)b.y * b.y + (double)c.y * c.y;
+      mu2 = fmax(mu2, fmax(ue, uo));
+      if (!isfinite(ue) || !isfinite(uo)) nf += 1.0;
+      continue;
+    }
+    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
+    const double kx = ix, ky = wavenum(iy, g.ny), kz = wavenum(iz, g.nz);
+    const double k2 = kx * kx + ky * ky + kz * kz;
+    if (da.kmax2 >= 0.0 && !(k2 < da.kmax2)) continue;
+    double q = (double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x + (double)b.y * b.y +
+               (double)c.x * c.x + (double)c.y * c.y;
+    if (!isfinite(q)) nf += 1.0;
+    if (ix == 0) q *= 0.5;
+    e += q;
+    k2q += k2 * q;
+    const double dr = kx * a.x + ky * b.x + kz * c.x, di = kx * a.y + ky * b.y + kz * c.y;
+    mdiv = fmax(mdiv, sqrt(dr * dr + di * di));
+    if (ns > 0) {
+      const int ll = (int)floor(sqrt(k2) + 0.5);
+      if (ll >= 1 && ll <= ns) atomicAdd(&shells[ll - 1], q);
+    }
+  }
+  double* out = da.partial + (long long)blockIdx.x * (DQ_N + ns);
+  double s;
+  s = block_sum<256>(e, red);
+  if (threadIdx.x == 0) out[DQ_ENERGY] = s;
+  s = block_sum<256>(k2q, red);
+  if (threadIdx.x == 0) out[DQ_K2Q] = s;
+  s = block_sum<256>(nf, red);
+  if (threadIdx.x == 0) out[DQ_NONFINITE] = s;
+  // maxima: reuse the sum tree with max
+  double m1 = warp_max(mdiv), m2 = warp_max(mu2);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = m1; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int i = 0; i < 8; ++i) m = fmax(m, red[i]);
+    out[DQ_MAXDIV] = m;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = m2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int i = 0; i < 8; ++i) m = fmax(m, red[i]);
+    out[DQ_MAXU2] = m;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) out[DQ_N + i] = shells[i];
+}
+
+// Column-wise reduction of the block partials in block order (deterministic).
+static __global__ void diag_final_kernel(const double* partial, int nblocks, int ncols, double* out) {
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+    double s = 0.0;
+    const bool isMax = (c == DQ_MAXDIV || c == DQ_MAXU2);
+    for (int b = 0; b < nblocks; ++b) {
+      const double x = partial[(long long)b * ncols + c];
+      s = isMax ? fmax(s, x) : s + x;
+    }
+    out[c] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// elementwise spectral operators
+// ---------------------------------------------------------------------------
+enum SpecOp {
+  OP_PROJECT = 0,       // projection.f90:16-30 on fields 0..2
+  OP_ZERO_PLANES = 1,   // symmetrize.f90:43-49 on fields 0..n-1
+  OP_KX0_COPY = 2,      // symmetrize.f90:52-62 (after OP_ZERO_PLANES)
+  OP_MASK = 3,          // zero k2 >= kcut2 (dealiasing.f90:35, dns-deform.f90:233-237)
+  OP_FORCE_ADD = 4,     // force.f90:24-29: f[0..2] += a * g[0..2] on k2 < fkmax2
+  OP_INIT_SHAPE = 5,    // initialize.f90:328-332 projection with +tiny
+  OP_INIT_AMP = 6,      // initialize.f90:349-360 amplitude (akp) or k^(-11/6) band
+  OP_SCALE = 7,         // f *= scalar (scalar from device or host value)
+  OP_AXPBY = 8          // f[c] = alpha f[c] + beta g[c]
+};
+
+template <typename T> struct SpecOpArgs {
+  int op;
+  int nfields;
+  C2<T>* f[6];
+  const C2<T>* gsrc[3];
+  double a, b;            // scalars
+  const double* dscal;    // device scalar (OP_SCALE: multiply by sqrt(a / *dscal) if set)
+  double kcut2;
+  double akp, u0, kmin, kmax;
+  int spectrum_kind;      // 0: akp shape, 1: k^(-11/6) band
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
+  using C = C2<T>;
+  const long long rows = (long long)g.ny * g.nz;
+  const long long total = (oa.op == OP_KX0_COPY) ? rows : rows * g.nxh;
+  T sfac = T(1);
+  if (oa.op == OP_SCALE) sfac = oa.dscal ? (T)sqrt(oa.a / *oa.dscal) : (T)oa.a;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    if (oa.op == OP_KX0_COPY) {
+      const int iy = (int)(t % g.ny), iz = (int)(t / g.ny);
+      if (!(iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2))) continue;
+      const int sy = (g.ny - iy) % g.ny, sz = (g.nz - iz) % g.nz;
+      const long long d = ((long long)iz * g.ny + iy) * g.nxp, s = ((long long)sz * g.ny + sy) * g.nxp;
+      for (int c = 0; c < oa.nfields; ++c) oa.f[c][d] = (iy == g.ny / 2) ? czero<C>() : cconj(oa.f[c][s]);
+      continue;
+    }
+    const long long row = t / g.nxh;
+    const int ix = (int)(t % g.nxh);
+    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
+    const long long idx = row * g.nxp + ix;
+    const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
+    const double k2d = (double)ix * ix + (double)ky * ky + (double)kz * kz;
+    switch (oa.op) {
+      case OP_PROJECT:
+      case OP_INIT_SHAPE: {
+        C w0 = oa.f[0][idx], w1 = oa.f[1][idx], w2 = oa.f[2][idx];
+        const T k2 = kx * kx + ky * ky + kz * kz;
+        if (k2 > T(0)) {
+          C tt = cadd(cadd(cscale(w0, kx), cscale(w1, ky)), cscale(w2, kz));
+          tt = mk<C>(tt.x / k2, tt.y / k2);
+          w0 = csub(w0, cscale(tt, kx));
+          w1 = csub(w1, cscale(tt, ky));
+          w2 = csub(w2, cscale(tt, kz));
+        }
+        oa.f[0][idx] = w0; oa.f[1][idx] = w1; oa.f[2][idx] = w2;
+        break;
+      }
+      case OP_ZERO_PLANES:
+        if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
+          for (int c = 0; c < oa.nfields; ++c) oa.f[c][idx] = czero<C>();
+        break;
+      case OP_MASK:
+        if (k2d >= oa.kcut2 && k2d > 0.0)
+          for (int c = 0; c < oa.nfields; ++c) oa.f[c][idx] = czero<C>();
+        break;
+      case OP_FORCE_ADD:
+        // k2(1,1,1) = tiny < fkmax^2: the mean mode is in the band too
+        if (k2d < oa.kcut2) {
+          const T a = (T)oa.a;
+          for (int c = 0; c < 3; ++c) oa.f[c][idx] = cadd(oa.f[c][idx], cscale(oa.gsrc[c][idx], a));
+        }
+        break;
+      case OP_INIT_AMP: {
+        // k2 at the mean mode is tiny(1.0_sp) (wavenumber.f90:156)
+        const double k2r = (k2d == 0.0) ? 1.1754943508222875e-38 : k2d;
+        double amp;
+        if (oa.spectrum_kind == 0) {
+          const double pi = 3.1415926536;
+          amp = oa.u0 * sqrt(8.0 * sqrt(2.0 / pi) / (3.0 * pi * pow(oa.akp, 5.0))) * sqrt(k2r) *
+                exp(-k2r / (oa.akp * oa.akp));
+        } else {
+          const double k = sqrt(k2r);
+          amp = (k >= oa.kmin && k <= oa.kmax) ? pow(k, -11.0 / 6.0) : 0.0;
+        }
+        for (int c = 0; c < 3; ++c) oa.f[c][idx] = cscale(oa.f[c][idx], (T)amp);
+        break;
+      }
+      case OP_SCALE:
+        for (int c = 0; c < oa.nfields; ++c) oa.f[c][idx] = cscale(oa.f[c][idx], sfac);
+        break;
+      case OP_AXPBY:
+        for (int c = 0; c < oa.nfields; ++c)
+          oa.f[c][idx] = cadd(cscale(oa.f[c][idx], (T)oa.a), cscale(oa.gsrc[c][idx], (T)oa.b));
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// strain rate in spectral space: S_ij = i (k_i v_j + k_j v_i)/2, order
+// 11 12 13 22 23 33 (smag.f90:21-32)
+// ---------------------------------------------------------------------------
+template <typename T> struct StrainArgs {
+  const C2<T>* v[3];
+  C2<T>* s[6];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) strain_kernel(StrainArgs<T> sa, Geom g) {
+  using C = C2<T>;
+  const long long total = (long long)g.ny * g.nz * g.nxh;
+  const T half = T(0.5);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long row = t / g.nxh;
+    const int ix = (int)(t % g.nxh);
+    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
+    const long long idx = row * g.nxp + ix;
+    const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
+    const C v0 = sa.v[0][idx], v1 = sa.v[1][idx], v2 = sa.v[2][idx];
+    sa.s[0][idx] = cmuli(cscale(v0, kx));
+    sa.s[1][idx] = cmuli(cscale(cadd(cscale(v1, kx), cscale(v0, ky)), half));
+    sa.s[2][idx] = cmuli(cscale(cadd(cscale(v2, kx), cscale(v0, kz)), half));
+    sa.s[3][idx] = cmuli(cscale(v1, ky));
+    sa.s[4][idx] = cmuli(cscale(cadd(cscale(v2, ky), cscale(v1, kz)), half));
+    sa.s[5][idx] = cmuli(cscale(v2, kz));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// physical-space pointwise kernels on packed rows (x = 2m: .x, x = 2m+1: .y)
+// ---------------------------------------------------------------------------
+enum PhysOp {
+  PH_TAU = 0,    // f[0..5] (S_ij) <- coef |S| S_ij, coef = -2 c1 delta^2 scale (smag.f90:41-64)
+  PH_DYN1 = 1,   // dynamic procedure, first products (dynsmag.f90:43-48, 103-115, 133-145)
+  PH_DYN2 = 2    // L_ij, M_ij and the box sums LM, MM (dynsmag.f90:71-76, 163-184)
+};
+
+template <typename T> struct PhysArgs {
+  int op;
+  C2<T>* f[24];
+  const double* c1;      // device scalar (c1 or cs2)
+  double delta2, delta_test2;
+  T scale;               // 1/(nx ny nz)
+  double* partial;       // PH_DYN2: [nblocks][2] (LM, MM)
+  int rows_per_block;
+};
+
+template <typename R>
+__device__ __forceinline__ R smag_abs(R s11, R s12, R s13, R s22, R s23, R s33) {
+  return sqrt(R(2) * (s11 * s11 + s22 * s22 + s33 * s33 + R(2) * (s12 * s12 + s13 * s13 + s23 * s23)));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) phys_kernel(PhysArgs<T> pa, Geom g) {
+  using C = C2<T>;
+  __shared__ double red[9];
+  const long long rows = (long long)g.ny * g.nz;
+  const int ncol = g.nx / 2;
+  const long long r0 = (long long)blockIdx.x * pa.rows_per_block;
+  const long long tot = (long long)pa.rows_per_block * ncol;
+  double lm = 0.0, mm = 0.0;
+  T coef = T(0);
+  if (pa.op == PH_TAU) coef = (T)(-2.0 * (*pa.c1) * pa.delta2) * pa.scale;
+  for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
+    const long long row = r0 + t / ncol;
+    if (row >= rows) break;
+    const long long idx = row * g.nxp + (t % ncol);
+    if (pa.op == PH_TAU) {
+      C s[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) s[q] = pa.f[q][idx];
+      const T ar = smag_abs(s[0].x, s[1].x, s[2].x, s[3].x, s[4].x, s[5].x);
+      const T ai = smag_abs(s[0].y, s[1].y, s[2].y, s[3].y, s[4].y, s[5].y);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) pa.f[q][idx] = mk<C>(ar * s[q].x * coef, ai * s[q].y * coef);
+    } else if (pa.op == PH_DYN1) {
+      // slots: u 0-2, gu 3-5, S 6-11, gS 12-17, D 18-23
+      C u[3], gu[3], s[6], gs[6];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) { u[q] = pa.f[q][idx]; gu[q] = pa.f[3 + q][idx]; }
+#pragma unroll
+      for (int q = 0; q < 6; ++q) { s[q] = pa.f[6 + q][idx]; gs[q] = pa.f[12 + q][idx]; }
+      const int ii[6] = {0, 0, 0, 1, 1, 2}, jj[6] = {0, 1, 2, 1, 2, 2};
+      const T sc = pa.scale;
+      const T ar = smag_abs(s[0].x, s[1].x, s[2].x, s[3].x, s[4].x, s[5].x);
+      const T ai = smag_abs(s[0].y, s[1].y, s[2].y, s[3].y, s[4].y, s[5].y);
+      const T gr = smag_abs(gs[0].x, gs[1].x, gs[2].x, gs[3].x, gs[4].x, gs[5].x);
+      const T gi = smag_abs(gs[0].y, gs[1].y, gs[2].y, gs[3].y, gs[4].y, gs[5].y);
+      const T c2 = (T)(2.0 * pa.delta2), ct2 = (T)(-2.0 * pa.delta_test2);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const C a = u[ii[q]], b = u[jj[q]];
+        pa.f[18 + q][idx] = mk<C>(a.x * b.x * sc, a.y * b.y * sc);           // u_i u_j / N^3
+        const C ga = gu[ii[q]], gb = gu[jj[q]];
+        pa.f[q][idx] = mk<C>(ga.x * gb.x, ga.y * gb.y);                       // (g u_i)(g u_j)
+        pa.f[6 + q][idx] = mk<C>(c2 * (ar * s[q].x) * sc, c2 * (ai * s[q].y) * sc);   // 2 D^2 |S| S / N^3
+        pa.f[12 + q][idx] = mk<C>(ct2 * (gr * gs[q].x), ct2 * (gi * gs[q].y));        // -2 Dt^2 |gS| gS
+      }
+    } else {
+      // slots: G 0-5, filt(s) 6-11, T 12-17, filt(D) 18-23
+      const T w[6] = {T(1), T(2), T(2), T(1), T(2), T(1)};
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const C G = pa.f[q][idx], fs = pa.f[6 + q][idx], Tq = pa.f[12 + q][idx], fD = pa.f[18 + q][idx];
+        const double Lr = (double)fD.x - G.x, Li = (double)fD.y - G.y;
+        const double Mr = (double)fs.x + Tq.x, Mi = (double)fs.y + Tq.y;
+        lm += w[q] * (Lr * Mr + Li * Mi);
+        mm += w[q] * (Mr * Mr + Mi * Mi);
+      }
+    }
+  }
+  if (pa.op == PH_DYN2) {
+    double s1 = block_sum<256>(lm, red);
+    if (threadIdx.x == 0) pa.partial[2 * blockIdx.x] = s1;
+    double s2 = block_sum<256>(mm, red);
+    if (threadIdx.x == 0) pa.partial[2 * blockIdx.x + 1] = s2;
+  }
+}
+
+// cs2 = LM/MM from the block partials in block order (dynsmag.f90:186).
+static __global__ void dyn_final_kernel(const double* partial, int nblocks, double* c1, double* lm_mm) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double lm = 0.0, mm = 0.0;
+  for (int b = 0; b < nblocks; ++b) { lm += partial[2 * b]; mm += partial[2 * b + 1]; }
+  lm_mm[0] = lm;
+  lm_mm[1] = mm;
+  *c1 = lm / mm;
+}
+
+}  // namespace sc

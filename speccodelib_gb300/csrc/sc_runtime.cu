@@ -1,0 +1,1029 @@
+// Host runtime behind include/specns.h: solver handles, the pass pipelines of
+// one right-hand side and of the time steppers, the reference-signature
+// operators, the seeded initial field and per-kernel CUDA-event timing.
+//
+// The hidden global state of the reference -- FFTW plan handles in module
+// mfftwplan3d (fftwplan.f90:5-15) and the caller-owned work arrays of the
+// solver programs (specdns-forced-omp-ft.f90:81-86) -- lives inside an
+// sc_handle: device fields, twiddle tables, integrating-factor tables and
+// reduction scratch, all allocated once at sc_create.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/specns.h"
+#include "sc_launch.h"
+#include "sc_ops.cuh"
+
+namespace {
+
+thread_local std::string g_err = "no error";
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define SC_CUDA(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(e_ == cudaErrorMemoryAllocation ? SC_ERR_NOMEM : SC_ERR_CUDA,          \
+                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+#define SC_TRY(call)              \
+  do {                            \
+    int r_ = (call);              \
+    if (r_ != SC_OK) return r_;   \
+  } while (0)
+
+int ilog2(int n) {
+  if (n <= 0 || (n & (n - 1))) return -1;
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+}  // namespace
+
+// field slots
+enum Slot { S_V = 0, S_S = 3, S_A = 6, S_W = 9 };
+
+struct sc_handle {
+  sc_params p{};
+  sc::Geom g{};
+  int logx = 0, logy = 0, logz = 0;
+  size_t csize = 8;               // bytes per complex element
+  int nwork = 6;
+  cudaStream_t own = nullptr, stream = nullptr;
+  void* fields = nullptr;         // (S_W + nwork) fields
+  void* tw = nullptr;             // twiddles: table of length L at offset L
+  void* ex = nullptr;
+  void* ey = nullptr;
+  void* ez = nullptr;
+  void* side = nullptr;           // kx = 0 plane, 3 components
+  double* kf_partial = nullptr;
+  int kf_tiles = 0;
+  double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch
+  double* dpart = nullptr;        // reduction partials
+  size_t dpart_len = 0;
+  double* dout = nullptr;         // reduction outputs
+  long long step = 0;             // RK4 steps taken (dynamic-coefficient cadence)
+  int ab2_pass = 0;
+  // profiling
+  bool prof = false;
+  struct Pend { std::string name; cudaEvent_t a, b; };
+  std::vector<Pend> pending;
+  std::vector<cudaEvent_t> pool;
+  std::map<std::string, std::pair<long long, double>> prof_acc;
+};
+
+namespace {
+
+cudaEvent_t ev_get(sc_handle* h) {
+  if (!h->pool.empty()) {
+    cudaEvent_t e = h->pool.back();
+    h->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Launch `f` on h->stream, bracketed by CUDA events when profiling.
+template <class F> int launch(sc_handle* h, const char* name, F&& f) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (h->prof) {
+    a = ev_get(h);
+    cudaEventRecord(a, h->stream);
+  }
+  cudaError_t e = f();
+  if (h->prof) {
+    b = ev_get(h);
+    cudaEventRecord(b, h->stream);
+    h->pending.push_back({name, a, b});
+  }
+  if (e != cudaSuccess) return fail(SC_ERR_CUDA, "launch of %s failed: %s", name, cudaGetErrorString(e));
+  return SC_OK;
+}
+
+int prof_drain(sc_handle* h) {
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  for (auto& p : h->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto& acc = h->prof_acc[p.name];
+    acc.first += 1;
+    acc.second += ms;
+    h->pool.push_back(p.a);
+    h->pool.push_back(p.b);
+  }
+  h->pending.clear();
+  return SC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// precision-templated implementation
+// ---------------------------------------------------------------------------
+template <typename T> struct Impl {
+  using C = sc::C2<T>;
+  using L = sc::Launch<T>;
+
+  static C* F(sc_handle* h, int i) { return reinterpret_cast<C*>(h->fields) + (size_t)i * h->g.field; }
+  static const C* tw(sc_handle* h, int len) { return reinterpret_cast<const C*>(h->tw) + len; }
+
+  static sc::FieldList<T> list(sc_handle* h, std::initializer_list<int> slots) {
+    sc::FieldList<T> fl{};
+    int i = 0;
+    for (int s : slots) fl.f[i++] = F(h, s);
+    return fl;
+  }
+  static sc::FieldList<T> range(sc_handle* h, int first, int n) {
+    sc::FieldList<T> fl{};
+    for (int i = 0; i < n; ++i) fl.f[i] = F(h, first + i);
+    return fl;
+  }
+
+  static int setup_tables(sc_handle* h) {
+    std::vector<C> t(4096);
+    for (int L = 2; L <= 2048; L *= 2)
+      for (int m = 0; m < L; ++m) {
+        const double a = 2.0 * M_PI * (double)m / (double)L;
+        t[L + m].x = (T)std::cos(a);
+        t[L + m].y = (T)(-std::sin(a));
+      }
+    t[0].x = t[0].y = t[1].x = t[1].y = 0;
+    SC_CUDA(cudaMemcpy(h->tw, t.data(), sizeof(C) * 4096, cudaMemcpyHostToDevice));
+    return set_dt(h, h->p.dt);
+  }
+
+  // 1D integrating-factor tables exp(-nu k_d^2 dt/2); E(k) = ex*ey*ez
+  // equals exp(-nu k^2 dt/2) of dns-deform.f90:90.
+  static int set_dt(sc_handle* h, double dt) {
+    h->p.dt = dt;
+    auto tab = [&](int n, int len, bool half) {
+      std::vector<T> v(len, T(0));
+      for (int i = 0; i < len; ++i) {
+        const double k = half ? (double)i : (double)(i < n / 2 ? i : i - n);
+        v[i] = (T)std::exp(-h->p.nu * k * k * dt / 2.0);
+      }
+      return v;
+    };
+    auto ex = tab(h->g.nx, h->g.nxp, true), ey = tab(h->g.ny, h->g.ny, false),
+         ez = tab(h->g.nz, h->g.nz, false);
+    SC_CUDA(cudaMemcpy(h->ex, ex.data(), sizeof(T) * ex.size(), cudaMemcpyHostToDevice));
+    SC_CUDA(cudaMemcpy(h->ey, ey.data(), sizeof(T) * ey.size(), cudaMemcpyHostToDevice));
+    SC_CUDA(cudaMemcpy(h->ez, ez.data(), sizeof(T) * ez.size(), cudaMemcpyHostToDevice));
+    return SC_OK;
+  }
+
+  static double kcut2(sc_handle* h) { return h->p.kcut * h->p.kcut; }
+  static double ktest2(sc_handle* h) {
+    const double kt = h->p.kcut / h->p.delta_ratio;
+    return kt * kt;
+  }
+
+  static sc::StageArgs<T> stage_args(sc_handle* h) {
+    sc::StageArgs<T> st{};
+    for (int c = 0; c < 3; ++c) {
+      st.v[c] = F(h, S_V + c);
+      st.sout[c] = F(h, S_S + c);
+      st.acc[c] = F(h, S_A + c);
+      st.w[c] = F(h, S_A + c);
+      st.v0[c] = F(h, S_S + c);
+    }
+    st.side = reinterpret_cast<C*>(h->side);
+    st.ex = reinterpret_cast<const T*>(h->ex);
+    st.ey = reinterpret_cast<const T*>(h->ey);
+    st.ez = reinterpret_cast<const T*>(h->ez);
+    st.dt = (T)h->p.dt;
+    st.forced = h->p.forced;
+    st.fkmax2 = h->p.fkmax * h->p.fkmax;
+    st.eps = h->p.eps;
+    st.kf_partial = h->kf_partial;
+    st.kf_tiles = h->kf_tiles;
+    st.kcut2 = kcut2(h);
+    st.mask_rhs = h->p.mask_mode == SC_MASK_RHS_AND_STEP;
+    st.symmetrize = 1;
+    st.project = 1;
+    return st;
+  }
+
+  static sc::PlainArgs<T> ypass_args(sc_handle* h, int nf) {
+    sc::PlainArgs<T> pa{};
+    pa.nfields = nf;
+    pa.axis_stride = h->g.nxp;
+    pa.outer_stride = (long long)h->g.ny * h->g.nxp;
+    pa.scale = T(1);
+    return pa;
+  }
+  static sc::PlainArgs<T> zpass_args(sc_handle* h, int nf) {
+    sc::PlainArgs<T> pa{};
+    pa.nfields = nf;
+    pa.axis_stride = (long long)h->g.ny * h->g.nxp;
+    pa.outer_stride = h->g.nxp;
+    pa.scale = T(1);
+    return pa;
+  }
+  static sc::XArgs<T> xargs(sc_handle* h) {
+    sc::XArgs<T> xa{};
+    xa.scale = (T)(1.0 / ((double)h->g.nx * h->g.ny * h->g.nz));
+    xa.c1 = h->dscal;
+    xa.delta2 = h->p.delta * h->p.delta;
+    xa.rows = (long long)h->g.ny * h->g.nz;
+    return xa;
+  }
+
+  // ---- generic transforms of groups of fields (in place) ----
+  // spectral -> packed physical; fields fl[0..nf-1], nf a multiple of 3
+  static int inverse(sc_handle* h, const sc::FieldList<T>& fl, int nf) {
+    auto* g = &h->g;
+    SC_TRY(launch(h, "zpass_inv", [&] { return L::plain(h->logz, true, fl, zpass_args(h, nf), *g, g->ny, tw(h, g->nz), h->stream); }));
+    SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, fl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+    for (int i = 0; i < nf; i += 3) {
+      sc::FieldList<T> sub{};
+      for (int c = 0; c < 3; ++c) sub.f[c] = fl.f[i + c];
+      SC_TRY(launch(h, "xpass_c2r", [&] { return L::xpass(h->logx - 1, sc::XP_C2R3, sub, sub, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+    }
+    return SC_OK;
+  }
+  static int forward(sc_handle* h, const sc::FieldList<T>& fl, int nf) {
+    auto* g = &h->g;
+    for (int i = 0; i < nf; i += 3) {
+      sc::FieldList<T> sub{};
+      for (int c = 0; c < 3; ++c) sub.f[c] = fl.f[i + c];
+      SC_TRY(launch(h, "xpass_r2c", [&] { return L::xpass(h->logx - 1, sc::XP_R2C3, sub, sub, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+    }
+    SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, fl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+    SC_TRY(launch(h, "zpass_fwd", [&] { return L::plain(h->logz, false, fl, zpass_args(h, nf), *g, g->ny, tw(h, g->nz), h->stream); }));
+    return SC_OK;
+  }
+
+  // ---- dynamic procedure: cs2 = <L:M>/<M:M> into dscal[0] (dynsmag.f90:27-194) ----
+  static int dyn_update(sc_handle* h, const C* vin[3]) {
+    auto* g = &h->g;
+    if (h->nwork < 24) return fail(SC_ERR_INVALID, "dynamic procedure needs a dynsmag handle");
+    sc::ZvArgs<T> za{};
+    for (int c = 0; c < 3; ++c) za.v[c] = vin[c];
+    za.ktest2 = ktest2(h);
+    auto w18 = range(h, S_W, 18);
+    SC_TRY(launch(h, "dyn_zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_DYN, za, w18, *g, tw(h, g->nz), h->stream); }));
+    SC_TRY(launch(h, "dyn_ypass", [&] { return L::plain(h->logy, true, w18, ypass_args(h, 18), *g, g->nz, tw(h, g->ny), h->stream); }));
+    for (int i = 0; i < 18; i += 3) {
+      auto sub = range(h, S_W + i, 3);
+      SC_TRY(launch(h, "dyn_xc2r", [&] { return L::xpass(h->logx - 1, sc::XP_C2R3, sub, sub, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+    }
+    sc::PhysArgs<T> pa{};
+    for (int i = 0; i < 24; ++i) pa.f[i] = F(h, S_W + i);
+    pa.c1 = h->dscal;
+    pa.delta2 = h->p.delta * h->p.delta;
+    const double dtest = h->p.delta_ratio * h->p.delta;
+    pa.delta_test2 = dtest * dtest;
+    pa.scale = (T)(1.0 / ((double)g->nx * g->ny * g->nz));
+    const long long rows = (long long)g->ny * g->nz;
+    pa.rows_per_block = (int)std::max<long long>(1, rows / 2048);
+    const int nb = (int)((rows + pa.rows_per_block - 1) / pa.rows_per_block);
+    pa.partial = h->dpart;
+    pa.op = sc::PH_DYN1;
+    SC_TRY(launch(h, "dyn_phys1", [&] { return L::phys(pa, nb, *g, nullptr, nullptr, h->stream); }));
+    // forward of D (18-23) and s (6-11), then test filter + inverse
+    sc::FieldList<T> fw{};
+    for (int i = 0; i < 6; ++i) { fw.f[i] = F(h, S_W + 6 + i); fw.f[6 + i] = F(h, S_W + 18 + i); }
+    SC_TRY(forward(h, fw, 12));
+    {
+      auto pz = zpass_args(h, 12);
+      pz.filter = 1;
+      pz.kmax2 = ktest2(h);
+      SC_TRY(launch(h, "dyn_zfilter", [&] { return L::plain(h->logz, true, fw, pz, *g, g->ny, tw(h, g->nz), h->stream); }));
+      SC_TRY(launch(h, "dyn_ypass", [&] { return L::plain(h->logy, true, fw, ypass_args(h, 12), *g, g->nz, tw(h, g->ny), h->stream); }));
+      for (int i = 0; i < 12; i += 3) {
+        sc::FieldList<T> sub{};
+        for (int c = 0; c < 3; ++c) sub.f[c] = fw.f[i + c];
+        SC_TRY(launch(h, "dyn_xc2r", [&] { return L::xpass(h->logx - 1, sc::XP_C2R3, sub, sub, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      }
+    }
+    pa.op = sc::PH_DYN2;
+    SC_TRY(launch(h, "dyn_phys2", [&] { return L::phys(pa, nb, *g, h->dscal, h->dscal + 1, h->stream); }));
+    return SC_OK;
+  }
+
+  // ---- one right-hand side through the fused passes ----
+  static int rhs_pipeline(sc_handle* h, const C* sin[3], sc::StageArgs<T> st) {
+    auto* g = &h->g;
+    const bool les = h->p.sgs != SC_SGS_NONE;
+    const int nw = les ? 12 : 6, nf = les ? 9 : 3;
+    for (int c = 0; c < 3; ++c) st.sin[c] = sin[c];
+    sc::ZvArgs<T> za{};
+    for (int c = 0; c < 3; ++c) za.v[c] = sin[c];
+    za.fs.enabled = h->p.forced && st.mode != sc::SM_LAMB;
+    za.fs.fkmax2 = h->p.fkmax * h->p.fkmax;
+    za.fs.partial = h->kf_partial;
+    auto wl = range(h, S_W, nw);
+    SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
+    SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, wl, ypass_args(h, nw), *g, g->nz, tw(h, g->ny), h->stream); }));
+    SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, les ? sc::XP_SMAG : sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+    SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, wl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+    SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_stage(h->logz, nf, wl, st, *g, tw(h, g->nz), h->stream); }));
+    if (st.symmetrize && st.mode != sc::SM_LAMB)
+      SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));
+    return SC_OK;
+  }
+
+  static int maybe_dyn(sc_handle* h, const C* sin[3], bool first_stage) {
+    if (h->p.sgs == SC_SGS_DYNSMAG && first_stage && (h->step % h->p.dyn_every) == 0)
+      return dyn_update(h, sin);
+    return SC_OK;
+  }
+
+  static int rk4_step(sc_handle* h) {
+    sc::StageArgs<T> st = stage_args(h);
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    const C* sin[3] = {F(h, S_S), F(h, S_S + 1), F(h, S_S + 2)};
+    SC_TRY(maybe_dyn(h, vin, true));
+    st.mode = sc::SM_RK1;
+    SC_TRY(rhs_pipeline(h, vin, st));
+    st.mode = sc::SM_RK2;
+    SC_TRY(rhs_pipeline(h, sin, st));
+    st.mode = sc::SM_RK3;
+    SC_TRY(rhs_pipeline(h, sin, st));
+    st.mode = sc::SM_RK4;
+    SC_TRY(rhs_pipeline(h, sin, st));
+    h->step += 1;
+    return SC_OK;
+  }
+
+  static int ab2_pass(sc_handle* h) {
+    sc::StageArgs<T> st = stage_args(h);
+    st.symmetrize = 0;   // specdns-forced-omp-ft.f90:180-221 has no symmetrize
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    if (h->ab2_pass == 0) {
+      // keep v(t=0) for the midpoint restart (the reference's ox,oy,oz)
+      for (int c = 0; c < 3; ++c)
+        SC_CUDA(cudaMemcpyAsync(F(h, S_S + c), F(h, S_V + c), h->csize * h->g.field, cudaMemcpyDeviceToDevice, h->stream));
+      st.mode = sc::SM_AB2_EULER;
+    } else if (h->ab2_pass == 1) {
+      st.mode = sc::SM_AB2_MID;
+    } else {
+      st.mode = sc::SM_AB2;
+    }
+    SC_TRY(maybe_dyn(h, vin, true));
+    SC_TRY(rhs_pipeline(h, vin, st));
+    h->ab2_pass += 1;
+    return SC_OK;
+  }
+
+  static int rhs_now(sc_handle* h) {
+    sc::StageArgs<T> st = stage_args(h);
+    st.mode = sc::SM_RHS;
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    SC_TRY(maybe_dyn(h, vin, true));
+    return rhs_pipeline(h, vin, st);
+  }
+
+  // ---- reductions ----
+  static int diag_run(sc_handle* h, const C* const v[3], int physical, double kmax2, int nshell, double* host_out) {
+    auto* g = &h->g;
+    sc::DiagArgs<T> da{};
+    for (int c = 0; c < 3; ++c) da.v[c] = v[c];
+    da.physical = physical;
+    da.kmax2 = kmax2;
+    da.nshell = nshell;
+    const long long rows = (long long)g->ny * g->nz;
+    da.rows_per_block = (int)std::max<long long>(1, rows / 1024);
+    da.nblocks = (int)((rows + da.rows_per_block - 1) / da.rows_per_block);
+    if ((size_t)da.nblocks * (sc::DQ_N + nshell) > h->dpart_len)
+      return fail(SC_ERR_INVALID, "reduction scratch too small");
+    da.partial = h->dpart;
+    da.out = h->dout;
+    SC_TRY(launch(h, "diag", [&] { return L::diag(da, *g, h->stream); }));
+    if (host_out) {
+      SC_CUDA(cudaMemcpyAsync(host_out, h->dout, sizeof(double) * (sc::DQ_N + nshell), cudaMemcpyDeviceToHost, h->stream));
+      SC_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return SC_OK;
+  }
+
+  static int specop(sc_handle* h, sc::SpecOpArgs<T> oa) {
+    return launch(h, "specop", [&] { return L::specop(oa, h->g, h->stream); });
+  }
+
+  static int symmetrize_fields(sc_handle* h, std::initializer_list<int> slots) {
+    sc::SpecOpArgs<T> oa{};
+    int n = 0;
+    for (int s : slots) oa.f[n++] = F(h, s);
+    oa.nfields = n;
+    oa.op = sc::OP_ZERO_PLANES;
+    SC_TRY(specop(h, oa));
+    oa.op = sc::OP_KX0_COPY;
+    return specop(h, oa);
+  }
+
+  static int diagnostics(sc_handle* h, sc_diag* d, double* eks) {
+    const int ns = h->g.nx / 2;
+    std::vector<double> out(sc::DQ_N + ns), outp(sc::DQ_N);
+    const C* v[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    SC_TRY(diag_run(h, v, 0, -1.0, ns, out.data()));
+    // max |u| from the physical field (copy, inverse transform, reduce)
+    for (int c = 0; c < 3; ++c)
+      SC_CUDA(cudaMemcpyAsync(F(h, S_W + c), F(h, S_V + c), h->csize * h->g.field, cudaMemcpyDeviceToDevice, h->stream));
+    SC_TRY(inverse(h, range(h, S_W, 3), 3));
+    const C* u[3] = {F(h, S_W), F(h, S_W + 1), F(h, S_W + 2)};
+    SC_TRY(diag_run(h, u, 1, -1.0, 0, outp.data()));
+    double sc3[3];
+    SC_CUDA(cudaMemcpy(sc3, h->dscal, sizeof sc3, cudaMemcpyDeviceToHost));
+    if (d) {
+      d->energy = out[sc::DQ_ENERGY];
+      d->enstrophy = out[sc::DQ_K2Q];
+      d->dissipation = 2.0 * h->p.nu * out[sc::DQ_K2Q];
+      d->max_div = out[sc::DQ_MAXDIV];
+      d->max_u = std::sqrt(outp[sc::DQ_MAXU2]);
+      d->nonfinite = out[sc::DQ_NONFINITE] + outp[sc::DQ_NONFINITE];
+      d->cs2 = sc3[0];
+      d->lm = sc3[1];
+      d->mm = sc3[2];
+    }
+    if (eks) std::memcpy(eks, out.data() + sc::DQ_N, sizeof(double) * ns);
+    if (out[sc::DQ_NONFINITE] + outp[sc::DQ_NONFINITE] > 0)
+      return fail(SC_ERR_NONFINITE, "state holds %.0f non-finite values",
+                  out[sc::DQ_NONFINITE] + outp[sc::DQ_NONFINITE]);
+    return SC_OK;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// host <-> device copies between the reference layout (pitch nx/2+1) and the
+// internal padded layout
+// ---------------------------------------------------------------------------
+int copy_in(sc_handle* h, void* dst, const void* src) {
+  const size_t w = h->csize * h->g.nxh;
+  SC_CUDA(cudaMemcpy2DAsync(dst, h->csize * h->g.nxp, src, w, w, (size_t)h->g.ny * h->g.nz,
+                            cudaMemcpyDefault, h->stream));
+  return SC_OK;
+}
+int copy_out(sc_handle* h, void* dst, const void* src) {
+  const size_t w = h->csize * h->g.nxh;
+  SC_CUDA(cudaMemcpy2DAsync(dst, w, src, h->csize * h->g.nxp, w, (size_t)h->g.ny * h->g.nz,
+                            cudaMemcpyDefault, h->stream));
+  return SC_OK;
+}
+void* slot(sc_handle* h, int i) {
+  return static_cast<char*>(h->fields) + (size_t)i * h->g.field * h->csize;
+}
+
+// ---------------------------------------------------------------------------
+// Numerical Recipes ran1 + Box-Muller (initialize.f90:507-548), draw order of
+// initialize.f90:305-326, for the seeded initial field.
+// ---------------------------------------------------------------------------
+struct Ran1 {
+  int32_t idum, iy = 0, iv[32] = {0};
+  explicit Ran1(int32_t seed) : idum(seed) {}
+  static int32_t lcg(int32_t x) {  // Park-Miller minimal standard, Schrage's method
+    const int32_t k = x / 127773;
+    x = 16807 * (x - k * 127773) - 2836 * k;
+    return x < 0 ? x + 2147483647 : x;
+  }
+  double next() {
+    if (idum <= 0 || iy == 0) {
+      int32_t x = -idum;   // max(-idum, 1)
+      if (x < 1) x = 1;
+      for (int j = 40; j >= 1; --j) {
+        x = lcg(x);
+        if (j <= 32) iv[j - 1] = x;
+      }
+      iy = iv[0];
+      idum = x;
+    }
+    idum = lcg(idum);
+    const int j = iy / (1 + (2147483647 - 1) / 32);
+    iy = iv[j];
+    iv[j] = idum;
+    const double r = (1.0 / 2147483647.0) * (double)iy;
+    return r < 1.0 - 1.2e-7 ? r : 1.0 - 1.2e-7;
+  }
+};
+
+template <typename T>
+int init_field(sc_handle* h, int seed, int kind, double akp, double u0, double kmin, double kmax) {
+  using C = sc::C2<T>;
+  using I = Impl<T>;
+  const int nxh = h->g.nxh, ny = h->g.ny, nz = h->g.nz;
+  const size_t plane = (size_t)nxh * ny * nz;
+  C* host = nullptr;
+  SC_CUDA(cudaMallocHost(&host, sizeof(C) * 3 * plane));
+  std::unique_ptr<C, decltype(&cudaFreeHost)> guard(host, &cudaFreeHost);
+  Ran1 rng(seed);
+  const double pi_ref = 3.1415926536;
+  for (int kk = 0; kk < nz; ++kk)
+    for (int jj = 0; jj < ny; ++jj)
+      for (int ii = 0; ii < nxh; ++ii) {
+        const size_t idx = ((size_t)kk * ny + jj) * nxh + ii;
+        for (int c = 0; c < 3; ++c) {
+          const double t1 = rng.next();
+          const double t2 = 2.0 * pi_ref * rng.next();
+          const double a = std::sqrt(-2.0 * std::log(t1));
+          host[c * plane + idx].x = (T)(a * std::cos(t2) / std::sqrt(2.0));
+          host[c * plane + idx].y = (T)(a * std::sin(t2) / std::sqrt(2.0));
+        }
+      }
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_V + c), host + c * plane));
+  sc::SpecOpArgs<T> oa{};
+  for (int c = 0; c < 3; ++c) oa.f[c] = I::F(h, S_V + c);
+  oa.nfields = 3;
+  oa.op = sc::OP_INIT_SHAPE;                         // initialize.f90:328-332
+  SC_TRY(I::specop(h, oa));
+  SC_TRY(I::symmetrize_fields(h, {S_V, S_V + 1, S_V + 2}));   // :337-339
+  oa.op = sc::OP_MASK;                               // :341-345
+  oa.kcut2 = h->p.kcut * h->p.kcut;
+  SC_TRY(I::specop(h, oa));
+  oa.op = sc::OP_INIT_AMP;                           // :349-360
+  oa.akp = akp;
+  oa.u0 = u0;
+  oa.kmin = kmin;
+  oa.kmax = kmax;
+  oa.spectrum_kind = kind;
+  SC_TRY(I::specop(h, oa));
+  const C* v[3] = {I::F(h, S_V), I::F(h, S_V + 1), I::F(h, S_V + 2)};
+  SC_TRY(I::diag_run(h, v, 0, -1.0, 0, nullptr));   // energy -> dout[0]
+  oa.op = sc::OP_SCALE;                              // :362-368
+  oa.a = 1.5 * u0 * u0;
+  oa.dscal = h->dout + sc::DQ_ENERGY;
+  SC_TRY(I::specop(h, oa));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  h->step = 0;
+  h->ab2_pass = 0;
+  return SC_OK;
+}
+
+int validate(const sc_params* p) {
+  if (!p) return fail(SC_ERR_INVALID, "null params");
+  if (p->precision != SC_FP32 && p->precision != SC_FP64) return fail(SC_ERR_INVALID, "precision must be SC_FP32 or SC_FP64");
+  for (int n : {p->nx, p->ny, p->nz}) {
+    const int l = ilog2(n);
+    if (l < 3 || l > 10) return fail(SC_ERR_INVALID, "grid size %d: each of nx, ny, nz must be a power of two in [8, 1024]", n);
+  }
+  if (!(p->dt > 0) || !(p->nu >= 0)) return fail(SC_ERR_INVALID, "need dt > 0 and nu >= 0");
+  if (p->sgs < SC_SGS_NONE || p->sgs > SC_SGS_DYNSMAG) return fail(SC_ERR_INVALID, "bad sgs model %d", p->sgs);
+  if (p->forced && !(p->fkmax > 0)) return fail(SC_ERR_INVALID, "forcing needs fkmax > 0");
+  return SC_OK;
+}
+
+template <typename T> int impl_dispatch_tile(int logz) {
+  return (sizeof(T) == 4 && logz < 9) ? 16 : 8;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* sc_last_error(void) { return g_err.c_str(); }
+
+int sc_default_params(sc_params* p, int n, int precision) {
+  if (!p) return fail(SC_ERR_INVALID, "null params");
+  std::memset(p, 0, sizeof *p);
+  p->nx = p->ny = p->nz = n;
+  p->precision = precision;
+  p->nu = 0.01;
+  p->dt = 2e-3;
+  p->forced = 1;
+  p->eps = 0.1;
+  p->fkmax = 2.5;
+  p->kcut = 0.0;
+  p->sgs = SC_SGS_NONE;
+  p->c1 = 0.026;
+  p->delta = 0.0;
+  p->delta_ratio = 2.0;
+  p->dyn_every = 10;
+  p->mask_mode = SC_MASK_AFTER_STEP;
+  return SC_OK;
+}
+
+int sc_create(const sc_params* pin, sc_handle** out) {
+  if (!out) return fail(SC_ERR_INVALID, "null output handle pointer");
+  *out = nullptr;
+  SC_TRY(validate(pin));
+  std::unique_ptr<sc_handle> h(new sc_handle());
+  h->p = *pin;
+  auto& p = h->p;
+  if (p.kcut <= 0) p.kcut = 2.0 * (p.nx / 2) / 3.0;
+  if (p.delta <= 0) p.delta = 3.1415926536 / p.kcut;
+  if (p.delta_ratio <= 0) p.delta_ratio = 2.0;
+  if (p.dyn_every <= 0) p.dyn_every = 10;
+  h->logx = ilog2(p.nx);
+  h->logy = ilog2(p.ny);
+  h->logz = ilog2(p.nz);
+  auto& g = h->g;
+  g.nx = p.nx;
+  g.ny = p.ny;
+  g.nz = p.nz;
+  g.nxh = p.nx / 2 + 1;
+  g.nxp = (g.nxh + 15) / 16 * 16;
+  g.field = (long long)g.nz * g.ny * g.nxp;
+  h->csize = p.precision == SC_FP32 ? 8 : 16;
+  h->nwork = p.sgs == SC_SGS_NONE ? 6 : (p.sgs == SC_SGS_SMAG ? 12 : 24);
+  const int ptile = p.precision == SC_FP32 ? impl_dispatch_tile<float>(h->logz) : impl_dispatch_tile<double>(h->logz);
+  const int ntiles = (g.nxh + ptile - 1) / ptile;
+  h->kf_tiles = 0;
+  while (h->kf_tiles < ntiles && (double)(h->kf_tiles * ptile) * (h->kf_tiles * ptile) < p.fkmax * p.fkmax) h->kf_tiles++;
+  SC_CUDA(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
+  h->stream = h->own;
+  const size_t nfields = S_W + h->nwork;
+  SC_CUDA(cudaMalloc(&h->fields, nfields * g.field * h->csize));
+  SC_CUDA(cudaMemsetAsync(h->fields, 0, nfields * g.field * h->csize, h->stream));
+  SC_CUDA(cudaMalloc(&h->tw, 4096 * h->csize));
+  const size_t rsz = h->csize / 2;
+  SC_CUDA(cudaMalloc(&h->ex, g.nxp * rsz));
+  SC_CUDA(cudaMalloc(&h->ey, g.ny * rsz));
+  SC_CUDA(cudaMalloc(&h->ez, g.nz * rsz));
+  SC_CUDA(cudaMalloc(&h->side, 3 * (size_t)g.ny * g.nz * h->csize));
+  SC_CUDA(cudaMalloc(&h->kf_partial, sizeof(double) * (size_t)ntiles * g.ny));
+  SC_CUDA(cudaMalloc(&h->dscal, sizeof(double) * 8));
+  h->dpart_len = (size_t)1024 * (sc::DQ_N + g.nx / 2) + 2 * 4096;
+  SC_CUDA(cudaMalloc(&h->dpart, sizeof(double) * h->dpart_len));
+  SC_CUDA(cudaMalloc(&h->dout, sizeof(double) * (sc::DQ_N + g.nx / 2)));
+  double c0[8] = {p.c1, 0, 0, 0, 0, 0, 0, 0};
+  SC_CUDA(cudaMemcpy(h->dscal, c0, sizeof c0, cudaMemcpyHostToDevice));
+  if (p.precision == SC_FP32) SC_TRY(Impl<float>::setup_tables(h.get()));
+  else SC_TRY(Impl<double>::setup_tables(h.get()));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  *out = h.release();
+  return SC_OK;
+}
+
+int sc_destroy(sc_handle* h) {
+  if (!h) return SC_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& pd : h->pending) { cudaEventDestroy(pd.a); cudaEventDestroy(pd.b); }
+  for (auto e : h->pool) cudaEventDestroy(e);
+  cudaFree(h->fields);
+  cudaFree(h->tw);
+  cudaFree(h->ex);
+  cudaFree(h->ey);
+  cudaFree(h->ez);
+  cudaFree(h->side);
+  cudaFree(h->kf_partial);
+  cudaFree(h->dscal);
+  cudaFree(h->dpart);
+  cudaFree(h->dout);
+  if (h->own) cudaStreamDestroy(h->own);
+  delete h;
+  return SC_OK;
+}
+
+int sc_set_stream(sc_handle* h, void* stream) {
+  if (!h) return fail(SC_ERR_INVALID, "null handle");
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own;
+  return SC_OK;
+}
+
+int sc_set_dt(sc_handle* h, double dt) {
+  if (!h || !(dt > 0)) return fail(SC_ERR_INVALID, "need a handle and dt > 0");
+  return h->p.precision == SC_FP32 ? Impl<float>::set_dt(h, dt) : Impl<double>::set_dt(h, dt);
+}
+
+int sc_set_state(sc_handle* h, const void* vx, const void* vy, const void* vz) {
+  if (!h || !vx || !vy || !vz) return fail(SC_ERR_INVALID, "null argument");
+  const void* v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_V + c), v[c]));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  h->step = 0;
+  h->ab2_pass = 0;
+  return SC_OK;
+}
+
+int sc_get_state(sc_handle* h, void* vx, void* vy, void* vz) {
+  if (!h || !vx || !vy || !vz) return fail(SC_ERR_INVALID, "null argument");
+  void* v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_out(h, v[c], slot(h, S_V + c)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+int sc_set_state_device(sc_handle* h, const void* vx, const void* vy, const void* vz) {
+  return sc_set_state(h, vx, vy, vz);   // cudaMemcpyDefault resolves device pointers
+}
+int sc_get_state_device(sc_handle* h, void* vx, void* vy, void* vz) {
+  return sc_get_state(h, vx, vy, vz);
+}
+
+int sc_init_field(sc_handle* h, int seed, int kind, double akp, double u0, double kmin, double kmax) {
+  if (!h) return fail(SC_ERR_INVALID, "null handle");
+  if (kind != 0 && kind != 1) return fail(SC_ERR_INVALID, "init kind must be 0 or 1");
+  return h->p.precision == SC_FP32 ? init_field<float>(h, seed, kind, akp, u0, kmin, kmax)
+                                   : init_field<double>(h, seed, kind, akp, u0, kmin, kmax);
+}
+
+int sc_rhs(sc_handle* h, void* wx, void* wy, void* wz) {
+  if (!h || !wx || !wy || !wz) return fail(SC_ERR_INVALID, "null argument");
+  SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rhs_now(h) : Impl<double>::rhs_now(h));
+  void* w[3] = {wx, wy, wz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_out(h, w[c], slot(h, S_A + c)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+int sc_rk4_steps(sc_handle* h, int nsteps) {
+  if (!h || nsteps < 0) return fail(SC_ERR_INVALID, "need a handle and nsteps >= 0");
+  for (int i = 0; i < nsteps; ++i)
+    SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rk4_step(h) : Impl<double>::rk4_step(h));
+  SC_CUDA(cudaGetLastError());
+  return SC_OK;
+}
+
+int sc_ab2_steps(sc_handle* h, int npasses) {
+  if (!h || npasses < 0) return fail(SC_ERR_INVALID, "need a handle and npasses >= 0");
+  for (int i = 0; i < npasses; ++i)
+    SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2_pass(h) : Impl<double>::ab2_pass(h));
+  return SC_OK;
+}
+
+int sc_diagnostics(sc_handle* h, sc_diag* d, double* eks) {
+  if (!h) return fail(SC_ERR_INVALID, "null handle");
+  return h->p.precision == SC_FP32 ? Impl<float>::diagnostics(h, d, eks) : Impl<double>::diagnostics(h, d, eks);
+}
+
+int sc_profile_enable(sc_handle* h, int on) {
+  if (!h) return fail(SC_ERR_INVALID, "null handle");
+  SC_TRY(prof_drain(h));
+  h->prof = on != 0;
+  h->prof_acc.clear();
+  return SC_OK;
+}
+
+int sc_profile_read(sc_handle* h, const char* name, long long* launches, double* ms) {
+  if (!h || !name) return fail(SC_ERR_INVALID, "null argument");
+  SC_TRY(prof_drain(h));
+  auto it = h->prof_acc.find(name);
+  if (launches) *launches = it == h->prof_acc.end() ? 0 : it->second.first;
+  if (ms) *ms = it == h->prof_acc.end() ? 0.0 : it->second.second;
+  return SC_OK;
+}
+
+int sc_step_bytes(sc_handle* h, double* bytes) {
+  if (!h || !bytes) return fail(SC_ERR_INVALID, "null argument");
+  // field-pass model: P = n_s + 4 n_i + 4 n_f + 12 per RHS, 4 RHS per step,
+  // field F = (nx/2+1) ny nz complex elements.
+  const bool les = h->p.sgs != SC_SGS_NONE;
+  const double ni = les ? 12 : 6, nf = les ? 9 : 3;
+  const double P = 3 + 4 * ni + 4 * nf + 12;
+  const double F = (double)h->g.nxh * h->g.ny * h->g.nz * h->csize;
+  *bytes = 4.0 * P * F;
+  return SC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// reference-signature operators: per-(shape, precision, model) scratch handles
+// ---------------------------------------------------------------------------
+static std::mutex g_scratch_mu;
+static std::map<std::tuple<int, int, int, int, int>, sc_handle*> g_scratch;
+
+static int scratch(int prec, int nx, int ny, int nz, int sgs, sc_handle** out) {
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  auto key = std::make_tuple(prec, nx, ny, nz, sgs);
+  auto it = g_scratch.find(key);
+  if (it != g_scratch.end()) { *out = it->second; return SC_OK; }
+  sc_params p;
+  sc_default_params(&p, nx, prec);
+  p.ny = ny;
+  p.nz = nz;
+  p.forced = 0;
+  p.sgs = sgs;
+  sc_handle* h = nullptr;
+  SC_TRY(sc_create(&p, &h));
+  g_scratch[key] = h;
+  *out = h;
+  return SC_OK;
+}
+
+static int shape_check(int lx1, int ly, int lz, int nx, int ny, int nz) {
+  if (lx1 != nx / 2 + 1 || ly != ny || lz != nz)
+    return fail(SC_ERR_INVALID, "array shape (%d,%d,%d) does not match grid (%d,%d,%d)", lx1, ly, lz, nx, ny, nz);
+  return SC_OK;
+}
+
+}  // extern "C"
+
+template <typename T> static int convec_impl(sc_handle* h, const void* const v[3], const void* const w[3], void* const o[3]) {
+  using I = Impl<T>;
+  auto* g = &h->g;
+  for (int c = 0; c < 3; ++c) {
+    SC_TRY(copy_in(h, slot(h, S_W + c), v[c]));
+    SC_TRY(copy_in(h, slot(h, S_W + 3 + c), w[c]));
+  }
+  auto w6 = I::range(h, S_W, 6);
+  SC_TRY(launch(h, "zpass_inv", [&] { return sc::Launch<T>::plain(h->logz, true, w6, I::zpass_args(h, 6), *g, g->ny, I::tw(h, g->nz), h->stream); }));
+  SC_TRY(launch(h, "ypass_inv", [&] { return sc::Launch<T>::plain(h->logy, true, w6, I::ypass_args(h, 6), *g, g->nz, I::tw(h, g->ny), h->stream); }));
+  SC_TRY(launch(h, "xpass", [&] { return sc::Launch<T>::xpass(h->logx - 1, sc::XP_DNS, w6, w6, *g, I::tw(h, g->nx / 2), I::tw(h, g->nx), I::xargs(h), h->stream); }));
+  SC_TRY(launch(h, "ypass_fwd", [&] { return sc::Launch<T>::plain(h->logy, false, w6, I::ypass_args(h, 3), *g, g->nz, I::tw(h, g->ny), h->stream); }));
+  sc::StageArgs<T> st = I::stage_args(h);
+  st.mode = sc::SM_LAMB;
+  SC_TRY(launch(h, "zfwd", [&] { return sc::Launch<T>::zfwd_stage(h->logz, 3, w6, st, *g, I::tw(h, g->nz), h->stream); }));
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_out(h, o[c], slot(h, S_A + c)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+extern "C" {
+
+int sc_convec_dns(int precision, const void* vx, const void* vy, const void* vz, void* wx, void* wy,
+                  void* wz, int lx1, int ly, int lz, int nx, int ny, int nz) {
+  if (!vx || !vy || !vz || !wx || !wy || !wz) return fail(SC_ERR_INVALID, "null array");
+  SC_TRY(shape_check(lx1, ly, lz, nx, ny, nz));
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, nx, ny, nz, SC_SGS_NONE, &h));
+  const void* v[3] = {vx, vy, vz};
+  const void* w[3] = {wx, wy, wz};
+  void* o[3] = {wx, wy, wz};
+  return precision == SC_FP32 ? convec_impl<float>(h, v, w, o) : convec_impl<double>(h, v, w, o);
+}
+
+}  // extern "C"
+
+template <typename T> static int specop_host(sc_handle* h, int op, int nf, void* const io[], double a, double kc2,
+                                             const void* const extra[3]) {
+  using I = Impl<T>;
+  for (int c = 0; c < nf; ++c) SC_TRY(copy_in(h, slot(h, S_W + c), io[c]));
+  if (extra)
+    for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_W + 3 + c), extra[c]));
+  sc::SpecOpArgs<T> oa{};
+  for (int c = 0; c < nf; ++c) oa.f[c] = I::F(h, S_W + c);
+  for (int c = 0; c < 3; ++c) oa.gsrc[c] = I::F(h, S_W + 3 + c);
+  oa.nfields = nf;
+  oa.a = a;
+  oa.kcut2 = kc2;
+  if (op == sc::OP_ZERO_PLANES) {
+    oa.op = sc::OP_ZERO_PLANES;
+    SC_TRY(I::specop(h, oa));
+    oa.op = sc::OP_KX0_COPY;
+    SC_TRY(I::specop(h, oa));
+  } else if (op == sc::OP_MASK) {   // dealiasing: symmetrize, then mask
+    oa.op = sc::OP_ZERO_PLANES;
+    SC_TRY(I::specop(h, oa));
+    oa.op = sc::OP_KX0_COPY;
+    SC_TRY(I::specop(h, oa));
+    oa.op = sc::OP_MASK;
+    SC_TRY(I::specop(h, oa));
+  } else {
+    oa.op = op;
+    SC_TRY(I::specop(h, oa));
+  }
+  for (int c = 0; c < nf; ++c) SC_TRY(copy_out(h, io[c], slot(h, S_W + c)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+extern "C" {
+
+int sc_projection(int precision, void* vx, void* vy, void* vz, int lx1, int ly, int lz) {
+  if (!vx || !vy || !vz) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  void* io[3] = {vx, vy, vz};
+  return precision == SC_FP32 ? specop_host<float>(h, sc::OP_PROJECT, 3, io, 0, 0, nullptr)
+                              : specop_host<double>(h, sc::OP_PROJECT, 3, io, 0, 0, nullptr);
+}
+
+int sc_symmetrize(int precision, void* c, int lx1, int ly, int lz) {
+  if (!c) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  void* io[1] = {c};
+  return precision == SC_FP32 ? specop_host<float>(h, sc::OP_ZERO_PLANES, 1, io, 0, 0, nullptr)
+                              : specop_host<double>(h, sc::OP_ZERO_PLANES, 1, io, 0, 0, nullptr);
+}
+
+int sc_dealiasing(int precision, void* c, int lx1, int ly, int lz) {
+  if (!c) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  void* io[1] = {c};
+  const double kc2 = (double)ly * ly / 9.0;   // dealiasing.f90:35
+  return precision == SC_FP32 ? specop_host<float>(h, sc::OP_MASK, 1, io, 0, kc2, nullptr)
+                              : specop_host<double>(h, sc::OP_MASK, 1, io, 0, kc2, nullptr);
+}
+
+int sc_force(int precision, void* wx, void* wy, void* wz, const void* vx, const void* vy, const void* vz,
+             int lx1, int ly, int lz, double fkmax, double eps) {
+  if (!wx || !wy || !wz || !vx || !vy || !vz) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  const void* v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_V + c), v[c]));
+  // K_f over the band (force.f90:16-22), FP64
+  double out[sc::DQ_N];
+  int r;
+  if (precision == SC_FP32) {
+    const sc::C2<float>* vv[3] = {Impl<float>::F(h, S_V), Impl<float>::F(h, S_V + 1), Impl<float>::F(h, S_V + 2)};
+    r = Impl<float>::diag_run(h, vv, 0, fkmax * fkmax, 0, out);
+  } else {
+    const sc::C2<double>* vv[3] = {Impl<double>::F(h, S_V), Impl<double>::F(h, S_V + 1), Impl<double>::F(h, S_V + 2)};
+    r = Impl<double>::diag_run(h, vv, 0, fkmax * fkmax, 0, out);
+  }
+  if (r != SC_OK) return r;
+  const double a = eps / (2.0 * out[sc::DQ_ENERGY]);
+  void* io[3] = {wx, wy, wz};
+  return precision == SC_FP32 ? specop_host<float>(h, sc::OP_FORCE_ADD, 3, io, a, fkmax * fkmax, v)
+                              : specop_host<double>(h, sc::OP_FORCE_ADD, 3, io, a, fkmax * fkmax, v);
+}
+
+// tau_ij of the current slots S_V (velocity) with coefficient *dscal.
+}  // extern "C"
+
+template <typename T> static int tau_impl(sc_handle* h, void* const t[6]) {
+  using I = Impl<T>;
+  auto* g = &h->g;
+  sc::StrainArgs<T> sa{};
+  for (int c = 0; c < 3; ++c) sa.v[c] = I::F(h, S_V + c);
+  for (int q = 0; q < 6; ++q) sa.s[q] = I::F(h, S_W + q);
+  SC_TRY(launch(h, "strain", [&] { return sc::Launch<T>::strain(sa, *g, h->stream); }));
+  auto w6 = I::range(h, S_W, 6);
+  SC_TRY(I::inverse(h, w6, 6));
+  sc::PhysArgs<T> pa{};
+  for (int q = 0; q < 6; ++q) pa.f[q] = I::F(h, S_W + q);
+  pa.op = sc::PH_TAU;
+  pa.c1 = h->dscal;
+  pa.delta2 = h->p.delta * h->p.delta;
+  pa.scale = (T)(1.0 / ((double)g->nx * g->ny * g->nz));
+  const long long rows = (long long)g->ny * g->nz;
+  pa.rows_per_block = (int)std::max<long long>(1, rows / 2048);
+  const int nb = (int)((rows + pa.rows_per_block - 1) / pa.rows_per_block);
+  SC_TRY(launch(h, "phys_tau", [&] { return sc::Launch<T>::phys(pa, nb, *g, nullptr, nullptr, h->stream); }));
+  SC_TRY(I::forward(h, w6, 6));
+  for (int q = 0; q < 6; ++q) SC_TRY(copy_out(h, t[q], slot(h, S_W + q)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+extern "C" {
+
+int sc_smag(int precision, const void* vx, const void* vy, const void* vz, void* t11, void* t12, void* t13,
+            void* t22, void* t23, void* t33, int lx1, int ly, int lz, int nx, int ny, int nz, double delta,
+            double c1) {
+  if (!vx || !vy || !vz || !t11 || !t12 || !t13 || !t22 || !t23 || !t33) return fail(SC_ERR_INVALID, "null array");
+  SC_TRY(shape_check(lx1, ly, lz, nx, ny, nz));
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, nx, ny, nz, SC_SGS_SMAG, &h));
+  h->p.delta = delta;
+  const void* v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_V + c), v[c]));
+  SC_CUDA(cudaMemcpyAsync(h->dscal, &c1, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  void* t[6] = {t11, t12, t13, t22, t23, t33};
+  return precision == SC_FP32 ? tau_impl<float>(h, t) : tau_impl<double>(h, t);
+}
+
+int sc_dynsmag(int precision, const void* ux, const void* uy, const void* uz, void* t11, void* t12, void* t13,
+               void* t22, void* t23, void* t33, int lx1, int ly, int lz, int nx, int ny, int nz, double k_test,
+               double delta, double delta_test, double* mm, double* lm, double* cs2, int update) {
+  if (!ux || !uy || !uz || !t11 || !t12 || !t13 || !t22 || !t23 || !t33 || !cs2)
+    return fail(SC_ERR_INVALID, "null argument");
+  SC_TRY(shape_check(lx1, ly, lz, nx, ny, nz));
+  if (!(delta > 0) || !(delta_test > 0) || !(k_test > 0)) return fail(SC_ERR_INVALID, "need delta, delta_test, k_test > 0");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, nx, ny, nz, SC_SGS_DYNSMAG, &h));
+  h->p.delta = delta;
+  h->p.delta_ratio = delta_test / delta;
+  h->p.kcut = k_test * h->p.delta_ratio;   // so that kcut/delta_ratio = k_test
+  const void* v[3] = {ux, uy, uz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_V + c), v[c]));
+  if (update) {
+    int r;
+    if (precision == SC_FP32) {
+      const sc::C2<float>* vv[3] = {Impl<float>::F(h, S_V), Impl<float>::F(h, S_V + 1), Impl<float>::F(h, S_V + 2)};
+      r = Impl<float>::dyn_update(h, vv);
+    } else {
+      const sc::C2<double>* vv[3] = {Impl<double>::F(h, S_V), Impl<double>::F(h, S_V + 1), Impl<double>::F(h, S_V + 2)};
+      r = Impl<double>::dyn_update(h, vv);
+    }
+    if (r != SC_OK) return r;
+    double s3[3];
+    SC_CUDA(cudaMemcpyAsync(s3, h->dscal, sizeof s3, cudaMemcpyDeviceToHost, h->stream));
+    SC_CUDA(cudaStreamSynchronize(h->stream));
+    *cs2 = s3[0];
+    if (lm) *lm = s3[1];
+    if (mm) *mm = s3[2];
+  } else {
+    SC_CUDA(cudaMemcpyAsync(h->dscal, cs2, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  }
+  void* t[6] = {t11, t12, t13, t22, t23, t33};
+  return precision == SC_FP32 ? tau_impl<float>(h, t) : tau_impl<double>(h, t);
+}
+
+}  // extern "C"

@@ -1,0 +1,255 @@
+"""Host-side mirror of the reference's hot-path interface over the C ABI.
+
+The functions here keep the names, argument meaning and in-place behaviour of
+the reference's Fortran subroutines (convec_dns.f90, projection.f90,
+force.f90, symmetrize.f90, dealiasing.f90, smag.f90, dynsmag.f90): arrays are
+NumPy arrays in the reference's half-complex layout -- shape
+``(nz, ny, nx//2 + 1)`` in C order, which is the memory of the Fortran array
+``c(lx1, ly, lz)`` -- of dtype complex64 (FP32 mode) or complex128 (FP64
+mode), and outputs overwrite the reference's ``intent(inout)`` arguments.
+
+`SpectralNS` wraps the handle API (device-resident state, RK4 / AB2 steps,
+diagnostics).  Every call goes through ``libspecns.so``; there is no CPU
+fallback, and a missing library raises at import.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+
+SC_OK = 0
+SC_FP32, SC_FP64 = 0, 1
+SC_SGS_NONE, SC_SGS_SMAG, SC_SGS_DYNSMAG = 0, 1, 2
+SC_MASK_AFTER_STEP, SC_MASK_RHS_AND_STEP = 0, 1
+ERRORS = {1: "SC_ERR_INVALID", 2: "SC_ERR_CUDA", 3: "SC_ERR_NONFINITE",
+          4: "SC_ERR_TIMEOUT", 5: "SC_ERR_NOMEM"}
+
+
+class SpecNSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("precision", C.c_int),
+                ("nu", C.c_double), ("dt", C.c_double), ("forced", C.c_int),
+                ("eps", C.c_double), ("fkmax", C.c_double), ("kcut", C.c_double),
+                ("sgs", C.c_int), ("c1", C.c_double), ("delta", C.c_double),
+                ("delta_ratio", C.c_double), ("dyn_every", C.c_int), ("mask_mode", C.c_int)]
+
+
+class Diag(C.Structure):
+    _fields_ = [("energy", C.c_double), ("enstrophy", C.c_double), ("dissipation", C.c_double),
+                ("max_div", C.c_double), ("max_u", C.c_double), ("nonfinite", C.c_double),
+                ("cs2", C.c_double), ("mm", C.c_double), ("lm", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def lib():
+    return _lib.load()
+
+
+def _check(rc):
+    if rc != SC_OK:
+        raise SpecNSError(rc, lib().sc_last_error().decode())
+
+
+def _prec_of(a):
+    if a.dtype == np.complex64:
+        return SC_FP32
+    if a.dtype == np.complex128:
+        return SC_FP64
+    raise TypeError("arrays must be complex64 (FP32) or complex128 (FP64), got %s" % a.dtype)
+
+
+def _ptr(a, writable=False):
+    if not isinstance(a, np.ndarray) or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous NumPy array in the (nz, ny, nx/2+1) layout")
+    if writable and not a.flags.writeable:
+        raise TypeError("output array is read-only")
+    return C.c_void_p(a.ctypes.data)
+
+
+def _same(*arrs):
+    a0 = arrs[0]
+    for a in arrs[1:]:
+        if a.shape != a0.shape or a.dtype != a0.dtype:
+            raise TypeError("all arrays must share shape and dtype")
+    if a0.ndim != 3:
+        raise TypeError("expected 3D arrays of shape (nz, ny, nx/2+1)")
+    nz, ny, lx1 = a0.shape
+    return _prec_of(a0), lx1, ny, nz
+
+
+# ---------------------------------------------------------------------------
+# reference-signature operators
+# ---------------------------------------------------------------------------
+def convec_dns(vx, vy, vz, wx, wy, wz, nx=None):
+    """convec_dns.f90:1 -- w <- spectral Lamb vector of (v, w); in place."""
+    prec, lx1, ly, lz = _same(vx, vy, vz, wx, wy, wz)
+    nx = nx or 2 * (lx1 - 1)
+    _check(lib().sc_convec_dns(prec, _ptr(vx), _ptr(vy), _ptr(vz), _ptr(wx, True), _ptr(wy, True),
+                               _ptr(wz, True), lx1, ly, lz, nx, ly, lz))
+
+
+def projection(vx, vy, vz):
+    """projection.f90:2 -- v <- v - k (k.v)/k^2; in place."""
+    prec, lx1, ly, lz = _same(vx, vy, vz)
+    _check(lib().sc_projection(prec, _ptr(vx, True), _ptr(vy, True), _ptr(vz, True), lx1, ly, lz))
+
+
+def force(wx, wy, wz, vx, vy, vz, fkmax, eps):
+    """force.f90:3 -- w += eps/(2 K_f) v on k2 < fkmax^2; in place on w."""
+    prec, lx1, ly, lz = _same(wx, wy, wz, vx, vy, vz)
+    _check(lib().sc_force(prec, _ptr(wx, True), _ptr(wy, True), _ptr(wz, True), _ptr(vx), _ptr(vy),
+                          _ptr(vz), lx1, ly, lz, C.c_double(fkmax), C.c_double(eps)))
+
+
+def symmetrize(c):
+    """symmetrize.f90:32 (3D) -- in place."""
+    prec, lx1, ly, lz = _same(c)
+    _check(lib().sc_symmetrize(prec, _ptr(c, True), lx1, ly, lz))
+
+
+def dealiasing(c):
+    """dealiasing.f90:2 -- symmetrize + zero k2 >= ly^2/9; in place."""
+    prec, lx1, ly, lz = _same(c)
+    _check(lib().sc_dealiasing(prec, _ptr(c, True), lx1, ly, lz))
+
+
+def smag(vx, vy, vz, delta, c1=0.026):
+    """smag.f90:1 -- returns [t11, t12, t13, t22, t23, t33] (spectral)."""
+    prec, lx1, ly, lz = _same(vx, vy, vz)
+    t = [np.empty_like(vx) for _ in range(6)]
+    nx = 2 * (lx1 - 1)
+    _check(lib().sc_smag(prec, _ptr(vx), _ptr(vy), _ptr(vz), *[_ptr(a, True) for a in t],
+                         lx1, ly, lz, nx, ly, lz, C.c_double(delta), C.c_double(c1)))
+    return t
+
+
+def dynsmag(ux, uy, uz, k_test, delta, delta_test, update, cs2=0.0):
+    """dynsmag.f90:1 -- returns (t, mm, lm, cs2); t = [t11 .. t33]."""
+    prec, lx1, ly, lz = _same(ux, uy, uz)
+    t = [np.empty_like(ux) for _ in range(6)]
+    nx = 2 * (lx1 - 1)
+    mm, lm, c = C.c_double(0), C.c_double(0), C.c_double(cs2)
+    _check(lib().sc_dynsmag(prec, _ptr(ux), _ptr(uy), _ptr(uz), *[_ptr(a, True) for a in t],
+                            lx1, ly, lz, nx, ly, lz, C.c_double(k_test), C.c_double(delta),
+                            C.c_double(delta_test), C.byref(mm), C.byref(lm), C.byref(c),
+                            1 if update else 0))
+    return t, (mm.value if update else None), (lm.value if update else None), c.value
+
+
+# ---------------------------------------------------------------------------
+# handle API
+# ---------------------------------------------------------------------------
+def default_params(n, precision=SC_FP32, **kw):
+    p = Params()
+    _check(lib().sc_default_params(C.byref(p), n, precision))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise TypeError("unknown parameter %s" % k)
+        setattr(p, k, v)
+    return p
+
+
+class SpectralNS:
+    """One solver instance (device-resident state) -- sc_create / sc_destroy."""
+
+    def __init__(self, params: Params):
+        self.p = params
+        self.h = C.c_void_p()
+        _check(lib().sc_create(C.byref(params), C.byref(self.h)))
+        self.dtype = np.complex64 if params.precision == SC_FP32 else np.complex128
+        self.shape = (params.nz, params.ny, params.nx // 2 + 1)
+
+    def close(self):
+        if self.h:
+            _check(lib().sc_destroy(self.h))
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def empty(self):
+        return np.zeros(self.shape, dtype=self.dtype)
+
+    def _arrs(self, arrs):
+        out = []
+        for a in arrs:
+            a = np.ascontiguousarray(a, dtype=self.dtype)
+            if a.shape != self.shape:
+                raise TypeError("expected shape %s, got %s" % (self.shape, a.shape))
+            out.append(a)
+        return out
+
+    def set_state(self, vx, vy, vz):
+        vx, vy, vz = self._arrs((vx, vy, vz))
+        _check(lib().sc_set_state(self.h, _ptr(vx), _ptr(vy), _ptr(vz)))
+
+    def get_state(self):
+        v = [self.empty() for _ in range(3)]
+        _check(lib().sc_get_state(self.h, *[_ptr(a, True) for a in v]))
+        return tuple(v)
+
+    def set_state_device(self, px, py, pz):
+        _check(lib().sc_set_state_device(self.h, C.c_void_p(px), C.c_void_p(py), C.c_void_p(pz)))
+
+    def get_state_device(self, px, py, pz):
+        _check(lib().sc_get_state_device(self.h, C.c_void_p(px), C.c_void_p(py), C.c_void_p(pz)))
+
+    def init_field(self, seed=1, kind=0, akp=4.0, u0=1.0 / np.sqrt(3.0), kmin=0.0, kmax=0.0):
+        _check(lib().sc_init_field(self.h, seed, kind, C.c_double(akp), C.c_double(u0),
+                                   C.c_double(kmin), C.c_double(kmax)))
+
+    def rhs(self):
+        w = [self.empty() for _ in range(3)]
+        _check(lib().sc_rhs(self.h, *[_ptr(a, True) for a in w]))
+        return tuple(w)
+
+    def rk4_steps(self, n=1):
+        _check(lib().sc_rk4_steps(self.h, n))
+
+    def ab2_steps(self, n=1):
+        _check(lib().sc_ab2_steps(self.h, n))
+
+    def set_dt(self, dt):
+        _check(lib().sc_set_dt(self.h, C.c_double(dt)))
+
+    def set_stream(self, stream_ptr):
+        _check(lib().sc_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def diagnostics(self):
+        d = Diag()
+        eks = np.zeros(self.p.nx // 2, dtype=np.float64)
+        _check(lib().sc_diagnostics(self.h, C.byref(d), eks.ctypes.data_as(C.c_void_p)))
+        return d.as_dict(), eks
+
+    def profile_enable(self, on=True):
+        _check(lib().sc_profile_enable(self.h, 1 if on else 0))
+
+    def profile_read(self, name):
+        n, ms = C.c_longlong(0), C.c_double(0)
+        _check(lib().sc_profile_read(self.h, name.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def step_bytes(self):
+        b = C.c_double(0)
+        _check(lib().sc_step_bytes(self.h, C.byref(b)))
+        return b.value

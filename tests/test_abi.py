@@ -1,0 +1,32 @@
+"""The C-ABI library loads and exports every symbol its headers declare (no GPU)."""
+import ctypes
+import glob
+import os
+
+from speccodelib_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol(specns_lib):
+    declared = _lib.declared_symbols(os.path.join(ROOT, "include", "specns.h"))
+    assert len(declared) >= 20
+    missing = [n for n in declared if not hasattr(specns_lib, n)]
+    assert missing == []
+
+
+def test_every_declared_symbol_has_a_binding():
+    declared = _lib.declared_symbols(os.path.join(ROOT, "include", "specns.h"))
+    assert sorted(declared) == sorted(_lib.SIGNATURES)
+
+
+def test_default_params_and_errors_without_gpu(specns_lib):
+    import speccodelib_gb300 as s
+    p = s.default_params(64, s.SC_FP64)
+    assert (p.nx, p.ny, p.nz) == (64, 64, 64)
+    assert p.nu == 0.01 and p.dt == 2e-3 and p.eps == 0.1 and p.fkmax == 2.5
+    bad = s.default_params(48)          # not a power of two -> SC_ERR_INVALID before any CUDA call
+    h = ctypes.c_void_p()
+    rc = specns_lib.sc_create(ctypes.byref(bad), ctypes.byref(h))
+    assert rc == 1 and b"power of two" in specns_lib.sc_last_error()
+    assert not h.value

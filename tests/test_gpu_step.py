@@ -1,0 +1,153 @@
+"""GPU parity of the right-hand side, the RK4 / AB2 steppers, the seeded
+initial field and the FP64 diagnostics against the FP64 oracle.
+
+Parity targets: FP64 mode relative L2 <= 1e-12 after 1 and 10 steps; FP32
+bulk mode <= 1e-5 against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import speccodelib_gb300 as S
+from oracle import spectral_ref as R
+from _util import hermitian_fields, rel_l2, solenoidal_init
+
+pytestmark = pytest.mark.gpu
+
+PRECS = [S.SC_FP64, S.SC_FP32]
+TOL = {S.SC_FP64: 1e-12, S.SC_FP32: 1e-5}
+
+
+def handle(n, prec, **kw):
+    p = S.default_params(n, prec, **kw)
+    return S.SpectralNS(p)
+
+
+def oracle_grid(n, **kw):
+    return R.Grid(R.Params(nx=n, **kw))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [16, 32])
+def test_init_field_matches_oracle(specns_lib, prec, n):
+    ref = solenoidal_init(n)
+    with handle(n, prec) as h:
+        h.init_field(seed=1, akp=4.0, u0=1 / np.sqrt(3))
+        v = h.get_state()
+    assert rel_l2(v, ref) < (1e-13 if prec == S.SC_FP64 else 1e-6)
+    assert abs(R.energy(v) - 0.5) < (1e-13 if prec == S.SC_FP64 else 1e-6)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [16, 32])
+def test_rhs_matches_ratesdudt(specns_lib, prec, n):
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3)
+    ref = R.ratesdudt(v, g)
+    with handle(n, prec) as h:
+        h.set_state(*v)
+        w = h.rhs()
+    assert rel_l2(w, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_rhs_on_unmasked_hermitian_input(specns_lib, prec):
+    """Stage inputs carry modes above the 2/3 cut; the RHS must too."""
+    n = 16
+    v = hermitian_fields((n, n, n), 21)
+    g = oracle_grid(n)
+    ref = R.ratesdudt(v, g)
+    with handle(n, prec) as h:
+        h.set_state(*v)
+        w = h.rhs()
+    assert rel_l2(w, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n,steps", [(16, 1), (16, 10), (32, 1), (32, 10), (64, 1)])
+def test_rk4_matches_oracle(specns_lib, prec, n, steps):
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3)
+    ref = R.rk4_run(v, g, steps)
+    with handle(n, prec) as h:
+        h.set_state(*v)
+        h.rk4_steps(steps)
+        out = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_rk4_non_cubic_and_unforced(specns_lib, prec):
+    nx, ny, nz = 32, 16, 64
+    p = S.default_params(nx, prec, ny=ny, nz=nz, forced=0, nu=0.02)
+    v = hermitian_fields((nx, ny, nz), 3, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.02, forced=False))
+    ref = R.rk4_run(tuple(v), g, 3)
+    with S.SpectralNS(p) as h:
+        h.set_state(*v)
+        h.rk4_steps(3)
+        out = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_rk4_mask_rhs_and_step(specns_lib, prec):
+    n = 32
+    v = solenoidal_init(n)
+    g = oracle_grid(n, mask="rhs_and_step")
+    ref = R.rk4_run(v, g, 2)
+    with handle(n, prec, mask_mode=S.SC_MASK_RHS_AND_STEP) as h:
+        h.set_state(*v)
+        h.rk4_steps(2)
+        out = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_roberts_flow_decays_exactly(specns_lib, prec):
+    """Beltrami flow: zero Lamb vector, so IF-RK4 reproduces exp(-2 nu t)."""
+    n = 32
+    x = np.arange(n) * 2 * np.pi / n
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    u = [np.sin(X) * np.cos(Y), -np.cos(X) * np.sin(Y), np.sqrt(2) * np.sin(X) * np.sin(Y)]
+    v = [R.r2c(a) / n ** 3 for a in u]
+    with handle(n, prec, forced=0, nu=0.05, dt=1e-2) as h:
+        h.set_state(*v)
+        h.rk4_steps(10)
+        out = h.get_state()
+    ref = [a * np.exp(-2 * 0.05 * 0.1) for a in v]
+    assert rel_l2(out, ref) < (1e-13 if prec == S.SC_FP64 else 1e-6)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_diagnostics(specns_lib, prec):
+    n = 32
+    v = solenoidal_init(n)
+    _, _, _, k2 = R.wavenumber(n, n, n)
+    kx, ky, kz, _ = R.wavenumber(n, n, n)
+    with handle(n, prec) as h:
+        h.set_state(*v)
+        d, eks = h.diagnostics()
+    tol = 1e-12 if prec == S.SC_FP64 else 1e-6
+    assert abs(d["energy"] - R.energy(v)) < tol * R.energy(v)
+    assert abs(d["dissipation"] - R.dissipation(v, k2, 0.01)) < tol * R.dissipation(v, k2, 0.01)
+    ref_eks = R.spectrum(v, k2, n)
+    assert np.max(np.abs(eks - ref_eks)) < tol * np.max(ref_eks)
+    assert d["max_div"] < (1e-12 if prec == S.SC_FP64 else 1e-5)
+    mu = R.max_velocity(v, n)
+    assert abs(d["max_u"] - mu) < (1e-12 if prec == S.SC_FP64 else 1e-5) * mu
+    assert d["nonfinite"] == 0
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_ab2_matches_oracle(specns_lib, prec):
+    n = 32
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3)
+    ref, _ = R.ab2_run(v, g, 6)
+    with handle(n, prec) as h:
+        h.set_state(*v)
+        h.ab2_steps(6)
+        out = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
