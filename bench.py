@@ -1,0 +1,358 @@
+"""Benchmark: integrating-factor RK4 steps/s of the forced 512^3 DNS on GB300.
+
+Workload (the reference's forced-DNS configuration at 512^3): incompressible
+Navier-Stokes in rotational form on [0, 2 pi]^3, 2/3 dealiasing, constant-power
+forcing eps = 0.1 on k2 < 2.5^2, nu = 1.5e-3, dt = 5e-4, initial field seeded
+by ran1 (seed 1) with E(k) ~ k^4 exp(-2 (k/4)^2) and energy 0.5.  One "step"
+is one full IF-RK4 step (4 right-hand sides).  The headline arm is the FP32-bulk
+mode; the plain-FP64 mode is timed beside it.
+
+`value`: steps/s with the state resident in HBM (CUDA events on the launch
+stream).  `e2e`: steps/s through the C ABI with host buffers, each step
+uploading the state from pinned host memory, stepping and downloading it.
+Every field (539 MB in FP32) is larger than L2 (129 MB), so no flush is
+needed between steps.
+
+`--impl reference` times the reference algorithm on the host cores instead:
+the FP64 NumPy/SciPy restatement of the reference (the reference's Fortran +
+FFTW sources cannot be compiled here), one right-hand side of the 512^3 step
+per sample (a quarter of an RK4 step), reported as steps/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 512
+NU, DT, EPS, FKMAX = 1.5e-3, 5e-4, 0.1, 2.5
+AKP, U0, SEED = 4.0, 1.0 / 3.0 ** 0.5, 1
+METRIC = "RK4 steps/s, 512^3 forced DNS (FP32 bulk; plain FP64 alongside)"
+UNIT = "steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler over the timed region (SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows)}
+
+
+# algorithmic bytes per launch, in fields F = (nx/2+1) ny nz complex elements
+# (exact reads + writes of each pass; RK stage average for zfwd)
+KERNEL_FIELDS = {"zinv": 9.0, "ypass_inv": 12.0, "xpass": 9.0, "ypass_fwd": 6.0,
+                 "zfwd": 13.5, "fixup": 0.0}
+
+
+def traffic_from_profiles(kernel):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic_512.txt")
+    try:
+        for line in open(path):
+            m = re.match(r"\s*%s\s+([0-9.eE+]+)\s*$" % re.escape(kernel), line)
+            if m:
+                return float(m.group(1))
+    except OSError:
+        pass
+    return None
+
+
+def cpu_reference_rhs(n, workers):
+    """Time one right-hand side of the oracle at n^3 (FP64) on the host."""
+    os.environ["SC_ORACLE_WORKERS"] = str(workers)
+    from oracle import spectral_ref as R
+    R.WORKERS = workers
+    import numpy as np
+    rng = np.random.default_rng(1)
+    v = []
+    for _ in range(3):
+        a = (rng.standard_normal((n, n, n // 2 + 1)) + 1j * rng.standard_normal((n, n, n // 2 + 1))) * 1e-3
+        v.append(a)
+    g = R.Grid(R.Params(nx=n, nu=NU, dt=DT))
+    t0 = time.perf_counter()
+    R.ratesdudt(tuple(v), g)
+    return time.perf_counter() - t0
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    workers = len(os.sched_getaffinity(0))
+    n = a.n
+    for _ in range(max(a.warmup, 0)):
+        cpu_reference_rhs(n, workers)
+    ts = [cpu_reference_rhs(n, workers) for _ in range(a.steps)]
+    t_rhs = sum(ts) / len(ts)
+    v = 1.0 / (4.0 * t_rhs)
+    sample = ("one right-hand side (1/4 of an RK4 step) of the %d^3 step per sample, FP64 "
+              "NumPy/scipy.fft restatement, workers=%d" % (n, workers))
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": 4000.0 * t_rhs, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+           "impl": "reference",
+           "config": {"workload": "forced DNS %d^3 IF-RK4 (one RHS per sample)" % n, "grid": n},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+    import speccodelib_gb300 as S
+    from speccodelib_gb300 import specns as SP
+
+    rank, world, local = dist_env()
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    SP._check(SP.lib().sc_set_device(local))
+    n = a.n
+    stream = torch.cuda.Stream()
+
+    def make(prec):
+        p = S.default_params(n, prec, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX)
+        h = S.SpectralNS(p)
+        h.set_stream(stream.cuda_stream)
+        h.init_field(seed=SEED, akp=AKP, u0=U0)
+        return h
+
+    def barrier():
+        if dist:
+            td.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        return float(t.item())
+
+    def time_steps(h, k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        h.rk4_steps(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return e0.elapsed_time(e1)
+
+    # ---- FP32 bulk: the headline ----
+    h = make(S.SC_FP32)
+    init32 = h.get_state()
+    h.rk4_steps(a.warmup)
+    torch.cuda.synchronize()
+    h.profile_enable(True)
+    with Clocks(local) as ck:
+        ms = time_steps(h, a.steps)
+    clocks = ck.summary()
+    ms = max_over_ranks(ms)
+    prof = {}
+    launches = 0
+    for name in ["zinv", "ypass_inv", "xpass", "ypass_fwd", "zfwd", "fixup"]:
+        cnt, tot = h.profile_read(name)
+        prof[name] = (cnt, tot)
+        launches += cnt
+    h.profile_enable(False)
+    value = world * a.steps / (ms / 1e3)
+    ms_step = ms / a.steps
+
+    F = (n // 2 + 1) * n * n * 8.0
+    dom = max(prof, key=lambda k: prof[k][1])
+    cnt, tot = prof[dom]
+    avg_ms = tot / max(cnt, 1)
+    alg = KERNEL_FIELDS[dom] * F
+    hbm, peak_kind = peaks()
+    achieved = alg / (avg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": peak_kind,
+                "traffic": traffic_from_profiles(dom),
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms}
+    step_bytes = h.step_bytes()
+    tot_all = max(sum(x[1] for x in prof.values()), 1e-9)
+    kernels = {k: {"launches": c, "ms_total": t, "avg_ms": t / max(c, 1), "share": t / tot_all,
+                   "achieved_gbs": (KERNEL_FIELDS[k] * F / (t / c / 1e3) / 1e9)
+                   if c and KERNEL_FIELDS[k] else None}
+               for k, (c, t) in prof.items()}
+
+    # ---- e2e through the C ABI with host buffers ----
+    e2e = None
+    if not a.no_e2e:
+        shape = (n, n, n // 2 + 1)
+        host = [torch.empty(shape, dtype=torch.complex64, pin_memory=True) for _ in range(3)]
+        hv = [x.numpy() for x in host]
+        for dst, src in zip(hv, init32):
+            dst[...] = src
+        ke = min(a.steps, 5)
+        SP._check(SP.lib().sc_set_state(h.h, *[SP._ptr(x) for x in hv]))
+        h.rk4_steps(1)
+        SP._check(SP.lib().sc_get_state(h.h, *[SP._ptr(x, True) for x in hv]))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            SP._check(SP.lib().sc_set_state(h.h, *[SP._ptr(x) for x in hv]))
+            h.rk4_steps(1)
+            SP._check(SP.lib().sc_get_state(h.h, *[SP._ptr(x, True) for x in hv]))
+        torch.cuda.synchronize()
+        te = max_over_ranks(time.perf_counter() - t0)
+        nbytes = 3 * (n // 2 + 1) * n * n * 8
+        e2e = {"value": world * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": ke,
+               "path": "sc_set_state(pinned host) + sc_rk4_steps(1) + sc_get_state(pinned host)"}
+        del host, hv
+
+    # FP32 diagnostics after 2 steps from the seeded field (compared with FP64 below)
+    h.set_state(*init32)
+    h.rk4_steps(2)
+    d32, e32 = h.diagnostics()
+    h.close()
+    del h, init32
+    torch.cuda.empty_cache()
+
+    # ---- plain FP64 beside it, and the FP32 error against it ----
+    fp64 = None
+    if not a.no_fp64:
+        k64 = 2
+        h64 = make(S.SC_FP64)
+        h64.rk4_steps(2)
+        d64, e64 = h64.diagnostics()
+        h64.rk4_steps(1)
+        ms64 = time_steps(h64, k64)
+        h64.close()
+        del h64
+        fp64 = {"steps_per_s": k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64,
+                "speedup_fp32_over_fp64": (value / world) / (k64 / (ms64 / 1e3))}
+        m = e64 > 1e-30
+        fp64["fp32_vs_fp64_after_2_steps"] = {
+            "Ek_max_rel_err": float(np.max(np.abs(e32[m] - e64[m]) / e64[m])),
+            "dissipation_rel_err": abs(d32["dissipation"] - d64["dissipation"]) / d64["dissipation"],
+            "energy_rel_err": abs(d32["energy"] - d64["energy"]) / d64["energy"],
+            "max_div_fp32": d32["max_div"], "max_div_fp64": d64["max_div"]}
+
+    cpu = None
+    if not a.no_cpu and rank == 0 and world == 1:
+        workers = len(os.sched_getaffinity(0))
+        t_rhs = cpu_reference_rhs(n, workers)
+        cpu = {"value": 1.0 / (4.0 * t_rhs), "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": "one right-hand side (1/4 RK4 step) of the %d^3 step, FP64 NumPy/scipy.fft "
+                         "restatement of the reference, workers=%d" % (n, workers)}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+               "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (ran1 seed 1 initial field, as the reference generates it)",
+               "config": {"workload": "forced DNS %d^3 IF-RK4, FP32 bulk" % n, "grid": n,
+                          "nu": NU, "dt": DT, "eps": EPS, "fkmax": FKMAX,
+                          "parallelism": "replicas" if world > 1 else "single GPU",
+                          "l2": "inputs larger than L2 (539 MB per field)"},
+               "gpu_launches": launches,
+               "roofline": roofline,
+               "step_model_bytes": step_bytes,
+               "step_model_gbs": step_bytes / (ms_step / 1e3) / 1e9,
+               "kernels": kernels,
+               "clocks": clocks,
+               "e2e": e2e,
+               "fp64": fp64,
+               "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    if dist:
+        td.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -81,6 +81,10 @@ int sc_default_params(sc_params* p, int n, int precision);
 int sc_create(const sc_params* p, sc_handle** out);
 int sc_destroy(sc_handle* h);
 
+/* Make CUDA device `device` current for this library on the calling thread
+ * (handles are created on the current device). */
+int sc_set_device(int device);
+
 /* Launch on this CUDA stream (cudaStream_t passed as void*; NULL = the
  * handle's own stream). */
 int sc_set_stream(sc_handle* h, void* stream);

@@ -26,6 +26,7 @@ SIGNATURES = {
     "sc_default_params": ([_P, _I, _I], _I),
     "sc_create": ([_P, _P], _I),
     "sc_destroy": ([_P], _I),
+    "sc_set_device": ([_I], _I),
     "sc_set_stream": ([_P, _P], _I),
     "sc_set_dt": ([_P, _D], _I),
     "sc_set_state": ([_P, _P, _P, _P], _I),

@@ -688,6 +688,11 @@ int sc_destroy(sc_handle* h) {
   return SC_OK;
 }
 
+int sc_set_device(int device) {
+  SC_CUDA(cudaSetDevice(device));
+  return SC_OK;
+}
+
 int sc_set_stream(sc_handle* h, void* stream) {
   if (!h) return fail(SC_ERR_INVALID, "null handle");
   h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own;
