@@ -58,6 +58,24 @@ def declared_symbols(header=HEADER):
     return sorted(set(re.findall(r"\b(sc_[a-z0-9_]+)\s*\(", src)))
 
 
+F77_HEADER = os.path.join(os.path.dirname(HERE), "include", "specns_f77.h")
+F77_LIBS = {"sp": os.path.join(HERE, "lib", "libspecns_f77_sp.so"),
+            "dp": os.path.join(HERE, "lib", "libspecns_f77_dp.so")}
+
+
+def declared_f77_symbols(header=F77_HEADER):
+    """Fortran entry points declared in include/specns_f77.h."""
+    src = open(header).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\bvoid\s+([A-Za-z0-9_]+)\s*\(", src)))
+
+
+def load_f77(prec="dp"):
+    """Load a Fortran-ABI shim library ('sp' or 'dp'); needs libspecns.so beside it."""
+    load()
+    return C.CDLL(F77_LIBS[prec])
+
+
 def load():
     global _LIB
     if _LIB is not None:

@@ -1,0 +1,103 @@
+// Fortran-callable shims with the reference's subroutine signatures
+// (include/specns_f77.h), forwarding to the C ABI of libspecns.so.
+// Built twice: -DSC_F77_SP (REAL = float) and -DSC_F77_DP (REAL = double).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+
+#include "specns.h"
+#include "specns_f77.h"
+
+namespace {
+
+#ifdef SC_F77_SP
+constexpr int kPrec = SC_FP32;
+#else
+constexpr int kPrec = SC_FP64;
+#endif
+
+void check(int rc, const char* where) {
+  if (rc != SC_OK) {
+    std::fprintf(stderr, "specns %s: %s\n", where, sc_last_error());
+    std::abort();
+  }
+}
+
+int wave(int i, int n) { return i < n / 2 ? i : i - n; }
+
+}  // namespace
+
+extern "C" {
+
+void convec_dns_(const void* vx, const void* vy, const void* vz, void* wx, void* wy, void* wz,
+                 const int* lx1, const int* ly, const int* lz, const int* nx, const int* ny,
+                 const int* nz) {
+  check(sc_convec_dns(kPrec, vx, vy, vz, wx, wy, wz, *lx1, *ly, *lz, *nx, *ny, *nz), "convec_dns");
+}
+
+void force_(void* wx, void* wy, void* wz, const void* vx, const void* vy, const void* vz,
+            const sc_f77_real*, const int* lx1, const int* ly, const int* lz,
+            const sc_f77_real* fkmax, const sc_f77_real* eps) {
+  check(sc_force(kPrec, wx, wy, wz, vx, vy, vz, *lx1, *ly, *lz, (double)*fkmax, (double)*eps), "force");
+}
+
+void projection_(void* vx, void* vy, void* vz, const sc_f77_real*, const sc_f77_real*,
+                 const sc_f77_real*, const int* lx1, const int* ly, const int* lz) {
+  check(sc_projection(kPrec, vx, vy, vz, *lx1, *ly, *lz), "projection");
+}
+
+void __msymmetrize_MOD_symmetrize3d(void* c, const int* lx1, const int* ly, const int* lz) {
+  check(sc_symmetrize(kPrec, c, *lx1, *ly, *lz), "symmetrize");
+}
+
+void symmetrize3d_(void* c, const int* lx1, const int* ly, const int* lz) {
+  check(sc_symmetrize(kPrec, c, *lx1, *ly, *lz), "symmetrize");
+}
+
+void dealiasing_(void* c, const sc_f77_real*, const int* lx1, const int* ly, const int* lz) {
+  check(sc_dealiasing(kPrec, c, *lx1, *ly, *lz), "dealiasing");
+}
+
+void smag_(const void* vx, const void* vy, const void* vz, void* t11, void* t12, void* t13,
+           void* t22, void* t23, void* t33, const sc_f77_real*, const sc_f77_real*,
+           const sc_f77_real*, const int* lx1, const int* ly, const int* lz, const int* nx,
+           const int* ny, const int* nz, const sc_f77_real* delta) {
+  check(sc_smag(kPrec, vx, vy, vz, t11, t12, t13, t22, t23, t33, *lx1, *ly, *lz, *nx, *ny, *nz,
+                (double)*delta, 0.026),
+        "smag");
+}
+
+void dynsmag_(const void* ux, const void* uy, const void* uz, void* t11, void* t12, void* t13,
+              void* t22, void* t23, void* t33, const sc_f77_real*, const sc_f77_real*,
+              const sc_f77_real*, const sc_f77_real* g_test, const int* lx1, const int* ly,
+              const int* lz, const int* nx, const int* ny, const int* nz, const int*,
+              const sc_f77_real* delta, const sc_f77_real* delta_test, sc_f77_real* mm,
+              sc_f77_real* lm, sc_f77_real* cs2, const int* update) {
+  // Recover k_test from the sharp filter: the largest k2 it passes.
+  long long k2in = -1, k2out = 1LL << 62;
+  for (int kk = 0; kk < *lz; ++kk)
+    for (int jj = 0; jj < *ly; ++jj)
+      for (int ii = 0; ii < *lx1; ++ii) {
+        const long long kz = wave(kk, *lz), ky = wave(jj, *ly);
+        const long long k2 = (long long)ii * ii + ky * ky + kz * kz;
+        const sc_f77_real gv = g_test[((long long)kk * *ly + jj) * *lx1 + ii];
+        if (gv != 0) { if (k2 > k2in) k2in = k2; }
+        else if (k2 < k2out) k2out = k2;
+      }
+  if (k2in >= k2out) {
+    std::fprintf(stderr, "specns dynsmag: g_test is not a sharp spherical filter\n");
+    std::abort();
+  }
+  const double k_test = std::sqrt((double)k2in + 0.5);
+  double dmm = 0, dlm = 0, dcs2 = (double)*cs2;
+  check(sc_dynsmag(kPrec, ux, uy, uz, t11, t12, t13, t22, t23, t33, *lx1, *ly, *lz, *nx, *ny, *nz,
+                   k_test, (double)*delta, (double)*delta_test, &dmm, &dlm, &dcs2, *update != 0),
+        "dynsmag");
+  if (*update) {
+    *mm = (sc_f77_real)dmm;
+    *lm = (sc_f77_real)dlm;
+    *cs2 = (sc_f77_real)dcs2;
+  }
+}
+
+}  // extern "C"

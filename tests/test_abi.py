@@ -30,3 +30,12 @@ def test_default_params_and_errors_without_gpu(specns_lib):
     rc = specns_lib.sc_create(ctypes.byref(bad), ctypes.byref(h))
     assert rc == 1 and b"power of two" in specns_lib.sc_last_error()
     assert not h.value
+
+
+def test_f77_shims_export_every_declared_symbol(specns_lib):
+    declared = _lib.declared_f77_symbols()
+    assert "convec_dns_" in declared and "dynsmag_" in declared and len(declared) == 8
+    for prec in ("sp", "dp"):
+        lib = _lib.load_f77(prec)
+        missing = [n for n in declared if not hasattr(lib, n)]
+        assert missing == [], (prec, missing)
