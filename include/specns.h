@@ -136,6 +136,24 @@ int sc_step_bytes(sc_handle* h, double* bytes_per_step);
 
 const char* sc_last_error(void);
 
+/* No counterpart in the reference.  FP64 diagnostics of a caller-owned
+ * spectral velocity field that allocate no device memory, for callers that
+ * cannot call cudaMalloc: a solver that reserves its whole device-memory
+ * budget at start-up and must not allocate inside its step loop, or one that
+ * cannot afford the device-wide synchronisation cudaMalloc/cudaFree may
+ * imply.  vx, vy, vz: device arrays in the reference layout (pitch nx/2+1),
+ * complex(4) for SC_FP32, complex(8) for SC_FP64.  out: device array of
+ * 5 + nx/2 doubles receiving [energy, sum k^2 q (enstrophy; dissipation =
+ * 2 nu times it), max |k.v|, non-finite count, 0, E(1..nx/2)].  Enqueued on
+ * `stream` (cudaStream_t as void*, NULL = default stream), asynchronous.
+ * Block partial sums live in one static device array of 4.04 MiB per GPU
+ * (held until exit), sized for nx, ny, nz <= 1024; larger grids are
+ * rejected.  All calls share that array: calls that overlap on the GPU race.
+ * The first call on a device looks up the array's address; make it before
+ * any stream capture. */
+int sc_diagnostics_noalloc(int precision, const void* vx, const void* vy, const void* vz, int nx,
+                           int ny, int nz, double* out, void* stream);
+
 /* ---------------------------------------------------------------------
  * Reference-signature operators (one call = one reference subroutine).
  * Arrays are host memory in the reference layout; integer sizes are passed

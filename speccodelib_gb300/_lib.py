@@ -41,6 +41,7 @@ SIGNATURES = {
     "sc_profile_enable": ([_P, _I], _I),
     "sc_profile_read": ([_P, C.c_char_p, _P, _P], _I),
     "sc_step_bytes": ([_P, _P], _I),
+    "sc_diagnostics_noalloc": ([_I, _P, _P, _P, _I, _I, _I, _P, _P], _I),
     "sc_convec_dns": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
     "sc_projection": ([_I, _P, _P, _P, _I, _I, _I], _I),
     "sc_force": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _D], _I),

@@ -589,6 +589,11 @@ template <typename T> int impl_dispatch_tile(int logz) {
 
 }  // namespace
 
+// Error channel for entry points defined in other translation units.
+namespace sc {
+int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace sc
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
