@@ -1,0 +1,47 @@
+"""Generate the golden fixtures under tests/golden/ from the FP64 oracle.
+
+    python tests/golden/make_golden.py
+
+Fixtures (NumPy .npz, complex128 spectral fields in the reference layout
+(nz, ny, nx/2+1)): the seeded 16^3 initial field (ran1 seed 1, akp = 4,
+E = 0.5), its right-hand side, the state after 1 and 10 IF-RK4 steps, after
+3 IF-AB2 passes, and the Smagorinsky / dynamic-Smagorinsky stresses.  The
+reference itself cannot be run here; these fixtures freeze the oracle's
+outputs so that both the oracle and the CUDA library are checked against the
+same committed numbers.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle import spectral_ref as R  # noqa: E402
+
+N = 16
+NU, DT = 0.01, 2e-3
+
+
+def main():
+    kcut = 2.0 * (N // 2) / 3.0
+    v0 = R.initialize_dealiased(N, N, N, 1, 4.0, 1.0 / np.sqrt(3.0), kcut)
+    g = R.Grid(R.Params(nx=N, nu=NU, dt=DT))
+    w0 = R.ratesdudt(v0, g)
+    v1 = R.rk4_run(v0, g, 1)
+    v10 = R.rk4_run(v0, g, 10)
+    vab, _ = R.ab2_run(v0, g, 3)
+    kx, ky, kz, k2 = R.wavenumber(N, N, N)
+    delta = R.PI_REF / kcut
+    ts = R.smag(*v0, kx, ky, kz, N, delta, 0.0289)
+    td, mm, lm, cs2 = R.dynsmag(*v0, kx, ky, kz, R.test_filter(k2, kcut / 2), N, delta, 2 * delta, True, 0.0)
+    np.savez_compressed(os.path.join(HERE, "dns16.npz"), v0=np.stack(v0), w0=np.stack(w0), v1=np.stack(v1),
+                        v10=np.stack(v10), vab3=np.stack(vab), nu=NU, dt=DT, n=N)
+    np.savez_compressed(os.path.join(HERE, "les16.npz"), tau_smag=np.stack(ts), tau_dyn=np.stack(td),
+                        mm=mm, lm=lm, cs2=cs2, c1=0.0289, delta=delta, n=N)
+    np.savez_compressed(os.path.join(HERE, "ran1_seed1.npz"), seq=R.ran1_sequence(1, 4096),
+                        seq_m7=R.ran1_sequence(-7, 4096))
+
+
+if __name__ == "__main__":
+    main()

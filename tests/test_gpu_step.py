@@ -151,3 +151,29 @@ def test_ab2_matches_oracle(specns_lib, prec):
         h.ab2_steps(6)
         out = h.get_state()
     assert rel_l2(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_against_committed_golden_fixtures(specns_lib, prec):
+    import os
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    d = np.load(os.path.join(gold, "dns16.npz"))
+    n = int(d["n"])
+    p = dict(nu=float(d["nu"]), dt=float(d["dt"]))
+    with handle(n, prec, **p) as h:
+        h.init_field(seed=1, akp=4.0, u0=1 / np.sqrt(3))
+        assert rel_l2(h.get_state(), list(d["v0"])) < (1e-14 if prec == S.SC_FP64 else 1e-6)
+        h.set_state(*d["v0"])
+        assert rel_l2(h.rhs(), list(d["w0"])) < TOL[prec]
+        h.rk4_steps(1)
+        assert rel_l2(h.get_state(), list(d["v1"])) < TOL[prec]
+        h.set_state(*d["v0"])
+        h.rk4_steps(10)
+        assert rel_l2(h.get_state(), list(d["v10"])) < TOL[prec]
+        h.set_state(*d["v0"])
+        h.ab2_steps(3)
+        assert rel_l2(h.get_state(), list(d["vab3"])) < TOL[prec]
+    les = np.load(os.path.join(gold, "les16.npz"))
+    v0 = [np.ascontiguousarray(a, np.complex128 if prec == S.SC_FP64 else np.complex64) for a in d["v0"]]
+    t = S.smag(*v0, float(les["delta"]), 0.0289)
+    assert rel_l2(t, list(les["tau_smag"])) < TOL[prec]

@@ -1,0 +1,168 @@
+"""Pins of the FP64 oracle (CPU only).
+
+The reference ships no tests or golden data and cannot be built here, so the
+oracle is pinned to the known answers its own source implies:
+* ran1 (initialize.f90:516-548): the C helper equals a pure-Python
+  restatement draw for draw; every positive seed restarts the seed-1 stream
+  (idum = max(-idum,1), :530).
+* FFTW convention (convec_dns.f90:15,40-47): unnormalised c2r = sum c e^{+ik.x},
+  r2c = sum u e^{-ik.x}; single modes map as expected.
+* Roberts flow (robertsflow.f90:23-25) is Beltrami: zero Lamb vector, and the
+  integrating-factor RK4 reproduces exp(-2 nu t).
+* initialize.f90:284-371: E = 3/2 u0^2, divergence-free, Hermitian on kx = 0,
+  zero beyond the 2/3 cut and on the Nyquist planes.
+* symmetrize.f90 / projection.f90 / force.f90 invariants, and the energy
+  budget of the right-hand side: d E/dt = eps exactly (the Lamb vector is
+  orthogonal to u pointwise).
+* the committed golden fixtures reproduce.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import spectral_ref as R
+from _util import hermitian_fields, rel_l2, solenoidal_init
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_ran1_c_matches_python_and_seed_quirk():
+    for seed in (1, -7, 123):
+        assert np.array_equal(R.ran1_sequence(seed, 5000), R.ran1_sequence_py(seed, 5000))
+    assert np.array_equal(R.ran1_sequence(5, 100), R.ran1_sequence(1, 100))
+    assert np.array_equal(R.ran1_sequence(1, 100), R.ran1_sequence(-1, 100))
+    assert not np.array_equal(R.ran1_sequence(-5, 100), R.ran1_sequence(1, 100))
+    s = R.ran1_sequence(1, 20000)
+    assert s.min() > 0 and s.max() < 1 and abs(s.mean() - 0.5) < 0.01
+
+
+def test_ran1_golden():
+    g = np.load(os.path.join(GOLD, "ran1_seed1.npz"))
+    assert np.array_equal(R.ran1_sequence(1, 4096), g["seq"])
+    assert np.array_equal(R.ran1_sequence(-7, 4096), g["seq_m7"])
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (16, 8, 32)])
+def test_fftw_convention_single_modes(shape):
+    nx, ny, nz = shape
+    z, y, x = np.meshgrid(*[np.arange(n) * 2 * np.pi / n for n in (nz, ny, nx)], indexing="ij")
+    for (a, b, c) in [(1, 0, 0), (2, 3, -1), (0, 1, 2)]:
+        u = np.cos(a * x + b * y + c * z)
+        ch = R.r2c(u) / (nx * ny * nz)
+        iy, iz = b % ny, c % nz
+        if a == 0:
+            assert abs(ch[iz, iy, 0] - 0.5) < 1e-14 and abs(ch[(-c) % nz, (-b) % ny, 0] - 0.5) < 1e-14
+        else:
+            assert abs(ch[iz, iy, a] - 0.5) < 1e-14
+        assert np.allclose(R.c2r(ch, nx), u, atol=1e-13)
+
+
+def roberts(n):
+    x = np.arange(n) * 2 * np.pi / n
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    u = [np.sin(X) * np.cos(Y), -np.cos(X) * np.sin(Y), np.sqrt(2) * np.sin(X) * np.sin(Y)]
+    return tuple(R.r2c(a) / n ** 3 for a in u)
+
+
+def test_roberts_flow_beltrami_and_exact_decay():
+    n = 16
+    v = roberts(n)
+    kx, ky, kz, _ = R.wavenumber(n, n, n)
+    w = R.vorticity(*v, kx, ky, kz)
+    assert max(np.abs(w[i] - np.sqrt(2) * v[i]).max() for i in range(3)) < 1e-15
+    lamb = R.convec_dns(*v, *w, n)
+    assert max(np.abs(a).max() for a in lamb) < 1e-15
+    g = R.Grid(R.Params(nx=n, nu=0.05, dt=1e-2, forced=False))
+    out = R.rk4_run(v, g, 20)
+    assert rel_l2(out, [a * np.exp(-2 * 0.05 * 0.2) for a in v]) < 1e-14
+
+
+@pytest.mark.parametrize("n", [16, 32])
+def test_initial_field_properties(n):
+    v = solenoidal_init(n)
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    assert abs(R.energy(v) - 0.5) < 1e-14
+    assert R.max_divergence(v, kx, ky, kz) < 1e-15
+    kcut = 2 * (n // 2) / 3
+    for a in v:
+        assert np.all(a[k2 >= kcut * kcut] == 0)
+        assert np.all(a[:, n // 2, :] == 0) and np.all(a[n // 2] == 0) and np.all(a[..., -1] == 0)
+        assert np.array_equal(R.symmetrize3d(a), a)
+        # Hermitian on kx = 0 => c2r o r2c is the identity
+        assert rel_l2(R.r2c(R.c2r(a, n)) / n ** 3, a) < 1e-14
+
+
+def test_symmetrize_projection_idempotent_and_div_free():
+    n = 16
+    rng = np.random.default_rng(0)
+    c = [rng.standard_normal((n, n, n // 2 + 1)) + 1j * rng.standard_normal((n, n, n // 2 + 1)) for _ in range(3)]
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    s = R.symmetrize3d(c[0])
+    assert np.array_equal(R.symmetrize3d(s), s)
+    p = R.projection(*c, kx, ky, kz)
+    assert R.max_divergence(p, kx, ky, kz) < 1e-12
+    assert rel_l2(R.projection(*p, kx, ky, kz), p) < 1e-15
+
+
+def test_rhs_energy_budget_equals_injection():
+    """sum 2 w_kx Re(conj(v) . R(v)) = eps: the Lamb vector does no work."""
+    n = 32
+    v = solenoidal_init(n)
+    g = R.Grid(R.Params(nx=n, eps=0.1))
+    w = R.ratesdudt(v, g)
+    rate = 0.0
+    for a, b in zip(v, w):
+        q = 2 * (np.conj(a) * b).real
+        q[:, :, 0] *= 0.5
+        rate += q.sum()
+    assert abs(rate - 0.1) < 1e-12
+
+
+def test_lawson_form_equals_reference_rk4():
+    n = 16
+    v = solenoidal_init(n)
+    g = R.Grid(R.Params(nx=n))
+    ref = R.rk4_step(v, g)
+    E = np.exp(-g.p.nu * g.k2 * g.p.dt / 2)
+    dt = g.p.dt
+    k1 = R.ratesdudt(v, g)
+    k2 = R.ratesdudt([E * (a + 0.5 * dt * b) for a, b in zip(v, k1)], g)
+    k3 = R.ratesdudt([E * a + 0.5 * dt * b for a, b in zip(v, k2)], g)
+    k4 = R.ratesdudt([E * E * a + E * dt * b for a, b in zip(v, k3)], g)
+    out = [E * E * a + dt * (E * E * b + 2 * E * c + 2 * E * d + e) / 6 for a, b, c, d, e in zip(v, k1, k2, k3, k4)]
+    out = R.mask_state(out, g)
+    assert rel_l2(out, ref) < 1e-14
+
+
+def test_force_injects_exactly_eps():
+    n = 16
+    v = hermitian_fields((n, n, n), 2)
+    _, _, _, k2 = R.wavenumber(n, n, n)
+    z = [np.zeros_like(a) for a in v]
+    f = R.force(*z, *v, k2, 2.5, 0.3)
+    rate = 0.0
+    for a, b in zip(v, f):
+        q = 2 * (np.conj(a) * b).real
+        q[:, :, 0] *= 0.5
+        rate += q.sum()
+    assert abs(rate - 0.3) < 1e-13
+
+
+def test_golden_fixtures_reproduce():
+    d = np.load(os.path.join(GOLD, "dns16.npz"))
+    n = int(d["n"])
+    v0 = solenoidal_init(n)
+    assert rel_l2(v0, list(d["v0"])) < 1e-15
+    g = R.Grid(R.Params(nx=n, nu=float(d["nu"]), dt=float(d["dt"])))
+    assert rel_l2(R.ratesdudt(v0, g), list(d["w0"])) < 1e-14
+    assert rel_l2(R.rk4_run(v0, g, 1), list(d["v1"])) < 1e-14
+    assert rel_l2(R.rk4_run(v0, g, 10), list(d["v10"])) < 1e-14
+    assert rel_l2(R.ab2_run(v0, g, 3)[0], list(d["vab3"])) < 1e-14
+    les = np.load(os.path.join(GOLD, "les16.npz"))
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    delta = float(les["delta"])
+    assert rel_l2(R.smag(*v0, kx, ky, kz, n, delta, 0.0289), list(les["tau_smag"])) < 1e-14
+    kcut = 2 * (n // 2) / 3
+    td, mm, lm, cs2 = R.dynsmag(*v0, kx, ky, kz, R.test_filter(k2, kcut / 2), n, delta, 2 * delta, True, 0.0)
+    assert rel_l2(td, list(les["tau_dyn"])) < 1e-14 and abs(cs2 - float(les["cs2"])) < 1e-14 * abs(cs2)
