@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--ny", type=int, default=0, help="non-cubic grid (profiling runs)")
+    ap.add_argument("--nz", type=int, default=0, help="non-cubic grid (profiling runs)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -195,7 +197,8 @@ def run_ours(a):
     stream = torch.cuda.Stream()
 
     def make(prec):
-        p = S.default_params(n, prec, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX)
+        p = S.default_params(n, prec, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX,
+                             ny=a.ny or n, nz=a.nz or n)
         h = S.SpectralNS(p)
         h.set_stream(stream.cuda_stream)
         h.init_field(seed=SEED, akp=AKP, u0=U0)
@@ -243,7 +246,7 @@ def run_ours(a):
     value = world * a.steps / (ms / 1e3)
     ms_step = ms / a.steps
 
-    F = (n // 2 + 1) * n * n * 8.0
+    F = (n // 2 + 1) * (a.ny or n) * (a.nz or n) * 8.0
     dom = max(prof, key=lambda k: prof[k][1])
     cnt, tot = prof[dom]
     avg_ms = tot / max(cnt, 1)

@@ -3,6 +3,7 @@
 #pragma once
 #include "sc_launch.h"
 #include "sc_ops.cuh"
+#include "sc_tma_passes.cuh"
 
 namespace sc {
 
@@ -63,7 +64,96 @@ cudaError_t launch_xpass(const FieldList<T>& fin, const FieldList<T>& fout, cons
   return cudaGetLastError();
 }
 
+template <typename T, int LOGN, bool INV>
+cudaError_t launch_plain_tma(const CUtensorMap& map, const TmaPass<T>& tp, const Geom& g, const C2<T>* tw,
+                             int nsm, cudaStream_t s) {
+  using Cfg = TmaCfg<T, LOGN>;
+  auto k = pencil_tma_kernel<T, LOGN, INV>;
+  constexpr size_t sm = Cfg::STAGES * Cfg::TILE_BYTES + kSmemAlignPad;
+  static cudaError_t attr = smem_attr(k, sm);
+  if (attr != cudaSuccess) return attr;
+  const long long total = (long long)tp.ntx * tp.nouter * tp.nf;
+  long long grid = (long long)nsm * 2;
+  if (grid > total) grid = total;
+  k<<<(unsigned)grid, Cfg::NT, sm, s>>>(map, tp, g, tw);
+  return cudaGetLastError();
+}
+
+template <typename T, int LOGN>
+cudaError_t launch_zinv_tma(const CUtensorMap& vmap, const ZvArgs<T>& za, const FieldList<T>& out,
+                            const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
+  using Cfg = TmaCfg<T, LOGN>;
+  auto k = zinv_tma_kernel<T, LOGN>;
+  constexpr size_t sm = 3 * Cfg::TILEZ_BYTES + Cfg::WORKZ_BYTES + kSmemAlignPad;
+  static cudaError_t attr = smem_attr(k, sm);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::PZ - 1) / Cfg::PZ, g.ny);
+  k<<<grid, Cfg::NTZ, sm, s>>>(vmap, za, out, g, tw, err);
+  return cudaGetLastError();
+}
+
+template <typename T, int LOGN>
+cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
+                            const C2<T>* tw, int* err, cudaStream_t s) {
+  using Cfg = TmaCfg<T, LOGN>;
+  auto k = zfwd_tma_kernel<T, LOGN>;
+  constexpr size_t sm = 3 * Cfg::TILE_BYTES + kSmemAlignPad;
+  static cudaError_t attr = smem_attr(k, sm);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
+  k<<<grid, Cfg::NT, sm, s>>>(lmap, st, g, tw, err);
+  return cudaGetLastError();
+}
+
 }  // namespace sc
+
+#define SC_TMA_TILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::P;
+#define SC_TMA_ZTILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::PZ;
+
+#define SC_DEFINE_TMA(T)                                                                         \
+  template <> int sc::Launch<T>::tma_tile(int logn) {                                            \
+    switch (logn) { SC_LOGN_CASES(SC_TMA_TILE_CASE) default: return 0; }                         \
+  }                                                                                              \
+  template <> int sc::Launch<T>::tma_ztile(int logn) {                                           \
+    switch (logn) { SC_LOGN_CASES(SC_TMA_ZTILE_CASE) default: return 0; }                        \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::plain_tma(int logn, bool inv, const CUtensorMap& map,               \
+                                       const TmaPass<T>& tp, const Geom& g, const C2<T>* tw,     \
+                                       int nsm, cudaStream_t s) {                                \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_PLAINTMA_CASE_##T)                                                        \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zinv_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,    \
+                                      const FieldList<T>& out, const Geom& g, const C2<T>* tw,   \
+                                      int* err, cudaStream_t s) {                                \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZINVTMA_CASE_##T)                                                         \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, \
+                                      const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) { \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZFWDTMA_CASE_##T)                                                         \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }
+
+#define SC_PLAINTMA_CASE_float(L) \
+  case L: return inv ? sc::launch_plain_tma<float, L, true>(map, tp, g, tw, nsm, s) \
+                     : sc::launch_plain_tma<float, L, false>(map, tp, g, tw, nsm, s);
+#define SC_PLAINTMA_CASE_double(L) \
+  case L: return inv ? sc::launch_plain_tma<double, L, true>(map, tp, g, tw, nsm, s) \
+                     : sc::launch_plain_tma<double, L, false>(map, tp, g, tw, nsm, s);
+#define SC_ZINVTMA_CASE_float(L) case L: return sc::launch_zinv_tma<float, L>(vmap, za, out, g, tw, err, s);
+#define SC_ZINVTMA_CASE_double(L) case L: return sc::launch_zinv_tma<double, L>(vmap, za, out, g, tw, err, s);
+#define SC_ZFWDTMA_CASE_float(L) case L: return sc::launch_zfwd_tma<float, L>(lmap, st, g, tw, err, s);
+#define SC_ZFWDTMA_CASE_double(L) case L: return sc::launch_zfwd_tma<double, L>(lmap, st, g, tw, err, s);
 
 #define SC_DEFINE_TILE(T) \
   template <> int sc::Launch<T>::tile() { return sc::Tile<T>::P; }

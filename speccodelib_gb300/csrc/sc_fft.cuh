@@ -90,7 +90,7 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C* v)
   else dft8<INV>(v);
 }
 
-template <typename T, int LOGN, int P, int PS, int NT, bool PFAST>
+template <typename T, int LOGN, int P, int PS, int NT, bool PFAST, int PADSHIFT = 0>
 struct FFTEngine {
   using C = C2<T>;
   static constexpr int N = 1 << LOGN;
@@ -101,7 +101,14 @@ struct FFTEngine {
   static constexpr int TOTL = P * (N / RL);
   static constexpr int J1 = (TOT1 + NT - 1) / NT;
   static constexpr int JL = (TOTL + NT - 1) / NT;
-  static constexpr int SMEM_ELEMS = N * PS;
+  // Shared-memory slot of point n.  With PADSHIFT = s one slot is skipped
+  // every 2^s points, which spreads the stride-R scatter of the first stage
+  // over all banks: s = 4 keeps both that scatter and 16-wide contiguous
+  // runs conflict-free for pencil-per-warp (j-fastest) layouts with odd PS;
+  // s = 3 does it for 8-wide p-fastest tiles (64-byte rows).
+  static constexpr int NPAD = PADSHIFT ? N + (N >> PADSHIFT) : N;
+  static constexpr int SMEM_ELEMS = NPAD * PS;
+  __device__ static __forceinline__ int sidx(int n) { return PADSHIFT ? n + (n >> PADSHIFT) : n; }
 
   template <int R>
   __device__ static __forceinline__ void decode(int job, int& p, int& j) {
@@ -156,7 +163,7 @@ struct FFTEngine {
       decode<R>(job, p, j);
       if ((TOT % NT == 0) || job < TOT) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[a][r] = sm[(j + r * NR) * PS + p];
+        for (int r = 0; r < R; ++r) v[a][r] = sm[sidx(j + r * NR) * PS + p];
       }
     }
     __syncthreads();
@@ -170,7 +177,7 @@ struct FFTEngine {
         dft<R, INV>(v[a]);
         const int d = (j / NSV) * NSV * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm[(d + r * NSV) * PS + p] = v[a][r];
+        for (int r = 0; r < R; ++r) sm[sidx(d + r * NSV) * PS + p] = v[a][r];
       }
     }
     __syncthreads();
@@ -182,6 +189,56 @@ struct FFTEngine {
       mid_stage<S, INV>(sm, tw);
       mid_stages<S + 1, INV>(sm, tw);
     }
+  }
+
+  template <int S, bool INV>
+  __device__ static __forceinline__ void all_stages(C* sm, const C* __restrict__ tw) {
+    if constexpr (S < NS) {
+      mid_stage<S, INV>(sm, tw);
+      all_stages<S + 1, INV>(sm, tw);
+    }
+  }
+
+  // Last stage: shared -> registers (last-stage layout).
+  template <bool INV>
+  __device__ static __forceinline__ void last_stage(C (&out)[JL][RL], C* sm, const C* __restrict__ tw) {
+    constexpr int NR = N / RL;
+    constexpr int NSV = fft_ns(LOGN, NS - 1);
+    static_assert(NSV == NR, "last stage spans the pencil");
+#pragma unroll
+    for (int a = 0; a < JL; ++a) {
+      int job = threadIdx.x + a * NT, p, j;
+      decode<RL>(job, p, j);
+      if ((TOTL % NT == 0) || job < TOTL) {
+#pragma unroll
+        for (int r = 0; r < RL; ++r) out[a][r] = sm[sidx(j + r * NR) * PS + p];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < JL; ++a) {
+      int job = threadIdx.x + a * NT, p, j;
+      decode<RL>(job, p, j);
+      if ((TOTL % NT == 0) || job < TOTL) {
+        twiddle<RL, NSV, INV>(out[a], j, tw);
+        dft<RL, INV>(out[a]);
+      }
+    }
+  }
+
+  // Input already in shared memory (natural order), output in registers.
+  // Ends with a barrier.
+  template <bool INV>
+  __device__ static void run_smem(C (&out)[JL][RL], C* sm, const C* __restrict__ tw) {
+    mid_stages<0, INV>(sm, tw);
+    last_stage<INV>(out, sm, tw);
+  }
+
+  // Input and output in shared memory, natural order, in place.  Ends with a
+  // barrier.
+  template <bool INV>
+  __device__ static void run_inplace(C* sm, const C* __restrict__ tw) {
+    all_stages<0, INV>(sm, tw);
   }
 
   // Full transform: registers (first-stage layout) -> registers (last-stage
@@ -204,7 +261,7 @@ struct FFTEngine {
         if ((TOT1 % NT == 0) || job < TOT1) {
           dft<R1, INV>(in[a]);
 #pragma unroll
-          for (int r = 0; r < R1; ++r) sm[(j * R1 + r) * PS + p] = in[a][r];
+          for (int r = 0; r < R1; ++r) sm[sidx(j * R1 + r) * PS + p] = in[a][r];
         }
       }
       __syncthreads();
@@ -219,7 +276,7 @@ struct FFTEngine {
         decode<RL>(job, p, j);
         if ((TOTL % NT == 0) || job < TOTL) {
 #pragma unroll
-          for (int r = 0; r < RL; ++r) out[a][r] = sm[(j + r * NR) * PS + p];
+          for (int r = 0; r < RL; ++r) out[a][r] = sm[sidx(j + r * NR) * PS + p];
         }
       }
       __syncthreads();

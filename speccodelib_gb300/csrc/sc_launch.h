@@ -3,6 +3,8 @@
 // launcher dispatches the runtime axis length to a compiled template
 // instance; lengths outside 8..1024 return cudaErrorInvalidValue.
 #pragma once
+#include <cuda.h>
+
 #include "sc_common.cuh"
 
 namespace sc {
@@ -15,6 +17,7 @@ template <typename T> struct DiagArgs;
 template <typename T> struct SpecOpArgs;
 template <typename T> struct StrainArgs;
 template <typename T> struct PhysArgs;
+template <typename T> struct TmaPass;
 
 template <typename T> struct Launch {
   static int tile();                                   // pencil tile width P
@@ -36,6 +39,17 @@ template <typename T> struct Launch {
   // physical-space pointwise op; PH_DYN2 also finishes cs2 into *c1_out
   static cudaError_t phys(const PhysArgs<T>& pa, int nblocks, const Geom& g, double* c1_out,
                           double* lm_mm, cudaStream_t s);
+  // TMA-fed strided passes (sc_tma_passes.cuh).  Tile widths and box extent
+  // the host needs to encode the tensor maps:
+  static int tma_tile(int logn);       // pencil_tma / zfwd_tma tile width
+  static int tma_ztile(int logn);      // zinv_tma tile width
+  static cudaError_t plain_tma(int logn, bool inverse, const CUtensorMap& map, const TmaPass<T>& tp,
+                               const Geom& g, const C2<T>* tw, int nsm, cudaStream_t s);
+  static cudaError_t zinv_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,
+                              const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
+                              cudaStream_t s);
+  static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
+                              const C2<T>* tw, int* err, cudaStream_t s);
 };
 
 }  // namespace sc

@@ -276,15 +276,29 @@ template <typename T> struct StageArgs {
   double fkmax2, eps;
   const double* kf_partial;
   int kf_tiles;
+  int kf_ptile;         // tile width of the zinv kernel that wrote kf_partial
   double kcut2;
   int mask_rhs;         // also truncate the RHS (mask = rhs_and_step)
   int symmetrize;       // apply symmetrize.f90:32-64 to w
   int project;          // apply projection.f90 to w
 };
 
+// What the update of a mode reads at each point besides w.
+__host__ __device__ constexpr bool mode_reads_v(int m) {
+  return m == SM_RK1 || m == SM_RK2 || m == SM_RK3 || m == SM_RK4 || m == SM_AB2_EULER || m == SM_AB2 ||
+         m == SM_AB2_MID;
+}
+__host__ __device__ constexpr bool mode_reads_acc(int m) {
+  return m == SM_RK2 || m == SM_RK3 || m == SM_RK4 || m == SM_AB2;
+}
+
+// Projection, optional RHS mask and the mode's update at one point, with the
+// state (v, or v0 for the AB2 midpoint pass) and accumulator values already
+// loaded.  w is the right-hand side after forcing and symmetrize.
 template <typename T>
-__device__ __forceinline__ void finish_point(const StageArgs<T>& st, const Geom& g, long long idx,
-                                             int ix, int iy, int iz, C2<T>* w) {
+__device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const Geom& g, long long idx,
+                                                 int ix, int iy, int iz, C2<T>* w, const C2<T>* vv,
+                                                 const C2<T>* av) {
   using C = C2<T>;
   const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
   const T k2 = kx * kx + ky * ky + kz * kz;
@@ -306,72 +320,82 @@ __device__ __forceinline__ void finish_point(const StageArgs<T>& st, const Geom&
   const T E = st.ex[ix] * st.ey[iy] * st.ez[iz];
   const T E2 = E * E;
   const T dt = st.dt, hdt = T(0.5) * st.dt;
+  const bool zero_mean_cut = cut || (ix == 0 && iy == 0 && iz == 0);
   switch (st.mode) {
     case SM_RK1:  // acc = E^2 dt w1 ; s2 = E (v + dt w1/2)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v = st.v[c][idx];
         st.acc[c][idx] = cscale(w[c], E2 * dt);
-        st.sout[c][idx] = cscale(cadd(v, cscale(w[c], hdt)), E);
+        st.sout[c][idx] = cscale(cadd(vv[c], cscale(w[c], hdt)), E);
       }
       break;
     case SM_RK2:  // acc += 2 E dt w2 ; s3 = E v + dt w2/2
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v = st.v[c][idx];
-        st.acc[c][idx] = cadd(st.acc[c][idx], cscale(w[c], T(2) * E * dt));
-        st.sout[c][idx] = cadd(cscale(v, E), cscale(w[c], hdt));
+        st.acc[c][idx] = cadd(av[c], cscale(w[c], T(2) * E * dt));
+        st.sout[c][idx] = cadd(cscale(vv[c], E), cscale(w[c], hdt));
       }
       break;
     case SM_RK3:  // acc += 2 E dt w3 ; s4 = E^2 v + E dt w3
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v = st.v[c][idx];
-        st.acc[c][idx] = cadd(st.acc[c][idx], cscale(w[c], T(2) * E * dt));
-        st.sout[c][idx] = cadd(cscale(v, E2), cscale(w[c], E * dt));
+        st.acc[c][idx] = cadd(av[c], cscale(w[c], T(2) * E * dt));
+        st.sout[c][idx] = cadd(cscale(vv[c], E2), cscale(w[c], E * dt));
       }
       break;
-    case SM_RK4: {  // v = E^2 v + (acc + dt w4)/6, then the 2/3 mask
+    case SM_RK4:  // v = E^2 v + (acc + dt w4)/6, then the 2/3 mask
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v = st.v[c][idx];
-        const C a = cadd(st.acc[c][idx], cscale(w[c], dt));
-        C vn = cadd(cscale(v, E2), cscale(a, T(1) / T(6)));
+        const C a = cadd(av[c], cscale(w[c], dt));
+        C vn = cadd(cscale(vv[c], E2), cscale(a, T(1) / T(6)));
         st.v[c][idx] = cut ? czero<C>() : vn;
       }
       break;
-    }
     case SM_AB2_EULER:  // v = (v + dt/2 w) sqrt(expk2) ; history = w
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v = st.v[c][idx];
-        C vn = cscale(cadd(v, cscale(w[c], hdt)), E);
+        C vn = cscale(cadd(vv[c], cscale(w[c], hdt)), E);
         st.acc[c][idx] = w[c];
-        st.v[c][idx] = (cut || (ix == 0 && iy == 0 && iz == 0)) ? czero<C>() : vn;
+        st.v[c][idx] = zero_mean_cut ? czero<C>() : vn;
       }
       break;
     case SM_AB2_MID:  // v = v0 expk2 + dt w sqrt(expk2)   (history kept)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v0 = st.v0[c][idx];
-        C vn = cadd(cscale(v0, E2), cscale(w[c], dt * E));
-        st.v[c][idx] = (cut || (ix == 0 && iy == 0 && iz == 0)) ? czero<C>() : vn;
+        C vn = cadd(cscale(vv[c], E2), cscale(w[c], dt * E));
+        st.v[c][idx] = zero_mean_cut ? czero<C>() : vn;
       }
       break;
     case SM_AB2:  // v = (v + (3 w - expk2 o) dt/2) expk2 ; o = w
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C v = st.v[c][idx];
-        const C o = st.acc[c][idx];
-        C d = csub(cscale(w[c], T(3)), cscale(o, E2));
-        C vn = cscale(cadd(v, cscale(d, hdt)), E2);
+        C d = csub(cscale(w[c], T(3)), cscale(av[c], E2));
+        C vn = cscale(cadd(vv[c], cscale(d, hdt)), E2);
         st.acc[c][idx] = w[c];
-        st.v[c][idx] = (cut || (ix == 0 && iy == 0 && iz == 0)) ? czero<C>() : vn;
+        st.v[c][idx] = zero_mean_cut ? czero<C>() : vn;
       }
       break;
     default:
       break;
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_state(const StageArgs<T>& st, long long idx, C2<T>* vv, C2<T>* av) {
+  const bool rv = mode_reads_v(st.mode), ra = mode_reads_acc(st.mode);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (rv) vv[c] = st.mode == SM_AB2_MID ? st.v0[c][idx] : st.v[c][idx];
+    if (ra) av[c] = st.acc[c][idx];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void finish_point(const StageArgs<T>& st, const Geom& g, long long idx,
+                                             int ix, int iy, int iz, C2<T>* w) {
+  C2<T> vv[3], av[3];
+  load_state<T>(st, idx, vv, av);
+  finish_point_pre<T>(st, g, idx, ix, iy, iz, w, vv, av);
 }
 
 // K_f of force.f90:16-22 from the zinv partial sums, fixed order.
@@ -473,7 +497,7 @@ zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __rest
   const bool fblock = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
   if (fblock) {
     if (threadIdx.x == 0) {
-      const double kf = forcing_energy(st.kf_partial, st.kf_tiles, P, g.ny, st.fkmax2);
+      const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
       s_coef = st.eps / (2.0 * kf);
     }
     __syncthreads();
@@ -559,14 +583,16 @@ template <typename T, int LOGM, int MODE> struct XpCfg {
   static constexpr int PB = RB * FOUT, PSB = PB | 1;
   static constexpr int JOBS = (PA * M / 8) > 0 ? PA * M / 8 : 1;
   static constexpr int NT = JOBS >= 256 ? 256 : ((JOBS + 31) / 32) * 32;
-  using EA = FFTEngine<T, LOGM, PA, PSA, NT, false>;
-  using EB = FFTEngine<T, LOGM, PB, PSB, NT, false>;
-  static constexpr int SMEM_ELEMS = (M * PSA > M * PSB ? M * PSA : M * PSB);
+  using EA = FFTEngine<T, LOGM, PA, PSA, NT, false, 3>;
+  using EB = FFTEngine<T, LOGM, PB, PSB, NT, false, 3>;
+  static constexpr int MP = EA::NPAD;   // padded point count (see FFTEngine::sidx)
+  static constexpr int SMEM_ELEMS = (MP * PSA > MP * PSB ? MP * PSA : MP * PSB);
   static constexpr size_t SMEM = sizeof(C2<T>) * SMEM_ELEMS;
+  static constexpr int MINB = SMEM * 3 <= 220 * 1024 ? 3 : 2;
 };
 
 template <typename T, int LOGM, int MODE>
-__global__ void __launch_bounds__(XpCfg<T, LOGM, MODE>::NT)
+__global__ void __launch_bounds__(XpCfg<T, LOGM, MODE>::NT, XpCfg<T, LOGM, MODE>::MINB)
 xpass_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restrict__ twM,
              const C2<T>* __restrict__ twN, XArgs<T> xa) {
   using Cfg = XpCfg<T, LOGM, MODE>;
@@ -622,7 +648,7 @@ xpass_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restric
 #pragma unroll
       for (int r = 0; r < EA::RL; ++r) {
         int p, m;
-        if (EA::out_pos(a, r, p, m)) sm[m * PSA + p] = outA[a][r];
+        if (EA::out_pos(a, r, p, m)) sm[EA::sidx(m) * PSA + p] = outA[a][r];
       }
     __syncthreads();
     // ---- physical-space products ----
@@ -638,7 +664,7 @@ xpass_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restric
         C res = czero<C>();
         if (ok) {
           const int gq = p / RB, rl = p % RB;
-          const C* row = sm + m * PSA + rl;
+          const C* row = sm + EA::sidx(m) * PSA + rl;
           auto U = [&](int c) { return row[c * RB]; };
           if (gq < 3) {
             // convec_dns.f90:30-42: Lamb vector u x w on even (re) / odd (im) points
@@ -680,7 +706,7 @@ xpass_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restric
 #pragma unroll
       for (int r = 0; r < EB::RL; ++r) {
         int p, m;
-        if (EB::out_pos(a, r, p, m)) sm[m * PSB + p] = outB[a][r];
+        if (EB::out_pos(a, r, p, m)) sm[EB::sidx(m) * PSB + p] = outB[a][r];
       }
     __syncthreads();
     constexpr int TOT = PB * (M + 1);
@@ -689,8 +715,8 @@ xpass_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restric
       const int gq = p / RB, rl = p % RB;
       const long long row = row0 + rl;
       if (row >= xa.rows) continue;
-      const C zk = sm[(k % M) * PSB + p];
-      const C zm = cconj(sm[((M - k) % M) * PSB + p]);
+      const C zk = sm[EB::sidx(k % M) * PSB + p];
+      const C zm = cconj(sm[EB::sidx((M - k) % M) * PSB + p]);
       const C e = cadd(zk, zm);
       const C d = cmul(csub(zk, zm), __ldg(&twN[k]));      // * e^{-2 pi i k/N}
       const C x = cscale(csub(e, cmuli(d)), T(0.5));

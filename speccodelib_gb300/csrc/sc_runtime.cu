@@ -7,11 +7,14 @@
 // solver programs (specdns-forced-omp-ft.f90:81-86) -- lives inside an
 // sc_handle: device fields, twiddle tables, integrating-factor tables and
 // reduction scratch, all allocated once at sc_create.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -23,6 +26,7 @@
 #include "../../include/specns.h"
 #include "sc_launch.h"
 #include "sc_ops.cuh"
+#include "sc_tma_passes.cuh"
 
 namespace {
 
@@ -78,7 +82,11 @@ struct sc_handle {
   void* ez = nullptr;
   void* side = nullptr;           // kx = 0 plane, 3 components
   double* kf_partial = nullptr;
-  int kf_tiles = 0;
+  int kf_ntiles_max = 0;          // capacity of kf_partial in tiles
+  int* derr = nullptr;            // device error word (bounded waits)
+  int nsm = 152;                  // SM count of the device
+  bool tma = true;                // TMA-fed strided passes
+  bool tma_zinv = false;          // TMA-fed zinv (the register-fed one is faster at 512^3)
   double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch
   double* dpart = nullptr;        // reduction partials
   size_t dpart_len = 0;
@@ -139,6 +147,55 @@ int prof_drain(sc_handle* h) {
 }
 
 // ---------------------------------------------------------------------------
+// tensor maps for the TMA passes (cuTensorMapEncodeTiled through the runtime's
+// driver entry point; no link-time dependency on libcuda)
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 4D map over `nf` fields starting at `base` (fields `field` elements apart):
+// dims (x: nxh complex, y, z, field) in 8-byte units; box (P, BOX, 1, 1) for
+// axis 1 (y) or (P, 1, BOX, 1) for axis 2 (z).
+int encode_fields(sc_handle* h, const void* base, int nf, int axis, int P, int N, CUtensorMap* out) {
+  auto enc = tmap_encoder();
+  if (!enc) return fail(SC_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const int U = (int)(h->csize / 8);
+  const int box = N < 256 ? N : 256;
+  cuuint64_t dims[4] = {(cuuint64_t)h->g.nxh * U, (cuuint64_t)h->g.ny, (cuuint64_t)h->g.nz, (cuuint64_t)nf};
+  cuuint64_t strides[3] = {(cuuint64_t)h->g.nxp * h->csize, (cuuint64_t)h->g.nxp * h->g.ny * h->csize,
+                           (cuuint64_t)h->g.field * h->csize};
+  cuuint32_t boxd[4] = {(cuuint32_t)(P * U), (cuuint32_t)(axis == 1 ? box : 1), (cuuint32_t)(axis == 2 ? box : 1), 1};
+  cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = enc(out, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<void*>(base), dims, strides, boxd, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(SC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return SC_OK;
+}
+
+int check_derr(sc_handle* h) {
+  int e = 0;
+  SC_CUDA(cudaMemcpyAsync(&e, h->derr, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  if (e != 0) {
+    cudaMemsetAsync(h->derr, 0, sizeof(int), h->stream);
+    return fail(SC_ERR_TIMEOUT, "a bounded device wait gave up (TMA load did not complete)");
+  }
+  return SC_OK;
+}
+
+// ---------------------------------------------------------------------------
 // precision-templated implementation
 // ---------------------------------------------------------------------------
 template <typename T> struct Impl {
@@ -194,6 +251,34 @@ template <typename T> struct Impl {
   }
 
   static double kcut2(sc_handle* h) { return h->p.kcut * h->p.kcut; }
+  static int pencil_tile(int logz) { return (sizeof(T) == 4 && logz < 9) ? 16 : 8; }
+
+  // ---- TMA-fed plain strided pass over nf equally spaced fields ----
+  static int plain_tma(sc_handle* h, const char* name, int axis, bool inv, C* base, int nf) {
+    auto* g = &h->g;
+    const int logn = axis == 1 ? h->logy : h->logz;
+    const int N = axis == 1 ? g->ny : g->nz;
+    const int P = L::tma_tile(logn);
+    CUtensorMap map;
+    SC_TRY(encode_fields(h, base, nf, axis, P, N, &map));
+    sc::TmaPass<T> tp{};
+    tp.base = base;
+    tp.field = g->field;
+    tp.axis = axis;
+    tp.axis_stride = axis == 1 ? (long long)g->nxp : (long long)g->ny * g->nxp;
+    tp.outer_stride = axis == 1 ? (long long)g->ny * g->nxp : (long long)g->nxp;
+    tp.nouter = axis == 1 ? g->nz : g->ny;
+    tp.ntx = (g->nxh + P - 1) / P;
+    tp.nf = nf;
+    tp.err = h->derr;
+    return launch(h, name, [&] { return L::plain_tma(logn, inv, map, tp, *g, tw(h, N), h->nsm, h->stream); });
+  }
+  // fields of a FieldList equally spaced from fl.f[0]?
+  static bool spaced(const sc::FieldList<T>& fl, int nf, long long field) {
+    for (int i = 1; i < nf; ++i)
+      if (fl.f[i] != fl.f[0] + (size_t)i * field) return false;
+    return true;
+  }
   static double ktest2(sc_handle* h) {
     const double kt = h->p.kcut / h->p.delta_ratio;
     return kt * kt;
@@ -217,7 +302,13 @@ template <typename T> struct Impl {
     st.fkmax2 = h->p.fkmax * h->p.fkmax;
     st.eps = h->p.eps;
     st.kf_partial = h->kf_partial;
-    st.kf_tiles = h->kf_tiles;
+    // tiles of the zinv kernel that writes the K_f partial sums
+    const int pt = (h->tma && h->tma_zinv && h->p.sgs == SC_SGS_NONE) ? L::tma_ztile(h->logz) : pencil_tile(h->logz);
+    int nt = 0;
+    const int ntiles = (h->g.nxh + pt - 1) / pt;
+    while (nt < ntiles && (double)(nt * pt) * (nt * pt) < h->p.fkmax * h->p.fkmax) ++nt;
+    st.kf_tiles = nt;
+    st.kf_ptile = pt;
     st.kcut2 = kcut2(h);
     st.mask_rhs = h->p.mask_mode == SC_MASK_RHS_AND_STEP;
     st.symmetrize = 1;
@@ -254,8 +345,13 @@ template <typename T> struct Impl {
   // spectral -> packed physical; fields fl[0..nf-1], nf a multiple of 3
   static int inverse(sc_handle* h, const sc::FieldList<T>& fl, int nf) {
     auto* g = &h->g;
-    SC_TRY(launch(h, "zpass_inv", [&] { return L::plain(h->logz, true, fl, zpass_args(h, nf), *g, g->ny, tw(h, g->nz), h->stream); }));
-    SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, fl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+    if (h->tma && spaced(fl, nf, g->field)) {
+      SC_TRY(plain_tma(h, "zpass_inv", 2, true, fl.f[0], nf));
+      SC_TRY(plain_tma(h, "ypass_inv", 1, true, fl.f[0], nf));
+    } else {
+      SC_TRY(launch(h, "zpass_inv", [&] { return L::plain(h->logz, true, fl, zpass_args(h, nf), *g, g->ny, tw(h, g->nz), h->stream); }));
+      SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, fl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+    }
     for (int i = 0; i < nf; i += 3) {
       sc::FieldList<T> sub{};
       for (int c = 0; c < 3; ++c) sub.f[c] = fl.f[i + c];
@@ -270,8 +366,13 @@ template <typename T> struct Impl {
       for (int c = 0; c < 3; ++c) sub.f[c] = fl.f[i + c];
       SC_TRY(launch(h, "xpass_r2c", [&] { return L::xpass(h->logx - 1, sc::XP_R2C3, sub, sub, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
     }
-    SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, fl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
-    SC_TRY(launch(h, "zpass_fwd", [&] { return L::plain(h->logz, false, fl, zpass_args(h, nf), *g, g->ny, tw(h, g->nz), h->stream); }));
+    if (h->tma && spaced(fl, nf, g->field)) {
+      SC_TRY(plain_tma(h, "ypass_fwd", 1, false, fl.f[0], nf));
+      SC_TRY(plain_tma(h, "zpass_fwd", 2, false, fl.f[0], nf));
+    } else {
+      SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, fl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+      SC_TRY(launch(h, "zpass_fwd", [&] { return L::plain(h->logz, false, fl, zpass_args(h, nf), *g, g->ny, tw(h, g->nz), h->stream); }));
+    }
     return SC_OK;
   }
 
@@ -335,11 +436,29 @@ template <typename T> struct Impl {
     za.fs.fkmax2 = h->p.fkmax * h->p.fkmax;
     za.fs.partial = h->kf_partial;
     auto wl = range(h, S_W, nw);
-    SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
-    SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, wl, ypass_args(h, nw), *g, g->nz, tw(h, g->ny), h->stream); }));
-    SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, les ? sc::XP_SMAG : sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
-    SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, wl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
-    SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_stage(h->logz, nf, wl, st, *g, tw(h, g->nz), h->stream); }));
+    const bool sin_spaced = sin[1] == sin[0] + g->field && sin[2] == sin[0] + 2 * g->field;
+    if (h->tma && !les && sin_spaced) {
+      CUtensorMap vmap, lmap;
+      const int PZ = L::tma_ztile(h->logz), P = L::tma_tile(h->logz);
+      SC_TRY(encode_fields(h, sin[0], 3, 2, PZ, g->nz, &vmap));
+      SC_TRY(encode_fields(h, wl.f[0], 3, 2, P, g->nz, &lmap));
+      if (h->tma_zinv)
+        SC_TRY(launch(h, "zinv", [&] { return L::zinv_tma(h->logz, vmap, za, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
+      else
+        SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
+      SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
+      SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
+      SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, st, *g, tw(h, g->nz), h->derr, h->stream); }));
+    } else {
+      SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
+      if (h->tma) SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
+      else SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, wl, ypass_args(h, nw), *g, g->nz, tw(h, g->ny), h->stream); }));
+      SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, les ? sc::XP_SMAG : sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      if (h->tma) SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
+      else SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, wl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
+      SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_stage(h->logz, nf, wl, st, *g, tw(h, g->nz), h->stream); }));
+    }
     if (st.symmetrize && st.mode != sc::SM_LAMB)
       SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));
     return SC_OK;
@@ -644,10 +763,19 @@ int sc_create(const sc_params* pin, sc_handle** out) {
   g.field = (long long)g.nz * g.ny * g.nxp;
   h->csize = p.precision == SC_FP32 ? 8 : 16;
   h->nwork = p.sgs == SC_SGS_NONE ? 6 : (p.sgs == SC_SGS_SMAG ? 12 : 24);
-  const int ptile = p.precision == SC_FP32 ? impl_dispatch_tile<float>(h->logz) : impl_dispatch_tile<double>(h->logz);
-  const int ntiles = (g.nxh + ptile - 1) / ptile;
-  h->kf_tiles = 0;
-  while (h->kf_tiles < ntiles && (double)(h->kf_tiles * ptile) * (h->kf_tiles * ptile) < p.fkmax * p.fkmax) h->kf_tiles++;
+  const int ntiles = (g.nxh + 3) / 4;   // narrowest zinv tile is 4 columns
+  h->kf_ntiles_max = ntiles;
+  {
+    const char* e = std::getenv("SPECNS_NO_TMA");
+    h->tma = !(e && e[0] == '1');
+    const char* z = std::getenv("SPECNS_TMA_ZINV");
+    h->tma_zinv = z && z[0] == '1';
+  }
+  {
+    int dev = 0;
+    SC_CUDA(cudaGetDevice(&dev));
+    SC_CUDA(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
   SC_CUDA(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
   h->stream = h->own;
   const size_t nfields = S_W + h->nwork;
@@ -661,6 +789,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
   SC_CUDA(cudaMalloc(&h->side, 3 * (size_t)g.ny * g.nz * h->csize));
   SC_CUDA(cudaMalloc(&h->kf_partial, sizeof(double) * (size_t)ntiles * g.ny));
   SC_CUDA(cudaMalloc(&h->dscal, sizeof(double) * 8));
+  SC_CUDA(cudaMalloc(&h->derr, sizeof(int)));
+  SC_CUDA(cudaMemset(h->derr, 0, sizeof(int)));
   h->dpart_len = (size_t)1024 * (sc::DQ_N + g.nx / 2) + 2 * 4096;
   SC_CUDA(cudaMalloc(&h->dpart, sizeof(double) * h->dpart_len));
   SC_CUDA(cudaMalloc(&h->dout, sizeof(double) * (sc::DQ_N + g.nx / 2)));
@@ -686,6 +816,7 @@ int sc_destroy(sc_handle* h) {
   cudaFree(h->side);
   cudaFree(h->kf_partial);
   cudaFree(h->dscal);
+  cudaFree(h->derr);
   cudaFree(h->dpart);
   cudaFree(h->dout);
   if (h->own) cudaStreamDestroy(h->own);
@@ -744,6 +875,7 @@ int sc_init_field(sc_handle* h, int seed, int kind, double akp, double u0, doubl
 int sc_rhs(sc_handle* h, void* wx, void* wy, void* wz) {
   if (!h || !wx || !wy || !wz) return fail(SC_ERR_INVALID, "null argument");
   SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rhs_now(h) : Impl<double>::rhs_now(h));
+  SC_TRY(check_derr(h));
   void* w[3] = {wx, wy, wz};
   for (int c = 0; c < 3; ++c) SC_TRY(copy_out(h, w[c], slot(h, S_A + c)));
   SC_CUDA(cudaStreamSynchronize(h->stream));
@@ -755,14 +887,14 @@ int sc_rk4_steps(sc_handle* h, int nsteps) {
   for (int i = 0; i < nsteps; ++i)
     SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rk4_step(h) : Impl<double>::rk4_step(h));
   SC_CUDA(cudaGetLastError());
-  return SC_OK;
+  return check_derr(h);
 }
 
 int sc_ab2_steps(sc_handle* h, int npasses) {
   if (!h || npasses < 0) return fail(SC_ERR_INVALID, "need a handle and npasses >= 0");
   for (int i = 0; i < npasses; ++i)
     SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2_pass(h) : Impl<double>::ab2_pass(h));
-  return SC_OK;
+  return check_derr(h);
 }
 
 int sc_diagnostics(sc_handle* h, sc_diag* d, double* eks) {

@@ -1,0 +1,307 @@
+// TMA-fed strided-axis passes (y and z).
+//
+// A pencil tile -- P consecutive kx columns by the N points of the pencil --
+// is one box of a 4D tensor map (x = kx, y, z, field), so one thread issues
+// the whole tile as one or two cp.async.bulk.tensor loads that land in shared
+// memory already in the FFT engine's layout sm[n*P + p].  Loads complete on
+// an mbarrier; the CTA transforms one buffer while the next tile streams into
+// the other, so HBM stays busy while the FFT stages run.
+//
+//   pencil_tma_kernel : plain y / z pass over nf fields, persistent over
+//                       (tile, outer, field) jobs, double-buffered.
+//   zinv_tma_kernel   : z-inverse pass of the right-hand side: v^ tile (3
+//                       fields) by TMA, the 6 outputs v^, i k x v^ generated
+//                       from shared memory, transformed, stored.
+//   zfwd_tma_kernel   : z-forward pass of the Lamb vector (3 fields by TMA,
+//                       transformed in place) + the spectral update.
+#pragma once
+#include "sc_passes.cuh"
+#include "sc_tma.cuh"
+
+namespace sc {
+
+template <typename T, int LOGN> struct TmaCfg {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int U = sizeof(T) / 4;   // 8-byte units per complex element
+  // tile width: 64-byte rows for long pencils (two buffers fit twice per SM)
+  static constexpr int P = sizeof(T) == 4 ? (LOGN <= 8 ? 16 : 8) : (LOGN <= 8 ? 8 : 4);
+  static constexpr int NT_RAW = P * N / 8;
+  static constexpr int NT = NT_RAW > 512 ? 512 : (NT_RAW < 32 ? 32 : NT_RAW);
+  static constexpr int BOX = N < 256 ? N : 256;   // TMA box extent limit
+  static constexpr int NBOX = N / BOX;
+  using Engine = FFTEngine<T, LOGN, P, P, NT, true>;
+  static constexpr size_t TILE_BYTES = sizeof(C2<T>) * N * P;
+  // pipeline depth of pencil_tma_kernel: tiles in flight per CTA
+  static constexpr int STAGES = TILE_BYTES <= 16384 ? 4 : 3;
+  // zinv uses a narrower tile: 3 inputs + 1 work buffer
+  static constexpr int PZ = P >= 8 ? P / 2 : P;
+  static constexpr int NTZ_RAW = PZ * N / 8;
+  static constexpr int NTZ = NTZ_RAW > 512 ? 512 : (NTZ_RAW < 32 ? 32 : NTZ_RAW);
+  // work buffer padded one slot per 8 points: conflict-free first-stage scatter
+  using EngineZ = FFTEngine<T, LOGN, PZ, PZ, NTZ, true, 3>;
+  static constexpr size_t TILEZ_BYTES = sizeof(C2<T>) * N * PZ;
+  static constexpr size_t WORKZ_BYTES = sizeof(C2<T>) * EngineZ::SMEM_ELEMS;
+};
+
+// Where a pencil lies: element (p, n) of tile (kx0, outer) of field f is
+// base + f*field + outer*outer_stride + n*axis_stride + kx0 + p.
+template <typename T> struct TmaPass {
+  C2<T>* base;            // field 0 of the group
+  long long field;        // elements between fields
+  long long axis_stride;
+  long long outer_stride;
+  int axis;               // 1 = y, 2 = z
+  int nouter;             // number of outer slabs (nz for y, ny for z)
+  int ntx;                // kx tiles
+  int nf;                 // fields
+  int* err;               // device error word
+};
+
+// Issue the loads of one field tile: box (P, BOX, 1) along y or (P, 1, BOX) along z.
+template <typename Cfg>
+__device__ __forceinline__ void tma_issue_tile(void* dst, const CUtensorMap* map, uint64_t* bar, int axis,
+                                               int kx0, int outer, int f, int P, size_t bytes) {
+  mbar_arrive_expect_tx(bar, (uint32_t)bytes);
+  for (int h = 0; h < Cfg::NBOX; ++h) {
+    char* d = static_cast<char*>(dst) + (size_t)h * Cfg::BOX * P * sizeof(C2<float>) * Cfg::U;
+    if (axis == 1) tma_load_4d(d, map, bar, kx0 * Cfg::U, h * Cfg::BOX, outer, f);
+    else tma_load_4d(d, map, bar, kx0 * Cfg::U, outer, h * Cfg::BOX, f);
+  }
+}
+
+template <typename T, int LOGN, bool INV>
+__global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
+pencil_tma_kernel(const __grid_constant__ CUtensorMap map, TmaPass<T> tp, Geom g, const C2<T>* __restrict__ tw) {
+  using Cfg = TmaCfg<T, LOGN>;
+  using E = typename Cfg::Engine;
+  using C = C2<T>;
+  constexpr int P = Cfg::P;
+  constexpr int NS = Cfg::STAGES;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  __shared__ __align__(8) uint64_t bars[NS];
+  const long long total = (long long)tp.ntx * tp.nouter * tp.nf;
+  if (launch_failed(tp.err)) return;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NS; ++b) mbar_init(&bars[b], 1);
+    fence_mbar_init();
+    fence_proxy_async();
+  }
+  __syncthreads();
+  auto buf = [&](int b) { return reinterpret_cast<C*>(smraw + (size_t)b * Cfg::TILE_BYTES); };
+  auto decode = [&](long long job, int& kx0, int& outer, int& f) {
+    f = (int)(job % tp.nf);
+    const long long t = job / tp.nf;
+    kx0 = (int)(t % tp.ntx) * P;
+    outer = (int)(t / tp.ntx);
+  };
+  auto issue = [&](long long job, int b) {
+    int kx0, outer, f;
+    decode(job, kx0, outer, f);
+    tma_issue_tile<Cfg>(buf(b), &map, &bars[b], tp.axis, kx0, outer, f, P, Cfg::TILE_BYTES);
+  };
+  // prologue: the first NS-1 jobs of this CTA in flight
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < NS - 1; ++k) {
+      const long long jk = blockIdx.x + (long long)k * gridDim.x;
+      if (jk < total) issue(jk, k);
+    }
+  }
+  long long job = blockIdx.x;
+  for (int it = 0; job < total; job += gridDim.x, ++it) {
+    const int b = it % NS;
+    const long long ahead = job + (long long)(NS - 1) * gridDim.x;
+    if (threadIdx.x == 0 && ahead < total) {
+      fence_proxy_async();
+      issue(ahead, (it + NS - 1) % NS);
+    }
+    if (!mbar_wait_bounded(&bars[b], (it / NS) & 1, tp.err)) return;
+    C out[E::JL][E::RL];
+    E::template run_smem<INV>(out, buf(b), tw);
+    int kx0, outer, f;
+    decode(job, kx0, outer, f);
+    const int nvalid = min(P, g.nxh - kx0);
+    C* __restrict__ fp = tp.base + f * tp.field + outer * tp.outer_stride + kx0;
+#pragma unroll
+    for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < E::RL; ++r) {
+        int p, n;
+        if (E::out_pos(a, r, p, n) && p < nvalid) fp[n * tp.axis_stride + p] = out[a][r];
+      }
+  }
+}
+
+// z-inverse pass of one right-hand side (DNS): outputs v (3) and w = i k x v (3).
+template <typename T, int LOGN>
+__global__ void __launch_bounds__(TmaCfg<T, LOGN>::NTZ, 3)
+zinv_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldList<T> out, Geom g,
+                const C2<T>* __restrict__ tw, int* err) {
+  using Cfg = TmaCfg<T, LOGN>;
+  using E = typename Cfg::EngineZ;
+  using C = C2<T>;
+  constexpr int P = Cfg::PZ;
+  constexpr int N = Cfg::N;
+  constexpr int NT = Cfg::NTZ;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  C* in[3];
+  for (int c = 0; c < 3; ++c) in[c] = reinterpret_cast<C*>(smraw + c * Cfg::TILEZ_BYTES);
+  C* work = reinterpret_cast<C*>(smraw + 3 * Cfg::TILEZ_BYTES);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double red[NT / 32 + 1];
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+  if (launch_failed(err)) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    mbar_arrive_expect_tx(&bar, (uint32_t)(3 * Cfg::TILEZ_BYTES));
+    for (int c = 0; c < 3; ++c)
+      for (int h = 0; h < Cfg::NBOX; ++h)
+        tma_load_4d(reinterpret_cast<char*>(in[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), &vmap, &bar,
+                    kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+  }
+  __syncthreads();
+  if (!mbar_wait_bounded(&bar, 0, err)) return;
+  // forcing band energy of the stage input (force.f90:16-22), FP64
+  const bool fsum = za.fs.enabled && ((double)kx0 * kx0 + (double)ky * ky < za.fs.fkmax2);
+  if (fsum) {
+    double q = 0.0;
+    for (int e = threadIdx.x; e < P * N; e += NT) {
+      const int p = e % P, n = e / P;
+      const double kx = kx0 + p, kz = wavenum(n, g.nz);
+      const double k2 = kx * kx + (double)ky * ky + kz * kz;
+      if (p < nvalid && k2 < za.fs.fkmax2) {
+        double s = 0.0;
+        for (int c = 0; c < 3; ++c) s += (double)in[c][e].x * in[c][e].x + (double)in[c][e].y * in[c][e].y;
+        q += (kx0 + p == 0) ? 0.5 * s : s;
+      }
+    }
+    double sum = block_sum<NT>(q, red);
+    if (threadIdx.x == 0) za.fs.partial[(long long)blockIdx.x * g.ny + iy] = sum;
+  }
+  for (int f = 0; f < 6; ++f) {
+    C x[E::J1][E::R1], o[E::JL][E::RL];
+#pragma unroll
+    for (int a = 0; a < E::J1; ++a)
+#pragma unroll
+      for (int r = 0; r < E::R1; ++r) {
+        int p, n;
+        E::in_pos(a, r, p, n);
+        const int e = n * P + p;
+        const T kx = (T)(kx0 + p), kz = (T)wavenum(n, g.nz);
+        x[a][r] = zv_gen<ZV_DNS>(f, in[0][e], in[1][e], in[2][e], kx, ky, kz, true);
+      }
+    E::template run<true>(x, o, work, tw);
+    C* __restrict__ fp = out.f[f] + base;
+#pragma unroll
+    for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < E::RL; ++r) {
+        int p, n;
+        if (E::out_pos(a, r, p, n) && p < nvalid) fp[n * zstride + p] = o[a][r];
+      }
+  }
+}
+
+// z-forward pass of the Lamb vector + the spectral update (DNS).
+template <typename T, int LOGN>
+__global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
+zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom g,
+                const C2<T>* __restrict__ tw, int* err) {
+  using Cfg = TmaCfg<T, LOGN>;
+  using E = typename Cfg::Engine;
+  using C = C2<T>;
+  constexpr int P = Cfg::P;
+  constexpr int N = Cfg::N;
+  constexpr int NT = Cfg::NT;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  C* w[3];
+  for (int c = 0; c < 3; ++c) w[c] = reinterpret_cast<C*>(smraw + c * Cfg::TILE_BYTES);
+  __shared__ __align__(8) uint64_t bars[3];
+  __shared__ double s_coef;
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+  if (launch_failed(err)) return;
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < 3; ++c) mbar_init(&bars[c], 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    for (int c = 0; c < 3; ++c) {
+      mbar_arrive_expect_tx(&bars[c], (uint32_t)Cfg::TILE_BYTES);
+      for (int h = 0; h < Cfg::NBOX; ++h)
+        tma_load_4d(reinterpret_cast<char*>(w[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), &lmap, &bars[c],
+                    kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+    }
+  }
+  const bool fblock = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
+  if (fblock && threadIdx.x == 0) {
+    const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
+    s_coef = st.eps / (2.0 * kf);
+  }
+  __syncthreads();
+  for (int c = 0; c < 3; ++c) {
+    if (!mbar_wait_bounded(&bars[c], 0, err)) return;
+    E::template run_inplace<false>(w[c], tw);
+  }
+  // Epilogue in batches of EB points per thread: all state loads of a batch
+  // are issued before any of them is used.
+  constexpr int EB = NT >= 512 ? 2 : 4;
+  for (int e0 = threadIdx.x; e0 < P * N; e0 += NT * EB) {
+    C wv[EB][3], vv[EB][3], av[EB][3];
+    bool act[EB];
+#pragma unroll
+    for (int i = 0; i < EB; ++i) {
+      const int e = e0 + i * NT;
+      const int p = e % P, iz = e / P;
+      act[i] = e < P * N && p < nvalid;
+      if (!act[i]) continue;
+      const long long idx = base + iz * zstride + p;
+      load_state<T>(st, idx, vv[i], av[i]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) wv[i][c] = w[c][e];
+    }
+#pragma unroll
+    for (int i = 0; i < EB; ++i) {
+      if (!act[i]) continue;
+      const int e = e0 + i * NT;
+      const int p = e % P, iz = e / P;
+      const int ix = kx0 + p;
+      const long long idx = base + iz * zstride + p;
+      C* wp = wv[i];
+      if (fblock) {
+        const double kz = wavenum(iz, g.nz);
+        const double k2 = (double)ix * ix + (double)ky * ky + kz * kz;
+        if (k2 < st.fkmax2) {
+          const T ac = (T)s_coef;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) wp[c] = cadd(wp[c], cscale(st.sin[c][idx], ac));
+        }
+      }
+      if (st.symmetrize) {
+        if (ix == 0) {
+          const long long s = ((long long)iz * g.ny + iy) * 3;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) st.side[s + c] = wp[c];
+          if (iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2)) continue;
+        }
+        if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
+          wp[0] = wp[1] = wp[2] = czero<C>();
+      }
+      finish_point_pre<T>(st, g, idx, ix, iy, iz, wp, vv[i], av[i]);
+    }
+  }
+}
+
+}  // namespace sc

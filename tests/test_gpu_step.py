@@ -177,3 +177,19 @@ def test_against_committed_golden_fixtures(specns_lib, prec):
     v0 = [np.ascontiguousarray(a, np.complex128 if prec == S.SC_FP64 else np.complex64) for a in d["v0"]]
     t = S.smag(*v0, float(les["delta"]), 0.0289)
     assert rel_l2(t, list(les["tau_smag"])) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [32, 64])
+def test_rk4_pre_tma_kernels_match(specns_lib, prec, n, monkeypatch):
+    """SPECNS_NO_TMA=1 selects the register-fed strided passes; both paths
+    must give the oracle's answer."""
+    monkeypatch.setenv("SPECNS_NO_TMA", "1")
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3)
+    ref = R.rk4_run(v, g, 2)
+    with handle(n, prec) as h:
+        h.set_state(*v)
+        h.rk4_steps(2)
+        out = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
