@@ -4,6 +4,7 @@
 #include "sc_launch.h"
 #include "sc_ops.cuh"
 #include "sc_tma_passes.cuh"
+#include "sc_xwarp.cuh"
 
 namespace sc {
 
@@ -105,7 +106,32 @@ cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, con
   return cudaGetLastError();
 }
 
+template <typename T, int LOGM>
+cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g, const C2<T>* twM,
+                         const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s) {
+  using Cfg = XwCfg<T, LOGM>;
+  auto k = xpass_warp_kernel<T, LOGM>;
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  if (attr != cudaSuccess) return attr;
+  const long long nb = (xa.rows + Cfg::WARPS - 1) / Cfg::WARPS;
+  k<<<(unsigned)nb, Cfg::NT, Cfg::SMEM, s>>>(fin, fout, g, twM, twN, xa);
+  return cudaGetLastError();
+}
+
 }  // namespace sc
+
+#define SC_DEFINE_XWARP(T, CASES)                                                                \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::xpass_warp(int logm, const FieldList<T>& fin, const FieldList<T>& fout, \
+                                        const Geom& g, const C2<T>* twM, const C2<T>* twN,       \
+                                        const XArgs<T>& xa, cudaStream_t s) {                    \
+    switch (logm) {                                                                              \
+      CASES                                                                                      \
+      default: return cudaErrorNotSupported;                                                     \
+    }                                                                                            \
+  }
+
+#define SC_XWARP_CASE(T, L) case L: return sc::launch_xwarp<T, L>(fin, fout, g, twM, twN, xa, s);
 
 #define SC_TMA_TILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::P;
 #define SC_TMA_ZTILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::PZ;

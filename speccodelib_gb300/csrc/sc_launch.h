@@ -50,6 +50,10 @@ template <typename T> struct Launch {
                               cudaStream_t s);
   static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
                               const C2<T>* tw, int* err, cudaStream_t s);
+  // warp-per-row x-pass (sc_xwarp.cuh), DNS product; cudaErrorNotSupported
+  // for lengths it has no instance for
+  static cudaError_t xpass_warp(int logm, const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g,
+                                const C2<T>* twM, const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s);
 };
 
 }  // namespace sc

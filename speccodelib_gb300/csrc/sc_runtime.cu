@@ -87,6 +87,7 @@ struct sc_handle {
   int nsm = 152;                  // SM count of the device
   bool tma = true;                // TMA-fed strided passes
   bool tma_zinv = false;          // TMA-fed zinv (the register-fed one is faster at 512^3)
+  bool xwarp = true;              // warp-per-row x-pass for the DNS product
   double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch
   double* dpart = nullptr;        // reduction partials
   size_t dpart_len = 0;
@@ -273,6 +274,19 @@ template <typename T> struct Impl {
     tp.err = h->derr;
     return launch(h, name, [&] { return L::plain_tma(logn, inv, map, tp, *g, tw(h, N), h->nsm, h->stream); });
   }
+  // x-pass of the DNS right-hand side: the warp-per-row kernel where it has
+  // an instance for this length, else the block kernel.
+  static int xpass_dns(sc_handle* h, const sc::FieldList<T>& wl) {
+    auto* g = &h->g;
+    return launch(h, "xpass", [&] {
+      if (h->xwarp) {
+        cudaError_t e = L::xpass_warp(h->logx - 1, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+        if (e != cudaErrorNotSupported) return e;
+      }
+      return L::xpass(h->logx - 1, sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+    });
+  }
+
   // fields of a FieldList equally spaced from fl.f[0]?
   static bool spaced(const sc::FieldList<T>& fl, int nf, long long field) {
     for (int i = 1; i < nf; ++i)
@@ -447,14 +461,15 @@ template <typename T> struct Impl {
       else
         SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
       SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
-      SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      SC_TRY(xpass_dns(h, wl));
       SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
       SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, st, *g, tw(h, g->nz), h->derr, h->stream); }));
     } else {
       SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
       if (h->tma) SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
       else SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, wl, ypass_args(h, nw), *g, g->nz, tw(h, g->ny), h->stream); }));
-      SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, les ? sc::XP_SMAG : sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      if (les) SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, sc::XP_SMAG, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      else SC_TRY(xpass_dns(h, wl));
       if (h->tma) SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
       else SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, wl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
       SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_stage(h->logz, nf, wl, st, *g, tw(h, g->nz), h->stream); }));
@@ -770,6 +785,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
     h->tma = !(e && e[0] == '1');
     const char* z = std::getenv("SPECNS_TMA_ZINV");
     h->tma_zinv = z && z[0] == '1';
+    const char* xw = std::getenv("SPECNS_NO_XWARP");
+    h->xwarp = !(xw && xw[0] == '1');
   }
   {
     int dev = 0;
@@ -973,7 +990,7 @@ template <typename T> static int convec_impl(sc_handle* h, const void* const v[3
   auto w6 = I::range(h, S_W, 6);
   SC_TRY(launch(h, "zpass_inv", [&] { return sc::Launch<T>::plain(h->logz, true, w6, I::zpass_args(h, 6), *g, g->ny, I::tw(h, g->nz), h->stream); }));
   SC_TRY(launch(h, "ypass_inv", [&] { return sc::Launch<T>::plain(h->logy, true, w6, I::ypass_args(h, 6), *g, g->nz, I::tw(h, g->ny), h->stream); }));
-  SC_TRY(launch(h, "xpass", [&] { return sc::Launch<T>::xpass(h->logx - 1, sc::XP_DNS, w6, w6, *g, I::tw(h, g->nx / 2), I::tw(h, g->nx), I::xargs(h), h->stream); }));
+  SC_TRY(I::xpass_dns(h, w6));
   SC_TRY(launch(h, "ypass_fwd", [&] { return sc::Launch<T>::plain(h->logy, false, w6, I::ypass_args(h, 3), *g, g->nz, I::tw(h, g->ny), h->stream); }));
   sc::StageArgs<T> st = I::stage_args(h);
   st.mode = sc::SM_LAMB;

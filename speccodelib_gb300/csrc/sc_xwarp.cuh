@@ -1,0 +1,261 @@
+// Warp-per-row x-axis pass of the right-hand side (c2r, Lamb vector, r2c).
+//
+// One warp owns one grid row (y, z): it transforms all six input fields of
+// the row and the three outputs without any block-wide barrier.  An M-point
+// FFT (M = nx/2 complex points, M = E * 32) runs as
+//   radix-E DFT in registers over the 32-strided points of each lane,
+//   twiddles W_M^{lane k1},
+//   transpose through a padded warp-private shared buffer,
+//   radix-E DFT in registers, twiddles W_32^{q u},
+//   (32/E)-point DFT across lanes by radix-2 warp-shuffle butterflies.
+// The inverse (natural in, digit-scrambled out) leaves every field in the
+// same scrambled order, so the Lamb product u x w is formed in registers; the
+// forward transform is the transposed network (scrambled in, natural out).
+//
+// The c2r/r2c of the reference's packed rows (convec_dns.f90:22-47) use the
+// half-length trick: z_m = x_{2m} + i x_{2m+1} is the M-point inverse of
+// Z_k = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) e^{+2 pi i k/N}, and
+// X_k = ((Z_k + conj Z_{M-k}) - i e^{-2 pi i k/N} (Z_k - conj Z_{M-k}))/2.
+#pragma once
+#include "sc_passes.cuh"
+
+namespace sc {
+
+template <typename R> struct W16;
+template <> struct W16<float> {
+  static constexpr float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+  static constexpr float h = 0.70710678118654752440f;
+};
+template <> struct W16<double> {
+  static constexpr double c1 = 0.92387953251128675613, s1 = 0.38268343236508977173;
+  static constexpr double h = 0.70710678118654752440;
+};
+
+// 16-point DFT in registers as 4 x 4 (n = n1 + 4 n2, k = k2 + 4 k1).
+template <bool INV, typename C> __device__ __forceinline__ void dft16(C* v) {
+  using R = decltype(C::x);
+  C a[4][4];
+#pragma unroll
+  for (int n1 = 0; n1 < 4; ++n1) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) a[n1][n2] = v[n1 + 4 * n2];
+    dft4<INV>(a[n1]);   // a[n1][k2]
+  }
+  // twiddles W16^{n1 k2}, exponent e = n1*k2 in 0..9
+#pragma unroll
+  for (int n1 = 1; n1 < 4; ++n1)
+#pragma unroll
+    for (int k2 = 1; k2 < 4; ++k2) {
+      const int e = n1 * k2;
+      R c, s;   // W16^e = cos(2 pi e/16) - i sin(2 pi e/16) (forward)
+      switch (e) {
+        case 1: c = W16<R>::c1; s = W16<R>::s1; break;
+        case 2: c = W16<R>::h; s = W16<R>::h; break;
+        case 3: c = W16<R>::s1; s = W16<R>::c1; break;
+        case 4: c = 0; s = 1; break;
+        case 6: c = -W16<R>::h; s = W16<R>::h; break;
+        default: c = -W16<R>::c1; s = -W16<R>::s1; break;   // e = 9
+      }
+      const C w = mk<C>(c, INV ? s : -s);
+      a[n1][k2] = cmul(a[n1][k2], w);
+    }
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) {
+    C b[4] = {a[0][k2], a[1][k2], a[2][k2], a[3][k2]};
+    dft4<INV>(b);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) v[k2 + 4 * k1] = b[k1];
+  }
+}
+
+template <int E, bool INV, typename C> __device__ __forceinline__ void dftE(C* v) {
+  if constexpr (E == 2) dft2<INV>(v);
+  else if constexpr (E == 4) dft4<INV>(v);
+  else if constexpr (E == 8) dft8<INV>(v);
+  else if constexpr (E == 16) dft16<INV>(v);
+}
+
+template <typename T, int LOGM> struct WarpFFT {
+  using C = C2<T>;
+  static constexpr int M = 1 << LOGM;
+  static constexpr int E = M / 32;          // points per lane
+  static constexpr int Q = 32 / E;          // lanes per row of the second level
+  static constexpr int ROW = 32 + Q;        // padded shared row: conflict-free transpose
+  static constexpr int SMEM = E * ROW;      // complex elements per warp
+
+  __device__ static __forceinline__ C twid(const C* __restrict__ tw, int m, bool inv) {
+    const C w = __ldg(&tw[m]);
+    return inv ? cconj(w) : w;
+  }
+
+  // natural (x[r] = point lane + 32 r) -> scrambled
+  // (x[u] = point k1 + E u + E^2 bitrev(q), k1 = lane / Q, q = lane % Q)
+  template <bool INV>
+  __device__ static __forceinline__ void nat_to_scr(C (&x)[E], C* sm, const C* __restrict__ tw, int lane) {
+    dftE<E, INV>(x);
+#pragma unroll
+    for (int k1 = 1; k1 < E; ++k1) x[k1] = cmul(x[k1], twid(tw, lane * k1, INV));
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) sm[k1 * ROW + lane] = x[k1];
+    __syncwarp();
+    const int k1 = lane / Q, q = lane % Q;
+#pragma unroll
+    for (int t = 0; t < E; ++t) x[t] = sm[k1 * ROW + q + Q * t];
+    __syncwarp();
+    dftE<E, INV>(x);
+#pragma unroll
+    for (int u = 1; u < E; ++u) x[u] = cmul(x[u], twid(tw, q * u * E, INV));
+#pragma unroll
+    for (int h = Q / 2; h >= 1; h >>= 1) {
+      const C w = twid(tw, (q & (h - 1)) * (M / (2 * h)), INV);
+      const bool up = (q & h) != 0;
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        C p;
+        p.x = __shfl_xor_sync(0xffffffffu, x[u].x, h);
+        p.y = __shfl_xor_sync(0xffffffffu, x[u].y, h);
+        x[u] = up ? cmul(csub(p, x[u]), w) : cadd(x[u], p);
+      }
+    }
+  }
+
+  // scrambled -> natural (the transposed network of nat_to_scr)
+  template <bool INV>
+  __device__ static __forceinline__ void scr_to_nat(C (&x)[E], C* sm, const C* __restrict__ tw, int lane) {
+    const int k1 = lane / Q, q = lane % Q;
+#pragma unroll
+    for (int h = 1; h <= Q / 2; h <<= 1) {
+      const C w = twid(tw, (q & (h - 1)) * (M / (2 * h)), INV);
+      const bool up = (q & h) != 0;
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        C p;
+        p.x = __shfl_xor_sync(0xffffffffu, x[u].x, h);
+        p.y = __shfl_xor_sync(0xffffffffu, x[u].y, h);
+        x[u] = up ? csub(p, cmul(w, x[u])) : cadd(x[u], cmul(w, p));
+      }
+    }
+#pragma unroll
+    for (int u = 1; u < E; ++u) x[u] = cmul(x[u], twid(tw, q * u * E, INV));
+    dftE<E, INV>(x);
+#pragma unroll
+    for (int t = 0; t < E; ++t) sm[k1 * ROW + q + Q * t] = x[t];
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < E; ++j) x[j] = sm[j * ROW + lane];
+    __syncwarp();
+#pragma unroll
+    for (int j = 1; j < E; ++j) x[j] = cmul(x[j], twid(tw, lane * j, INV));
+    dftE<E, INV>(x);
+  }
+};
+
+template <typename T, int LOGM> struct XwCfg {
+  static constexpr int WARPS = 8;
+  static constexpr int NT = 32 * WARPS;
+  // per warp: the transpose buffer + the three velocity rows (scrambled order)
+  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + 3 * WarpFFT<T, LOGM>::M;
+  static constexpr size_t SMEM = sizeof(C2<T>) * PER_WARP * WARPS;
+};
+
+// c2r of the 6 operands (u, w), u x w / N^3, r2c of the 3 products.
+template <typename T, int LOGM>
+__global__ void __launch_bounds__(XwCfg<T, LOGM>::NT, 2)
+xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restrict__ twM,
+                  const C2<T>* __restrict__ twN, XArgs<T> xa) {
+  using WF = WarpFFT<T, LOGM>;
+  using C = C2<T>;
+  constexpr int M = WF::M, E = WF::E;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  C* sm = reinterpret_cast<C*>(smraw) + warp * XwCfg<T, LOGM>::PER_WARP;
+  C* us = sm + WF::SMEM;   // u_c at [(c * E + i) * 32 + lane]
+  const long long row = (long long)blockIdx.x * XwCfg<T, LOGM>::WARPS + warp;
+  if (row >= xa.rows) return;
+  const long long off = row * g.nxp;
+
+  // half-length c2r pre-processing of row `f` into natural-order Z
+  auto load_z = [&](int f, C (&x)[E]) {
+    const C* __restrict__ rp = fin.f[f] + off;
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const int k = lane + 32 * r;
+      C xk = rp[k], xm = rp[M - k];
+      if (k == 0) { xk.y = 0; xm.y = 0; }   // DC and Nyquist are real
+      const C e = cadd(xk, cconj(xm));
+      const C o = cmulc(csub(xk, cconj(xm)), __ldg(&twN[k]));
+      x[r] = cadd(e, cmuli(o));
+    }
+  };
+
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    C x[E];
+    load_z(c, x);
+    WF::template nat_to_scr<true>(x, sm, twM, lane);
+#pragma unroll
+    for (int i = 0; i < E; ++i) us[(c * E + i) * 32 + lane] = x[i];
+  }
+  auto U = [&](int c, int i) { return us[(c * E + i) * 32 + lane]; };
+  // Lamb vector accumulated as the vorticity components arrive
+  // (convec_dns.f90:30-38, even points in .x, odd points in .y)
+  C lamb[3][E];
+  {
+    C w[E];
+    load_z(3, w);   // w_x: L_y = u_z w_x - ..., L_z = ... - u_y w_x
+    WF::template nat_to_scr<true>(w, sm, twM, lane);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const C u1 = U(1, i), u2 = U(2, i);
+      lamb[1][i] = mk<C>(u2.x * w[i].x, u2.y * w[i].y);
+      lamb[2][i] = mk<C>(-(u1.x * w[i].x), -(u1.y * w[i].y));
+    }
+    load_z(4, w);   // w_y: L_x = ... - u_z w_y, L_z = u_x w_y - u_y w_x
+    WF::template nat_to_scr<true>(w, sm, twM, lane);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const C u0 = U(0, i), u2 = U(2, i);
+      lamb[0][i] = mk<C>(-(u2.x * w[i].x), -(u2.y * w[i].y));
+      lamb[2][i] = mk<C>(u0.x * w[i].x + lamb[2][i].x, u0.y * w[i].y + lamb[2][i].y);
+    }
+    load_z(5, w);   // w_z: L_x = u_y w_z - u_z w_y, L_y = u_z w_x - u_x w_z
+    WF::template nat_to_scr<true>(w, sm, twM, lane);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const C u0 = U(0, i), u1 = U(1, i);
+      lamb[0][i] = mk<C>(u1.x * w[i].x + lamb[0][i].x, u1.y * w[i].y + lamb[0][i].y);
+      lamb[1][i] = mk<C>(lamb[1][i].x - u0.x * w[i].x, lamb[1][i].y - u0.y * w[i].y);
+    }
+  }
+  const T sc = xa.scale;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    C x[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[i] = cscale(lamb[c][i], sc);
+    WF::template scr_to_nat<false>(x, sm, twM, lane);
+    // r2c post-processing: needs Z_{M-k}; k = lane + 32 r pairs with lane
+    // (32 - lane) % 32, register E-1-r (lane 0: its own register (E - r) % E)
+    C* __restrict__ op = fout.f[c] + off;
+    const int src = (32 - lane) & 31;
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      C zm;
+      zm.x = __shfl_sync(0xffffffffu, x[E - 1 - r].x, src);
+      zm.y = __shfl_sync(0xffffffffu, x[E - 1 - r].y, src);
+      if (lane == 0) zm = x[(E - r) % E];
+      const int k = lane + 32 * r;
+      const C zk = x[r];
+      const C zmc = cconj(zm);
+      const C e = cadd(zk, zmc);
+      const C d = cmul(csub(zk, zmc), __ldg(&twN[k]));
+      op[k] = cscale(csub(e, cmuli(d)), T(0.5));
+      if (k == 0) {   // X_M from Z_0
+        const C d0 = cmul(csub(zk, zmc), __ldg(&twN[M]));
+        op[M] = cscale(csub(e, cmuli(d0)), T(0.5));
+      }
+    }
+  }
+}
+
+}  // namespace sc

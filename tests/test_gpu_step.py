@@ -193,3 +193,21 @@ def test_rk4_pre_tma_kernels_match(specns_lib, prec, n, monkeypatch):
         h.rk4_steps(2)
         out = h.get_state()
     assert rel_l2(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_rhs_block_and_warp_xpass_agree(specns_lib, prec, n, monkeypatch):
+    """The warp-per-row x-pass (nx = 128..512) and the block x-pass give the
+    oracle's right-hand side."""
+    v = hermitian_fields((n, n, n), 41)
+    g = oracle_grid(n)
+    ref = R.ratesdudt(v, g)
+    outs = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_XWARP", env)
+        with handle(n, prec) as h:
+            h.set_state(*v)
+            outs.append(h.rhs())
+    for w in outs:
+        assert rel_l2(w, ref) < TOL[prec]
