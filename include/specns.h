@@ -120,6 +120,17 @@ int sc_rk4_steps(sc_handle* h, int nsteps);
  * the AB2 solver's own: no symmetrize (specdns-forced-omp-ft.f90:180-221). */
 int sc_ab2_steps(sc_handle* h, int npasses);
 
+/* Discrete adjoint of nsteps IF-RK4 steps (DNS right-hand side) for
+ * J = sum over shells kmin..kmax (floor(|k| + 1/2)) of k^2 q(k) at the final
+ * time (q = 1/2-weighted |v|^2, the shell enstrophy).  Writes J and
+ * dJ/dv_0 (host arrays, reference layout): g = dJ/dRe v + i dJ/dIm v for every
+ * stored entry, so dJ = sum Re(conj(g) dv).  The state is checkpointed every
+ * `checkpoint_every` steps and each segment is recomputed once, keeping its
+ * stage inputs, before the backward sweep.  The handle's state is left at v_0.
+ * No counterpart in the reference (its solvers have no adjoint). */
+int sc_adjoint_rk4(sc_handle* h, int nsteps, int checkpoint_every, int kmin, int kmax, void* gx,
+                   void* gy, void* gz, double* J);
+
 /* FP64 diagnostics of the current state; eks (may be NULL) receives the
  * shell spectrum E(k), k = 1..nx/2 (specdns-forced-omp-ft.f90:159-176). */
 int sc_diagnostics(sc_handle* h, sc_diag* d, double* eks);

@@ -743,3 +743,170 @@ def energy2d(wz):
     q[0, 0] = 0.0
     q[:, 0] *= 0.5
     return float(np.sum(q))
+
+
+# --------------------------------------------------------------------------
+# discrete adjoint of the IF-RK4 step (DNS right-hand side)
+#
+# Gradients are with respect to the real and imaginary parts of every stored
+# half-complex entry: g = dJ/dRe(v) + i dJ/dIm(v), so dJ = sum Re(conj(g) dv).
+# --------------------------------------------------------------------------
+def r2c_T(lam, nx):
+    """Transpose of the unnormalised r2c (physical reals -> stored half
+    spectrum) under real inner products: 1/2 c2r with the kx = 0 and kx = nx/2
+    planes doubled."""
+    l = np.array(lam, dtype=np.complex128, copy=True)
+    l[..., 0] *= 2.0
+    l[..., -1] *= 2.0
+    return 0.5 * c2r(l, nx)
+
+
+def c2r_T(mu):
+    """Transpose of the unnormalised c2r: r2c with the interior kx columns
+    doubled (the kx = 0 and kx = nx/2 entries enter c2r once, and only through
+    their real parts)."""
+    X = r2c(mu)
+    X[..., 1:-1] *= 2.0
+    return X
+
+
+def symmetrize3d_T(c):
+    """Transpose of symmetrize3d (real-linear): the conjugate copies on the
+    kx = 0 plane become accumulations into their sources, then the zeroing."""
+    c = np.array(c, dtype=np.complex128, copy=True)
+    nz, ny, nxh = c.shape
+    jz = np.arange(nz // 2 + 1, nz)
+    jy = np.arange(ny)
+    src_y = np.mod(ny - jy, ny)
+    src_z = nz - jz
+    jy2 = np.arange(ny // 2 + 1, ny)
+    # copies were applied in the order (plane part, then kz = 0 line); undo in reverse
+    c[0, ny - jy2, 0] += np.conj(c[0, jy2, 0])
+    c[0, jy2, 0] = 0.0
+    tgt = c[jz[:, None], jy[None, :], 0].copy()
+    np.add.at(c, (src_z[:, None].repeat(ny, 1), src_y[None, :].repeat(len(jz), 0), 0), np.conj(tgt))
+    c[jz[:, None], jy[None, :], 0] = 0.0
+    c[:, ny // 2, :] = 0.0
+    c[nz // 2, :, :] = 0.0
+    c[:, :, nxh - 1] = 0.0
+    c[0, 0, 0] = 0.0
+    return c
+
+
+def cross(a, b):
+    return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+
+def ratesdudt_adj(s, lam_w, grid: Grid):
+    """lam_s = R'(s)^T lam_w for the DNS right-hand side of ratesdudt."""
+    p = grid.p
+    kx, ky, kz, k2 = grid.kx, grid.ky, grid.kz, grid.k2
+    nx, ny, nz = p.nx, p.ny, p.nz
+    N3 = float(nx * ny * nz)
+    mu = list(projection(*lam_w, kx, ky, kz))
+    if p.mask == "rhs_and_step":
+        m = k2 >= p.kcut * p.kcut
+        mu = [np.where(m, 0.0, a) for a in mu]
+    mu = [symmetrize3d_T(a) for a in mu]
+    lam = [np.zeros_like(a) for a in s]
+    if p.forced:
+        kf = forcing_energy(*s, k2, p.fkmax)
+        a = p.eps / (2.0 * kf)
+        m = k2 < p.fkmax * p.fkmax
+        c = sum(float(np.sum(np.where(m, (np.conj(x) * y).real, 0.0))) for x, y in zip(mu, s))
+        w = np.ones(k2.shape)
+        w[:, :, 0] = 0.5
+        lam = [l + np.where(m, a * x - (a * c / kf) * 2.0 * w * y, 0.0) for l, x, y in zip(lam, mu, s)]
+    u = [c2r(a, nx) for a in s]
+    om = [c2r(a, nx) for a in vorticity(*s, kx, ky, kz)]
+    phi = [r2c_T(a, nx) / N3 for a in mu]
+    au = cross(om, phi)
+    aw = cross(phi, u)
+    gu = [c2r_T(a) for a in au]
+    gw = vorticity(*[c2r_T(a) for a in aw], kx, ky, kz)   # the curl is self-adjoint
+    return [l + x + y for l, x, y in zip(lam, gu, gw)]
+
+
+def rk4_step_adj(v, lam_next, grid: Grid):
+    """lam_n = S'(v_n)^T lam_{n+1} for one IF-RK4 step in the division-free
+    form v' = M[E^2 v + (E^2 dt w1 + 2E dt w2 + 2E dt w3 + dt w4)/6]."""
+    p = grid.p
+    dt = p.dt
+    E = np.exp(-p.nu * grid.k2 * dt / 2)
+    s1 = list(v)
+    w1 = ratesdudt(s1, grid)
+    s2 = [E * a + 0.5 * dt * E * b for a, b in zip(v, w1)]
+    w2 = ratesdudt(s2, grid)
+    s3 = [E * a + 0.5 * dt * b for a, b in zip(v, w2)]
+    w3 = ratesdudt(s3, grid)
+    s4 = [E * E * a + E * dt * b for a, b in zip(v, w3)]
+    m = grid.k2 >= p.kcut * p.kcut
+    lt = [np.where(m, 0.0, a) for a in lam_next]
+    lv = [E * E * a for a in lt]
+    lw = [dt / 6.0 * a for a in lt]
+    ls = ratesdudt_adj(s4, lw, grid)
+    lv = [x + E * E * y for x, y in zip(lv, ls)]
+    lw = [2 * E * dt / 6.0 * a + E * dt * b for a, b in zip(lt, ls)]
+    ls = ratesdudt_adj(s3, lw, grid)
+    lv = [x + E * y for x, y in zip(lv, ls)]
+    lw = [2 * E * dt / 6.0 * a + 0.5 * dt * b for a, b in zip(lt, ls)]
+    ls = ratesdudt_adj(s2, lw, grid)
+    lv = [x + E * y for x, y in zip(lv, ls)]
+    lw = [E * E * dt / 6.0 * a + 0.5 * E * dt * b for a, b in zip(lt, ls)]
+    ls = ratesdudt_adj(s1, lw, grid)
+    return [x + y for x, y in zip(lv, ls)]
+
+
+def rk4_step_lawson(v, grid: Grid):
+    """The division-free form of rk4_step (the map rk4_step_adj transposes)."""
+    p = grid.p
+    dt = p.dt
+    E = np.exp(-p.nu * grid.k2 * dt / 2)
+    w1 = ratesdudt(v, grid)
+    w2 = ratesdudt([E * a + 0.5 * dt * E * b for a, b in zip(v, w1)], grid)
+    w3 = ratesdudt([E * a + 0.5 * dt * b for a, b in zip(v, w2)], grid)
+    w4 = ratesdudt([E * E * a + E * dt * b for a, b in zip(v, w3)], grid)
+    out = [E * E * a + dt * (E * E * b + 2 * E * c + 2 * E * d + e) / 6.0
+           for a, b, c, d, e in zip(v, w1, w2, w3, w4)]
+    return mask_state(out, grid)
+
+
+def shell_mask(k2, kmin, kmax):
+    ll = np.floor(np.sqrt(k2) + 0.5)
+    return (ll >= kmin) & (ll <= kmax)
+
+
+def shell_enstrophy(v, k2, kmin=8, kmax=16):
+    """J = sum over shells kmin..kmax of k^2 q(k) (q = 1/2-weighted |v|^2 at kx = 0)."""
+    m = shell_mask(k2, kmin, kmax)
+    q = _q(v)
+    return float(np.sum(np.where(m, k2 * q, 0.0)))
+
+
+def shell_enstrophy_grad(v, k2, kmin=8, kmax=16):
+    m = shell_mask(k2, kmin, kmax)
+    w = np.ones(k2.shape)
+    w[:, :, 0] = 0.5
+    return [np.where(m, 2.0 * w * k2 * a, 0.0) for a in v]
+
+
+def adjoint_gradient(v0, grid: Grid, nsteps, kmin=8, kmax=16, checkpoint=0):
+    """dJ/dv0 for J = shell_enstrophy(v_T) after nsteps Lawson IF-RK4 steps,
+    with checkpoints every `checkpoint` steps (0: keep every state)."""
+    K = checkpoint or nsteps
+    cps = {0: [a.copy() for a in v0]}
+    v = list(v0)
+    for n in range(nsteps):
+        v = rk4_step_lawson(v, grid)
+        if (n + 1) % K == 0 and n + 1 < nsteps:
+            cps[n + 1] = [a.copy() for a in v]
+    lam = shell_enstrophy_grad(v, grid.k2, kmin, kmax)
+    for seg in range((nsteps - 1) // K, -1, -1):
+        n0 = seg * K
+        n1 = min(nsteps, n0 + K)
+        states = [cps[n0]]
+        for n in range(n0, n1 - 1):
+            states.append(rk4_step_lawson(states[-1], grid))
+        for n in range(n1 - 1, n0 - 1, -1):
+            lam = rk4_step_adj(states[n - n0], lam, grid)
+    return lam, shell_enstrophy(v, grid.k2, kmin, kmax)

@@ -5,6 +5,7 @@
 #include "sc_ops.cuh"
 #include "sc_tma_passes.cuh"
 #include "sc_xwarp.cuh"
+#include "sc_adjoint.cuh"
 
 namespace sc {
 
@@ -118,7 +119,46 @@ cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, cons
   return cudaGetLastError();
 }
 
+template <typename T, int LOGN>
+cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const Geom& g, const C2<T>* tw,
+                            cudaStream_t s) {
+  using Cfg = PencilCfg<T, LOGN>;
+  auto k = zfwd_adj_kernel<T, LOGN>;
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
+  k<<<grid, Cfg::NT, Cfg::SMEM, s>>>(fin, aa, g, tw);
+  return cudaGetLastError();
+}
+
 }  // namespace sc
+
+#define SC_ZFWDADJ_CASE(L) case L: return sc::launch_zfwd_adj<ADJ_T, L>(fin, aa, g, tw, s);
+#define SC_DEFINE_ADJ(T)                                                                         \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zfwd_adj(int logn, const FieldList<T>& fin, const AdjArgs<T>& aa,   \
+                                      const Geom& g, const C2<T>* tw, cudaStream_t s) {          \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZFWDADJ_CASE)                                                             \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::adj_copyT(const FieldList<T>& lw, const Geom& g, cudaStream_t s) {  \
+    long long n = (long long)g.ny * g.nz;                                                        \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 4096) nb = 4096;                                                                    \
+    sc::adj_copyT_kernel<T><<<nb, 256, 0, s>>>(lw, g);                                           \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::adj_op(const AdjOpArgs<T>& ao, const Geom& g, cudaStream_t s) {     \
+    long long n = (long long)g.ny * g.nz * g.nxh;                                                \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 152 * 16) nb = 152 * 16;                                                            \
+    sc::adj_op_kernel<T><<<nb, 256, 0, s>>>(ao, g);                                              \
+    return cudaGetLastError();                                                                   \
+  }
 
 #define SC_DEFINE_XWARP(T, CASES)                                                                \
   template <>                                                                                    \
@@ -286,6 +326,7 @@ cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, cons
       case sc::ZV_DNS: return sc::launch_zinv<T, L, sc::ZV_DNS>(za, out, g, tw, s);   \
       case sc::ZV_SMAG: return sc::launch_zinv<T, L, sc::ZV_SMAG>(za, out, g, tw, s); \
       case sc::ZV_DYN: return sc::launch_zinv<T, L, sc::ZV_DYN>(za, out, g, tw, s);   \
+      case sc::ZV_ADJ: return sc::launch_zinv<T, L, sc::ZV_ADJ>(za, out, g, tw, s);   \
       default: return cudaErrorInvalidValue;                                    \
     }
 #define SC_ZINV_CASE_float(L) SC_ZINV_BODY(float, L)
@@ -303,6 +344,7 @@ cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, cons
       case sc::XP_SMAG: return sc::launch_xpass<T, L, sc::XP_SMAG>(fin, fout, g, twM, twN, xa, s); \
       case sc::XP_C2R3: return sc::launch_xpass<T, L, sc::XP_C2R3>(fin, fout, g, twM, twN, xa, s); \
       case sc::XP_R2C3: return sc::launch_xpass<T, L, sc::XP_R2C3>(fin, fout, g, twM, twN, xa, s); \
+      case sc::XP_ADJ: return sc::launch_xpass<T, L, sc::XP_ADJ>(fin, fout, g, twM, twN, xa, s);   \
       default: return cudaErrorInvalidValue;                                          \
     }
 #define SC_XPASS_CASE_float(L) SC_XPASS_BODY(float, L)

@@ -18,6 +18,8 @@ template <typename T> struct SpecOpArgs;
 template <typename T> struct StrainArgs;
 template <typename T> struct PhysArgs;
 template <typename T> struct TmaPass;
+template <typename T> struct AdjArgs;
+template <typename T> struct AdjOpArgs;
 
 template <typename T> struct Launch {
   static int tile();                                   // pencil tile width P
@@ -50,6 +52,11 @@ template <typename T> struct Launch {
                               cudaStream_t s);
   static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
                               const C2<T>* tw, int* err, cudaStream_t s);
+  // discrete adjoint (sc_adjoint.cuh)
+  static cudaError_t zfwd_adj(int logn, const FieldList<T>& fin, const AdjArgs<T>& aa, const Geom& g,
+                              const C2<T>* tw, cudaStream_t s);
+  static cudaError_t adj_copyT(const FieldList<T>& lw, const Geom& g, cudaStream_t s);
+  static cudaError_t adj_op(const AdjOpArgs<T>& ao, const Geom& g, cudaStream_t s);
   // warp-per-row x-pass (sc_xwarp.cuh), DNS product; cudaErrorNotSupported
   // for lengths it has no instance for
   static cudaError_t xpass_warp(int logm, const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g,

@@ -25,6 +25,7 @@ template <typename T> struct DiagArgs {
   double* partial;        // [gridDim.x][DQ_N + nshell]
   double* out;            // [DQ_N + nshell]
   int nblocks;
+  int shell_lo, shell_hi; // shell_hi > 0: only shells lo..hi (floor(|k| + 1/2))
 };
 
 template <typename T>
@@ -57,6 +58,10 @@ __global__ void __launch_bounds__(256) diag_partial_kernel(DiagArgs<T> da, Geom 
     const double kx = ix, ky = wavenum(iy, g.ny), kz = wavenum(iz, g.nz);
     const double k2 = kx * kx + ky * ky + kz * kz;
     if (da.kmax2 >= 0.0 && !(k2 < da.kmax2)) continue;
+    if (da.shell_hi > 0) {
+      const int sh = (int)floor(sqrt(k2) + 0.5);
+      if (sh < da.shell_lo || sh > da.shell_hi) continue;
+    }
     double q = (double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x + (double)b.y * b.y +
                (double)c.x * c.x + (double)c.y * c.y;
     if (!isfinite(q)) nf += 1.0;

@@ -122,11 +122,12 @@ pencil_plain_kernel(FieldList<T> fl, PlainArgs<T> pa, Geom g, const C2<T>* __res
 // ---------------------------------------------------------------------------
 // zinv: z-axis inverse pass generating the physical-space operands from v^
 // ---------------------------------------------------------------------------
-enum ZvMode { ZV_DNS = 0, ZV_SMAG = 1, ZV_DYN = 2 };
+enum ZvMode { ZV_DNS = 0, ZV_SMAG = 1, ZV_DYN = 2, ZV_ADJ = 3 };
 template <int MODE> struct ZvOut;
 template <> struct ZvOut<ZV_DNS> { static constexpr int n = 6; };
 template <> struct ZvOut<ZV_SMAG> { static constexpr int n = 12; };
 template <> struct ZvOut<ZV_DYN> { static constexpr int n = 18; };
+template <> struct ZvOut<ZV_ADJ> { static constexpr int n = 6; };   // + 3 adjoint outputs
 
 struct ForceSum {
   int enabled;
@@ -138,7 +139,37 @@ template <typename T> struct ZvArgs {
   const C2<T>* v[3];
   ForceSum fs;
   double ktest2;     // ZV_DYN: test filter k2 <= ktest2
+  // ZV_ADJ: adjoint of the right-hand side at stage input v, for the RHS
+  // adjoint lam (kx = 0 copies already transposed): outputs 6..8 are
+  // phi^ = D (zero P lam) / (2 N^3), D = 2 on the kx = 0 and kx = nx/2 planes.
+  const C2<T>* lam[3];
+  double* cpartial;  // forcing adjoint: sum over the band of Re(conj(mu) v)
+  int mask_rhs;
+  double kcut2;
+  double inv_n3;
 };
+
+// zero (symmetrize's planes and mean), optional RHS mask, then projection:
+// mu = zero P lam at wavenumber (ix, ky, kz).
+template <typename C, typename R>
+__device__ __forceinline__ void adj_mu(C* m, int ix, int iy, int iz, const Geom& g, int mask_rhs,
+                                       double kcut2) {
+  const R kx = (R)ix, ky = (R)wavenum(iy, g.ny), kz = (R)wavenum(iz, g.nz);
+  const R k2 = kx * kx + ky * ky + kz * kz;
+  const bool zero = iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0) ||
+                    (mask_rhs && (double)k2 >= kcut2);
+  if (zero) {
+    m[0] = m[1] = m[2] = czero<C>();
+    return;
+  }
+  if (k2 > R(0)) {
+    C t = cadd(cadd(cscale(m[0], kx), cscale(m[1], ky)), cscale(m[2], kz));
+    t = mk<C>(t.x / k2, t.y / k2);
+    m[0] = csub(m[0], cscale(t, kx));
+    m[1] = csub(m[1], cscale(t, ky));
+    m[2] = csub(m[2], cscale(t, kz));
+  }
+}
 
 // Output field `f` of the generator at wavenumber (kx, ky, kz).
 //   ZV_DNS : v (3), w = i k x v (3)                      dns-deform.f90:265-273
@@ -235,7 +266,7 @@ zinv_vel_kernel(ZvArgs<T> za, FieldList<T> out, Geom g, const C2<T>* __restrict_
           const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
           gin = k2 <= za.ktest2;
         }
-        in[a][r] = zv_gen<MODE>(f, vr[a][r][0], vr[a][r][1], vr[a][r][2], kx, ky, kz, gin);
+        in[a][r] = zv_gen<MODE == ZV_ADJ ? ZV_DNS : MODE>(f, vr[a][r][0], vr[a][r][1], vr[a][r][2], kx, ky, kz, gin);
       }
     E::template run<true>(in, o, sm, tw);
     C* __restrict__ fp = out.f[f] + base;
@@ -246,6 +277,55 @@ zinv_vel_kernel(ZvArgs<T> za, FieldList<T> out, Geom g, const C2<T>* __restrict_
         int p, n;
         if (E::out_pos(a, r, p, n) && p < nvalid) fp[n * zstride + p] = o[a][r];
       }
+  }
+  if constexpr (MODE == ZV_ADJ) {
+    // mu = zero P lam; the band sum c = sum Re(conj(mu) v) for the forcing
+    // adjoint; outputs phi^ = D mu / (2 N^3)
+    double q = 0.0;
+#pragma unroll
+    for (int a = 0; a < E::J1; ++a)
+#pragma unroll
+      for (int r = 0; r < E::R1; ++r) {
+        int p, n;
+        bool ok = E::in_pos(a, r, p, n) && p < nvalid;
+        C m[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) m[c] = ok ? za.lam[c][base + n * zstride + p] : czero<C>();
+        if (ok) adj_mu<C, T>(m, kx0 + p, iy, n, g, za.mask_rhs, za.kcut2);
+        if (fsum && ok) {
+          const double kx = kx0 + p, kz = wavenum(n, g.nz);
+          if (kx * kx + (double)ky * ky + kz * kz < za.fs.fkmax2)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const C sv = za.v[c][base + n * zstride + p];
+              q += (double)m[c].x * sv.x + (double)m[c].y * sv.y;
+            }
+        }
+        const int ix = kx0 + p;
+        const T d = (T)((ix == 0 || ix == g.nxh - 1) ? za.inv_n3 : 0.5 * za.inv_n3);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vr[a][r][c] = cscale(m[c], d);
+      }
+    if (fsum) {
+      double s2 = block_sum<NT>(q, red);
+      if (threadIdx.x == 0) za.cpartial[(long long)blockIdx.x * g.ny + iy] = s2;
+    }
+    for (int c = 0; c < 3; ++c) {
+      C in[E::J1][E::R1], o[E::JL][E::RL];
+#pragma unroll
+      for (int a = 0; a < E::J1; ++a)
+#pragma unroll
+        for (int r = 0; r < E::R1; ++r) in[a][r] = c == 0 ? vr[a][r][0] : (c == 1 ? vr[a][r][1] : vr[a][r][2]);
+      E::template run<true>(in, o, sm, tw);
+      C* __restrict__ fp = out.f[6 + c] + base;
+#pragma unroll
+      for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+        for (int r = 0; r < E::RL; ++r) {
+          int p, n;
+          if (E::out_pos(a, r, p, n) && p < nvalid) fp[n * zstride + p] = o[a][r];
+        }
+    }
   }
 }
 
@@ -261,7 +341,8 @@ enum StageMode {
 
 template <typename T> struct StageArgs {
   int mode;
-  C2<T>* v[3];          // state v^_n (read; written by the final stage)
+  C2<T>* v[3];          // state v^_n (read)
+  C2<T>* vout[3];       // where the final stage writes v^_{n+1} (normally == v)
   const C2<T>* sin[3];  // stage input (forcing reads it)
   C2<T>* sout[3];       // next stage input
   C2<T>* acc[3];        // RK accumulator / AB2 history
@@ -348,7 +429,7 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
       for (int c = 0; c < 3; ++c) {
         const C a = cadd(av[c], cscale(w[c], dt));
         C vn = cadd(cscale(vv[c], E2), cscale(a, T(1) / T(6)));
-        st.v[c][idx] = cut ? czero<C>() : vn;
+        st.vout[c][idx] = cut ? czero<C>() : vn;
       }
       break;
     case SM_AB2_EULER:  // v = (v + dt/2 w) sqrt(expk2) ; history = w
@@ -356,14 +437,14 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
       for (int c = 0; c < 3; ++c) {
         C vn = cscale(cadd(vv[c], cscale(w[c], hdt)), E);
         st.acc[c][idx] = w[c];
-        st.v[c][idx] = zero_mean_cut ? czero<C>() : vn;
+        st.vout[c][idx] = zero_mean_cut ? czero<C>() : vn;
       }
       break;
     case SM_AB2_MID:  // v = v0 expk2 + dt w sqrt(expk2)   (history kept)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         C vn = cadd(cscale(vv[c], E2), cscale(w[c], dt * E));
-        st.v[c][idx] = zero_mean_cut ? czero<C>() : vn;
+        st.vout[c][idx] = zero_mean_cut ? czero<C>() : vn;
       }
       break;
     case SM_AB2:  // v = (v + (3 w - expk2 o) dt/2) expk2 ; o = w
@@ -372,7 +453,7 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
         C d = csub(cscale(w[c], T(3)), cscale(av[c], E2));
         C vn = cscale(cadd(vv[c], cscale(d, hdt)), E2);
         st.acc[c][idx] = w[c];
-        st.v[c][idx] = zero_mean_cut ? czero<C>() : vn;
+        st.vout[c][idx] = zero_mean_cut ? czero<C>() : vn;
       }
       break;
     default:
@@ -558,12 +639,13 @@ __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
 // ---------------------------------------------------------------------------
 // xpass: per-row c2r, physical-space product, r2c
 // ---------------------------------------------------------------------------
-enum XpMode { XP_DNS = 0, XP_SMAG = 1, XP_C2R3 = 2, XP_R2C3 = 3 };
+enum XpMode { XP_DNS = 0, XP_SMAG = 1, XP_C2R3 = 2, XP_R2C3 = 3, XP_ADJ = 4 };
 template <int MODE> struct XpIO;
 template <> struct XpIO<XP_DNS> { static constexpr int fin = 6, fout = 3; };
 template <> struct XpIO<XP_SMAG> { static constexpr int fin = 12, fout = 9; };
 template <> struct XpIO<XP_C2R3> { static constexpr int fin = 3, fout = 3; };
 template <> struct XpIO<XP_R2C3> { static constexpr int fin = 3, fout = 3; };
+template <> struct XpIO<XP_ADJ> { static constexpr int fin = 9, fout = 6; };   // (u, w, phi) -> (w x phi, phi x u)
 
 template <typename T> struct XArgs {
   T scale;                 // 1/(nx ny nz)
@@ -666,7 +748,13 @@ xpass_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restric
           const int gq = p / RB, rl = p % RB;
           const C* row = sm + EA::sidx(m) * PSA + rl;
           auto U = [&](int c) { return row[c * RB]; };
-          if (gq < 3) {
+          if (MODE == XP_ADJ) {
+            // adjoint of the Lamb product: a_u = w x phi, a_w = phi x u
+            const int c1 = (gq + 1) % 3, c2 = (gq + 2) % 3;
+            const int A = gq < 3 ? 3 : 6, B = gq < 3 ? 6 : 0;
+            const C pa = U(A + c1), pb = U(A + c2), qa = U(B + c1), qb = U(B + c2);
+            res = mk<C>(pa.x * qb.x - pb.x * qa.x, pa.y * qb.y - pb.y * qa.y);
+          } else if (gq < 3) {
             // convec_dns.f90:30-42: Lamb vector u x w on even (re) / odd (im) points
             const int c1 = (gq + 1) % 3, c2 = (gq + 2) % 3;
             const C ua = U(c1), ub = U(c2), wa = U(3 + c1), wb = U(3 + c2);

@@ -27,6 +27,7 @@
 #include "sc_launch.h"
 #include "sc_ops.cuh"
 #include "sc_tma_passes.cuh"
+#include "sc_adjoint.cuh"
 
 namespace {
 
@@ -92,6 +93,10 @@ struct sc_handle {
   double* dpart = nullptr;        // reduction partials
   size_t dpart_len = 0;
   double* dout = nullptr;         // reduction outputs
+  // discrete adjoint (allocated on first use)
+  void* adj = nullptr;            // work 9 | lam, lt, lv, lw | stage store | checkpoints
+  size_t adj_fields = 0;
+  double* cpart = nullptr;        // forcing-adjoint band sums
   long long step = 0;             // RK4 steps taken (dynamic-coefficient cadence)
   int ab2_pass = 0;
   // profiling
@@ -302,6 +307,7 @@ template <typename T> struct Impl {
     sc::StageArgs<T> st{};
     for (int c = 0; c < 3; ++c) {
       st.v[c] = F(h, S_V + c);
+      st.vout[c] = F(h, S_V + c);
       st.sout[c] = F(h, S_S + c);
       st.acc[c] = F(h, S_A + c);
       st.w[c] = F(h, S_A + c);
@@ -519,6 +525,167 @@ template <typename T> struct Impl {
     SC_TRY(maybe_dyn(h, vin, true));
     SC_TRY(rhs_pipeline(h, vin, st));
     h->ab2_pass += 1;
+    return SC_OK;
+  }
+
+  // ---- one IF-RK4 step with every stage input kept: st[0] = v_n (read),
+  // st[1..3] = s2..s4 (written), v_{n+1} written to vout ----
+  static int rk4_step_store(sc_handle* h, C* const st[4][3], C* const vout[3]) {
+    sc::StageArgs<T> a = stage_args(h);
+    for (int c = 0; c < 3; ++c) { a.v[c] = st[0][c]; a.vout[c] = vout[c]; }
+    for (int k = 0; k < 3; ++k) {
+      a.mode = sc::SM_RK1 + k;
+      for (int c = 0; c < 3; ++c) a.sout[c] = st[k + 1][c];
+      const C* sin[3] = {st[k][0], st[k][1], st[k][2]};
+      SC_TRY(rhs_pipeline(h, sin, a));
+    }
+    a.mode = sc::SM_RK4;
+    const C* sin[3] = {st[3][0], st[3][1], st[3][2]};
+    return rhs_pipeline(h, sin, a);
+  }
+
+  static C* AF(sc_handle* h, size_t i) { return reinterpret_cast<C*>(h->adj) + i * h->g.field; }
+
+  // adjoint of one right-hand side at stage input s; aa.lw holds its adjoint
+  static int adj_rhs(sc_handle* h, sc::AdjArgs<T> aa) {
+    auto* g = &h->g;
+    sc::FieldList<T> lw{};
+    for (int c = 0; c < 3; ++c) lw.f[c] = aa.lw[c];
+    SC_TRY(launch(h, "adj_copyT", [&] { return L::adj_copyT(lw, *g, h->stream); }));
+    sc::ZvArgs<T> za{};
+    for (int c = 0; c < 3; ++c) { za.v[c] = aa.s[c]; za.lam[c] = aa.lw[c]; }
+    za.fs.enabled = h->p.forced;
+    za.fs.fkmax2 = h->p.fkmax * h->p.fkmax;
+    za.fs.partial = h->kf_partial;
+    za.cpartial = h->cpart;
+    za.mask_rhs = h->p.mask_mode == SC_MASK_RHS_AND_STEP;
+    za.kcut2 = kcut2(h);
+    za.inv_n3 = 1.0 / ((double)g->nx * g->ny * g->nz);
+    sc::FieldList<T> w9{};
+    for (int i = 0; i < 9; ++i) w9.f[i] = AF(h, i);
+    SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_ADJ, za, w9, *g, tw(h, g->nz), h->stream); }));
+    if (h->tma) SC_TRY(plain_tma(h, "adj_ypass_inv", 1, true, w9.f[0], 9));
+    else SC_TRY(launch(h, "adj_ypass_inv", [&] { return L::plain(h->logy, true, w9, ypass_args(h, 9), *g, g->nz, tw(h, g->ny), h->stream); }));
+    SC_TRY(launch(h, "adj_xpass", [&] { return L::xpass(h->logx - 1, sc::XP_ADJ, w9, w9, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+    if (h->tma) SC_TRY(plain_tma(h, "adj_ypass_fwd", 1, false, w9.f[0], 6));
+    else SC_TRY(launch(h, "adj_ypass_fwd", [&] { return L::plain(h->logy, false, w9, ypass_args(h, 6), *g, g->nz, tw(h, g->ny), h->stream); }));
+    aa.kf_partial = h->kf_partial;
+    aa.c_partial = h->cpart;
+    const int pt = pencil_tile(h->logz);
+    int nt = 0;
+    const int ntiles = (g->nxh + pt - 1) / pt;
+    while (nt < ntiles && (double)(nt * pt) * (nt * pt) < h->p.fkmax * h->p.fkmax) ++nt;
+    aa.kf_tiles = nt;
+    aa.kf_ptile = pt;
+    return launch(h, "adj_zfwd", [&] { return L::zfwd_adj(h->logz, w9, aa, *g, tw(h, g->nz), h->stream); });
+  }
+
+  // lam_n = S'(v_n)^T lam_{n+1}; st = the step's stage inputs; lam in slots 9..11
+  static int adj_step(sc_handle* h, C* const st[4][3]) {
+    auto* g = &h->g;
+    sc::AdjOpArgs<T> ao{};
+    ao.op = sc::AO_INIT;
+    for (int c = 0; c < 3; ++c) { ao.in[c] = AF(h, 9 + c); ao.out1[c] = AF(h, 12 + c); ao.out2[c] = AF(h, 18 + c); }
+    ao.dt = (T)h->p.dt;
+    ao.kcut2 = kcut2(h);
+    SC_TRY(launch(h, "adj_init", [&] { return L::adj_op(ao, *g, h->stream); }));
+    sc::AdjArgs<T> aa{};
+    for (int c = 0; c < 3; ++c) {
+      aa.lam[c] = AF(h, 9 + c);
+      aa.lt[c] = AF(h, 12 + c);
+      aa.lv[c] = AF(h, 15 + c);
+      aa.lw[c] = AF(h, 18 + c);
+    }
+    aa.ex = reinterpret_cast<const T*>(h->ex);
+    aa.ey = reinterpret_cast<const T*>(h->ey);
+    aa.ez = reinterpret_cast<const T*>(h->ez);
+    aa.dt = (T)h->p.dt;
+    aa.forced = h->p.forced;
+    aa.fkmax2 = h->p.fkmax * h->p.fkmax;
+    aa.eps = h->p.eps;
+    aa.mask_rhs = h->p.mask_mode == SC_MASK_RHS_AND_STEP;
+    aa.kcut2 = kcut2(h);
+    for (int stage = 4; stage >= 1; --stage) {
+      aa.stage = stage;
+      for (int c = 0; c < 3; ++c) aa.s[c] = st[stage - 1][c];
+      SC_TRY(adj_rhs(h, aa));
+    }
+    return SC_OK;
+  }
+
+  static int adjoint(sc_handle* h, int nsteps, int K, int kmin, int kmax, double* J) {
+    auto* g = &h->g;
+    if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the adjoint covers the DNS right-hand side (sgs = none)");
+    if (nsteps < 1 || K < 1) return fail(SC_ERR_INVALID, "need nsteps >= 1 and checkpoint interval >= 1");
+    if (K > nsteps) K = nsteps;
+    const int ncp = (nsteps + K - 1) / K;
+    const size_t need = 21 + 12 * (size_t)K + 3 * (size_t)ncp;
+    if (h->adj_fields < need) {
+      cudaFree(h->adj);
+      h->adj = nullptr;
+      h->adj_fields = 0;
+      SC_CUDA(cudaMalloc(&h->adj, need * g->field * h->csize));
+      SC_CUDA(cudaMemsetAsync(h->adj, 0, need * g->field * h->csize, h->stream));
+      h->adj_fields = need;
+      if (!h->cpart) SC_CUDA(cudaMalloc(&h->cpart, sizeof(double) * (size_t)h->kf_ntiles_max * g->ny));
+    }
+    const size_t st0 = 21, cp0 = 21 + 12 * (size_t)K;
+    auto store = [&](int i, int k, int c) { return AF(h, st0 + 12 * (size_t)i + 3 * k + c); };
+    auto cpf = [&](int j, int c) { return AF(h, cp0 + 3 * (size_t)j + c); };
+    const size_t fb = h->csize * g->field;
+    for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(cpf(0, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+    const long long step0 = h->step;
+    for (int n = 0; n < nsteps; ++n) {
+      SC_TRY(rk4_step(h));
+      if ((n + 1) % K == 0 && n + 1 < nsteps)
+        for (int c = 0; c < 3; ++c)
+          SC_CUDA(cudaMemcpyAsync(cpf((n + 1) / K, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    // J and dJ/dv_T
+    {
+      sc::DiagArgs<T> da{};
+      for (int c = 0; c < 3; ++c) da.v[c] = F(h, S_V + c);
+      da.kmax2 = -1.0;
+      const long long rows = (long long)g->ny * g->nz;
+      da.rows_per_block = (int)std::max<long long>(1, rows / 1024);
+      da.nblocks = (int)((rows + da.rows_per_block - 1) / da.rows_per_block);
+      da.partial = h->dpart;
+      da.out = h->dout;
+      da.shell_lo = kmin;
+      da.shell_hi = kmax;
+      SC_TRY(launch(h, "diag", [&] { return L::diag(da, *g, h->stream); }));
+      double out[sc::DQ_N];
+      SC_CUDA(cudaMemcpyAsync(out, h->dout, sizeof out, cudaMemcpyDeviceToHost, h->stream));
+      SC_CUDA(cudaStreamSynchronize(h->stream));
+      if (J) *J = out[sc::DQ_K2Q];
+      sc::AdjOpArgs<T> ao{};
+      ao.op = sc::AO_SHELL_GRAD;
+      ao.kmin = kmin;
+      ao.kmax = kmax;
+      for (int c = 0; c < 3; ++c) { ao.in[c] = F(h, S_V + c); ao.out1[c] = AF(h, 9 + c); }
+      SC_TRY(launch(h, "adj_grad", [&] { return L::adj_op(ao, *g, h->stream); }));
+    }
+    for (int seg = ncp - 1; seg >= 0; --seg) {
+      const int n0 = seg * K, len = std::min(nsteps, n0 + K) - n0;
+      for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(store(0, 0, c), cpf(seg, c), fb, cudaMemcpyDeviceToDevice, h->stream));
+      for (int i = 0; i < len; ++i) {
+        C* st[4][3];
+        for (int k = 0; k < 4; ++k)
+          for (int c = 0; c < 3; ++c) st[k][c] = store(i, k, c);
+        C* vo[3];
+        for (int c = 0; c < 3; ++c) vo[c] = (i + 1 < len) ? store(i + 1, 0, c) : F(h, S_V + c);
+        SC_TRY(rk4_step_store(h, st, vo));
+      }
+      for (int i = len - 1; i >= 0; --i) {
+        C* st[4][3];
+        for (int k = 0; k < 4; ++k)
+          for (int c = 0; c < 3; ++c) st[k][c] = store(i, k, c);
+        SC_TRY(adj_step(h, st));
+      }
+    }
+    // restore the state v_0
+    for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(F(h, S_V + c), cpf(0, c), fb, cudaMemcpyDeviceToDevice, h->stream));
+    h->step = step0;
     return SC_OK;
   }
 
@@ -836,6 +1003,8 @@ int sc_destroy(sc_handle* h) {
   cudaFree(h->derr);
   cudaFree(h->dpart);
   cudaFree(h->dout);
+  cudaFree(h->adj);
+  cudaFree(h->cpart);
   if (h->own) cudaStreamDestroy(h->own);
   delete h;
   return SC_OK;
@@ -912,6 +1081,21 @@ int sc_ab2_steps(sc_handle* h, int npasses) {
   for (int i = 0; i < npasses; ++i)
     SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2_pass(h) : Impl<double>::ab2_pass(h));
   return check_derr(h);
+}
+
+int sc_adjoint_rk4(sc_handle* h, int nsteps, int checkpoint_every, int kmin, int kmax, void* gx, void* gy,
+                   void* gz, double* J) {
+  if (!h) return fail(SC_ERR_INVALID, "null handle");
+  SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::adjoint(h, nsteps, checkpoint_every, kmin, kmax, J)
+                                   : Impl<double>::adjoint(h, nsteps, checkpoint_every, kmin, kmax, J));
+  SC_TRY(check_derr(h));
+  if (gx && gy && gz) {
+    void* gr[3] = {gx, gy, gz};
+    for (int c = 0; c < 3; ++c)
+      SC_TRY(copy_out(h, gr[c], static_cast<char*>(h->adj) + (size_t)(9 + c) * h->g.field * h->csize));
+  }
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
 }
 
 int sc_diagnostics(sc_handle* h, sc_diag* d, double* eks) {

@@ -241,6 +241,15 @@ class SpectralNS:
         _check(lib().sc_diagnostics(self.h, C.byref(d), eks.ctypes.data_as(C.c_void_p)))
         return d.as_dict(), eks
 
+    def adjoint(self, nsteps, checkpoint_every=20, kmin=8, kmax=16):
+        """(J, grad) for J = shell enstrophy after nsteps RK4 steps; grad =
+        dJ/dRe v0 + i dJ/dIm v0 in the reference layout."""
+        g = [self.empty() for _ in range(3)]
+        J = C.c_double(0)
+        _check(lib().sc_adjoint_rk4(self.h, nsteps, checkpoint_every, kmin, kmax,
+                                    *[_ptr(a, True) for a in g], C.byref(J)))
+        return J.value, tuple(g)
+
     def profile_enable(self, on=True):
         _check(lib().sc_profile_enable(self.h, 1 if on else 0))
 
