@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -311,12 +312,48 @@ def run_ours(a):
         del h64
         fp64 = {"steps_per_s": k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64,
                 "speedup_fp32_over_fp64": (value / world) / (k64 / (ms64 / 1e3))}
-        m = e64 > 1e-30
+        # shells holding energy above the FP32 round-off floor of the total
+        m = e64 > 1e-10 * float(np.sum(e64))
         fp64["fp32_vs_fp64_after_2_steps"] = {
             "Ek_max_rel_err": float(np.max(np.abs(e32[m] - e64[m]) / e64[m])),
+            "Ek_shells_compared": int(np.sum(m)),
+            "Ek_max_abs_err_over_total": float(np.max(np.abs(e32 - e64)) / float(np.sum(e64))),
             "dissipation_rel_err": abs(d32["dissipation"] - d64["dissipation"]) / d64["dissipation"],
             "energy_rel_err": abs(d32["energy"] - d64["energy"]) / d64["energy"],
             "max_div_fp32": d32["max_div"], "max_div_fp64": d64["max_div"]}
+
+    # ---- discrete adjoint cost (256^3 FP32, T = 200, checkpoints every 20) ----
+    adjoint = None
+    if not a.no_adjoint:
+        na, Ta, Ka = 256, 200, 20
+        p = S.default_params(na, S.SC_FP32, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX)
+        ha = S.SpectralNS(p)
+        ha.set_stream(stream.cuda_stream)
+        ha.init_field(seed=SEED, akp=AKP, u0=U0)
+        init_a = ha.get_state()
+        ha.rk4_steps(3)
+        ha.set_state(*init_a)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ha.rk4_steps(Ta)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        ha.set_state(*init_a)
+        ha.adjoint(Ta, Ka, kmin=8, kmax=16)   # warm-up (allocates the checkpoint store)
+        ha.set_state(*init_a)
+        t0 = time.perf_counter()
+        Ja, _ = ha.adjoint(Ta, Ka, kmin=8, kmax=16)
+        torch.cuda.synchronize()
+        t_adj = time.perf_counter() - t0
+        ha.close()
+        del ha, init_a
+        adjoint = {"grid": na, "steps": Ta, "checkpoint_every": Ka, "J": Ja,
+                   "forward_ms_per_step": 1e3 * t_fwd / Ta,
+                   "adjoint_call_ms_per_step": 1e3 * t_adj / Ta,
+                   "cost_ratio_total": t_adj / t_fwd,
+                   "cost_ratio_backward": (t_adj - t_fwd) / t_fwd,
+                   "note": "adjoint call = forward with checkpoints + per-segment recompute + backward sweep"}
+        torch.cuda.empty_cache()
 
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
@@ -343,6 +380,7 @@ def run_ours(a):
                "clocks": clocks,
                "e2e": e2e,
                "fp64": fp64,
+               "adjoint": adjoint,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if dist:

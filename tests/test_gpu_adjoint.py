@@ -69,3 +69,47 @@ def test_adjoint_fp32_against_fp64(specns_lib):
             h.set_state(*v)
             grads.append(h.adjoint(T, K, kmin=8, kmax=16)[1])
     assert rel_l2(grads[1], grads[0]) < 1e-4
+
+
+def solenoidal_direction(n, rng):
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    d = [R.r2c(rng.standard_normal((n, n, n))) / n ** 3 for _ in range(3)]
+    d = list(R.projection(*d, kx, ky, kz))
+    d = [R.symmetrize3d(a) for a in d]
+    return [np.where(k2 >= (2 * (n // 2) / 3) ** 2, 0.0, a) for a in d]
+
+
+@pytest.mark.slow
+def test_adjoint_sensitivity_config_128(specns_lib):
+    """Gradient of the final-time enstrophy over shells 8..16 after T = 200
+    RK4 steps at 128^3, checkpoints every K = 20 steps: the FP64 adjoint
+    against central differences along 16 seeded random solenoidal directions
+    (step 1e-4 relative, FP64 forward), and the FP32 adjoint against FP64."""
+    n, T, K = 128, 200, 20
+    v = solenoidal_init(n)
+    _, _, _, k2 = R.wavenumber(n, n, n)
+    grads = {}
+    for prec in (S.SC_FP64, S.SC_FP32):
+        with S.SpectralNS(S.default_params(n, prec)) as h:
+            h.set_state(*v)
+            grads[prec] = h.adjoint(T, K, kmin=8, kmax=16)
+    J, g64 = grads[S.SC_FP64]
+    g32 = grads[S.SC_FP32][1]
+    assert rel_l2(g32, g64) < 1e-3
+    rng = np.random.default_rng(2024)
+    vn = np.sqrt(sum(float(np.sum(np.abs(a) ** 2)) for a in v))
+    worst64 = worst32 = 0.0
+    with S.SpectralNS(S.default_params(n, S.SC_FP64)) as h:
+        def Jof(vv):
+            h.set_state(*vv)
+            h.rk4_steps(T)
+            return R.shell_enstrophy(h.get_state(), k2, 8, 16)
+        for _ in range(16):
+            d = solenoidal_direction(n, rng)
+            dn = np.sqrt(sum(float(np.sum(np.abs(a) ** 2)) for a in d))
+            eps = 1e-4 * vn / dn
+            fd = (Jof([a + eps * b for a, b in zip(v, d)]) - Jof([a - eps * b for a, b in zip(v, d)])) / (2 * eps)
+            worst64 = max(worst64, abs(dot(g64, d) - fd) / abs(fd))
+            worst32 = max(worst32, abs(dot(g32, d) - fd) / abs(fd))
+    assert worst64 < 1e-6
+    assert worst32 < 1e-3
