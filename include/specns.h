@@ -147,6 +147,36 @@ int sc_step_bytes(sc_handle* h, double* bytes_per_step);
 
 const char* sc_last_error(void);
 
+/* ---------------------------------------------------------------------
+ * Batched 2D vorticity ensembles.  Independent periodic 2D runs of mixed
+ * size N (powers of two, 64..1024) advance together: vorticity w^ (N, N/2+1
+ * complex, kx fastest), u^ = i ky w^/k^2, v^ = -i kx w^/k^2, nonlinear term
+ * -(i kx (u w)^ + i ky (v w)^) with symmetrize2d (symmetrize.f90:8-30) and
+ * the 2/3 mask, linear damping alpha and hyperviscosity nu8 (del^8) through
+ * the integrating factor exp(-(alpha + nu8 k^8) dt/2) in the IF-RK4.  The
+ * physics restates the reference's 2D solvers (spectral_dns_2d.f90:94,160-188,
+ * turb_2d.f90:288-403); the reference has no ensemble driver.
+ * ------------------------------------------------------------------- */
+typedef struct sc_ensemble sc_ensemble;
+int sc_ens_create(int precision, int nmembers, const int* n, const double* dt, const double* nu8,
+                  double alpha, sc_ensemble** out);
+int sc_ens_destroy(sc_ensemble* e);
+int sc_ens_set_stream(sc_ensemble* e, void* stream);
+/* member m's vorticity, host array (N, N/2+1) complex */
+int sc_ens_set_member(sc_ensemble* e, int m, const void* w);
+int sc_ens_get_member(sc_ensemble* e, int m, void* w);
+/* seeded random vorticity with E(k) ~ k exp(-(k/kpeak)^2), energy `energy`
+ * (ran1 draws in the order of initialize.f90:485-492, then symmetrize2d and
+ * the 2/3 mask); seeds[m] per member (only seeds <= 0 select distinct ran1
+ * streams, initialize.f90:530) */
+int sc_ens_init(sc_ensemble* e, const int* seeds, double kpeak, double energy);
+/* nsteps IF-RK4 steps of every member.  mode 0: one cooperative launch per
+ * stage for all members, a whole step replayed as a CUDA graph; mode 1: the
+ * same launches without the graph; mode 2: the members one at a time. */
+int sc_ens_rk4_steps(sc_ensemble* e, int nsteps, int mode);
+/* 1 if mode 0 is running from a captured graph */
+int sc_ens_uses_graph(sc_ensemble* e);
+
 /* No counterpart in the reference.  FP64 diagnostics of a caller-owned
  * spectral velocity field that allocate no device memory, for callers that
  * cannot call cudaMalloc: a solver that reserves its whole device-memory

@@ -43,6 +43,14 @@ SIGNATURES = {
     "sc_profile_read": ([_P, C.c_char_p, _P, _P], _I),
     "sc_step_bytes": ([_P, _P], _I),
     "sc_diagnostics_noalloc": ([_I, _P, _P, _P, _I, _I, _I, _P, _P], _I),
+    "sc_ens_create": ([_I, _I, _P, _P, _P, _D, _P], _I),
+    "sc_ens_destroy": ([_P], _I),
+    "sc_ens_set_stream": ([_P, _P], _I),
+    "sc_ens_set_member": ([_P, _I, _P], _I),
+    "sc_ens_get_member": ([_P, _I, _P], _I),
+    "sc_ens_init": ([_P, _P, _D, _D], _I),
+    "sc_ens_rk4_steps": ([_P, _I, _I], _I),
+    "sc_ens_uses_graph": ([_P], _I),
     "sc_convec_dns": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
     "sc_projection": ([_I, _P, _P, _P, _I, _I, _I], _I),
     "sc_force": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _D], _I),

@@ -1,0 +1,350 @@
+// Batched 2D vorticity ensembles: members of mixed size N advance together,
+// one persistent (cooperative) launch per RK stage.
+//
+// Physics per member (restated from the 2D solvers of the reference:
+// spectral_dns_2d.f90:94,160-188 and turb_2d.f90:288-403):
+//   u^ = i ky w^/k^2, v^ = -i kx w^/k^2,
+//   N^ = -(i kx (u w)^ + i ky (v w)^), then symmetrize2d (symmetrize.f90:8-30)
+//   and the 2/3 mask; integrating factor E = exp(-(alpha + nu8 k^8) dt/2)
+//   in the division-free IF-RK4 (dns-deform.f90:160-230 rewritten).
+// Layout per member: (N, nxp) complex rows (ky, kx), kx fastest, nxp >= N/2+1.
+//
+// One stage = three phases separated by a grid barrier:
+//   P1 y-inverse: per kx-tile, generate u^, v^, w^ from the stage input and
+//                 transform along ky (3 work fields);
+//   P2 x-pass   : warp per row, c2r of u, v, w, products u w / N^2, v w / N^2,
+//                 r2c (into work fields 0, 1);
+//   P3 y-forward: transform the two products, form N^, symmetrize (the kx = 0
+//                 conjugate pairs lie in one pencil: exchanged in shared
+//                 memory), mask, and apply the RK stage.
+// The grid barrier is a counter/generation pair with a bounded wait; a wait
+// that gives up records an error and the launch returns.
+#pragma once
+#include "sc_xwarp.cuh"
+
+namespace sc {
+
+template <typename T> struct EnsMember {
+  int n, logn, nxh, nxp, ptile, ntx;
+  long long field;         // elements per field
+  C2<T>* w;                // state
+  C2<T>* s;                // stage input
+  C2<T>* acc;              // RK accumulator
+  C2<T>* work;             // 3 work fields
+  T dt, alpha, nu8, scale; // scale = 1/N^2
+  int item_y0, item_x0;    // first item of this member in the y phases / x phase
+};
+
+template <typename T> struct EnsArgs {
+  const EnsMember<T>* m;
+  int nm;
+  int items_y, items_x;    // totals over members
+  int stage;               // 1..4
+  const C2<T>* tw;         // twiddles: table of length L at offset L
+  unsigned* bar;           // [0] arrivals, [1] generation
+  int* err;
+};
+
+constexpr int kEnsNT = 256;
+constexpr int kEnsWarps = kEnsNT / 32;
+
+template <typename T, int LOGN> struct EnsY {
+  static constexpr int N = 1 << LOGN;
+  // tile width: 4096 points per tile (2 radix-8 jobs per thread), at most 16
+  static constexpr int P = (4096 / N) > 16 ? 16 : (4096 / N);
+  using E = FFTEngine<T, LOGN, P, P, kEnsNT, true>;
+};
+
+// Bounded grid-wide barrier for a cooperative launch.
+__device__ __forceinline__ bool ens_grid_sync(unsigned* bar, int* err) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = bar + 1;
+    const unsigned gen = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(bar, 1u);
+    ok = 1;
+    if (arrived == gridDim.x - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long it = 0;
+      while (*vgen == gen) {
+        if (++it > (1LL << 24)) {   // ~1 s of 64 ns sleeps
+          atomicExch(err, 4);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ int ens_member_of(const EnsArgs<T>& ea, int item, bool xphase) {
+  int lo = 0;
+  for (int i = 1; i < ea.nm; ++i) {
+    const int s = xphase ? ea.m[i].item_x0 : ea.m[i].item_y0;
+    if (item >= s) lo = i;
+  }
+  return lo;
+}
+
+// P1: y-inverse of u^, v^, w^ generated from the stage input
+template <typename T, int LOGN>
+__device__ void ens_yinv(const EnsMember<T>& mb, int tile, C2<T>* sm, const C2<T>* __restrict__ tw) {
+  using Y = EnsY<T, LOGN>;
+  using E = typename Y::E;
+  using C = C2<T>;
+  constexpr int P = Y::P;
+  const int kx0 = tile * P;
+  const int nvalid = min(P, mb.nxh - kx0);
+  for (int f = 0; f < 3; ++f) {
+    C in[E::J1][E::R1], o[E::JL][E::RL];
+#pragma unroll
+    for (int a = 0; a < E::J1; ++a)
+#pragma unroll
+      for (int r = 0; r < E::R1; ++r) {
+        int p, n;
+        const bool ok = E::in_pos(a, r, p, n) && p < nvalid;
+        const T kx = (T)(kx0 + p), ky = (T)wavenum(n, mb.n);
+        const T k2 = kx * kx + ky * ky;
+        const T ik2 = k2 > T(0) ? T(1) / k2 : T(0);
+        const C x = ok ? mb.s[(long long)n * mb.nxp + kx0 + p] : czero<C>();
+        in[a][r] = f == 0 ? cmuli(cscale(x, ky * ik2)) : (f == 1 ? cmulmi(cscale(x, kx * ik2)) : x);
+      }
+    E::template run<true>(in, o, sm, tw + Y::N);
+    C* __restrict__ fp = mb.work + f * mb.field + kx0;
+#pragma unroll
+    for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < E::RL; ++r) {
+        int p, n;
+        if (E::out_pos(a, r, p, n) && p < nvalid) fp[(long long)n * mb.nxp + p] = o[a][r];
+      }
+  }
+}
+
+// P2: one warp per row: c2r of u, v, w; products; r2c into work fields 0, 1
+template <typename T, int LOGM>
+__device__ void ens_xrow(const EnsMember<T>& mb, int row, C2<T>* smw, const C2<T>* __restrict__ tw) {
+  using WF = WarpFFT<T, LOGM>;
+  using C = C2<T>;
+  constexpr int M = WF::M, E = WF::E;
+  const int lane = threadIdx.x & 31;
+  const C* __restrict__ twM = tw + M;
+  const C* __restrict__ twN = tw + 2 * M;
+  const long long off = (long long)row * mb.nxp;
+  auto load_z = [&](int f, C (&x)[E]) {
+    const C* __restrict__ rp = mb.work + f * mb.field + off;
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const int k = lane + 32 * r;
+      C xk = rp[k], xm = rp[M - k];
+      if (k == 0) { xk.y = 0; xm.y = 0; }
+      const C e = cadd(xk, cconj(xm));
+      const C o = cmulc(csub(xk, cconj(xm)), __ldg(&twN[k]));
+      x[r] = cadd(e, cmuli(o));
+    }
+  };
+  C a[E];
+  C* wsm = smw + WF::SMEM;   // w (scrambled order) at [i * 32 + lane]
+  load_z(2, a);
+  WF::template nat_to_scr<true>(a, smw, twM, lane);
+#pragma unroll
+  for (int i = 0; i < E; ++i) wsm[i * 32 + lane] = a[i];
+  const T sc = mb.scale;
+  for (int f = 0; f < 2; ++f) {
+    load_z(f, a);
+    WF::template nat_to_scr<true>(a, smw, twM, lane);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const C wv = wsm[i * 32 + lane];
+      a[i] = mk<C>(a[i].x * wv.x * sc, a[i].y * wv.y * sc);
+    }
+    WF::template scr_to_nat<false>(a, smw, twM, lane);
+    C* __restrict__ op = mb.work + f * mb.field + off;
+    const int src = (32 - lane) & 31;
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      C zm;
+      zm.x = __shfl_sync(0xffffffffu, a[E - 1 - r].x, src);
+      zm.y = __shfl_sync(0xffffffffu, a[E - 1 - r].y, src);
+      if (lane == 0) zm = a[(E - r) % E];
+      const int k = lane + 32 * r;
+      const C zmc = cconj(zm);
+      const C e = cadd(a[r], zmc);
+      const C d = cmul(csub(a[r], zmc), __ldg(&twN[k]));
+      op[k] = cscale(csub(e, cmuli(d)), T(0.5));
+      if (k == 0) {
+        const C d0 = cmul(csub(a[r], zmc), __ldg(&twN[M]));
+        op[M] = cscale(csub(e, cmuli(d0)), T(0.5));
+      }
+    }
+  }
+}
+
+// P3: y-forward of the products, N^, symmetrize2d, mask, RK stage
+template <typename T, int LOGN>
+__device__ void ens_yfwd(const EnsMember<T>& mb, int tile, int stage, C2<T>* sm, const C2<T>* __restrict__ tw) {
+  using Y = EnsY<T, LOGN>;
+  using E = typename Y::E;
+  using C = C2<T>;
+  constexpr int P = Y::P, N = Y::N;
+  const int kx0 = tile * P;
+  const int nvalid = min(P, mb.nxh - kx0);
+  C nl[E::JL][E::RL];
+  for (int f = 0; f < 2; ++f) {
+    C in[E::J1][E::R1], o[E::JL][E::RL];
+#pragma unroll
+    for (int a = 0; a < E::J1; ++a)
+#pragma unroll
+      for (int r = 0; r < E::R1; ++r) {
+        int p, n;
+        bool ok = E::in_pos(a, r, p, n) && p < nvalid;
+        in[a][r] = ok ? mb.work[f * mb.field + (long long)n * mb.nxp + kx0 + p] : czero<C>();
+      }
+    E::template run<false>(in, o, sm, tw + N);
+#pragma unroll
+    for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < E::RL; ++r) {
+        int p, n;
+        E::out_pos(a, r, p, n);
+        const T k = f == 0 ? (T)(kx0 + p) : (T)wavenum(n, N);
+        const C t = cmulmi(cscale(o[a][r], k));   // -i k X
+        nl[a][r] = f == 0 ? t : cadd(nl[a][r], t);
+      }
+  }
+  // symmetrize2d: zero ky = -N/2, kx = N/2 and the mean; kx = 0 copies
+  const double kc = 2.0 * (N / 2) / 3.0;
+  if (kx0 == 0) {
+#pragma unroll
+    for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < E::RL; ++r) {
+        int p, n;
+        if (E::out_pos(a, r, p, n) && p == 0) sm[n] = (n == N / 2 || n == 0) ? czero<C>() : nl[a][r];
+      }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < E::RL; ++r) {
+        int p, n;
+        if (E::out_pos(a, r, p, n) && p == 0 && n > N / 2) nl[a][r] = cconj(sm[N - n]);
+      }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+    for (int r = 0; r < E::RL; ++r) {
+      int p, n;
+      if (!(E::out_pos(a, r, p, n) && p < nvalid)) continue;
+      const int ix = kx0 + p;
+      const double ky = wavenum(n, N);
+      const double k2 = (double)ix * ix + ky * ky;
+      C w = nl[a][r];
+      if (n == N / 2 || ix == mb.nxh - 1 || (ix == 0 && n == 0) || k2 >= kc * kc) w = czero<C>();
+      const T arg = (T)((double)mb.alpha + (double)mb.nu8 * k2 * k2 * k2 * k2) * mb.dt * T(0.5);
+      const T Ef = exp(-arg);
+      const T E2 = Ef * Ef, dt = mb.dt, hdt = T(0.5) * mb.dt;
+      const long long idx = (long long)n * mb.nxp + ix;
+      const C v = mb.w[idx];
+      switch (stage) {
+        case 1:
+          mb.acc[idx] = cscale(w, E2 * dt);
+          mb.s[idx] = cscale(cadd(v, cscale(w, hdt)), Ef);
+          break;
+        case 2:
+          mb.acc[idx] = cadd(mb.acc[idx], cscale(w, T(2) * Ef * dt));
+          mb.s[idx] = cadd(cscale(v, Ef), cscale(w, hdt));
+          break;
+        case 3:
+          mb.acc[idx] = cadd(mb.acc[idx], cscale(w, T(2) * Ef * dt));
+          mb.s[idx] = cadd(cscale(v, E2), cscale(w, Ef * dt));
+          break;
+        default: {
+          const C ac = cadd(mb.acc[idx], cscale(w, dt));
+          mb.w[idx] = cadd(cscale(v, E2), cscale(ac, T(1) / T(6)));
+          break;
+        }
+      }
+    }
+}
+
+// dynamic shared memory of ens_stage_kernel (complex elements)
+constexpr int ens_smem_elems() {
+  return 4096 > kEnsWarps * (544 + 512) ? 4096 : kEnsWarps * (544 + 512);
+}
+
+// One RK stage for every member.  Stage 1 reads the state as its input (the
+// host points s at w for that stage through `stage_input_is_state`).
+template <typename T>
+__global__ void __launch_bounds__(kEnsNT, 2) ens_stage_kernel(EnsArgs<T> ea) {
+  using C = C2<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  // P1
+  for (int item = blockIdx.x; item < ea.items_y; item += gridDim.x) {
+    const int mi = ens_member_of(ea, item, false);
+    EnsMember<T> mb = ea.m[mi];
+    if (ea.stage == 1) mb.s = mb.w;
+    const int t = item - mb.item_y0;
+    switch (mb.logn) {
+      case 4: ens_yinv<T, 4>(mb, t, sm, ea.tw); break;
+      case 5: ens_yinv<T, 5>(mb, t, sm, ea.tw); break;
+      case 6: ens_yinv<T, 6>(mb, t, sm, ea.tw); break;
+      case 7: ens_yinv<T, 7>(mb, t, sm, ea.tw); break;
+      case 8: ens_yinv<T, 8>(mb, t, sm, ea.tw); break;
+      case 9: ens_yinv<T, 9>(mb, t, sm, ea.tw); break;
+      default: ens_yinv<T, 10>(mb, t, sm, ea.tw); break;
+    }
+  }
+  if (!ens_grid_sync(ea.bar, ea.err)) return;
+  // P2: kEnsWarps rows per item
+  {
+    const int warp = threadIdx.x >> 5;
+    for (int item = blockIdx.x; item < ea.items_x; item += gridDim.x) {
+      const int mi = ens_member_of(ea, item, true);
+      const EnsMember<T>& mb = ea.m[mi];
+      const int row = (item - mb.item_x0) * kEnsWarps + warp;
+      if (row >= mb.n) continue;
+      C* smw = sm + warp * (WarpFFT<T, 9>::SMEM + 512);   // transpose buffer + w row, largest size
+      const C* tw = ea.tw;   // WarpFFT needs the tables of M and N = 2M at tw + M, tw + 2M
+      switch (mb.logn - 1) {
+        case 5: ens_xrow<T, 5>(mb, row, smw, tw); break;
+        case 6: ens_xrow<T, 6>(mb, row, smw, tw); break;
+        case 7: ens_xrow<T, 7>(mb, row, smw, tw); break;
+        case 8: ens_xrow<T, 8>(mb, row, smw, tw); break;
+        default: ens_xrow<T, 9>(mb, row, smw, tw); break;
+      }
+    }
+  }
+  if (!ens_grid_sync(ea.bar, ea.err)) return;
+  // P3
+  for (int item = blockIdx.x; item < ea.items_y; item += gridDim.x) {
+    const int mi = ens_member_of(ea, item, false);
+    EnsMember<T> mb = ea.m[mi];
+    const int t = item - mb.item_y0;
+    switch (mb.logn) {
+      case 4: ens_yfwd<T, 4>(mb, t, ea.stage, sm, ea.tw); break;
+      case 5: ens_yfwd<T, 5>(mb, t, ea.stage, sm, ea.tw); break;
+      case 6: ens_yfwd<T, 6>(mb, t, ea.stage, sm, ea.tw); break;
+      case 7: ens_yfwd<T, 7>(mb, t, ea.stage, sm, ea.tw); break;
+      case 8: ens_yfwd<T, 8>(mb, t, ea.stage, sm, ea.tw); break;
+      case 9: ens_yfwd<T, 9>(mb, t, ea.stage, sm, ea.tw); break;
+      default: ens_yfwd<T, 10>(mb, t, ea.stage, sm, ea.tw); break;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace sc

@@ -31,41 +31,44 @@ template <> struct W16<double> {
   static constexpr double h = 0.70710678118654752440;
 };
 
-// 16-point DFT in registers as 4 x 4 (n = n1 + 4 n2, k = k2 + 4 k1).
+// 16-point DFT in registers as 4 x 4 (n = n1 + 4 n2, k = k2 + 4 k1), in
+// place: radix-4 over n2 for each n1, twiddles W16^{n1 k2}, radix-4 over n1
+// for each k2, then a 4 x 4 register transpose into natural order.
 template <bool INV, typename C> __device__ __forceinline__ void dft16(C* v) {
   using R = decltype(C::x);
-  C a[4][4];
 #pragma unroll
   for (int n1 = 0; n1 < 4; ++n1) {
+    C t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+    dft4<INV>(t);
 #pragma unroll
-    for (int n2 = 0; n2 < 4; ++n2) a[n1][n2] = v[n1 + 4 * n2];
-    dft4<INV>(a[n1]);   // a[n1][k2]
+    for (int k2 = 0; k2 < 4; ++k2) v[n1 + 4 * k2] = t[k2];
   }
-  // twiddles W16^{n1 k2}, exponent e = n1*k2 in 0..9
 #pragma unroll
   for (int n1 = 1; n1 < 4; ++n1)
 #pragma unroll
     for (int k2 = 1; k2 < 4; ++k2) {
       const int e = n1 * k2;
-      R c, s;   // W16^e = cos(2 pi e/16) - i sin(2 pi e/16) (forward)
+      R c, sn;   // W16^e = cos(2 pi e/16) - i sin(2 pi e/16) (forward)
       switch (e) {
-        case 1: c = W16<R>::c1; s = W16<R>::s1; break;
-        case 2: c = W16<R>::h; s = W16<R>::h; break;
-        case 3: c = W16<R>::s1; s = W16<R>::c1; break;
-        case 4: c = 0; s = 1; break;
-        case 6: c = -W16<R>::h; s = W16<R>::h; break;
-        default: c = -W16<R>::c1; s = -W16<R>::s1; break;   // e = 9
+        case 1: c = W16<R>::c1; sn = W16<R>::s1; break;
+        case 2: c = W16<R>::h; sn = W16<R>::h; break;
+        case 3: c = W16<R>::s1; sn = W16<R>::c1; break;
+        case 4: c = 0; sn = 1; break;
+        case 6: c = -W16<R>::h; sn = W16<R>::h; break;
+        default: c = -W16<R>::c1; sn = -W16<R>::s1; break;   // e = 9
       }
-      const C w = mk<C>(c, INV ? s : -s);
-      a[n1][k2] = cmul(a[n1][k2], w);
+      v[n1 + 4 * k2] = cmul(v[n1 + 4 * k2], mk<C>(c, INV ? sn : -sn));
     }
 #pragma unroll
-  for (int k2 = 0; k2 < 4; ++k2) {
-    C b[4] = {a[0][k2], a[1][k2], a[2][k2], a[3][k2]};
-    dft4<INV>(b);
+  for (int k2 = 0; k2 < 4; ++k2) dft4<INV>(v + 4 * k2);   // X[k2 + 4 k1] now at v[k1 + 4 k2]
 #pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1) v[k2 + 4 * k1] = b[k1];
-  }
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j) {
+      const C t = v[j + 4 * i];
+      v[j + 4 * i] = v[i + 4 * j];
+      v[i + 4 * j] = t;
+    }
 }
 
 template <int E, bool INV, typename C> __device__ __forceinline__ void dftE(C* v) {

@@ -262,3 +262,59 @@ class SpectralNS:
         b = C.c_double(0)
         _check(lib().sc_step_bytes(self.h, C.byref(b)))
         return b.value
+
+
+class Ensemble2D:
+    """Batched 2D vorticity ensemble (sc_ens_*): members of mixed N, each a
+    (N, N/2+1) complex vorticity in the reference's 2D layout."""
+
+    def __init__(self, sizes, dts, nu8s, alpha, precision=SC_FP32):
+        self.n = [int(x) for x in sizes]
+        self.prec = precision
+        self.dtype = np.complex64 if precision == SC_FP32 else np.complex128
+        nm = len(self.n)
+        a_n = (C.c_int * nm)(*self.n)
+        a_dt = (C.c_double * nm)(*[float(x) for x in dts])
+        a_nu = (C.c_double * nm)(*[float(x) for x in nu8s])
+        self.h = C.c_void_p()
+        _check(lib().sc_ens_create(precision, nm, a_n, a_dt, a_nu, C.c_double(alpha), C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            _check(lib().sc_ens_destroy(self.h))
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init(self, seeds, kpeak=6.0, energy=0.5):
+        s = (C.c_int * len(seeds))(*[int(x) for x in seeds])
+        _check(lib().sc_ens_init(self.h, s, C.c_double(kpeak), C.c_double(energy)))
+
+    def set_member(self, m, w):
+        w = np.ascontiguousarray(w, dtype=self.dtype)
+        assert w.shape == (self.n[m], self.n[m] // 2 + 1)
+        _check(lib().sc_ens_set_member(self.h, m, _ptr(w)))
+
+    def get_member(self, m):
+        w = np.zeros((self.n[m], self.n[m] // 2 + 1), dtype=self.dtype)
+        _check(lib().sc_ens_get_member(self.h, m, _ptr(w, True)))
+        return w
+
+    def rk4_steps(self, nsteps, mode=0):
+        _check(lib().sc_ens_rk4_steps(self.h, nsteps, mode))
+
+    def uses_graph(self):
+        return bool(lib().sc_ens_uses_graph(self.h))
+
+    def set_stream(self, stream_ptr):
+        _check(lib().sc_ens_set_stream(self.h, C.c_void_p(stream_ptr)))
