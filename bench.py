@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     return ap.parse_args()
 
 
@@ -121,9 +122,17 @@ class Clocks:
 
 
 # algorithmic bytes per launch, in fields F = (nx/2+1) ny nz complex elements
-# (exact reads + writes of each pass; RK stage average for zfwd)
-KERNEL_FIELDS = {"zinv": 9.0, "ypass_inv": 12.0, "xpass": 9.0, "ypass_fwd": 6.0,
-                 "zfwd": 13.5, "fixup": 0.0}
+# (exact reads + writes of each pass; RK stage averages).  Unfused, zfwd runs
+# all four stages (12, 15, 15, 12 F).  With stages 1-3 fused into zfwd_zinv
+# (15, 18, 18 F: the RHS, v, acc read; acc and the next u, w written) zfwd
+# runs stage 4 only (12 F); zinv runs once per step and zinv_kx0 covers one
+# kx tile (not counted).
+KERNELS = ["zinv", "ypass_inv", "xpass", "ypass_fwd", "zfwd", "zfwd_zinv", "zinv_kx0", "fixup"]
+
+
+def kernel_fields(fused):
+    return {"zinv": 9.0, "ypass_inv": 12.0, "xpass": 9.0, "ypass_fwd": 6.0,
+            "zfwd": 12.0 if fused else 13.5, "zfwd_zinv": 17.0, "zinv_kx0": 0.0, "fixup": 0.0}
 
 
 def traffic_from_profiles(kernel):
@@ -239,10 +248,12 @@ def run_ours(a):
     ms = max_over_ranks(ms)
     prof = {}
     launches = 0
-    for name in ["zinv", "ypass_inv", "xpass", "ypass_fwd", "zfwd", "fixup"]:
+    for name in KERNELS:
         cnt, tot = h.profile_read(name)
-        prof[name] = (cnt, tot)
+        if cnt:
+            prof[name] = (cnt, tot)
         launches += cnt
+    KERNEL_FIELDS = kernel_fields("zfwd_zinv" in prof)
     h.profile_enable(False)
     value = world * a.steps / (ms / 1e3)
     ms_step = ms / a.steps
@@ -355,6 +366,43 @@ def run_ours(a):
                    "note": "adjoint call = forward with checkpoints + per-segment recompute + backward sweep"}
         torch.cuda.empty_cache()
 
+    # ---- batched 2D ensemble: 24 x 256^2, 24 x 512^2, 16 x 1024^2 ----
+    ensemble = None
+    if not a.no_ensemble:
+        sizes = [256] * 24 + [512] * 24 + [1024] * 16
+        dts, nus = [], []
+        for n2 in sizes:
+            kmax = 2.0 * (n2 // 2) / 3.0
+            dt2 = 0.5 / n2                      # CFL ~0.5 at |u| ~ 1 (E = 0.5)
+            dts.append(dt2)
+            nus.append(1.0 / (kmax ** 8 * dt2))  # nu8 kmax^8 dt = 1
+        ens = S.Ensemble2D(sizes, dts, nus, 0.01, S.SC_FP32)
+        ens.set_stream(stream.cuda_stream)
+        ens.init([-(i + 1) for i in range(len(sizes))], kpeak=6.0, energy=0.5)
+        ens.rk4_steps(5, 0)
+        torch.cuda.synchronize()
+        ke = 1000
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ens.rk4_steps(ke, 0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_b = e0.elapsed_time(e1) / 1e3
+        k1 = 50
+        e0.record(stream)
+        ens.rk4_steps(k1, 2)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_1 = e0.elapsed_time(e1) / 1e3
+        ensemble = {"members": len(sizes), "sizes": "24x256^2 + 24x512^2 + 16x1024^2", "alpha": 0.01,
+                    "dt": "0.5/N", "nu8": "1/(kmax^8 dt), kmax = N/3",
+                    "graph": ens.uses_graph(), "steps": ke,
+                    "ensemble_steps_per_s": ke / t_b,
+                    "one_at_a_time_steps_per_s": k1 / t_1,
+                    "speedup_vs_one_at_a_time": (ke / t_b) / (k1 / t_1)}
+        ens.close()
+        del ens
+
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
         workers = len(os.sched_getaffinity(0))
@@ -381,6 +429,7 @@ def run_ours(a):
                "e2e": e2e,
                "fp64": fp64,
                "adjoint": adjoint,
+               "ensemble2d": ensemble,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if dist:

@@ -131,6 +131,13 @@ int sc_ab2_steps(sc_handle* h, int npasses);
 int sc_adjoint_rk4(sc_handle* h, int nsteps, int checkpoint_every, int kmin, int kmax, void* gx,
                    void* gy, void* gz, double* J);
 
+/* Vector-Jacobian product of nsteps IF-RK4 steps: given lam_T (host arrays,
+ * reference layout, same convention as the gradient above) returns
+ * g = (dv_T/dv_0)^T lam_T for the handle's current state v_0, which is left
+ * in place.  Same checkpointing as sc_adjoint_rk4.  No reference counterpart. */
+int sc_adjoint_rk4_vjp(sc_handle* h, int nsteps, int checkpoint_every, const void* lx, const void* ly,
+                       const void* lz, void* gx, void* gy, void* gz);
+
 /* FP64 diagnostics of the current state; eks (may be NULL) receives the
  * shell spectrum E(k), k = 1..nx/2 (specdns-forced-omp-ft.f90:159-176). */
 int sc_diagnostics(sc_handle* h, sc_diag* d, double* eks);

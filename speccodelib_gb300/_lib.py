@@ -39,6 +39,7 @@ SIGNATURES = {
     "sc_ab2_steps": ([_P, _I], _I),
     "sc_diagnostics": ([_P, _P, _P], _I),
     "sc_adjoint_rk4": ([_P, _I, _I, _I, _I, _P, _P, _P, _P], _I),
+    "sc_adjoint_rk4_vjp": ([_P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
     "sc_profile_enable": ([_P, _I], _I),
     "sc_profile_read": ([_P, C.c_char_p, _P, _P], _I),
     "sc_step_bytes": ([_P, _P], _I),

@@ -26,6 +26,10 @@ F77_LIBS = {"sp": os.path.join(LIBDIR, "libspecns_f77_sp.so"),
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr"]
+# Extra preprocessor definitions for tuning builds, e.g.
+# SPECNS_NVCC_DEFINES="SC_NO_F32X2 ZI_DIV=8"; a change rebuilds every object.
+DEFINES = ["-D" + d for d in os.environ.get("SPECNS_NVCC_DEFINES", "").split()]
+STAMP = os.path.join(BUILD, "defines.txt")
 
 
 def nvcc():
@@ -57,7 +61,7 @@ def _compile(src, verbose):
     deps = [os.path.join(CSRC, src)] + _headers()
     if not _stale(obj, deps):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj + ".tmp"]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *DEFINES, "-c", os.path.join(CSRC, src), "-o", obj + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s" % (src, r.stderr[-4000:]))
@@ -71,6 +75,14 @@ def build(verbose=False, jobs=None):
     """Compile (incrementally) and link; returns the path of libspecns.so."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
+    stamp = " ".join(DEFINES)
+    old = open(STAMP).read() if os.path.exists(STAMP) else ""
+    if old != stamp:
+        for f in os.listdir(BUILD):
+            if f.endswith(".o"):
+                os.remove(os.path.join(BUILD, f))
+        with open(STAMP, "w") as fh:
+            fh.write(stamp)
     srcs = _sources()
     jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
     with cf.ThreadPoolExecutor(jobs) as ex:

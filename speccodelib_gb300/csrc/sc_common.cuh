@@ -40,6 +40,37 @@ template <typename C> __device__ __forceinline__ C cmulmi(C a) { return mk<C>(a.
 template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) { return mk<C>(a.x * s, a.y * s); }
 template <typename C> __device__ __forceinline__ C czero() { return mk<C>(0, 0); }
 
+#ifndef SC_NO_F32X2
+// FP32 complex add, subtract and real scale as single packed sm_100-family
+// instructions (add/sub/mul.rn.f32x2): each component is rounded exactly as
+// the scalar form, but the butterflies issue half the instructions.
+__device__ __forceinline__ unsigned long long f2_pack(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(d);
+}
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(d);
+}
+template <> __device__ __forceinline__ float2 cscale<float2, float>(float2 a, float s) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(make_float2(s, s))));
+  return f2_unpack(d);
+}
+#endif
+
 // Signed wavenumber of index i on an axis of length n: 0..n/2-1, -n/2..-1
 // (the FFTW ordering, wavenumber.f90:109,115).
 __device__ __forceinline__ int wavenum(int i, int n) { return i < n / 2 ? i : i - n; }

@@ -6,6 +6,7 @@
 #include "sc_tma_passes.cuh"
 #include "sc_xwarp.cuh"
 #include "sc_adjoint.cuh"
+#include "sc_fused.cuh"
 
 namespace sc {
 
@@ -38,6 +39,7 @@ cudaError_t launch_zinv(const ZvArgs<T>& za, const FieldList<T>& out, const Geom
   static cudaError_t attr = smem_attr(k, Cfg::SMEM);
   if (attr != cudaSuccess) return attr;
   dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
+  if (za.tiles_x > 0 && (unsigned)za.tiles_x < grid.x) grid.x = za.tiles_x;
   k<<<grid, Cfg::NT, Cfg::SMEM, s>>>(za, out, g, tw);
   return cudaGetLastError();
 }
@@ -105,6 +107,39 @@ cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, con
   dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
   k<<<grid, Cfg::NT, sm, s>>>(lmap, st, g, tw, err);
   return cudaGetLastError();
+}
+
+template <typename T, int LOGN>
+cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const StageArgs<T>& st, const FusedArgs<T>& fa,
+                             const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
+  using Z = ZiCfg<T, LOGN>;
+  if constexpr (!Z::SUPPORTED) {
+    return cudaErrorNotSupported;
+  } else {
+    auto k = zfwd_zinv_tma_kernel<T, LOGN>;
+    static cudaError_t attr = smem_attr(k, Z::SMEM);
+    if (attr != cudaSuccess) return attr;
+    dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
+    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, st, fa, g, tw, err);
+    return cudaGetLastError();
+  }
+}
+
+template <typename T, int LOGN>
+cudaError_t launch_zinv5(const CUtensorMap& vmap, const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g,
+                         const C2<T>* tw, int* err, cudaStream_t s) {
+  using Z = ZiCfg<T, LOGN>;
+  if constexpr (!Z::SUPPORTED) {
+    return cudaErrorNotSupported;
+  } else {
+    auto k = zinv5_tma_kernel<T, LOGN>;
+    static cudaError_t attr = smem_attr(k, Z::SMEM);
+    if (attr != cudaSuccess) return attr;
+    dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
+    if (za.tiles_x > 0 && (unsigned)za.tiles_x < grid.x) grid.x = za.tiles_x;
+    k<<<grid, Z::NT, Z::SMEM, s>>>(vmap, za, out, g, tw, err);
+    return cudaGetLastError();
+  }
 }
 
 template <typename T, int LOGM>
@@ -349,3 +384,34 @@ cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const
     }
 #define SC_XPASS_CASE_float(L) SC_XPASS_BODY(float, L)
 #define SC_XPASS_CASE_double(L) SC_XPASS_BODY(double, L)
+
+#define SC_FUSED_CASE_float(L) \
+  case L: return sc::launch_zfwd_zinv<float, L>(lmap, st, fa, g, tw, err, s);
+#define SC_FUSED_CASE_double(L) \
+  case L: return sc::launch_zfwd_zinv<double, L>(lmap, st, fa, g, tw, err, s);
+#define SC_ZINV5_CASE_float(L) case L: return sc::launch_zinv5<float, L>(vmap, za, out, g, tw, err, s);
+#define SC_ZINV5_CASE_double(L) case L: return sc::launch_zinv5<double, L>(vmap, za, out, g, tw, err, s);
+#define SC_ZI_OK_CASE_float(L) case L: return sc::ZiCfg<float, L>::SUPPORTED;
+#define SC_ZI_OK_CASE_double(L) case L: return sc::ZiCfg<double, L>::SUPPORTED;
+#define SC_DEFINE_FUSED(T)                                                                       \
+  template <> bool sc::Launch<T>::zinv5_supported(int logn) {                                   \
+    switch (logn) { SC_LOGN_CASES(SC_ZI_OK_CASE_##T) default: return false; }                    \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, \
+                                           const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, \
+                                           int* err, cudaStream_t s) {                           \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_FUSED_CASE_##T)                                                           \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zinv5_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,   \
+                                       const FieldList<T>& out, const Geom& g, const C2<T>* tw,  \
+                                       int* err, cudaStream_t s) {                               \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZINV5_CASE_##T)                                                           \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }

@@ -90,7 +90,7 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C* v)
   else dft8<INV>(v);
 }
 
-template <typename T, int LOGN, int P, int PS, int NT, bool PFAST, int PADSHIFT = 0>
+template <typename T, int LOGN, int P, int PS, int NT, bool PFAST, int PADSHIFT = 0, bool ROTATE = false>
 struct FFTEngine {
   using C = C2<T>;
   static constexpr int N = 1 << LOGN;
@@ -136,6 +136,40 @@ struct FFTEngine {
     return (TOTL % NT == 0) || job < TOTL;
   }
 
+  // Stage-0 writes go to rows j*R + r.  With p fastest, the 32/P jobs of a
+  // warp write rows R apart; for rows narrower than the 128-byte bank window
+  // and r the same across the warp they all fall in one part of the window
+  // (a 4-way conflict for 64-byte rows).  Each job therefore writes its rows
+  // in the order r ^ m, m = j mod (rows per window), which spreads the warp
+  // over the whole window; the values are permuted in registers to match.
+  // Opt-in (ROTATE): the selects cost registers and issue slots, which the
+  // 64-register pencil passes cannot spare.
+  static constexpr int ROWB = PS * (int)sizeof(C);
+  static constexpr int WIN = (ROTATE && PFAST && PADSHIFT == 0 && ROWB < 128 && 32 % P == 0) ? 128 / ROWB : 1;
+  template <int R>
+  __device__ static __forceinline__ void store_stage0(C (&v)[R], C* sm, int j, int p) {
+    constexpr int W = WIN < R ? WIN : R;
+    if constexpr (W > 1) {
+      const int m = j & (W - 1);
+#pragma unroll
+      for (int b = 1; b < W; b <<= 1) {
+        const bool sw = (m & b) != 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (!(r & b)) {
+            const C lo = v[r], hi = v[r | b];
+            v[r] = sw ? hi : lo;
+            v[r | b] = sw ? lo : hi;
+          }
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[sidx(j * R + (r ^ m)) * PS + p] = v[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[sidx(j * R + r) * PS + p] = v[r];
+    }
+  }
+
   template <int R, int NSV, bool INV>
   __device__ static __forceinline__ void twiddle(C* v, int k, const C* __restrict__ tw) {
     if constexpr (NSV > 1) {
@@ -175,9 +209,13 @@ struct FFTEngine {
         const int k = j % NSV;
         twiddle<R, NSV, INV>(v[a], k, tw);
         dft<R, INV>(v[a]);
-        const int d = (j / NSV) * NSV * R + k;
+        if constexpr (S == 0) {
+          store_stage0<R>(v[a], sm, j, p);
+        } else {
+          const int d = (j / NSV) * NSV * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm[sidx(d + r * NSV) * PS + p] = v[a][r];
+          for (int r = 0; r < R; ++r) sm[sidx(d + r * NSV) * PS + p] = v[a][r];
+        }
       }
     }
     __syncthreads();
@@ -260,8 +298,7 @@ struct FFTEngine {
         decode<R1>(job, p, j);
         if ((TOT1 % NT == 0) || job < TOT1) {
           dft<R1, INV>(in[a]);
-#pragma unroll
-          for (int r = 0; r < R1; ++r) sm[sidx(j * R1 + r) * PS + p] = in[a][r];
+          store_stage0<R1>(in[a], sm, j, p);
         }
       }
       __syncthreads();

@@ -1,0 +1,289 @@
+// z-inverse pass of the DNS right-hand side from a stage input held in shared
+// memory, and the z-forward pass of IF-RK4 stages 1-3 fused with it.
+//
+// Unfused, stage k ends with zfwd (transform the Lamb vector along z, force,
+// symmetrize, project, RK update: write acc and the next stage input s) and
+// stage k+1 starts with zinv (read s, transform s and i k x s back along z).
+// Both walk the same (kx tile, ky) pencils, so zfwd_zinv does both per tile
+// and s never goes through HBM: 6 field passes fewer per right-hand side
+// (write s, read s) and one launch fewer.
+//
+// The exception is the kx = 0 column: symmetrize copies conj(s(-ky, -kz))
+// into its targets, values that belong to another tile.  Tiles with kx0 = 0
+// therefore store s as the unfused kernel does; after the kx = 0 fix-up a
+// one-tile zinv (grid.x = 1) produces their outputs.  Tiles inside the
+// forcing band (kx0^2 + ky^2 < fkmax^2) also store s, which the next stage's
+// forcing reads.
+//
+// Five transforms instead of six: kx and ky are constant along a z pencil, so
+// w_z = i kx u_y - i ky u_x is formed pointwise from the transformed u; only
+// w_x = i (ky s_z - kz s_y) and w_y = i (kz s_x - kx s_z) carry kz and are
+// transformed, half a tile (P/2 pencils) at a time through a half-size work
+// buffer.  Shared memory per CTA: the three s tiles + the half work tile,
+// 112 KB for 32 KB tiles, so two CTAs share an SM.
+#pragma once
+#include "sc_tma_passes.cuh"
+
+#ifndef ZI_DIV
+#define ZI_DIV 16
+#endif
+#ifndef ZI_MAX
+#define ZI_MAX 256
+#endif
+
+namespace sc {
+
+template <typename T> struct FusedArgs {
+  FieldList<T> out;   // next stage: u (0-2) and w = i k x u (3-5), z-inverse done
+  double* kf_next;    // forcing band sums of the next stage input [tile * ny + iy]
+};
+
+template <typename T, int LOGN> struct ZiCfg {
+  using Cfg = TmaCfg<T, LOGN>;
+  static constexpr int P = Cfg::P;
+  static constexpr int N = Cfg::N;
+  // two points per thread and radix-8 job at most 256 threads (ZI_DIV 16,
+  // ZI_MAX 256), or one job per thread up to 512 (ZI_DIV 8, ZI_MAX 512)
+  static constexpr int NT_RAW = P * N / ZI_DIV;
+  static constexpr int NT = NT_RAW > ZI_MAX ? ZI_MAX : (NT_RAW < 32 ? 32 : NT_RAW);
+  static constexpr int EB = NT >= 512 ? 2 : 4;   // epilogue batch
+  using EngF = FFTEngine<T, LOGN, P, P, NT, true, 0, true>;           // whole tile, in place
+  using EngH = FFTEngine<T, LOGN, P / 2, P / 2, NT, true, 0, true>;   // half tile
+  static constexpr size_t TILE = Cfg::TILE_BYTES;
+  static constexpr size_t SMEM = 3 * TILE + TILE / 2 + kSmemAlignPad;
+  static constexpr bool SUPPORTED = P >= 2 && SMEM <= 113 * 1024;
+};
+
+// Steps after the stage input s of tile (kx0, iy) is in the three tiles rt
+// (natural order, element (p, n) at n*P + p): transform w_x, w_y (half tiles
+// through `work`), then s in place, and store u and w.  Starts with the tiles
+// complete (caller's barrier); ends with a barrier.
+template <typename T, int LOGN>
+__device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work, int kx0, int iy, int nvalid,
+                                                long long base, long long zstride, const FieldList<T>& out,
+                                                const Geom& g, const C2<T>* __restrict__ tw) {
+  using Z = ZiCfg<T, LOGN>;
+  using EH = typename Z::EngH;
+  using EF = typename Z::EngF;
+  using C = C2<T>;
+  constexpr int P = Z::P;
+  constexpr int N = Z::N;
+  constexpr int NT = Z::NT;
+  constexpr int PH = P / 2;
+  const T ky = (T)wavenum(iy, g.ny);
+#pragma unroll 1
+  for (int f = 3; f < 5; ++f) {
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      C x[EH::J1][EH::R1], o[EH::JL][EH::RL];
+#pragma unroll
+      for (int a = 0; a < EH::J1; ++a)
+#pragma unroll
+        for (int r = 0; r < EH::R1; ++r) {
+          int p, n;
+          const bool ok = EH::in_pos(a, r, p, n);
+          const int e = ok ? n * P + h * PH + p : 0;   // padding jobs (tiny N) read nothing
+          const T kx = (T)(kx0 + h * PH + p), kz = (T)wavenum(n, g.nz);
+          x[a][r] = ok ? zv_gen<ZV_DNS>(f, rt[0][e], rt[1][e], rt[2][e], kx, ky, kz, true) : czero<C>();
+        }
+      EH::template run<true>(x, o, work, tw);
+      C* __restrict__ fp = out.f[f] + base + h * PH;
+#pragma unroll
+      for (int a = 0; a < EH::JL; ++a)
+#pragma unroll
+        for (int r = 0; r < EH::RL; ++r) {
+          int p, n;
+          if (EH::out_pos(a, r, p, n) && h * PH + p < nvalid) fp[n * zstride + p] = o[a][r];
+        }
+    }
+  }
+  for (int c = 0; c < 3; ++c) EF::template run_inplace<true>(rt[c], tw);
+  // u and w_z = i kx u_y - i ky u_x, 64-byte row segments
+  for (int e = threadIdx.x; e < P * N; e += NT) {
+    const int p = e % P, n = e / P;
+    if (p >= nvalid) continue;
+    const C ux = rt[0][e], uy = rt[1][e], uz = rt[2][e];
+    const long long idx = base + n * zstride + p;
+    out.f[0][idx] = ux;
+    out.f[1][idx] = uy;
+    out.f[2][idx] = uz;
+    const T kx = (T)(kx0 + p);
+    out.f[5][idx] = cmuli(csub(cscale(uy, kx), cscale(ux, ky)));
+  }
+  __syncthreads();
+}
+
+// Standalone z-inverse (DNS): the stage input tile by TMA, K_f partial sums,
+// then zinv_from_tiles.  grid = (kx tiles or za.tiles_x, ny).
+template <typename T, int LOGN>
+__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, 2)
+zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldList<T> out, Geom g,
+                 const C2<T>* __restrict__ tw, int* err) {
+  using Z = ZiCfg<T, LOGN>;
+  using Cfg = TmaCfg<T, LOGN>;
+  using C = C2<T>;
+  constexpr int P = Z::P;
+  constexpr int N = Z::N;
+  constexpr int NT = Z::NT;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  C* rt[3];
+  for (int c = 0; c < 3; ++c) rt[c] = reinterpret_cast<C*>(smraw + c * Z::TILE);
+  C* work = reinterpret_cast<C*>(smraw + 3 * Z::TILE);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double red[NT / 32 + 1];
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+  if (launch_failed(err)) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    mbar_arrive_expect_tx(&bar, (uint32_t)(3 * Z::TILE));
+    for (int c = 0; c < 3; ++c)
+      for (int h = 0; h < Cfg::NBOX; ++h)
+        tma_load_4d(reinterpret_cast<char*>(rt[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), &vmap, &bar,
+                    kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+  }
+  __syncthreads();
+  if (!mbar_wait_bounded(&bar, 0, err)) return;
+  // forcing band energy of the stage input (force.f90:16-22), FP64
+  if (za.fs.enabled && ((double)kx0 * kx0 + (double)ky * ky < za.fs.fkmax2)) {
+    double q = 0.0;
+    for (int e = threadIdx.x; e < P * N; e += NT) {
+      const int p = e % P, n = e / P;
+      const double kx = kx0 + p, kz = wavenum(n, g.nz);
+      const double k2 = kx * kx + (double)ky * ky + kz * kz;
+      if (p < nvalid && k2 < za.fs.fkmax2) {
+        double s = 0.0;
+        for (int c = 0; c < 3; ++c) s += (double)rt[c][e].x * rt[c][e].x + (double)rt[c][e].y * rt[c][e].y;
+        q += (kx0 + p == 0) ? 0.5 * s : s;
+      }
+    }
+    const double sum = block_sum<NT>(q, red);
+    if (threadIdx.x == 0) za.fs.partial[(long long)blockIdx.x * g.ny + iy] = sum;
+  }
+  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, out, g, tw);
+}
+
+// z-forward pass of RK stages 1-3 fused with the next stage's z-inverse.
+// grid = (kx tiles, ny).
+template <typename T, int LOGN>
+__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, 2)
+zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, FusedArgs<T> fa, Geom g,
+                     const C2<T>* __restrict__ tw, int* err) {
+  using Z = ZiCfg<T, LOGN>;
+  using Cfg = TmaCfg<T, LOGN>;
+  using EF = typename Z::EngF;
+  using C = C2<T>;
+  constexpr int P = Z::P;
+  constexpr int N = Z::N;
+  constexpr int NT = Z::NT;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  C* rt[3];
+  for (int c = 0; c < 3; ++c) rt[c] = reinterpret_cast<C*>(smraw + c * Z::TILE);
+  C* work = reinterpret_cast<C*>(smraw + 3 * Z::TILE);
+  __shared__ __align__(8) uint64_t bars[3];
+  __shared__ double s_coef;
+  __shared__ double red[NT / 32 + 1];
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+  const bool tile0 = kx0 == 0;
+  const bool band = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
+  if (launch_failed(err)) return;
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < 3; ++c) mbar_init(&bars[c], 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    for (int c = 0; c < 3; ++c) {
+      mbar_arrive_expect_tx(&bars[c], (uint32_t)Z::TILE);
+      for (int h = 0; h < Cfg::NBOX; ++h)
+        tma_load_4d(reinterpret_cast<char*>(rt[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), &lmap, &bars[c],
+                    kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+    }
+    if (band) {
+      const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
+      s_coef = st.eps / (2.0 * kf);
+    }
+  }
+  __syncthreads();
+  for (int c = 0; c < 3; ++c) {
+    if (!mbar_wait_bounded(&bars[c], 0, err)) return;
+    EF::template run_inplace<false>(rt[c], tw);
+  }
+  // spectral update; the next stage input goes back into the tiles
+  double q = 0.0;
+  constexpr int EB = Z::EB;
+  for (int e0 = threadIdx.x; e0 < P * N; e0 += NT * EB) {
+    C wv[EB][3], vv[EB][3], av[EB][3];
+    bool act[EB];
+#pragma unroll
+    for (int i = 0; i < EB; ++i) {
+      const int e = e0 + i * NT;
+      const int p = e % P, iz = e / P;
+      act[i] = e < P * N && p < nvalid;
+      if (!act[i]) continue;
+      const long long idx = base + iz * zstride + p;
+      load_state<T>(st, idx, vv[i], av[i]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) wv[i][c] = rt[c][e];
+    }
+#pragma unroll
+    for (int i = 0; i < EB; ++i) {
+      if (!act[i]) continue;
+      const int e = e0 + i * NT;
+      const int p = e % P, iz = e / P;
+      const int ix = kx0 + p;
+      const long long idx = base + iz * zstride + p;
+      C* wp = wv[i];
+      const double kz = wavenum(iz, g.nz);
+      const double k2 = (double)ix * ix + (double)ky * ky + kz * kz;
+      if (band && k2 < st.fkmax2) {
+        const T ac = (T)s_coef;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) wp[c] = cadd(wp[c], cscale(st.sin[c][idx], ac));
+      }
+      if (ix == 0) {
+        const long long sd = ((long long)iz * g.ny + iy) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) st.side[sd + c] = wp[c];
+        if (iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2)) continue;
+      }
+      if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
+        wp[0] = wp[1] = wp[2] = czero<C>();
+      C sn[3];
+      finish_point_pre<T>(st, g, idx, ix, iy, iz, wp, vv[i], av[i], sn);
+      if (tile0 || band) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) st.sout[c][idx] = sn[c];
+      }
+      if (!tile0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rt[c][e] = sn[c];
+        if (band && k2 < st.fkmax2) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) q += (double)sn[c].x * sn[c].x + (double)sn[c].y * sn[c].y;
+        }
+      }
+    }
+  }
+  if (tile0) return;
+  __syncthreads();
+  // forcing band energy of the next stage input (force.f90:16-22), FP64
+  if (band && fa.kf_next) {
+    const double sum = block_sum<NT>(q, red);
+    if (threadIdx.x == 0) fa.kf_next[(long long)blockIdx.x * g.ny + iy] = sum;
+  }
+  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, fa.out, g, tw);
+}
+
+}  // namespace sc

@@ -20,6 +20,7 @@ template <typename T> struct PhysArgs;
 template <typename T> struct TmaPass;
 template <typename T> struct AdjArgs;
 template <typename T> struct AdjOpArgs;
+template <typename T> struct FusedArgs;
 
 template <typename T> struct Launch {
   static int tile();                                   // pencil tile width P
@@ -52,6 +53,17 @@ template <typename T> struct Launch {
                               cudaStream_t s);
   static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
                               const C2<T>* tw, int* err, cudaStream_t s);
+  // z-inverse of the DNS operands with five transforms from TMA-loaded stage
+  // input tiles, and the z-forward pass of RK stages 1-3 fused with it
+  // (sc_fused.cuh); both use the tma_tile width.  zinv5_supported: whether the
+  // tiles fit shared memory for this length (else cudaErrorNotSupported).
+  static bool zinv5_supported(int logn);
+  static cudaError_t zinv5_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,
+                               const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
+                               cudaStream_t s);
+  static cudaError_t zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st,
+                                   const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, int* err,
+                                   cudaStream_t s);
   // discrete adjoint (sc_adjoint.cuh)
   static cudaError_t zfwd_adj(int logn, const FieldList<T>& fin, const AdjArgs<T>& aa, const Geom& g,
                               const C2<T>* tw, cudaStream_t s);

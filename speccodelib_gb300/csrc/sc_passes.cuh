@@ -147,6 +147,7 @@ template <typename T> struct ZvArgs {
   int mask_rhs;
   double kcut2;
   double inv_n3;
+  int tiles_x;       // > 0: only the first tiles_x kx tiles (grid.x)
 };
 
 // zero (symmetrize's planes and mean), optional RHS mask, then projection:
@@ -375,11 +376,13 @@ __host__ __device__ constexpr bool mode_reads_acc(int m) {
 
 // Projection, optional RHS mask and the mode's update at one point, with the
 // state (v, or v0 for the AB2 midpoint pass) and accumulator values already
-// loaded.  w is the right-hand side after forcing and symmetrize.
+// loaded.  w is the right-hand side after forcing and symmetrize.  With
+// `snext` given, RK stages 1-3 return the next stage input there instead of
+// storing it to st.sout.
 template <typename T>
 __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const Geom& g, long long idx,
                                                  int ix, int iy, int iz, C2<T>* w, const C2<T>* vv,
-                                                 const C2<T>* av) {
+                                                 const C2<T>* av, C2<T>* snext = nullptr) {
   using C = C2<T>;
   const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
   const T k2 = kx * kx + ky * ky + kz * kz;
@@ -407,21 +410,27 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         st.acc[c][idx] = cscale(w[c], E2 * dt);
-        st.sout[c][idx] = cscale(cadd(vv[c], cscale(w[c], hdt)), E);
+        const C sn = cscale(cadd(vv[c], cscale(w[c], hdt)), E);
+        if (snext) snext[c] = sn;
+        else st.sout[c][idx] = sn;
       }
       break;
     case SM_RK2:  // acc += 2 E dt w2 ; s3 = E v + dt w2/2
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         st.acc[c][idx] = cadd(av[c], cscale(w[c], T(2) * E * dt));
-        st.sout[c][idx] = cadd(cscale(vv[c], E), cscale(w[c], hdt));
+        const C sn = cadd(cscale(vv[c], E), cscale(w[c], hdt));
+        if (snext) snext[c] = sn;
+        else st.sout[c][idx] = sn;
       }
       break;
     case SM_RK3:  // acc += 2 E dt w3 ; s4 = E^2 v + E dt w3
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         st.acc[c][idx] = cadd(av[c], cscale(w[c], T(2) * E * dt));
-        st.sout[c][idx] = cadd(cscale(vv[c], E2), cscale(w[c], E * dt));
+        const C sn = cadd(cscale(vv[c], E2), cscale(w[c], E * dt));
+        if (snext) snext[c] = sn;
+        else st.sout[c][idx] = sn;
       }
       break;
     case SM_RK4:  // v = E^2 v + (acc + dt w4)/6, then the 2/3 mask

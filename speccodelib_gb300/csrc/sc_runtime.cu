@@ -28,6 +28,7 @@
 #include "sc_ops.cuh"
 #include "sc_tma_passes.cuh"
 #include "sc_adjoint.cuh"
+#include "sc_fused.cuh"
 
 namespace {
 
@@ -89,6 +90,8 @@ struct sc_handle {
   bool tma = true;                // TMA-fed strided passes
   bool tma_zinv = false;          // TMA-fed zinv (the register-fed one is faster at 512^3)
   bool xwarp = true;              // warp-per-row x-pass for the DNS product
+  bool zinv5 = true;              // TMA-fed five-transform zinv (DNS)
+  bool fuse = true;               // RK stages 1-3: zfwd fused with the next zinv
   double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch
   double* dpart = nullptr;        // reduction partials
   size_t dpart_len = 0;
@@ -204,6 +207,8 @@ int check_derr(sc_handle* h) {
 // ---------------------------------------------------------------------------
 // precision-templated implementation
 // ---------------------------------------------------------------------------
+int copy_in(sc_handle* h, void* dst, const void* src);  // host -> padded device field
+
 template <typename T> struct Impl {
   using C = sc::C2<T>;
   using L = sc::Launch<T>;
@@ -444,8 +449,24 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
+  // RK stages 1-3 may fuse their zfwd with the next stage's zinv
+  // (sc_fused.cuh): DNS, TMA passes, the fused kernel compiled for this
+  // length, and its tile equal to zinv's so the K_f partial sums line up.
+  static bool use_zinv5(sc_handle* h) {
+    return h->zinv5 && h->tma && !h->tma_zinv && h->p.sgs == SC_SGS_NONE && L::zinv5_supported(h->logz) &&
+           L::tma_tile(h->logz) == pencil_tile(h->logz);
+  }
+  static bool can_fuse(sc_handle* h) { return h->fuse && use_zinv5(h); }
+
+  enum { FUSE_IN = 1, FUSE_OUT = 2 };
+
   // ---- one right-hand side through the fused passes ----
-  static int rhs_pipeline(sc_handle* h, const C* sin[3], sc::StageArgs<T> st) {
+  // fuse & FUSE_IN : u, w of this stage were produced by the previous stage's
+  //                  fused zfwd (no zinv here); st.kf_partial holds their K_f sums
+  // fuse & FUSE_OUT: this stage's zfwd also runs the next stage's zinv,
+  //                  writing that stage's K_f sums to kf_next
+  static int rhs_pipeline(sc_handle* h, const C* sin[3], sc::StageArgs<T> st, int fuse = 0,
+                          double* kf_next = nullptr) {
     auto* g = &h->g;
     const bool les = h->p.sgs != SC_SGS_NONE;
     const int nw = les ? 12 : 6, nf = les ? 9 : 3;
@@ -454,21 +475,42 @@ template <typename T> struct Impl {
     for (int c = 0; c < 3; ++c) za.v[c] = sin[c];
     za.fs.enabled = h->p.forced && st.mode != sc::SM_LAMB;
     za.fs.fkmax2 = h->p.fkmax * h->p.fkmax;
-    za.fs.partial = h->kf_partial;
+    za.fs.partial = const_cast<double*>(st.kf_partial);
     auto wl = range(h, S_W, nw);
     const bool sin_spaced = sin[1] == sin[0] + g->field && sin[2] == sin[0] + 2 * g->field;
     if (h->tma && !les && sin_spaced) {
       CUtensorMap vmap, lmap;
+      const bool z5 = use_zinv5(h);
       const int PZ = L::tma_ztile(h->logz), P = L::tma_tile(h->logz);
-      SC_TRY(encode_fields(h, sin[0], 3, 2, PZ, g->nz, &vmap));
+      SC_TRY(encode_fields(h, sin[0], 3, 2, z5 ? P : PZ, g->nz, &vmap));
       SC_TRY(encode_fields(h, wl.f[0], 3, 2, P, g->nz, &lmap));
-      if (h->tma_zinv)
+      if (fuse & FUSE_IN) {
+        // produced by the previous stage
+      } else if (z5) {
+        SC_TRY(launch(h, "zinv", [&] { return L::zinv5_tma(h->logz, vmap, za, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
+      } else if (h->tma_zinv) {
         SC_TRY(launch(h, "zinv", [&] { return L::zinv_tma(h->logz, vmap, za, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
-      else
+      } else {
         SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
+      }
       SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
       SC_TRY(xpass_dns(h, wl));
       SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
+      if (fuse & FUSE_OUT) {
+        sc::FusedArgs<T> fa{};
+        fa.out = wl;
+        fa.kf_next = kf_next;
+        SC_TRY(launch(h, "zfwd_zinv", [&] { return L::zfwd_zinv_tma(h->logz, lmap, st, fa, *g, tw(h, g->nz), h->derr, h->stream); }));
+        SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));
+        // the kx = 0 tile of the next stage's zinv, after the fix-up
+        CUtensorMap smap;
+        SC_TRY(encode_fields(h, st.sout[0], 3, 2, P, g->nz, &smap));
+        sc::ZvArgs<T> z0 = za;
+        for (int c = 0; c < 3; ++c) z0.v[c] = st.sout[c];
+        z0.fs.partial = kf_next;
+        z0.tiles_x = 1;
+        return launch(h, "zinv_kx0", [&] { return L::zinv5_tma(h->logz, smap, z0, wl, *g, tw(h, g->nz), h->derr, h->stream); });
+      }
       SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, st, *g, tw(h, g->nz), h->derr, h->stream); }));
     } else {
       SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
@@ -496,14 +538,33 @@ template <typename T> struct Impl {
     const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
     const C* sin[3] = {F(h, S_S), F(h, S_S + 1), F(h, S_S + 2)};
     SC_TRY(maybe_dyn(h, vin, true));
-    st.mode = sc::SM_RK1;
-    SC_TRY(rhs_pipeline(h, vin, st));
-    st.mode = sc::SM_RK2;
-    SC_TRY(rhs_pipeline(h, sin, st));
-    st.mode = sc::SM_RK3;
-    SC_TRY(rhs_pipeline(h, sin, st));
-    st.mode = sc::SM_RK4;
-    SC_TRY(rhs_pipeline(h, sin, st));
+    const bool sin_spaced = sin[1] == sin[0] + h->g.field && sin[2] == sin[0] + 2 * h->g.field;
+    if (can_fuse(h) && sin_spaced && st.symmetrize) {
+      // K_f sums alternate between the two halves of kf_partial
+      double* kfa = h->kf_partial;
+      double* kfb = h->kf_partial + (size_t)h->kf_ntiles_max * h->g.ny;
+      st.mode = sc::SM_RK1;
+      st.kf_partial = kfa;
+      SC_TRY(rhs_pipeline(h, vin, st, FUSE_OUT, kfb));
+      st.mode = sc::SM_RK2;
+      st.kf_partial = kfb;
+      SC_TRY(rhs_pipeline(h, sin, st, FUSE_IN | FUSE_OUT, kfa));
+      st.mode = sc::SM_RK3;
+      st.kf_partial = kfa;
+      SC_TRY(rhs_pipeline(h, sin, st, FUSE_IN | FUSE_OUT, kfb));
+      st.mode = sc::SM_RK4;
+      st.kf_partial = kfb;
+      SC_TRY(rhs_pipeline(h, sin, st, FUSE_IN));
+    } else {
+      st.mode = sc::SM_RK1;
+      SC_TRY(rhs_pipeline(h, vin, st));
+      st.mode = sc::SM_RK2;
+      SC_TRY(rhs_pipeline(h, sin, st));
+      st.mode = sc::SM_RK3;
+      SC_TRY(rhs_pipeline(h, sin, st));
+      st.mode = sc::SM_RK4;
+      SC_TRY(rhs_pipeline(h, sin, st));
+    }
     h->step += 1;
     return SC_OK;
   }
@@ -613,7 +674,9 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
-  static int adjoint(sc_handle* h, int nsteps, int K, int kmin, int kmax, double* J) {
+  // seed == NULL: J = shell enstrophy (kmin..kmax) of v_T and lam_T = dJ/dv_T;
+  // otherwise lam_T is read from the three host arrays in seed.
+  static int adjoint(sc_handle* h, int nsteps, int K, int kmin, int kmax, double* J, const void* const* seed) {
     auto* g = &h->g;
     if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the adjoint covers the DNS right-hand side (sgs = none)");
     if (nsteps < 1 || K < 1) return fail(SC_ERR_INVALID, "need nsteps >= 1 and checkpoint interval >= 1");
@@ -642,7 +705,9 @@ template <typename T> struct Impl {
           SC_CUDA(cudaMemcpyAsync(cpf((n + 1) / K, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
     }
     // J and dJ/dv_T
-    {
+    if (seed) {
+      for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, AF(h, 9 + c), seed[c]));
+    } else {
       sc::DiagArgs<T> da{};
       for (int c = 0; c < 3; ++c) da.v[c] = F(h, S_V + c);
       da.kmax2 = -1.0;
@@ -954,6 +1019,10 @@ int sc_create(const sc_params* pin, sc_handle** out) {
     h->tma_zinv = z && z[0] == '1';
     const char* xw = std::getenv("SPECNS_NO_XWARP");
     h->xwarp = !(xw && xw[0] == '1');
+    const char* fu = std::getenv("SPECNS_NO_FUSE");
+    h->fuse = !(fu && fu[0] == '1');
+    const char* z5 = std::getenv("SPECNS_NO_ZINV5");
+    h->zinv5 = !(z5 && z5[0] == '1');
   }
   {
     int dev = 0;
@@ -971,7 +1040,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
   SC_CUDA(cudaMalloc(&h->ey, g.ny * rsz));
   SC_CUDA(cudaMalloc(&h->ez, g.nz * rsz));
   SC_CUDA(cudaMalloc(&h->side, 3 * (size_t)g.ny * g.nz * h->csize));
-  SC_CUDA(cudaMalloc(&h->kf_partial, sizeof(double) * (size_t)ntiles * g.ny));
+  // two halves: a fused stage reads one and writes the other
+  SC_CUDA(cudaMalloc(&h->kf_partial, 2 * sizeof(double) * (size_t)ntiles * g.ny));
   SC_CUDA(cudaMalloc(&h->dscal, sizeof(double) * 8));
   SC_CUDA(cudaMalloc(&h->derr, sizeof(int)));
   SC_CUDA(cudaMemset(h->derr, 0, sizeof(int)));
@@ -1086,14 +1156,28 @@ int sc_ab2_steps(sc_handle* h, int npasses) {
 int sc_adjoint_rk4(sc_handle* h, int nsteps, int checkpoint_every, int kmin, int kmax, void* gx, void* gy,
                    void* gz, double* J) {
   if (!h) return fail(SC_ERR_INVALID, "null handle");
-  SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::adjoint(h, nsteps, checkpoint_every, kmin, kmax, J)
-                                   : Impl<double>::adjoint(h, nsteps, checkpoint_every, kmin, kmax, J));
+  SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::adjoint(h, nsteps, checkpoint_every, kmin, kmax, J, nullptr)
+                                   : Impl<double>::adjoint(h, nsteps, checkpoint_every, kmin, kmax, J, nullptr));
   SC_TRY(check_derr(h));
   if (gx && gy && gz) {
     void* gr[3] = {gx, gy, gz};
     for (int c = 0; c < 3; ++c)
       SC_TRY(copy_out(h, gr[c], static_cast<char*>(h->adj) + (size_t)(9 + c) * h->g.field * h->csize));
   }
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+int sc_adjoint_rk4_vjp(sc_handle* h, int nsteps, int checkpoint_every, const void* lx, const void* ly,
+                       const void* lz, void* gx, void* gy, void* gz) {
+  if (!h || !lx || !ly || !lz || !gx || !gy || !gz) return fail(SC_ERR_INVALID, "null handle or array");
+  const void* seed[3] = {lx, ly, lz};
+  SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::adjoint(h, nsteps, checkpoint_every, 0, 0, nullptr, seed)
+                                   : Impl<double>::adjoint(h, nsteps, checkpoint_every, 0, 0, nullptr, seed));
+  SC_TRY(check_derr(h));
+  void* gr[3] = {gx, gy, gz};
+  for (int c = 0; c < 3; ++c)
+    SC_TRY(copy_out(h, gr[c], static_cast<char*>(h->adj) + (size_t)(9 + c) * h->g.field * h->csize));
   SC_CUDA(cudaStreamSynchronize(h->stream));
   return SC_OK;
 }

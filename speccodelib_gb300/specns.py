@@ -250,6 +250,15 @@ class SpectralNS:
                                     *[_ptr(a, True) for a in g], C.byref(J)))
         return J.value, tuple(g)
 
+    def adjoint_vjp(self, nsteps, lam, checkpoint_every=20):
+        """(dv_T/dv_0)^T lam for the current state v_0 (left in place); lam and
+        the result use the gradient convention of `adjoint`."""
+        lam = self._arrs(lam)
+        g = [self.empty() for _ in range(3)]
+        _check(lib().sc_adjoint_rk4_vjp(self.h, nsteps, checkpoint_every, *[_ptr(a) for a in lam],
+                                        *[_ptr(a, True) for a in g]))
+        return tuple(g)
+
     def profile_enable(self, on=True):
         _check(lib().sc_profile_enable(self.h, 1 if on else 0))
 

@@ -113,3 +113,46 @@ def test_adjoint_sensitivity_config_128(specns_lib):
             worst32 = max(worst32, abs(dot(g32, d) - fd) / abs(fd))
     assert worst64 < 1e-6
     assert worst32 < 1e-3
+
+
+def test_autograd_function_matches_adjoint_and_fd(specns_lib):
+    """The harness's torch.autograd.Function (sc_adjoint_rk4_vjp in backward)
+    gives the shell-enstrophy gradient of sc_adjoint_rk4 and matches central
+    differences of a generic real loss."""
+    torch = pytest.importorskip("torch")
+    from _autograd import rk4_steps
+    n, T, K = 16, 5, 2
+    v = solenoidal_init(n)
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    shell = np.floor(np.sqrt(k2) + 0.5)
+    wk2 = np.where((shell >= 2) & (shell <= 5), k2, 0.0) * np.where(kx == 0, 0.5, 1.0)
+    rng = np.random.default_rng(3)
+    c = [rng.standard_normal(v[0].shape) + 1j * rng.standard_normal(v[0].shape) for _ in range(3)]
+    with S.SpectralNS(S.default_params(n, S.SC_FP64)) as h:
+        h.set_state(*v)
+        Jad, gad = h.adjoint(T, K, kmin=2, kmax=5)
+        vt = [torch.tensor(a, requires_grad=True) for a in v]
+        out = rk4_steps(h, T, K, vt)
+        J = sum((torch.from_numpy(wk2) * o.abs() ** 2).sum() for o in out)
+        J.backward()
+        assert abs(J.item() - Jad) < 1e-12 * abs(Jad)
+        assert rel_l2([t.grad.numpy() for t in vt], gad) < 1e-12
+
+        def loss(vv):
+            h.set_state(*vv)
+            h.rk4_steps(T)
+            o = h.get_state()
+            return sum(float(np.sum((np.conj(ci) * oi).real + 0.25 * np.abs(oi) ** 4)) for ci, oi in zip(c, o))
+
+        vt = [torch.tensor(a, requires_grad=True) for a in v]
+        out = rk4_steps(h, T, K, vt)
+        L = sum(((torch.from_numpy(ci).conj() * o).real + 0.25 * o.abs() ** 4).sum() for ci, o in zip(c, out))
+        L.backward()
+        grad = [t.grad.numpy() for t in vt]
+        assert abs(L.item() - loss(v)) < 1e-12 * abs(L.item())
+        d = [rng.standard_normal(v[0].shape) + 1j * rng.standard_normal(v[0].shape) for _ in range(3)]
+        vn = np.sqrt(sum(float(np.sum(np.abs(a) ** 2)) for a in v))
+        dn = np.sqrt(sum(float(np.sum(np.abs(a) ** 2)) for a in d))
+        eps = 1e-4 * vn / dn
+        fd = (loss([a + eps * b for a, b in zip(v, d)]) - loss([a - eps * b for a, b in zip(v, d)])) / (2 * eps)
+        assert abs(fd - dot(grad, d)) <= 1e-7 * abs(fd)

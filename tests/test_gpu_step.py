@@ -211,3 +211,28 @@ def test_rhs_block_and_warp_xpass_agree(specns_lib, prec, n, monkeypatch):
             outs.append(h.rhs())
     for w in outs:
         assert rel_l2(w, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n,fkmax", [(64, 2.5), (64, 20.0), (128, 2.5)])
+def test_fused_stage_passes_match_oracle(specns_lib, prec, n, fkmax, monkeypatch):
+    """Three z-pass arrangements give the oracle's step: RK stages 1-3 with
+    zfwd fused into the next stage's five-transform zinv (default), the
+    five-transform zinv alone (SPECNS_NO_FUSE=1) and the register-fed zinv
+    (SPECNS_NO_ZINV5=1).  fkmax = 20 puts kx tiles other than the first
+    inside the forcing band."""
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3, fkmax=fkmax)
+    ref = R.rk4_run(v, g, 2)
+    outs = []
+    for nofuse, noz5 in (("0", "0"), ("1", "0"), ("1", "1")):
+        monkeypatch.setenv("SPECNS_NO_FUSE", nofuse)
+        monkeypatch.setenv("SPECNS_NO_ZINV5", noz5)
+        with handle(n, prec, fkmax=fkmax) as h:
+            h.set_state(*v)
+            h.rk4_steps(2)
+            outs.append(h.get_state())
+    for o in outs:
+        assert rel_l2(o, ref) < TOL[prec]
+    for o in outs[1:]:
+        assert rel_l2(outs[0], o) < (1e-13 if prec == S.SC_FP64 else 2e-6)
