@@ -241,11 +241,13 @@ def run_ours(a):
     init32 = h.get_state()
     h.rk4_steps(a.warmup)
     torch.cuda.synchronize()
-    h.profile_enable(True)
     with Clocks(local) as ck:
         ms = time_steps(h, a.steps)
     clocks = ck.summary()
     ms = max_over_ranks(ms)
+    # per-kernel times: the same K steps again, with CUDA events around every launch
+    h.profile_enable(True)
+    time_steps(h, a.steps)
     prof = {}
     launches = 0
     for name in KERNELS:
@@ -349,21 +351,30 @@ def run_ours(a):
         ha.rk4_steps(Ta)
         torch.cuda.synchronize()
         t_fwd = time.perf_counter() - t0
-        ha.set_state(*init_a)
-        ha.adjoint(Ta, Ka, kmin=8, kmax=16)   # warm-up (allocates the checkpoint store)
-        ha.set_state(*init_a)
-        t0 = time.perf_counter()
-        Ja, _ = ha.adjoint(Ta, Ka, kmin=8, kmax=16)
-        torch.cuda.synchronize()
-        t_adj = time.perf_counter() - t0
+        schedules = {}
+        Ja = None
+        for mode, budget in (("stage_inputs_kept", -1.0), ("checkpoint_recompute", 0.0)):
+            ha.set_adjoint_budget(budget)
+            ha.set_state(*init_a)
+            ha.adjoint(Ta, Ka, kmin=8, kmax=16)   # warm-up (allocates the store)
+            ha.set_state(*init_a)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Ja, _ = ha.adjoint(Ta, Ka, kmin=8, kmax=16)
+            torch.cuda.synchronize()
+            t_adj = time.perf_counter() - t0
+            schedules[mode] = {"kept_segments": ha.adjoint_kept_segments(),
+                               "adjoint_call_ms_per_step": 1e3 * t_adj / Ta,
+                               "cost_ratio": t_adj / t_fwd}
         ha.close()
         del ha, init_a
         adjoint = {"grid": na, "steps": Ta, "checkpoint_every": Ka, "J": Ja,
-                   "forward_ms_per_step": 1e3 * t_fwd / Ta,
-                   "adjoint_call_ms_per_step": 1e3 * t_adj / Ta,
-                   "cost_ratio_total": t_adj / t_fwd,
-                   "cost_ratio_backward": (t_adj - t_fwd) / t_fwd,
-                   "note": "adjoint call = forward with checkpoints + per-segment recompute + backward sweep"}
+                   "forward_ms_per_step": 1e3 * t_fwd / Ta, "schedules": schedules,
+                   "note": "cost_ratio = adjoint call (forward sweep + any segment recompute + backward "
+                           "sweep) / plain forward of the same steps; stage_inputs_kept: the default "
+                           "memory budget keeps every segment's stage inputs (12 fields per step) from "
+                           "the forward sweep; checkpoint_recompute: budget 0, state checkpoints every "
+                           "K steps and each segment recomputed"}
         torch.cuda.empty_cache()
 
     # ---- batched 2D ensemble: 24 x 256^2, 24 x 512^2, 16 x 1024^2 ----

@@ -126,10 +126,22 @@ int sc_ab2_steps(sc_handle* h, int npasses);
  * dJ/dv_0 (host arrays, reference layout): g = dJ/dRe v + i dJ/dIm v for every
  * stored entry, so dJ = sum Re(conj(g) dv).  The state is checkpointed every
  * `checkpoint_every` steps and each segment is recomputed once, keeping its
- * stage inputs, before the backward sweep.  The handle's state is left at v_0.
+ * stage inputs, before the backward sweep (segments within the memory budget
+ * of sc_set_adjoint_budget keep them from the forward sweep instead).  The
+ * handle's state is left at v_0.
  * No counterpart in the reference (its solvers have no adjoint). */
 int sc_adjoint_rk4(sc_handle* h, int nsteps, int checkpoint_every, int kmin, int kmax, void* gx,
                    void* gy, void* gz, double* J);
+
+/* Memory for the adjoint's stage-input store, in bytes (default -1: 90% of
+ * the device memory free at the call).  The adjoint checkpoints the state
+ * every `checkpoint_every` steps and recomputes a segment's stage inputs
+ * before its backward sweep, except for the trailing segments whose stage
+ * inputs (12 fields per step) fit this budget: the forward sweep keeps those.
+ * 0 selects pure checkpointing.  sc_adjoint_kept_segments reports how many
+ * segments the last adjoint call kept.  No reference counterpart. */
+int sc_set_adjoint_budget(sc_handle* h, double bytes);
+int sc_adjoint_kept_segments(sc_handle* h, int* kept);
 
 /* Vector-Jacobian product of nsteps IF-RK4 steps: given lam_T (host arrays,
  * reference layout, same convention as the gradient above) returns

@@ -40,6 +40,8 @@ SIGNATURES = {
     "sc_diagnostics": ([_P, _P, _P], _I),
     "sc_adjoint_rk4": ([_P, _I, _I, _I, _I, _P, _P, _P, _P], _I),
     "sc_adjoint_rk4_vjp": ([_P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
+    "sc_set_adjoint_budget": ([_P, _D], _I),
+    "sc_adjoint_kept_segments": ([_P, _P], _I),
     "sc_profile_enable": ([_P, _I], _I),
     "sc_profile_read": ([_P, C.c_char_p, _P, _P], _I),
     "sc_step_bytes": ([_P, _P], _I),

@@ -15,6 +15,7 @@
 // zfwd_adj below, whose epilogue applies the transposed Lawson RK4 stage.
 #pragma once
 #include "sc_passes.cuh"
+#include "sc_tma.cuh"
 
 namespace sc {
 
@@ -39,6 +40,147 @@ template <typename T> struct AdjArgs {
   int mask_rhs;
   double kcut2;
 };
+
+// Add transformed product field f (0-2: w x phi, 3-5: phi x u), in the
+// engine's output layout, to the adjoint lam_s: D' t for f < 3, the curl of
+// D' t (i k x t) for f >= 3.
+template <typename E, typename T>
+__device__ __forceinline__ void adj_accum(C2<T> (&l)[E::JL][E::RL][3], const C2<T> (&o)[E::JL][E::RL], int f,
+                                          int kx0, T ky, const Geom& g) {
+#pragma unroll
+  for (int a = 0; a < E::JL; ++a)
+#pragma unroll
+    for (int r = 0; r < E::RL; ++r) {
+      int p, n;
+      E::out_pos(a, r, p, n);
+      const int ix = kx0 + p;
+      const T dp = (ix == 0 || ix == g.nxh - 1) ? T(1) : T(2);
+      const C2<T> t = cscale(o[a][r], dp);
+      if (f < 3) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (c == f) l[a][r][c] = cadd(l[a][r][c], t);
+      } else {
+        // curl of (phi x u)^: i k x t
+        const T kx = (T)ix, kz = (T)wavenum(n, g.nz);
+        switch (f - 3) {
+          case 0:
+            l[a][r][1] = cadd(l[a][r][1], cmuli(cscale(t, kz)));
+            l[a][r][2] = csub(l[a][r][2], cmuli(cscale(t, ky)));
+            break;
+          case 1:
+            l[a][r][0] = csub(l[a][r][0], cmuli(cscale(t, kz)));
+            l[a][r][2] = cadd(l[a][r][2], cmuli(cscale(t, kx)));
+            break;
+          default:
+            l[a][r][0] = cadd(l[a][r][0], cmuli(cscale(t, ky)));
+            l[a][r][1] = csub(l[a][r][1], cmuli(cscale(t, kx)));
+            break;
+        }
+      }
+    }
+}
+
+// Forcing adjoint and the transposed Lawson RK4 stage for lam_s held in the
+// engine's output layout.  Thread 0 evaluates the band coefficients; the
+// caller's barrier makes them visible (fblock is uniform over the block).
+// The state arrays are read through restrict-qualified copies, two points
+// at a time with every load issued before the first store: the stores to
+// lv / lw would otherwise order each point's loads behind the last point's
+// stores.
+template <typename E, typename T>
+__device__ __forceinline__ void adj_epilogue(C2<T> (&l)[E::JL][E::RL][3], const AdjArgs<T>& aa, const Geom& g,
+                                             int kx0, int iy, int nvalid, long long base, long long zstride,
+                                             bool fblock, double s_a, double s_b) {
+  using C = C2<T>;
+  constexpr int NP = E::JL * E::RL;
+  constexpr int B = 2;
+  const C* __restrict__ lt[3] = {aa.lt[0], aa.lt[1], aa.lt[2]};
+  C* __restrict__ lv[3] = {aa.lv[0], aa.lv[1], aa.lv[2]};
+  C* __restrict__ lw[3] = {aa.lw[0], aa.lw[1], aa.lw[2]};
+  C* __restrict__ lam[3] = {aa.lam[0], aa.lam[1], aa.lam[2]};
+  const int stage = aa.stage;
+  const T dt = aa.dt;
+#pragma unroll
+  for (int q0 = 0; q0 < NP; q0 += B) {
+    long long idx[B];
+    bool ok[B];
+    int ixs[B], izs[B];
+    C ltv[B][3], lvv[B][3];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int q = q0 + b;
+      int p = 0, n = 0;
+      ok[b] = q < NP && E::out_pos(q / E::RL, q % E::RL, p, n) && p < nvalid;
+      ixs[b] = kx0 + p;
+      izs[b] = n;
+      idx[b] = base + n * zstride + p;
+      if (!ok[b]) continue;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (stage != ADJ1) ltv[b][c] = lt[c][idx[b]];
+        if (stage == ADJ3 || stage == ADJ2 || stage == ADJ1) lvv[b][c] = lv[c][idx[b]];
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      if (!ok[b]) continue;
+      const int q = q0 + b;
+      C* ls = l[q / E::RL][q % E::RL];
+      const int ix = ixs[b], iz = izs[b];
+      if (fblock) {
+        const double kz = wavenum(iz, g.nz), ky = wavenum(iy, g.ny);
+        if ((double)ix * ix + ky * ky + kz * kz < aa.fkmax2) {
+          C m[3] = {lw[0][idx[b]], lw[1][idx[b]], lw[2][idx[b]]};
+          adj_mu<C, T>(m, ix, iy, iz, g, aa.mask_rhs, aa.kcut2);
+          const T sa = (T)s_a, sb = (T)(ix == 0 ? 0.5 * s_b : s_b);
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            ls[c] = cadd(ls[c], csub(cscale(m[c], sa), cscale(aa.s[c][idx[b]], sb)));
+        }
+      }
+      const T Ef = aa.ex[ix] * aa.ey[iy] * aa.ez[iz];
+      switch (stage) {
+        case ADJ4:   // lv = E^2 (lt + ls) ; lw = E dt (lt/3 + ls)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            lv[c][idx[b]] = cscale(cadd(ltv[b][c], ls[c]), Ef * Ef);
+            lw[c][idx[b]] = cadd(cscale(ltv[b][c], Ef * dt / T(3)), cscale(ls[c], Ef * dt));
+          }
+          break;
+        case ADJ3:   // lv += E ls ; lw = E dt lt/3 + dt/2 ls
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            lv[c][idx[b]] = cadd(lvv[b][c], cscale(ls[c], Ef));
+            lw[c][idx[b]] = cadd(cscale(ltv[b][c], Ef * dt / T(3)), cscale(ls[c], T(0.5) * dt));
+          }
+          break;
+        case ADJ2:   // lv += E ls ; lw = E^2 dt lt/6 + E dt/2 ls
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            lv[c][idx[b]] = cadd(lvv[b][c], cscale(ls[c], Ef));
+            lw[c][idx[b]] = cadd(cscale(ltv[b][c], Ef * Ef * dt / T(6)), cscale(ls[c], T(0.5) * Ef * dt));
+          }
+          break;
+        default:     // stage 1: lam = lv + ls
+#pragma unroll
+          for (int c = 0; c < 3; ++c) lam[c][idx[b]] = cadd(lvv[b][c], ls[c]);
+          break;
+      }
+    }
+  }
+}
+
+// Band coefficients of the forcing adjoint (thread 0): a = eps / (2 K_f),
+// b = 2 a c / K_f.
+template <typename T>
+__device__ __forceinline__ void adj_band_coef(const AdjArgs<T>& aa, const Geom& g, double& s_a, double& s_b) {
+  const double kf = forcing_energy(aa.kf_partial, aa.kf_tiles, aa.kf_ptile, g.ny, aa.fkmax2);
+  const double cc = forcing_energy(aa.c_partial, aa.kf_tiles, aa.kf_ptile, g.ny, aa.fkmax2);
+  const double a = aa.eps / (2.0 * kf);
+  s_a = a;
+  s_b = 2.0 * a * cc / kf;
+}
 
 template <typename T, int LOGN>
 __global__ void __launch_bounds__(PencilCfg<T, LOGN>::NT, PencilCfg<T, LOGN>::MINB_FUSED)
@@ -74,103 +216,95 @@ zfwd_adj_kernel(FieldList<T> fin, AdjArgs<T> aa, Geom g, const C2<T>* __restrict
         in[a][r] = ok ? fp[n * zstride + p] : czero<C>();
       }
     E::template run<false>(in, o, sm, tw);
-#pragma unroll
-    for (int a = 0; a < E::JL; ++a)
-#pragma unroll
-      for (int r = 0; r < E::RL; ++r) {
-        int p, n;
-        E::out_pos(a, r, p, n);
-        const int ix = kx0 + p;
-        const T dp = (ix == 0 || ix == g.nxh - 1) ? T(1) : T(2);
-        const C t = cscale(o[a][r], dp);
-        if (f < 3) {
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            if (c == f) l[a][r][c] = cadd(l[a][r][c], t);
-        } else {
-          // curl of (phi x u)^: i k x t
-          const T kx = (T)ix, kz = (T)wavenum(n, g.nz);
-          switch (f - 3) {
-            case 0:
-              l[a][r][1] = cadd(l[a][r][1], cmuli(cscale(t, kz)));
-              l[a][r][2] = csub(l[a][r][2], cmuli(cscale(t, ky)));
-              break;
-            case 1:
-              l[a][r][0] = csub(l[a][r][0], cmuli(cscale(t, kz)));
-              l[a][r][2] = cadd(l[a][r][2], cmuli(cscale(t, kx)));
-              break;
-            default:
-              l[a][r][0] = cadd(l[a][r][0], cmuli(cscale(t, ky)));
-              l[a][r][1] = csub(l[a][r][1], cmuli(cscale(t, kx)));
-              break;
-          }
-        }
-      }
+    adj_accum<E, T>(l, o, f, kx0, ky, g);
   }
   const bool fblock = aa.forced && ((double)kx0 * kx0 + (double)ky * ky < aa.fkmax2);
   if (fblock) {
     if (threadIdx.x == 0) {
-      const double kf = forcing_energy(aa.kf_partial, aa.kf_tiles, aa.kf_ptile, g.ny, aa.fkmax2);
-      const double cc = forcing_energy(aa.c_partial, aa.kf_tiles, aa.kf_ptile, g.ny, aa.fkmax2);
-      const double a = aa.eps / (2.0 * kf);
+      double a, b;
+      adj_band_coef<T>(aa, g, a, b);
       s_a = a;
-      s_b = 2.0 * a * cc / kf;
+      s_b = b;
     }
     __syncthreads();
   }
+  adj_epilogue<E, T>(l, aa, g, kx0, iy, nvalid, base, zstride, fblock, s_a, s_b);
+}
+
+// The same with the six product tiles fetched by TMA, two in flight: field
+// f + 2 loads while field f is transformed.  fidx maps the kernel's field
+// order (0-2: w x phi, 3-5: phi x u) to the tensor map's field index.
+template <typename T, int LOGN> struct AdjTmaCfg {
+  using Cfg = TmaCfg<T, LOGN>;
+  static constexpr int P = Cfg::P;
+  static constexpr int NT = Cfg::NT;
+  using Engine = FFTEngine<T, LOGN, P, P, NT, true>;
+  static constexpr size_t SMEM = 2 * Cfg::TILE_BYTES + kSmemAlignPad;
+};
+
+template <typename T, int LOGN>
+__global__ void __launch_bounds__(AdjTmaCfg<T, LOGN>::NT, 1)
+zfwd_adj_tma_kernel(const __grid_constant__ CUtensorMap pmap, int4 fidx_lo, int2 fidx_hi, AdjArgs<T> aa, Geom g,
+                    const C2<T>* __restrict__ tw, int* err) {
+  using AC = AdjTmaCfg<T, LOGN>;
+  using Cfg = TmaCfg<T, LOGN>;
+  using E = typename AC::Engine;
+  using C = C2<T>;
+  constexpr int P = AC::P;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  C* buf[2] = {reinterpret_cast<C*>(smraw), reinterpret_cast<C*>(smraw + Cfg::TILE_BYTES)};
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ double s_a, s_b;
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+  const int fidx[6] = {fidx_lo.x, fidx_lo.y, fidx_lo.z, fidx_lo.w, fidx_hi.x, fidx_hi.y};
+  if (launch_failed(err)) return;
+  auto issue = [&](int f) {
+    mbar_arrive_expect_tx(&bars[f & 1], (uint32_t)Cfg::TILE_BYTES);
+    for (int h = 0; h < Cfg::NBOX; ++h)
+      tma_load_4d(reinterpret_cast<char*>(buf[f & 1]) + (size_t)h * Cfg::BOX * P * sizeof(C), &pmap, &bars[f & 1],
+                  kx0 * Cfg::U, iy, h * Cfg::BOX, fidx[f]);
+  };
+  const bool fblock = aa.forced && ((double)kx0 * kx0 + (double)ky * ky < aa.fkmax2);
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    issue(0);
+    issue(1);
+    if (fblock) {
+      double a, b;
+      adj_band_coef<T>(aa, g, a, b);
+      s_a = a;
+      s_b = b;
+    }
+  }
+  __syncthreads();
+  C l[E::JL][E::RL][3];
 #pragma unroll
   for (int a = 0; a < E::JL; ++a)
 #pragma unroll
-    for (int r = 0; r < E::RL; ++r) {
-      int p, n;
-      if (!(E::out_pos(a, r, p, n) && p < nvalid)) continue;
-      const int ix = kx0 + p, iz = n;
-      const long long idx = base + n * zstride + p;
-      C* ls = l[a][r];
-      if (fblock) {
-        const double kz = wavenum(iz, g.nz);
-        if ((double)ix * ix + (double)ky * ky + kz * kz < aa.fkmax2) {
-          C m[3] = {aa.lw[0][idx], aa.lw[1][idx], aa.lw[2][idx]};
-          adj_mu<C, T>(m, ix, iy, iz, g, aa.mask_rhs, aa.kcut2);
-          const T sa = (T)s_a, sb = (T)(ix == 0 ? 0.5 * s_b : s_b);
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            ls[c] = cadd(ls[c], csub(cscale(m[c], sa), cscale(aa.s[c][idx], sb)));
-        }
-      }
-      const T Ef = aa.ex[ix] * aa.ey[iy] * aa.ez[iz];
-      const T dt = aa.dt;
-      switch (aa.stage) {
-        case ADJ4:   // lv = E^2 (lt + ls) ; lw = E dt (lt/3 + ls)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const C lt = aa.lt[c][idx];
-            aa.lv[c][idx] = cscale(cadd(lt, ls[c]), Ef * Ef);
-            aa.lw[c][idx] = cadd(cscale(lt, Ef * dt / T(3)), cscale(ls[c], Ef * dt));
-          }
-          break;
-        case ADJ3:   // lv += E ls ; lw = E dt lt/3 + dt/2 ls
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const C lt = aa.lt[c][idx];
-            aa.lv[c][idx] = cadd(aa.lv[c][idx], cscale(ls[c], Ef));
-            aa.lw[c][idx] = cadd(cscale(lt, Ef * dt / T(3)), cscale(ls[c], T(0.5) * dt));
-          }
-          break;
-        case ADJ2:   // lv += E ls ; lw = E^2 dt lt/6 + E dt/2 ls
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const C lt = aa.lt[c][idx];
-            aa.lv[c][idx] = cadd(aa.lv[c][idx], cscale(ls[c], Ef));
-            aa.lw[c][idx] = cadd(cscale(lt, Ef * Ef * dt / T(6)), cscale(ls[c], T(0.5) * Ef * dt));
-          }
-          break;
-        default:     // stage 1: lam = lv + ls
-#pragma unroll
-          for (int c = 0; c < 3; ++c) aa.lam[c][idx] = cadd(aa.lv[c][idx], ls[c]);
-          break;
-      }
+    for (int r = 0; r < E::RL; ++r) l[a][r][0] = l[a][r][1] = l[a][r][2] = czero<C>();
+  for (int f = 0; f < 6; ++f) {
+    if (!mbar_wait_bounded(&bars[f & 1], (f >> 1) & 1, err)) {
+      if (threadIdx.x == 0 && f + 1 < 6) mbar_wait_bounded(&bars[(f + 1) & 1], ((f + 1) >> 1) & 1, nullptr);
+      return;
     }
+    C o[E::JL][E::RL];
+    E::template run_smem<false>(o, buf[f & 1], tw);   // ends with a barrier: the buffer is free
+    if (threadIdx.x == 0 && f + 2 < 6) {
+      fence_proxy_async();
+      issue(f + 2);
+    }
+    adj_accum<E, T>(l, o, f, kx0, ky, g);
+  }
+  adj_epilogue<E, T>(l, aa, g, kx0, iy, nvalid, base, zstride, fblock, s_a, s_b);
 }
 
 // Transpose of symmetrize's kx = 0 conjugate copies, in place on lw:

@@ -126,6 +126,22 @@ cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const StageArgs<T>& st, co
 }
 
 template <typename T, int LOGN>
+cudaError_t launch_zinv_phi(const CUtensorMap& lmap, const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g,
+                            const C2<T>* tw, int* err, cudaStream_t s) {
+  using Z = ZiCfg<T, LOGN>;
+  if constexpr (!Z::SUPPORTED) {
+    return cudaErrorNotSupported;
+  } else {
+    auto k = zinv_phi_tma_kernel<T, LOGN>;
+    static cudaError_t attr = smem_attr(k, Z::SMEM);
+    if (attr != cudaSuccess) return attr;
+    dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
+    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, za, out, g, tw, err);
+    return cudaGetLastError();
+  }
+}
+
+template <typename T, int LOGN>
 cudaError_t launch_zinv5(const CUtensorMap& vmap, const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g,
                          const C2<T>* tw, int* err, cudaStream_t s) {
   using Z = ZiCfg<T, LOGN>;
@@ -142,11 +158,11 @@ cudaError_t launch_zinv5(const CUtensorMap& vmap, const ZvArgs<T>& za, const Fie
   }
 }
 
-template <typename T, int LOGM>
+template <typename T, int LOGM, int MODE>
 cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g, const C2<T>* twM,
                          const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s) {
   using Cfg = XwCfg<T, LOGM>;
-  auto k = xpass_warp_kernel<T, LOGM>;
+  auto k = xpass_warp_kernel<T, LOGM, MODE>;
   static cudaError_t attr = smem_attr(k, Cfg::SMEM);
   if (attr != cudaSuccess) return attr;
   const long long nb = (xa.rows + Cfg::WARPS - 1) / Cfg::WARPS;
@@ -166,10 +182,34 @@ cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const
   return cudaGetLastError();
 }
 
+template <typename T, int LOGN>
+cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], const AdjArgs<T>& aa, const Geom& g,
+                                const C2<T>* tw, int* err, cudaStream_t s) {
+  using AC = AdjTmaCfg<T, LOGN>;
+  auto k = zfwd_adj_tma_kernel<T, LOGN>;
+  static cudaError_t attr = smem_attr(k, AC::SMEM);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + AC::P - 1) / AC::P, g.ny);
+  const int4 lo = make_int4(fidx[0], fidx[1], fidx[2], fidx[3]);
+  const int2 hi = make_int2(fidx[4], fidx[5]);
+  k<<<grid, AC::NT, AC::SMEM, s>>>(pmap, lo, hi, aa, g, tw, err);
+  return cudaGetLastError();
+}
+
 }  // namespace sc
 
+#define SC_ZFWDADJTMA_CASE(L) case L: return sc::launch_zfwd_adj_tma<ADJ_T, L>(pmap, fidx, aa, g, tw, err, s);
 #define SC_ZFWDADJ_CASE(L) case L: return sc::launch_zfwd_adj<ADJ_T, L>(fin, aa, g, tw, s);
 #define SC_DEFINE_ADJ(T)                                                                         \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zfwd_adj_tma(int logn, const CUtensorMap& pmap, const int fidx[6],  \
+                                          const AdjArgs<T>& aa, const Geom& g, const C2<T>* tw,  \
+                                          int* err, cudaStream_t s) {                            \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZFWDADJTMA_CASE)                                                          \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
   template <>                                                                                    \
   cudaError_t sc::Launch<T>::zfwd_adj(int logn, const FieldList<T>& fin, const AdjArgs<T>& aa,   \
                                       const Geom& g, const C2<T>* tw, cudaStream_t s) {          \
@@ -197,8 +237,9 @@ cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const
 
 #define SC_DEFINE_XWARP(T, CASES)                                                                \
   template <>                                                                                    \
-  cudaError_t sc::Launch<T>::xpass_warp(int logm, const FieldList<T>& fin, const FieldList<T>& fout, \
-                                        const Geom& g, const C2<T>* twM, const C2<T>* twN,       \
+  cudaError_t sc::Launch<T>::xpass_warp(int logm, int mode, const FieldList<T>& fin,             \
+                                        const FieldList<T>& fout, const Geom& g,                 \
+                                        const C2<T>* twM, const C2<T>* twN,                      \
                                         const XArgs<T>& xa, cudaStream_t s) {                    \
     switch (logm) {                                                                              \
       CASES                                                                                      \
@@ -206,7 +247,10 @@ cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const
     }                                                                                            \
   }
 
-#define SC_XWARP_CASE(T, L) case L: return sc::launch_xwarp<T, L>(fin, fout, g, twM, twN, xa, s);
+#define SC_XWARP_CASE(T, L)                                                                      \
+  case L:                                                                                        \
+    return mode == sc::XW_ADJ ? sc::launch_xwarp<T, L, sc::XW_ADJ>(fin, fout, g, twM, twN, xa, s) \
+                              : sc::launch_xwarp<T, L, sc::XW_DNS>(fin, fout, g, twM, twN, xa, s);
 
 #define SC_TMA_TILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::P;
 #define SC_TMA_ZTILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::PZ;
@@ -391,6 +435,8 @@ cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const
   case L: return sc::launch_zfwd_zinv<double, L>(lmap, st, fa, g, tw, err, s);
 #define SC_ZINV5_CASE_float(L) case L: return sc::launch_zinv5<float, L>(vmap, za, out, g, tw, err, s);
 #define SC_ZINV5_CASE_double(L) case L: return sc::launch_zinv5<double, L>(vmap, za, out, g, tw, err, s);
+#define SC_ZPHI_CASE_float(L) case L: return sc::launch_zinv_phi<float, L>(lmap, za, out, g, tw, err, s);
+#define SC_ZPHI_CASE_double(L) case L: return sc::launch_zinv_phi<double, L>(lmap, za, out, g, tw, err, s);
 #define SC_ZI_OK_CASE_float(L) case L: return sc::ZiCfg<float, L>::SUPPORTED;
 #define SC_ZI_OK_CASE_double(L) case L: return sc::ZiCfg<double, L>::SUPPORTED;
 #define SC_DEFINE_FUSED(T)                                                                       \
@@ -403,6 +449,15 @@ cudaError_t launch_zfwd_adj(const FieldList<T>& fin, const AdjArgs<T>& aa, const
                                            int* err, cudaStream_t s) {                           \
     switch (logn) {                                                                              \
       SC_LOGN_CASES(SC_FUSED_CASE_##T)                                                           \
+      default: return cudaErrorInvalidValue;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zinv_phi_tma(int logn, const CUtensorMap& lmap, const ZvArgs<T>& za, \
+                                          const FieldList<T>& out, const Geom& g, const C2<T>* tw, \
+                                          int* err, cudaStream_t s) {                            \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZPHI_CASE_##T)                                                            \
       default: return cudaErrorInvalidValue;                                                     \
     }                                                                                            \
   }                                                                                              \

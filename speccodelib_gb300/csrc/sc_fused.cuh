@@ -36,6 +36,7 @@ namespace sc {
 template <typename T> struct FusedArgs {
   FieldList<T> out;   // next stage: u (0-2) and w = i k x u (3-5), z-inverse done
   double* kf_next;    // forcing band sums of the next stage input [tile * ny + iy]
+  int store_all;      // also store every tile of the next stage input (adjoint)
 };
 
 template <typename T, int LOGN> struct ZiCfg {
@@ -170,6 +171,87 @@ zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldLi
   zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, out, g, tw);
 }
 
+// Third operand of the adjoint right-hand side along z:
+// phi^ = D (zero P lam) / (2 N^3) (D = 2 on the kx = 0 and kx = nx/2 planes,
+// the weights of C2R^T), with the forcing-adjoint band sums
+// c = sum Re(conj(mu) v) of the stage input v.  lam tiles by TMA, mu formed
+// in shared memory, three in-place transforms.  grid = (kx tiles, ny).
+template <typename T, int LOGN>
+__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, 2)
+zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, FieldList<T> out, Geom g,
+                    const C2<T>* __restrict__ tw, int* err) {
+  using Z = ZiCfg<T, LOGN>;
+  using Cfg = TmaCfg<T, LOGN>;
+  using EF = typename Z::EngF;
+  using C = C2<T>;
+  constexpr int P = Z::P;
+  constexpr int N = Z::N;
+  constexpr int NT = Z::NT;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  C* rt[3];
+  for (int c = 0; c < 3; ++c) rt[c] = reinterpret_cast<C*>(smraw + c * Z::TILE);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double red[NT / 32 + 1];
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const double ky = wavenum(iy, g.ny);
+  if (launch_failed(err)) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    mbar_arrive_expect_tx(&bar, (uint32_t)(3 * Z::TILE));
+    for (int c = 0; c < 3; ++c)
+      for (int h = 0; h < Cfg::NBOX; ++h)
+        tma_load_4d(reinterpret_cast<char*>(rt[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), &lmap, &bar,
+                    kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+  }
+  __syncthreads();
+  if (!mbar_wait_bounded(&bar, 0, err)) return;
+  const bool fsum = za.fs.enabled && ((double)kx0 * kx0 + ky * ky < za.fs.fkmax2);
+  double q = 0.0;
+  for (int e = threadIdx.x; e < P * N; e += NT) {
+    const int p = e % P, n = e / P;
+    if (p >= nvalid) continue;   // columns beyond nx/2: zeros, never stored
+    const int ix = kx0 + p;
+    C m[3] = {rt[0][e], rt[1][e], rt[2][e]};
+    adj_mu<C, T>(m, ix, iy, n, g, za.mask_rhs, za.kcut2);
+    if (fsum) {
+      const double kz = wavenum(n, g.nz);
+      if ((double)ix * ix + ky * ky + kz * kz < za.fs.fkmax2)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const C sv = za.v[c][base + n * zstride + p];
+          q += (double)m[c].x * sv.x + (double)m[c].y * sv.y;
+        }
+    }
+    const T d = (T)((ix == 0 || ix == g.nxh - 1) ? za.inv_n3 : 0.5 * za.inv_n3);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rt[c][e] = cscale(m[c], d);
+  }
+  __syncthreads();
+  if (fsum) {
+    const double s2 = block_sum<NT>(q, red);
+    if (threadIdx.x == 0) za.cpartial[(long long)blockIdx.x * g.ny + iy] = s2;
+  }
+  for (int c = 0; c < 3; ++c) {
+    C o[EF::JL][EF::RL];
+    EF::template run_smem<true>(o, rt[c], tw);
+    C* __restrict__ fp = out.f[c] + base;
+#pragma unroll
+    for (int a = 0; a < EF::JL; ++a)
+#pragma unroll
+      for (int r = 0; r < EF::RL; ++r) {
+        int p, n;
+        if (EF::out_pos(a, r, p, n) && p < nvalid) fp[n * zstride + p] = o[a][r];
+      }
+  }
+}
+
 // z-forward pass of RK stages 1-3 fused with the next stage's z-inverse.
 // grid = (kx tiles, ny).
 template <typename T, int LOGN>
@@ -262,7 +344,7 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, 
         wp[0] = wp[1] = wp[2] = czero<C>();
       C sn[3];
       finish_point_pre<T>(st, g, idx, ix, iy, iz, wp, vv[i], av[i], sn);
-      if (tile0 || band) {
+      if (tile0 || band || fa.store_all) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) st.sout[c][idx] = sn[c];
       }

@@ -61,18 +61,29 @@ template <typename T> struct Launch {
   static cudaError_t zinv5_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,
                                const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                                cudaStream_t s);
+  // phi^ of the adjoint right-hand side from TMA-loaded lam tiles (za.lam is
+  // unused; the map covers lam), with the forcing-adjoint band sums
+  static cudaError_t zinv_phi_tma(int logn, const CUtensorMap& lmap, const ZvArgs<T>& za,
+                                  const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
+                                  cudaStream_t s);
   static cudaError_t zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st,
                                    const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, int* err,
                                    cudaStream_t s);
   // discrete adjoint (sc_adjoint.cuh)
   static cudaError_t zfwd_adj(int logn, const FieldList<T>& fin, const AdjArgs<T>& aa, const Geom& g,
                               const C2<T>* tw, cudaStream_t s);
+  // the same, the six product tiles by TMA (tma_tile width); fidx maps the
+  // kernel's field order (w x phi, phi x u) to the tensor map's fields
+  static cudaError_t zfwd_adj_tma(int logn, const CUtensorMap& pmap, const int fidx[6], const AdjArgs<T>& aa,
+                                  const Geom& g, const C2<T>* tw, int* err, cudaStream_t s);
   static cudaError_t adj_copyT(const FieldList<T>& lw, const Geom& g, cudaStream_t s);
   static cudaError_t adj_op(const AdjOpArgs<T>& ao, const Geom& g, cudaStream_t s);
-  // warp-per-row x-pass (sc_xwarp.cuh), DNS product; cudaErrorNotSupported
-  // for lengths it has no instance for
-  static cudaError_t xpass_warp(int logm, const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g,
-                                const C2<T>* twM, const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s);
+  // warp-per-row x-pass (sc_xwarp.cuh): mode XW_DNS (Lamb product) or
+  // XW_ADJ (its adjoint); cudaErrorNotSupported for lengths it has no
+  // instance for
+  static cudaError_t xpass_warp(int logm, int mode, const FieldList<T>& fin, const FieldList<T>& fout,
+                                const Geom& g, const C2<T>* twM, const C2<T>* twN, const XArgs<T>& xa,
+                                cudaStream_t s);
 };
 
 }  // namespace sc

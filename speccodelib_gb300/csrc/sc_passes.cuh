@@ -649,6 +649,8 @@ __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
 // xpass: per-row c2r, physical-space product, r2c
 // ---------------------------------------------------------------------------
 enum XpMode { XP_DNS = 0, XP_SMAG = 1, XP_C2R3 = 2, XP_R2C3 = 3, XP_ADJ = 4 };
+// modes of the warp-per-row x-pass (sc_xwarp.cuh)
+enum XwMode { XW_DNS = 0, XW_ADJ = 1 };
 template <int MODE> struct XpIO;
 template <> struct XpIO<XP_DNS> { static constexpr int fin = 6, fout = 3; };
 template <> struct XpIO<XP_SMAG> { static constexpr int fin = 12, fout = 9; };

@@ -92,6 +92,11 @@ struct sc_handle {
   bool xwarp = true;              // warp-per-row x-pass for the DNS product
   bool zinv5 = true;              // TMA-fed five-transform zinv (DNS)
   bool fuse = true;               // RK stages 1-3: zfwd fused with the next zinv
+  bool graph = true;              // replay captured CUDA graphs (steps, adjoint)
+  cudaGraphExec_t step_exec = nullptr;   // one RK4 step
+  cudaGraphExec_t adj_exec = nullptr;    // one adjoint call, for adj_key
+  long long adj_key[7] = {0, 0, 0, 0, 0, 0, 0};
+  double* jpin = nullptr;         // pinned host word for J
   double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch
   double* dpart = nullptr;        // reduction partials
   size_t dpart_len = 0;
@@ -99,6 +104,8 @@ struct sc_handle {
   // discrete adjoint (allocated on first use)
   void* adj = nullptr;            // work 9 | lam, lt, lv, lw | stage store | checkpoints
   size_t adj_fields = 0;
+  double adj_budget = -1.0;       // bytes for the adjoint buffer; < 0: 90% of free memory
+  int adj_kept = 0;               // segments of the last adjoint whose stage inputs were kept
   double* cpart = nullptr;        // forcing-adjoint band sums
   long long step = 0;             // RK4 steps taken (dynamic-coefficient cadence)
   int ab2_pass = 0;
@@ -209,6 +216,31 @@ int check_derr(sc_handle* h) {
 // ---------------------------------------------------------------------------
 int copy_in(sc_handle* h, void* dst, const void* src);  // host -> padded device field
 
+void drop_graphs(sc_handle* h) {
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+  if (h->adj_exec) cudaGraphExecDestroy(h->adj_exec);
+  h->step_exec = nullptr;
+  h->adj_exec = nullptr;
+  for (auto& k : h->adj_key) k = 0;
+}
+
+// Record the launches `body` issues on h->stream into an executable graph.
+template <class B> int capture(sc_handle* h, cudaGraphExec_t* out, B&& body) {
+  SC_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = body();
+  cudaGraph_t gr = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
+  if (rc != SC_OK) {
+    if (gr) cudaGraphDestroy(gr);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(SC_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+  const cudaError_t ei = cudaGraphInstantiate(out, gr, 0);
+  cudaGraphDestroy(gr);
+  if (ei != cudaSuccess) return fail(SC_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(ei));
+  return SC_OK;
+}
+
 template <typename T> struct Impl {
   using C = sc::C2<T>;
   using L = sc::Launch<T>;
@@ -244,6 +276,7 @@ template <typename T> struct Impl {
   // 1D integrating-factor tables exp(-nu k_d^2 dt/2); E(k) = ex*ey*ez
   // equals exp(-nu k^2 dt/2) of dns-deform.f90:90.
   static int set_dt(sc_handle* h, double dt) {
+    drop_graphs(h);   // the stage arguments hold dt
     h->p.dt = dt;
     auto tab = [&](int n, int len, bool half) {
       std::vector<T> v(len, T(0));
@@ -290,7 +323,7 @@ template <typename T> struct Impl {
     auto* g = &h->g;
     return launch(h, "xpass", [&] {
       if (h->xwarp) {
-        cudaError_t e = L::xpass_warp(h->logx - 1, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+        cudaError_t e = L::xpass_warp(h->logx - 1, sc::XW_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
         if (e != cudaErrorNotSupported) return e;
       }
       return L::xpass(h->logx - 1, sc::XP_DNS, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
@@ -466,7 +499,7 @@ template <typename T> struct Impl {
   // fuse & FUSE_OUT: this stage's zfwd also runs the next stage's zinv,
   //                  writing that stage's K_f sums to kf_next
   static int rhs_pipeline(sc_handle* h, const C* sin[3], sc::StageArgs<T> st, int fuse = 0,
-                          double* kf_next = nullptr) {
+                          double* kf_next = nullptr, bool store_all = false) {
     auto* g = &h->g;
     const bool les = h->p.sgs != SC_SGS_NONE;
     const int nw = les ? 12 : 6, nf = les ? 9 : 3;
@@ -500,6 +533,7 @@ template <typename T> struct Impl {
         sc::FusedArgs<T> fa{};
         fa.out = wl;
         fa.kf_next = kf_next;
+        fa.store_all = store_all;
         SC_TRY(launch(h, "zfwd_zinv", [&] { return L::zfwd_zinv_tma(h->logz, lmap, st, fa, *g, tw(h, g->nz), h->derr, h->stream); }));
         SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));
         // the kx = 0 tile of the next stage's zinv, after the fix-up
@@ -533,38 +567,47 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
-  static int rk4_step(sc_handle* h) {
-    sc::StageArgs<T> st = stage_args(h);
-    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
-    const C* sin[3] = {F(h, S_S), F(h, S_S + 1), F(h, S_S + 2)};
-    SC_TRY(maybe_dyn(h, vin, true));
-    const bool sin_spaced = sin[1] == sin[0] + h->g.field && sin[2] == sin[0] + 2 * h->g.field;
-    if (can_fuse(h) && sin_spaced && st.symmetrize) {
-      // K_f sums alternate between the two halves of kf_partial
-      double* kfa = h->kf_partial;
-      double* kfb = h->kf_partial + (size_t)h->kf_ntiles_max * h->g.ny;
-      st.mode = sc::SM_RK1;
-      st.kf_partial = kfa;
-      SC_TRY(rhs_pipeline(h, vin, st, FUSE_OUT, kfb));
-      st.mode = sc::SM_RK2;
-      st.kf_partial = kfb;
-      SC_TRY(rhs_pipeline(h, sin, st, FUSE_IN | FUSE_OUT, kfa));
-      st.mode = sc::SM_RK3;
-      st.kf_partial = kfa;
-      SC_TRY(rhs_pipeline(h, sin, st, FUSE_IN | FUSE_OUT, kfb));
-      st.mode = sc::SM_RK4;
-      st.kf_partial = kfb;
-      SC_TRY(rhs_pipeline(h, sin, st, FUSE_IN));
-    } else {
-      st.mode = sc::SM_RK1;
-      SC_TRY(rhs_pipeline(h, vin, st));
-      st.mode = sc::SM_RK2;
-      SC_TRY(rhs_pipeline(h, sin, st));
-      st.mode = sc::SM_RK3;
-      SC_TRY(rhs_pipeline(h, sin, st));
-      st.mode = sc::SM_RK4;
-      SC_TRY(rhs_pipeline(h, sin, st));
+  // One IF-RK4 step from v_n = st[0]: stage inputs s2..s4 go to st[1..3]
+  // (the S_S slots three times for a plain step, distinct slots when the
+  // adjoint keeps them), v_{n+1} to vout.  Stages 1-3 fuse their zfwd with
+  // the next zinv where possible; store_all then still writes every tile of
+  // the stage inputs.
+  static int rk4_core(sc_handle* h, C* const st[4][3], C* const vout[3], bool store_all) {
+    sc::StageArgs<T> a = stage_args(h);
+    for (int c = 0; c < 3; ++c) { a.v[c] = st[0][c]; a.vout[c] = vout[c]; }
+    bool spaced = true;
+    for (int k = 0; k < 4; ++k)
+      spaced = spaced && st[k][1] == st[k][0] + h->g.field && st[k][2] == st[k][0] + 2 * h->g.field;
+    const bool fuse = can_fuse(h) && spaced && a.symmetrize;
+    // K_f sums alternate between the two halves of kf_partial when fused
+    double* kf[2] = {h->kf_partial, h->kf_partial + (size_t)h->kf_ntiles_max * h->g.ny};
+    for (int k = 0; k < 4; ++k) {
+      a.mode = sc::SM_RK1 + k;
+      if (k < 3)
+        for (int c = 0; c < 3; ++c) a.sout[c] = st[k + 1][c];
+      const C* sin[3] = {st[k][0], st[k][1], st[k][2]};
+      if (fuse) {
+        a.kf_partial = kf[k & 1];
+        const int f = (k > 0 ? FUSE_IN : 0) | (k < 3 ? FUSE_OUT : 0);
+        SC_TRY(rhs_pipeline(h, sin, a, f, kf[(k + 1) & 1], store_all));
+      } else {
+        SC_TRY(rhs_pipeline(h, sin, a));
+      }
     }
+    return SC_OK;
+  }
+
+  static int rk4_step(sc_handle* h) {
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    SC_TRY(maybe_dyn(h, vin, true));
+    C* st[4][3];
+    C* vout[3];
+    for (int c = 0; c < 3; ++c) {
+      st[0][c] = F(h, S_V + c);
+      st[1][c] = st[2][c] = st[3][c] = F(h, S_S + c);
+      vout[c] = F(h, S_V + c);
+    }
+    SC_TRY(rk4_core(h, st, vout, false));
     h->step += 1;
     return SC_OK;
   }
@@ -589,22 +632,6 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
-  // ---- one IF-RK4 step with every stage input kept: st[0] = v_n (read),
-  // st[1..3] = s2..s4 (written), v_{n+1} written to vout ----
-  static int rk4_step_store(sc_handle* h, C* const st[4][3], C* const vout[3]) {
-    sc::StageArgs<T> a = stage_args(h);
-    for (int c = 0; c < 3; ++c) { a.v[c] = st[0][c]; a.vout[c] = vout[c]; }
-    for (int k = 0; k < 3; ++k) {
-      a.mode = sc::SM_RK1 + k;
-      for (int c = 0; c < 3; ++c) a.sout[c] = st[k + 1][c];
-      const C* sin[3] = {st[k][0], st[k][1], st[k][2]};
-      SC_TRY(rhs_pipeline(h, sin, a));
-    }
-    a.mode = sc::SM_RK4;
-    const C* sin[3] = {st[3][0], st[3][1], st[3][2]};
-    return rhs_pipeline(h, sin, a);
-  }
-
   static C* AF(sc_handle* h, size_t i) { return reinterpret_cast<C*>(h->adj) + i * h->g.field; }
 
   // adjoint of one right-hand side at stage input s; aa.lw holds its adjoint
@@ -624,12 +651,45 @@ template <typename T> struct Impl {
     za.inv_n3 = 1.0 / ((double)g->nx * g->ny * g->nz);
     sc::FieldList<T> w9{};
     for (int i = 0; i < 9; ++i) w9.f[i] = AF(h, i);
-    SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_ADJ, za, w9, *g, tw(h, g->nz), h->stream); }));
+    const bool spaced3 = aa.s[1] == aa.s[0] + g->field && aa.s[2] == aa.s[0] + 2 * g->field &&
+                         aa.lw[1] == aa.lw[0] + g->field && aa.lw[2] == aa.lw[0] + 2 * g->field;
+    if (use_zinv5(h) && spaced3) {
+      // u, w of the stage input (five transforms) and phi from lam, both TMA-fed
+      const int P = L::tma_tile(h->logz);
+      CUtensorMap smap, lmap;
+      SC_TRY(encode_fields(h, aa.s[0], 3, 2, P, g->nz, &smap));
+      SC_TRY(encode_fields(h, aa.lw[0], 3, 2, P, g->nz, &lmap));
+      SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv5_tma(h->logz, smap, za, w9, *g, tw(h, g->nz), h->derr, h->stream); }));
+      sc::FieldList<T> phi{};
+      for (int c = 0; c < 3; ++c) phi.f[c] = w9.f[6 + c];
+      SC_TRY(launch(h, "adj_zphi", [&] { return L::zinv_phi_tma(h->logz, lmap, za, phi, *g, tw(h, g->nz), h->derr, h->stream); }));
+    } else {
+      SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_ADJ, za, w9, *g, tw(h, g->nz), h->stream); }));
+    }
     if (h->tma) SC_TRY(plain_tma(h, "adj_ypass_inv", 1, true, w9.f[0], 9));
     else SC_TRY(launch(h, "adj_ypass_inv", [&] { return L::plain(h->logy, true, w9, ypass_args(h, 9), *g, g->nz, tw(h, g->ny), h->stream); }));
-    SC_TRY(launch(h, "adj_xpass", [&] { return L::xpass(h->logx - 1, sc::XP_ADJ, w9, w9, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
-    if (h->tma) SC_TRY(plain_tma(h, "adj_ypass_fwd", 1, false, w9.f[0], 6));
-    else SC_TRY(launch(h, "adj_ypass_fwd", [&] { return L::plain(h->logy, false, w9, ypass_args(h, 6), *g, g->nz, tw(h, g->ny), h->stream); }));
+    // products: the warp x-pass leaves w x phi in the phi slots (6-8) and
+    // phi x u in the w slots (3-5); the block x-pass in slots 0-5
+    sc::FieldList<T> a6{};
+    bool warp = false;
+    SC_TRY(launch(h, "adj_xpass", [&] {
+      if (h->xwarp) {
+        sc::FieldList<T> o{};
+        for (int c = 0; c < 3; ++c) { o.f[c] = w9.f[6 + c]; o.f[3 + c] = w9.f[3 + c]; }
+        cudaError_t e = L::xpass_warp(h->logx - 1, sc::XW_ADJ, w9, o, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+        if (e != cudaErrorNotSupported) { warp = true; return e; }
+      }
+      return L::xpass(h->logx - 1, sc::XP_ADJ, w9, w9, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+    }));
+    for (int c = 0; c < 3; ++c) {
+      a6.f[c] = warp ? w9.f[6 + c] : w9.f[c];
+      a6.f[3 + c] = w9.f[3 + c];
+    }
+    // y-forward over the six product fields, equally spaced from their lowest slot
+    sc::FieldList<T> yf{};
+    for (int i = 0; i < 6; ++i) yf.f[i] = w9.f[(warp ? 3 : 0) + i];
+    if (h->tma) SC_TRY(plain_tma(h, "adj_ypass_fwd", 1, false, yf.f[0], 6));
+    else SC_TRY(launch(h, "adj_ypass_fwd", [&] { return L::plain(h->logy, false, yf, ypass_args(h, 6), *g, g->nz, tw(h, g->ny), h->stream); }));
     aa.kf_partial = h->kf_partial;
     aa.c_partial = h->cpart;
     const int pt = pencil_tile(h->logz);
@@ -638,7 +698,15 @@ template <typename T> struct Impl {
     while (nt < ntiles && (double)(nt * pt) * (nt * pt) < h->p.fkmax * h->p.fkmax) ++nt;
     aa.kf_tiles = nt;
     aa.kf_ptile = pt;
-    return launch(h, "adj_zfwd", [&] { return L::zfwd_adj(h->logz, w9, aa, *g, tw(h, g->nz), h->stream); });
+    if (h->tma) {
+      // products equally spaced from yf.f[0]; kernel field f lives at a6.f[f]
+      CUtensorMap pmap;
+      SC_TRY(encode_fields(h, yf.f[0], 6, 2, L::tma_tile(h->logz), g->nz, &pmap));
+      int fidx[6];
+      for (int f = 0; f < 6; ++f) fidx[f] = (int)((a6.f[f] - yf.f[0]) / g->field);
+      return launch(h, "adj_zfwd", [&] { return L::zfwd_adj_tma(h->logz, pmap, fidx, aa, *g, tw(h, g->nz), h->derr, h->stream); });
+    }
+    return launch(h, "adj_zfwd", [&] { return L::zfwd_adj(h->logz, a6, aa, *g, tw(h, g->nz), h->stream); });
   }
 
   // lam_n = S'(v_n)^T lam_{n+1}; st = the step's stage inputs; lam in slots 9..11
@@ -674,35 +742,127 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
+  // Fields of the adjoint buffer for a schedule that keeps the stage inputs of
+  // the last `kept` checkpoint segments: 21 work fields, 12 per kept step, a
+  // 12 K recompute area and 3 per checkpoint when some segment is recomputed.
+  static size_t adj_need(int nsteps, int K, int kept) {
+    const int ncp = (nsteps + K - 1) / K;
+    size_t steps = 0;
+    for (int s = ncp - kept; s < ncp; ++s) steps += std::min(nsteps, (s + 1) * K) - s * K;
+    size_t need = 21 + 12 * steps;
+    if (kept < ncp) need += 12 * (size_t)K + 3 * (size_t)(ncp - kept);
+    return need;
+  }
+
   // seed == NULL: J = shell enstrophy (kmin..kmax) of v_T and lam_T = dJ/dv_T;
   // otherwise lam_T is read from the three host arrays in seed.
+  //
+  // Schedule: the state is checkpointed every K steps and each segment's
+  // stage inputs are recomputed before its backward sweep, except for the
+  // last `kept` segments, whose stage inputs the forward sweep stores
+  // directly, as many as the memory budget (sc_set_adjoint_budget) allows.
+  // The whole call is stream-ordered (J arrives in the pinned word h->jpin),
+  // so it is captured once per schedule and replayed as one CUDA graph; the
+  // seeded form reads host arrays and runs eagerly.
   static int adjoint(sc_handle* h, int nsteps, int K, int kmin, int kmax, double* J, const void* const* seed) {
-    auto* g = &h->g;
     if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the adjoint covers the DNS right-hand side (sgs = none)");
     if (nsteps < 1 || K < 1) return fail(SC_ERR_INVALID, "need nsteps >= 1 and checkpoint interval >= 1");
     if (K > nsteps) K = nsteps;
+    if (!h->jpin) SC_CUDA(cudaMallocHost(&h->jpin, sizeof(double)));
+    const long long step0 = h->step;
+    // the schedule (and the buffer) is settled before any capture
+    SC_TRY(adjoint_plan(h, nsteps, K));
+    if (!h->graph || h->prof || seed) {
+      SC_TRY(adjoint_body(h, nsteps, K, kmin, kmax, seed));
+    } else {
+      const long long key[7] = {nsteps, K, h->adj_kept, kmin, kmax, (long long)(uintptr_t)h->adj,
+                                (long long)h->adj_fields};
+      bool same = true;
+      for (int i = 0; i < 7; ++i) same = same && key[i] == h->adj_key[i];
+      if (!same) {
+        // first call with this schedule: run eagerly, capture on the next one
+        if (h->adj_exec) cudaGraphExecDestroy(h->adj_exec);
+        h->adj_exec = nullptr;
+        for (int i = 0; i < 7; ++i) h->adj_key[i] = key[i];
+        SC_TRY(adjoint_body(h, nsteps, K, kmin, kmax, nullptr));
+      } else {
+        if (!h->adj_exec)
+          SC_TRY(capture(h, &h->adj_exec, [&] { return adjoint_body(h, nsteps, K, kmin, kmax, nullptr); }));
+        SC_CUDA(cudaGraphLaunch(h->adj_exec, h->stream));
+      }
+    }
+    SC_CUDA(cudaStreamSynchronize(h->stream));
+    if (J && !seed) *J = *h->jpin;
+    h->step = step0;
+    return SC_OK;
+  }
+
+  // Settle the schedule: how many trailing segments keep their stage inputs
+  // within the budget, and an adjoint buffer large enough for it.
+  static int adjoint_plan(sc_handle* h, int nsteps, int K) {
     const int ncp = (nsteps + K - 1) / K;
-    const size_t need = 21 + 12 * (size_t)K + 3 * (size_t)ncp;
+    const size_t fb = h->csize * h->g.field;
+    double budget = h->adj_budget;
+    if (budget < 0) {
+      size_t fr = 0, tot = 0;
+      SC_CUDA(cudaMemGetInfo(&fr, &tot));
+      budget = 0.9 * ((double)fr + (double)h->adj_fields * fb - 4e9);
+    }
+    int kept = 0;
+    for (int m = ncp; m >= 1; --m)
+      if ((double)adj_need(nsteps, K, m) * fb <= budget) { kept = m; break; }
+    const size_t need = adj_need(nsteps, K, kept);
     if (h->adj_fields < need) {
+      if (h->adj_exec) cudaGraphExecDestroy(h->adj_exec);
+      h->adj_exec = nullptr;
       cudaFree(h->adj);
       h->adj = nullptr;
       h->adj_fields = 0;
-      SC_CUDA(cudaMalloc(&h->adj, need * g->field * h->csize));
-      SC_CUDA(cudaMemsetAsync(h->adj, 0, need * g->field * h->csize, h->stream));
+      SC_CUDA(cudaMalloc(&h->adj, need * fb));
+      SC_CUDA(cudaMemsetAsync(h->adj, 0, need * fb, h->stream));
       h->adj_fields = need;
-      if (!h->cpart) SC_CUDA(cudaMalloc(&h->cpart, sizeof(double) * (size_t)h->kf_ntiles_max * g->ny));
     }
-    const size_t st0 = 21, cp0 = 21 + 12 * (size_t)K;
-    auto store = [&](int i, int k, int c) { return AF(h, st0 + 12 * (size_t)i + 3 * k + c); };
-    auto cpf = [&](int j, int c) { return AF(h, cp0 + 3 * (size_t)j + c); };
+    if (!h->cpart) SC_CUDA(cudaMalloc(&h->cpart, sizeof(double) * (size_t)h->kf_ntiles_max * h->g.ny));
+    h->adj_kept = kept;
+    return SC_OK;
+  }
+
+  static int adjoint_body(sc_handle* h, int nsteps, int K, int kmin, int kmax, const void* const* seed) {
+    auto* g = &h->g;
+    const int ncp = (nsteps + K - 1) / K;
     const size_t fb = h->csize * g->field;
-    for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(cpf(0, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+    auto seg_len = [&](int sg) { return std::min(nsteps, (sg + 1) * K) - sg * K; };
+    const int kept = h->adj_kept;
+    const int first_kept = ncp - kept;
+    // layout: work 0..20 | kept segments' stage inputs | recompute area | checkpoints
+    std::vector<size_t> seg0(ncp, 0);
+    size_t off = 21;
+    for (int sg = first_kept; sg < ncp; ++sg) { seg0[sg] = off; off += 12 * (size_t)seg_len(sg); }
+    const size_t ra0 = off;
+    const size_t cp0 = ra0 + (kept < ncp ? 12 * (size_t)K : 0);
+    auto slot = [&](size_t base, int i, int k, int c) { return AF(h, base + 12 * (size_t)i + 3 * k + c); };
+    auto cpf = [&](int sg, int c) { return AF(h, cp0 + 3 * (size_t)sg + c); };
+    // one step from slot (base, i) keeping its stage inputs; v_{n+1} to the next slot or the state
+    auto kept_step = [&](size_t base, int i, int len) {
+      C* st[4][3];
+      C* vo[3];
+      for (int k = 0; k < 4; ++k)
+        for (int c = 0; c < 3; ++c) st[k][c] = slot(base, i, k, c);
+      for (int c = 0; c < 3; ++c) vo[c] = (i + 1 < len) ? slot(base, i + 1, 0, c) : F(h, S_V + c);
+      return rk4_core(h, st, vo, true);
+    };
     const long long step0 = h->step;
-    for (int n = 0; n < nsteps; ++n) {
-      SC_TRY(rk4_step(h));
-      if ((n + 1) % K == 0 && n + 1 < nsteps)
+    // forward sweep
+    for (int sg = 0; sg < ncp; ++sg) {
+      const int len = seg_len(sg);
+      if (sg < first_kept) {
+        for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(cpf(sg, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+        for (int i = 0; i < len; ++i) SC_TRY(rk4_step(h));
+      } else {
         for (int c = 0; c < 3; ++c)
-          SC_CUDA(cudaMemcpyAsync(cpf((n + 1) / K, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+          SC_CUDA(cudaMemcpyAsync(slot(seg0[sg], 0, 0, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+        for (int i = 0; i < len; ++i) SC_TRY(kept_step(seg0[sg], i, len));
+      }
     }
     // J and dJ/dv_T
     if (seed) {
@@ -719,10 +879,7 @@ template <typename T> struct Impl {
       da.shell_lo = kmin;
       da.shell_hi = kmax;
       SC_TRY(launch(h, "diag", [&] { return L::diag(da, *g, h->stream); }));
-      double out[sc::DQ_N];
-      SC_CUDA(cudaMemcpyAsync(out, h->dout, sizeof out, cudaMemcpyDeviceToHost, h->stream));
-      SC_CUDA(cudaStreamSynchronize(h->stream));
-      if (J) *J = out[sc::DQ_K2Q];
+      SC_CUDA(cudaMemcpyAsync(h->jpin, h->dout + sc::DQ_K2Q, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
       sc::AdjOpArgs<T> ao{};
       ao.op = sc::AO_SHELL_GRAD;
       ao.kmin = kmin;
@@ -730,26 +887,27 @@ template <typename T> struct Impl {
       for (int c = 0; c < 3; ++c) { ao.in[c] = F(h, S_V + c); ao.out1[c] = AF(h, 9 + c); }
       SC_TRY(launch(h, "adj_grad", [&] { return L::adj_op(ao, *g, h->stream); }));
     }
-    for (int seg = ncp - 1; seg >= 0; --seg) {
-      const int n0 = seg * K, len = std::min(nsteps, n0 + K) - n0;
-      for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(store(0, 0, c), cpf(seg, c), fb, cudaMemcpyDeviceToDevice, h->stream));
-      for (int i = 0; i < len; ++i) {
-        C* st[4][3];
-        for (int k = 0; k < 4; ++k)
-          for (int c = 0; c < 3; ++c) st[k][c] = store(i, k, c);
-        C* vo[3];
-        for (int c = 0; c < 3; ++c) vo[c] = (i + 1 < len) ? store(i + 1, 0, c) : F(h, S_V + c);
-        SC_TRY(rk4_step_store(h, st, vo));
+    // backward sweep
+    for (int sg = ncp - 1; sg >= 0; --sg) {
+      const int len = seg_len(sg);
+      size_t base = seg0[sg];
+      if (sg < first_kept) {
+        base = ra0;
+        for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(slot(ra0, 0, 0, c), cpf(sg, c), fb, cudaMemcpyDeviceToDevice, h->stream));
+        for (int i = 0; i < len; ++i) SC_TRY(kept_step(ra0, i, len));
       }
       for (int i = len - 1; i >= 0; --i) {
         C* st[4][3];
         for (int k = 0; k < 4; ++k)
-          for (int c = 0; c < 3; ++c) st[k][c] = store(i, k, c);
+          for (int c = 0; c < 3; ++c) st[k][c] = slot(base, i, k, c);
         SC_TRY(adj_step(h, st));
       }
     }
     // restore the state v_0
-    for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(F(h, S_V + c), cpf(0, c), fb, cudaMemcpyDeviceToDevice, h->stream));
+    for (int c = 0; c < 3; ++c) {
+      const C* v0 = first_kept > 0 ? cpf(0, c) : slot(seg0[0], 0, 0, c);
+      SC_CUDA(cudaMemcpyAsync(F(h, S_V + c), v0, fb, cudaMemcpyDeviceToDevice, h->stream));
+    }
     h->step = step0;
     return SC_OK;
   }
@@ -1023,6 +1181,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
     h->fuse = !(fu && fu[0] == '1');
     const char* z5 = std::getenv("SPECNS_NO_ZINV5");
     h->zinv5 = !(z5 && z5[0] == '1');
+    const char* gr = std::getenv("SPECNS_NO_GRAPH");
+    h->graph = !(gr && gr[0] == '1');
   }
   {
     int dev = 0;
@@ -1060,6 +1220,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
 int sc_destroy(sc_handle* h) {
   if (!h) return SC_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  if (h->jpin) cudaFreeHost(h->jpin);
   for (auto& pd : h->pending) { cudaEventDestroy(pd.a); cudaEventDestroy(pd.b); }
   for (auto e : h->pool) cudaEventDestroy(e);
   cudaFree(h->fields);
@@ -1140,8 +1302,23 @@ int sc_rhs(sc_handle* h, void* wx, void* wy, void* wz) {
 
 int sc_rk4_steps(sc_handle* h, int nsteps) {
   if (!h || nsteps < 0) return fail(SC_ERR_INVALID, "need a handle and nsteps >= 0");
-  for (int i = 0; i < nsteps; ++i)
-    SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rk4_step(h) : Impl<double>::rk4_step(h));
+  auto step = [&] { return h->p.precision == SC_FP32 ? Impl<float>::rk4_step(h) : Impl<double>::rk4_step(h); };
+  // A step is the same launch sequence every time (the dynamic procedure's
+  // cadence is the exception), so it is captured once and replayed.
+  if (h->graph && !h->prof && h->p.sgs != SC_SGS_DYNSMAG && nsteps > 1) {
+    if (!h->step_exec) {
+      // one eager step first: kernel attributes are set on first launch
+      SC_TRY(step());
+      --nsteps;
+      const long long s0 = h->step;
+      SC_TRY(capture(h, &h->step_exec, step));
+      h->step = s0;
+    }
+    for (int i = 0; i < nsteps; ++i) SC_CUDA(cudaGraphLaunch(h->step_exec, h->stream));
+    h->step += nsteps;
+  } else {
+    for (int i = 0; i < nsteps; ++i) SC_TRY(step());
+  }
   SC_CUDA(cudaGetLastError());
   return check_derr(h);
 }
@@ -1165,6 +1342,18 @@ int sc_adjoint_rk4(sc_handle* h, int nsteps, int checkpoint_every, int kmin, int
       SC_TRY(copy_out(h, gr[c], static_cast<char*>(h->adj) + (size_t)(9 + c) * h->g.field * h->csize));
   }
   SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+int sc_set_adjoint_budget(sc_handle* h, double bytes) {
+  if (!h) return fail(SC_ERR_INVALID, "null handle");
+  h->adj_budget = bytes;
+  return SC_OK;
+}
+
+int sc_adjoint_kept_segments(sc_handle* h, int* kept) {
+  if (!h || !kept) return fail(SC_ERR_INVALID, "null argument");
+  *kept = h->adj_kept;
   return SC_OK;
 }
 
@@ -1192,6 +1381,13 @@ int sc_profile_enable(sc_handle* h, int on) {
   SC_TRY(prof_drain(h));
   h->prof = on != 0;
   h->prof_acc.clear();
+  // events are created here, not per launch: creation costs far more host
+  // time than recording, and a launch loop must stay ahead of the GPU
+  while (h->prof && h->pool.size() < 2048) {
+    cudaEvent_t e = nullptr;
+    SC_CUDA(cudaEventCreate(&e));
+    h->pool.push_back(e);
+  }
   return SC_OK;
 }
 

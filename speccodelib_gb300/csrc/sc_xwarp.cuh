@@ -156,30 +156,26 @@ template <typename T, int LOGM> struct WarpFFT {
 template <typename T, int LOGM> struct XwCfg {
   static constexpr int WARPS = 8;
   static constexpr int NT = 32 * WARPS;
-  // per warp: the transpose buffer + the three velocity rows (scrambled order)
+  // per warp: the transpose buffer + three rows kept in scrambled order
   static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + 3 * WarpFFT<T, LOGM>::M;
   static constexpr size_t SMEM = sizeof(C2<T>) * PER_WARP * WARPS;
 };
 
-// c2r of the 6 operands (u, w), u x w / N^3, r2c of the 3 products.
-template <typename T, int LOGM>
-__global__ void __launch_bounds__(XwCfg<T, LOGM>::NT, 2)
-xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restrict__ twM,
-                  const C2<T>* __restrict__ twN, XArgs<T> xa) {
+// One warp's view of one grid row (y, z) at element offset `off` of every field.
+template <typename T, int LOGM> struct XwRow {
   using WF = WarpFFT<T, LOGM>;
   using C = C2<T>;
-  constexpr int M = WF::M, E = WF::E;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  C* sm = reinterpret_cast<C*>(smraw) + warp * XwCfg<T, LOGM>::PER_WARP;
-  C* us = sm + WF::SMEM;   // u_c at [(c * E + i) * 32 + lane]
-  const long long row = (long long)blockIdx.x * XwCfg<T, LOGM>::WARPS + warp;
-  if (row >= xa.rows) return;
-  const long long off = row * g.nxp;
+  static constexpr int M = WF::M, E = WF::E;
+  C* sm;         // transpose buffer
+  C* as;         // three rows a_c at [(c * E + i) * 32 + lane], scrambled order
+  const C* twM;
+  const C* twN;
+  long long off;
+  int lane;
 
-  // half-length c2r pre-processing of row `f` into natural-order Z
-  auto load_z = [&](int f, C (&x)[E]) {
-    const C* __restrict__ rp = fin.f[f] + off;
+  // half-length c2r pre-processing of a row into natural-order Z
+  __device__ __forceinline__ void load_z(const C* __restrict__ fp, C (&x)[E]) const {
+    const C* __restrict__ rp = fp + off;
 #pragma unroll
     for (int r = 0; r < E; ++r) {
       const int k = lane + 32 * r;
@@ -189,75 +185,120 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
       const C o = cmulc(csub(xk, cconj(xm)), __ldg(&twN[k]));
       x[r] = cadd(e, cmuli(o));
     }
-  };
+  }
 
+  // a_c = c2r of rows f[0..2], kept in shared memory
+  __device__ __forceinline__ void load_a(const C* const f[3]) const {
 #pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    C x[E];
-    load_z(c, x);
-    WF::template nat_to_scr<true>(x, sm, twM, lane);
+    for (int c = 0; c < 3; ++c) {
+      C x[E];
+      load_z(f[c], x);
+      WF::template nat_to_scr<true>(x, sm, twM, lane);
 #pragma unroll
-    for (int i = 0; i < E; ++i) us[(c * E + i) * 32 + lane] = x[i];
-  }
-  auto U = [&](int c, int i) { return us[(c * E + i) * 32 + lane]; };
-  // Lamb vector accumulated as the vorticity components arrive
-  // (convec_dns.f90:30-38, even points in .x, odd points in .y)
-  C lamb[3][E];
-  {
-    C w[E];
-    load_z(3, w);   // w_x: L_y = u_z w_x - ..., L_z = ... - u_y w_x
-    WF::template nat_to_scr<true>(w, sm, twM, lane);
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const C u1 = U(1, i), u2 = U(2, i);
-      lamb[1][i] = mk<C>(u2.x * w[i].x, u2.y * w[i].y);
-      lamb[2][i] = mk<C>(-(u1.x * w[i].x), -(u1.y * w[i].y));
-    }
-    load_z(4, w);   // w_y: L_x = ... - u_z w_y, L_z = u_x w_y - u_y w_x
-    WF::template nat_to_scr<true>(w, sm, twM, lane);
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const C u0 = U(0, i), u2 = U(2, i);
-      lamb[0][i] = mk<C>(-(u2.x * w[i].x), -(u2.y * w[i].y));
-      lamb[2][i] = mk<C>(u0.x * w[i].x + lamb[2][i].x, u0.y * w[i].y + lamb[2][i].y);
-    }
-    load_z(5, w);   // w_z: L_x = u_y w_z - u_z w_y, L_y = u_z w_x - u_x w_z
-    WF::template nat_to_scr<true>(w, sm, twM, lane);
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const C u0 = U(0, i), u1 = U(1, i);
-      lamb[0][i] = mk<C>(u1.x * w[i].x + lamb[0][i].x, u1.y * w[i].y + lamb[0][i].y);
-      lamb[1][i] = mk<C>(lamb[1][i].x - u0.x * w[i].x, lamb[1][i].y - u0.y * w[i].y);
+      for (int i = 0; i < E; ++i) as[(c * E + i) * 32 + lane] = x[i];
     }
   }
-  const T sc = xa.scale;
+
+  // out = r2c(sc * (a x b)), b = c2r of rows bf[0..2]; the cross product is
+  // accumulated as the b components arrive (convec_dns.f90:30-38: even
+  // points in .x, odd points in .y)
+  __device__ __forceinline__ void cross_store(const C* const bf[3], C* const of[3], T sc) const {
+    auto A = [&](int c, int i) { return as[(c * E + i) * 32 + lane]; };
+    C l[3][E];
+    {
+      C b[E];
+      load_z(bf[0], b);   // b_x: L_y = a_z b_x - ..., L_z = ... - a_y b_x
+      WF::template nat_to_scr<true>(b, sm, twM, lane);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    C x[E];
+      for (int i = 0; i < E; ++i) {
+        const C a1 = A(1, i), a2 = A(2, i);
+        l[1][i] = mk<C>(a2.x * b[i].x, a2.y * b[i].y);
+        l[2][i] = mk<C>(-(a1.x * b[i].x), -(a1.y * b[i].y));
+      }
+      load_z(bf[1], b);   // b_y: L_x = ... - a_z b_y, L_z = a_x b_y - a_y b_x
+      WF::template nat_to_scr<true>(b, sm, twM, lane);
 #pragma unroll
-    for (int i = 0; i < E; ++i) x[i] = cscale(lamb[c][i], sc);
-    WF::template scr_to_nat<false>(x, sm, twM, lane);
-    // r2c post-processing: needs Z_{M-k}; k = lane + 32 r pairs with lane
-    // (32 - lane) % 32, register E-1-r (lane 0: its own register (E - r) % E)
-    C* __restrict__ op = fout.f[c] + off;
-    const int src = (32 - lane) & 31;
+      for (int i = 0; i < E; ++i) {
+        const C a0 = A(0, i), a2 = A(2, i);
+        l[0][i] = mk<C>(-(a2.x * b[i].x), -(a2.y * b[i].y));
+        l[2][i] = mk<C>(a0.x * b[i].x + l[2][i].x, a0.y * b[i].y + l[2][i].y);
+      }
+      load_z(bf[2], b);   // b_z: L_x = a_y b_z - a_z b_y, L_y = a_z b_x - a_x b_z
+      WF::template nat_to_scr<true>(b, sm, twM, lane);
 #pragma unroll
-    for (int r = 0; r < E; ++r) {
-      C zm;
-      zm.x = __shfl_sync(0xffffffffu, x[E - 1 - r].x, src);
-      zm.y = __shfl_sync(0xffffffffu, x[E - 1 - r].y, src);
-      if (lane == 0) zm = x[(E - r) % E];
-      const int k = lane + 32 * r;
-      const C zk = x[r];
-      const C zmc = cconj(zm);
-      const C e = cadd(zk, zmc);
-      const C d = cmul(csub(zk, zmc), __ldg(&twN[k]));
-      op[k] = cscale(csub(e, cmuli(d)), T(0.5));
-      if (k == 0) {   // X_M from Z_0
-        const C d0 = cmul(csub(zk, zmc), __ldg(&twN[M]));
-        op[M] = cscale(csub(e, cmuli(d0)), T(0.5));
+      for (int i = 0; i < E; ++i) {
+        const C a0 = A(0, i), a1 = A(1, i);
+        l[0][i] = mk<C>(a1.x * b[i].x + l[0][i].x, a1.y * b[i].y + l[0][i].y);
+        l[1][i] = mk<C>(l[1][i].x - a0.x * b[i].x, l[1][i].y - a0.y * b[i].y);
       }
     }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      C x[E];
+#pragma unroll
+      for (int i = 0; i < E; ++i) x[i] = cscale(l[c][i], sc);
+      WF::template scr_to_nat<false>(x, sm, twM, lane);
+      // r2c post-processing: needs Z_{M-k}; k = lane + 32 r pairs with lane
+      // (32 - lane) % 32, register E-1-r (lane 0: its own register (E - r) % E)
+      C* __restrict__ op = of[c] + off;
+      const int src = (32 - lane) & 31;
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+        C zm;
+        zm.x = __shfl_sync(0xffffffffu, x[E - 1 - r].x, src);
+        zm.y = __shfl_sync(0xffffffffu, x[E - 1 - r].y, src);
+        if (lane == 0) zm = x[(E - r) % E];
+        const int k = lane + 32 * r;
+        const C zk = x[r];
+        const C zmc = cconj(zm);
+        const C e = cadd(zk, zmc);
+        const C d = cmul(csub(zk, zmc), __ldg(&twN[k]));
+        op[k] = cscale(csub(e, cmuli(d)), T(0.5));
+        if (k == 0) {   // X_M from Z_0
+          const C d0 = cmul(csub(zk, zmc), __ldg(&twN[M]));
+          op[M] = cscale(csub(e, cmuli(d0)), T(0.5));
+        }
+      }
+    }
+  }
+};
+
+// XW_DNS: fin = (u, w) -> fout[0..2] = r2c(u x w / N^3), in place allowed.
+// XW_ADJ: fin = (u, w, phi) -> adjoint of the Lamb product (no scale):
+//   w x phi = -(phi x w) into fout[0..2], then phi x u into fout[3..5];
+//   fout must not alias u (read by the second product) -- the host passes
+//   the w and phi slots.
+template <typename T, int LOGM, int MODE>
+__global__ void __launch_bounds__(XwCfg<T, LOGM>::NT, 2)
+xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restrict__ twM,
+                  const C2<T>* __restrict__ twN, XArgs<T> xa) {
+  using C = C2<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long row = (long long)blockIdx.x * XwCfg<T, LOGM>::WARPS + warp;
+  if (row >= xa.rows) return;
+  XwRow<T, LOGM> R;
+  R.sm = reinterpret_cast<C*>(smraw) + warp * XwCfg<T, LOGM>::PER_WARP;
+  R.as = R.sm + WarpFFT<T, LOGM>::SMEM;
+  R.twM = twM;
+  R.twN = twN;
+  R.off = row * g.nxp;
+  R.lane = lane;
+  if constexpr (MODE == XW_DNS) {
+    const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
+    const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
+    C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
+    R.load_a(a);
+    R.cross_store(b, o, xa.scale);
+  } else {
+    const C* phi[3] = {fin.f[6], fin.f[7], fin.f[8]};
+    const C* w[3] = {fin.f[3], fin.f[4], fin.f[5]};
+    const C* u[3] = {fin.f[0], fin.f[1], fin.f[2]};
+    C* o1[3] = {fout.f[0], fout.f[1], fout.f[2]};
+    C* o2[3] = {fout.f[3], fout.f[4], fout.f[5]};
+    R.load_a(phi);
+    R.cross_store(w, o1, T(-1));
+    R.cross_store(u, o2, T(1));
   }
 }
 

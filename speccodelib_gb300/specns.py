@@ -250,6 +250,16 @@ class SpectralNS:
                                     *[_ptr(a, True) for a in g], C.byref(J)))
         return J.value, tuple(g)
 
+    def set_adjoint_budget(self, nbytes):
+        """Bytes for the adjoint's stage-input store (< 0: 90% of free memory,
+        0: pure checkpointing with recomputation)."""
+        _check(lib().sc_set_adjoint_budget(self.h, C.c_double(nbytes)))
+
+    def adjoint_kept_segments(self):
+        k = C.c_int(0)
+        _check(lib().sc_adjoint_kept_segments(self.h, C.byref(k)))
+        return k.value
+
     def adjoint_vjp(self, nsteps, lam, checkpoint_every=20):
         """(dv_T/dv_0)^T lam for the current state v_0 (left in place); lam and
         the result use the gradient convention of `adjoint`."""

@@ -156,3 +156,57 @@ def test_autograd_function_matches_adjoint_and_fd(specns_lib):
         eps = 1e-4 * vn / dn
         fd = (loss([a + eps * b for a, b in zip(v, d)]) - loss([a - eps * b for a, b in zip(v, d)])) / (2 * eps)
         assert abs(fd - dot(grad, d)) <= 1e-7 * abs(fd)
+
+
+def test_adjoint_schedules_agree(specns_lib):
+    """Pure checkpointing (budget 0: every segment recomputed), one kept
+    segment, and every segment kept from the forward sweep give the same J
+    and gradient; the state is left at v_0 each time."""
+    n, T, K = 16, 7, 3   # segments of 3, 3, 1 steps
+    v = solenoidal_init(n)
+    nxp = (n // 2 + 1 + 15) // 16 * 16
+    fb = 16 * n * n * nxp
+    res = []
+    with S.SpectralNS(S.default_params(n, S.SC_FP64)) as h:
+        for budget, kept in ((0.0, 0), (80.0 * fb, 1), (-1.0, 3)):
+            h.set_adjoint_budget(budget)
+            h.set_state(*v)
+            J, grad = h.adjoint(T, K, kmin=2, kmax=5)
+            assert h.adjoint_kept_segments() == kept
+            assert rel_l2(h.get_state(), v) == 0.0
+            res.append((J, grad))
+    for J, grad in res[1:]:
+        assert J == res[0][0]
+        assert rel_l2(grad, res[0][1]) < 1e-15
+
+
+@pytest.mark.parametrize("prec,tol", [(S.SC_FP64, 1e-12), (S.SC_FP32, 1e-5)])
+def test_adjoint_warp_and_block_xpass_agree(specns_lib, prec, tol, monkeypatch):
+    """nx = 128 runs the adjoint product through the warp-per-row x-pass;
+    SPECNS_NO_XWARP=1 through the block x-pass.  Same gradient."""
+    n, T, K = 128, 2, 1
+    v = solenoidal_init(n)
+    grads = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_XWARP", env)
+        with S.SpectralNS(S.default_params(n, prec)) as h:
+            h.set_state(*v)
+            grads.append(h.adjoint(T, K, kmin=8, kmax=16)[1])
+    assert rel_l2(grads[0], grads[1]) < tol
+
+
+def test_adjoint_graph_replay_matches_eager(specns_lib, monkeypatch):
+    """The second and later adjoint calls with one schedule replay a captured
+    CUDA graph; J and the gradient equal the eager call's bit for bit."""
+    n, T, K = 32, 5, 2
+    v = solenoidal_init(n)
+    res = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_GRAPH", env)
+        with S.SpectralNS(S.default_params(n, S.SC_FP64)) as h:
+            for _ in range(3):
+                h.set_state(*v)
+                res.append(h.adjoint(T, K, kmin=4, kmax=9))
+    for J, grad in res[1:]:
+        assert J == res[0][0]
+        assert rel_l2(grad, res[0][1]) == 0.0

@@ -236,3 +236,23 @@ def test_fused_stage_passes_match_oracle(specns_lib, prec, n, fkmax, monkeypatch
         assert rel_l2(o, ref) < TOL[prec]
     for o in outs[1:]:
         assert rel_l2(outs[0], o) < (1e-13 if prec == S.SC_FP64 else 2e-6)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_graph_replay_matches_eager(specns_lib, prec, monkeypatch):
+    """sc_rk4_steps replays one captured RK4 step as a CUDA graph; the result
+    is bit-identical to launching every kernel (SPECNS_NO_GRAPH=1), across
+    repeated calls and a change of dt."""
+    n = 32
+    v = solenoidal_init(n)
+    outs = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_GRAPH", env)
+        with handle(n, prec) as h:
+            h.set_state(*v)
+            h.rk4_steps(4)
+            h.rk4_steps(3)
+            h.set_dt(1e-3)
+            h.rk4_steps(2)
+            outs.append(h.get_state())
+    assert rel_l2(outs[0], outs[1]) == 0.0
