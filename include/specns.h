@@ -196,6 +196,23 @@ int sc_ens_rk4_steps(sc_ensemble* e, int nsteps, int mode);
 /* 1 if mode 0 is running from a captured graph */
 int sc_ens_uses_graph(sc_ensemble* e);
 
+/* Launch-shape autotuner.  The stage kernel is compiled in several shapes
+ * (threads per CTA, CTAs per SM, points per y tile, largest FFT radix);
+ * sc_ens_tune times each on this ensemble (`trial_steps` steps each, the
+ * member states saved and restored) and keeps the fastest.  The first
+ * sc_ens_rk4_steps call tunes with 3 trial steps unless a variant was set
+ * (sc_ens_set_variant, or SPECNS_ENS_VARIANT) or SPECNS_ENS_TUNE=0.
+ * Variants round differently (FP32 results agree to ~1e-6); pin one for
+ * bit-reproducible runs.  sc_ens_variant reports the current variant, the
+ * number of variants, the last tuning's ms per step per variant
+ * (tune_ms[count], -1 = not timed) and the shape {threads, CTAs per SM,
+ * tile points, radix, phases out of line} (shape[5]); any pointer may be
+ * NULL.
+ * No reference counterpart. */
+int sc_ens_tune(sc_ensemble* e, int trial_steps, int* chosen);
+int sc_ens_set_variant(sc_ensemble* e, int variant);
+int sc_ens_variant(sc_ensemble* e, int* variant, int* count, double* tune_ms, int* shape);
+
 /* No counterpart in the reference.  FP64 diagnostics of a caller-owned
  * spectral velocity field that allocate no device memory, for callers that
  * cannot call cudaMalloc: a solver that reserves its whole device-memory

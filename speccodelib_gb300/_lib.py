@@ -54,6 +54,9 @@ SIGNATURES = {
     "sc_ens_init": ([_P, _P, _D, _D], _I),
     "sc_ens_rk4_steps": ([_P, _I, _I], _I),
     "sc_ens_uses_graph": ([_P], _I),
+    "sc_ens_tune": ([_P, _I, _P], _I),
+    "sc_ens_set_variant": ([_P, _I], _I),
+    "sc_ens_variant": ([_P, _P, _P, _P, _P], _I),
     "sc_convec_dns": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
     "sc_projection": ([_I, _P, _P, _P, _I, _I, _I], _I),
     "sc_force": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _D], _I),

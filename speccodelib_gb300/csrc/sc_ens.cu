@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -53,9 +54,18 @@ struct sc_ensemble {
   std::vector<long long> field;    // per member: elements per field
   std::vector<int> nxp;
   cudaGraphExec_t graph = nullptr;
+  // launch shape: the autotuner's choice among the compiled variants
+  int variant = 0;
+  bool tuned = false;
+  std::vector<double> tune_ms;     // per variant: ms per step of the last tuning (< 0: not run)
 };
 
 namespace {
+
+int nvariants(const sc_ensemble* e) { return e->prec == SC_FP32 ? sc::kEnsVariantsF32 : sc::kEnsVariantsF64; }
+sc::EnsVariant variant(const sc_ensemble* e, int v) {
+  return e->prec == SC_FP32 ? sc::ens_variant_f32(v) : sc::ens_variant_f64(v);
+}
 
 template <typename T> int launch_stage(sc_ensemble* e, int stage, const sc::EnsMember<T>* members, int nm,
                                        int items_y, int items_x) {
@@ -71,7 +81,8 @@ template <typename T> int launch_stage(sc_ensemble* e, int stage, const sc::EnsM
   const int grid = std::max(1, std::min(e->grid, std::max(items_y, items_x)));
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(sc::kEnsNT);
+  const sc::EnsVariant v = variant(e, e->variant);
+  cfg.blockDim = dim3(v.nt);
   cfg.dynamicSmemBytes = e->smem;
   cfg.stream = e->stream;
   cudaLaunchAttribute attr[1];
@@ -79,21 +90,76 @@ template <typename T> int launch_stage(sc_ensemble* e, int stage, const sc::EnsM
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  EC(cudaLaunchKernelEx(&cfg, sc::ens_stage_kernel<T>, ea));
+  void* args[] = {&ea};
+  EC(cudaLaunchKernelExC(&cfg, v.kernel, args));
+  return SC_OK;
+}
+
+// Make variant vi the launch shape: shared-memory limit, co-resident grid,
+// and the member tables (tile widths and item ranges depend on the shape).
+template <typename T> int select_variant(sc_ensemble* e, int vi) {
+  using C = sc::C2<T>;
+  const sc::EnsVariant v = variant(e, vi);
+  if (!v.kernel) return efail(SC_ERR_INVALID, "no such ensemble variant");
+  const size_t smem = sizeof(C) * (size_t)v.smem_elems;
+  EC(cudaFuncSetAttribute(v.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int dev = 0, nsm = 0, per = 0;
+  EC(cudaGetDevice(&dev));
+  EC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  EC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, v.kernel, v.nt, smem));
+  if (per < 1) return efail(SC_ERR_CUDA, "ensemble stage kernel does not fit on an SM");
+  e->smem = smem;
+  e->grid = nsm * per;
+  const int warps = v.nt / 32;
+  std::vector<sc::EnsMember<T>> mb(2 * e->nm);
+  C* base = static_cast<C*>(e->mem);
+  int iy = 0, ix = 0;
+  e->my_items_y.resize(e->nm);
+  e->my_items_x.resize(e->nm);
+  for (int m = 0; m < e->nm; ++m) {
+    auto& d = mb[m];
+    const int N = e->n[m];
+    d.n = N;
+    d.logn = ilog(N);
+    d.nxh = N / 2 + 1;
+    d.nxp = e->nxp[m];
+    d.ptile = v.ypts / N > 16 ? 16 : (v.ypts / N < 1 ? 1 : v.ypts / N);
+    d.ntx = (d.nxh + d.ptile - 1) / d.ptile;
+    d.field = e->field[m];
+    C* f = base + e->field_off[m];
+    d.w = f;
+    d.s = f + d.field;
+    d.acc = f + 2 * d.field;
+    d.work = f + 3 * d.field;
+    d.dt = (T)e->dt[m];
+    d.alpha = (T)e->alpha;
+    d.nu8 = (T)e->nu8[m];
+    d.scale = (T)(1.0 / ((double)N * N));
+    d.item_y0 = iy;
+    d.item_x0 = ix;
+    e->my_items_y[m] = d.ntx;
+    e->my_items_x[m] = (N + warps - 1) / warps;
+    iy += d.ntx;
+    ix += e->my_items_x[m];
+    mb[e->nm + m] = d;
+    mb[e->nm + m].item_y0 = 0;
+    mb[e->nm + m].item_x0 = 0;
+  }
+  e->items_y = iy;
+  e->items_x = ix;
+  EC(cudaMemcpyAsync(e->dmem_members, mb.data(), sizeof(sc::EnsMember<T>) * mb.size(), cudaMemcpyHostToDevice,
+                     e->stream));
+  EC(cudaStreamSynchronize(e->stream));
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  e->variant = vi;
   return SC_OK;
 }
 
 template <typename T> int setup(sc_ensemble* e) {
   using C = sc::C2<T>;
-  auto k = sc::ens_stage_kernel<T>;
-  e->smem = sizeof(C) * sc::ens_smem_elems();
-  EC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
-  int dev = 0, nsm = 0, per = 0;
-  EC(cudaGetDevice(&dev));
-  EC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  EC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, sc::kEnsNT, e->smem));
-  if (per < 1) return efail(SC_ERR_CUDA, "ensemble stage kernel does not fit on an SM");
-  e->grid = nsm * per;
   // twiddles
   std::vector<C> t(4096);
   for (int L = 2; L <= 2048; L *= 2)
@@ -118,49 +184,77 @@ template <typename T> int setup(sc_ensemble* e) {
   }
   EC(cudaMalloc(&e->mem, sizeof(C) * total));
   EC(cudaMemsetAsync(e->mem, 0, sizeof(C) * total, e->stream));
-  std::vector<sc::EnsMember<T>> mb(2 * e->nm);
-  C* base = static_cast<C*>(e->mem);
-  int iy = 0, ix = 0;
-  e->my_items_y.resize(e->nm);
-  e->my_items_x.resize(e->nm);
-  for (int m = 0; m < e->nm; ++m) {
-    auto& d = mb[m];
-    const int N = e->n[m];
-    d.n = N;
-    d.logn = ilog(N);
-    d.nxh = N / 2 + 1;
-    d.nxp = e->nxp[m];
-    d.ptile = (4096 / N) > 16 ? 16 : 4096 / N;
-    d.ntx = (d.nxh + d.ptile - 1) / d.ptile;
-    d.field = e->field[m];
-    C* f = base + e->field_off[m];
-    d.w = f;
-    d.s = f + d.field;
-    d.acc = f + 2 * d.field;
-    d.work = f + 3 * d.field;
-    d.dt = (T)e->dt[m];
-    d.alpha = (T)e->alpha;
-    d.nu8 = (T)e->nu8[m];
-    d.scale = (T)(1.0 / ((double)N * N));
-    d.item_y0 = iy;
-    d.item_x0 = ix;
-    e->my_items_y[m] = d.ntx;
-    e->my_items_x[m] = (N + sc::kEnsWarps - 1) / sc::kEnsWarps;
-    iy += d.ntx;
-    ix += e->my_items_x[m];
-    mb[e->nm + m] = d;
-    mb[e->nm + m].item_y0 = 0;
-    mb[e->nm + m].item_x0 = 0;
-  }
-  e->items_y = iy;
-  e->items_x = ix;
-  EC(cudaMalloc(&e->dmem_members, sizeof(sc::EnsMember<T>) * mb.size()));
-  EC(cudaMemcpy(e->dmem_members, mb.data(), sizeof(sc::EnsMember<T>) * mb.size(), cudaMemcpyHostToDevice));
+  EC(cudaMalloc(&e->dmem_members, sizeof(sc::EnsMember<T>) * 2 * e->nm));
   EC(cudaMalloc(&e->bar, 2 * sizeof(unsigned)));
   EC(cudaMemset(e->bar, 0, 2 * sizeof(unsigned)));
   EC(cudaMalloc(&e->err, sizeof(int)));
   EC(cudaMemset(e->err, 0, sizeof(int)));
-  return SC_OK;
+  e->tune_ms.assign(nvariants(e), -1.0);
+  // a pinned variant (SPECNS_ENS_VARIANT) skips the autotuner
+  int v0 = 0;
+  if (const char* pv = std::getenv("SPECNS_ENS_VARIANT")) {
+    v0 = std::atoi(pv);
+    if (v0 < 0 || v0 >= nvariants(e)) return efail(SC_ERR_INVALID, "SPECNS_ENS_VARIANT out of range");
+    e->tuned = true;
+  }
+  return select_variant<T>(e, v0);
+}
+
+template <typename T> int step_batched(sc_ensemble* e);
+
+// Autotuner: time every compiled variant on this ensemble (one warm-up and
+// `trial` plain steps each, CUDA events on the ensemble's stream) and keep
+// the fastest.  The member states are saved first and restored after every
+// trial, so tuning leaves the ensemble where it was.
+template <typename T> int tune(sc_ensemble* e, int trial) {
+  using C = sc::C2<T>;
+  if (trial < 1) trial = 1;
+  size_t wbytes = 0;
+  for (int m = 0; m < e->nm; ++m) wbytes += sizeof(C) * (size_t)e->field[m];
+  void* save = nullptr;
+  EC(cudaMalloc(&save, wbytes));
+  auto copy_states = [&](bool to_save) -> int {
+    size_t off = 0;
+    for (int m = 0; m < e->nm; ++m) {
+      char* w = static_cast<char*>(e->mem) + sizeof(C) * e->field_off[m];
+      char* b = static_cast<char*>(save) + off;
+      const size_t nb = sizeof(C) * (size_t)e->field[m];
+      EC(cudaMemcpyAsync(to_save ? b : w, to_save ? w : b, nb, cudaMemcpyDeviceToDevice, e->stream));
+      off += nb;
+    }
+    return SC_OK;
+  };
+  cudaEvent_t a = nullptr, b = nullptr;
+  int rc = copy_states(true);
+  if (rc == SC_OK && cudaEventCreate(&a) != cudaSuccess) rc = efail(SC_ERR_CUDA, "event creation failed");
+  if (rc == SC_OK && cudaEventCreate(&b) != cudaSuccess) rc = efail(SC_ERR_CUDA, "event creation failed");
+  int best = e->variant;
+  double best_ms = 1e300;
+  for (int v = 0; rc == SC_OK && v < nvariants(e); ++v) {
+    rc = select_variant<T>(e, v);
+    if (rc == SC_OK) rc = step_batched<T>(e);
+    if (rc == SC_OK && cudaEventRecord(a, e->stream) != cudaSuccess) rc = efail(SC_ERR_CUDA, "event record failed");
+    for (int i = 0; rc == SC_OK && i < trial; ++i) rc = step_batched<T>(e);
+    if (rc == SC_OK && cudaEventRecord(b, e->stream) != cudaSuccess) rc = efail(SC_ERR_CUDA, "event record failed");
+    float ms = 0.f;
+    if (rc == SC_OK && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
+      rc = efail(SC_ERR_CUDA, "event timing failed");
+    if (rc == SC_OK) rc = copy_states(false);
+    if (rc == SC_OK) {
+      e->tune_ms[v] = ms / trial;
+      if (ms / trial < best_ms) {
+        best_ms = ms / trial;
+        best = v;
+      }
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (rc == SC_OK) rc = select_variant<T>(e, best);
+  cudaStreamSynchronize(e->stream);
+  cudaFree(save);
+  if (rc == SC_OK) e->tuned = true;
+  return rc;
 }
 
 template <typename T> int step_batched(sc_ensemble* e) {
@@ -342,9 +436,50 @@ int sc_ens_init(sc_ensemble* e, const int* seeds, double kpeak, double energy) {
   return SC_OK;
 }
 
+int sc_ens_tune(sc_ensemble* e, int trial_steps, int* chosen) {
+  if (!e) return efail(SC_ERR_INVALID, "null ensemble");
+  const int r = e->prec == SC_FP32 ? tune<float>(e, trial_steps) : tune<double>(e, trial_steps);
+  if (r) return r;
+  if (chosen) *chosen = e->variant;
+  return check_err(e);
+}
+
+int sc_ens_set_variant(sc_ensemble* e, int v) {
+  if (!e || v < 0 || v >= nvariants(e)) return efail(SC_ERR_INVALID, "sc_ens_set_variant: bad arguments");
+  const int r = e->prec == SC_FP32 ? select_variant<float>(e, v) : select_variant<double>(e, v);
+  if (r) return r;
+  e->tuned = true;
+  return SC_OK;
+}
+
+int sc_ens_variant(sc_ensemble* e, int* v, int* count, double* tune_ms, int* shape) {
+  if (!e) return efail(SC_ERR_INVALID, "null ensemble");
+  if (v) *v = e->variant;
+  if (count) *count = nvariants(e);
+  if (tune_ms)
+    for (int i = 0; i < nvariants(e); ++i) tune_ms[i] = e->tune_ms[i];
+  if (shape) {
+    const sc::EnsVariant s = variant(e, e->variant);
+    shape[0] = s.nt;
+    shape[1] = s.minb;
+    shape[2] = s.ypts;
+    shape[3] = s.rmax;
+    shape[4] = s.outline;
+  }
+  return SC_OK;
+}
+
 int sc_ens_rk4_steps(sc_ensemble* e, int nsteps, int mode) {
   if (!e || nsteps < 0 || mode < 0 || mode > 2) return efail(SC_ERR_INVALID, "sc_ens_rk4_steps: bad arguments");
   const bool f32 = e->prec == SC_FP32;
+  if (!e->tuned && nsteps > 0) {
+    const char* t = std::getenv("SPECNS_ENS_TUNE");
+    if (t && t[0] == '0') {
+      e->tuned = true;
+    } else if (int r = f32 ? tune<float>(e, 3) : tune<double>(e, 3)) {
+      return r;
+    }
+  }
   if (mode == 2) {
     int r = f32 ? steps_one_at_a_time<float>(e, nsteps) : steps_one_at_a_time<double>(e, nsteps);
     if (r) return r;

@@ -45,14 +45,29 @@ template <typename T> struct EnsArgs {
   int* err;
 };
 
-constexpr int kEnsNT = 256;
-constexpr int kEnsWarps = kEnsNT / 32;
+// Launch shape of the stage kernel, the autotuner's search space: threads
+// per CTA, CTAs per SM (the register budget), points per y-phase tile
+// (tile width P = YPTS / N pencils, at most 16) and the FFT's largest radix.
+// OUTLINE: the phase functions are called out of line, each allocated its
+// own registers, and the y-forward accumulator sits in shared memory (fewer
+// spills, but call overhead); otherwise everything is inlined.
+template <int NT_, int MINB_, int YPTS_, int RMAX_, bool OUTLINE_> struct EnsShape {
+  static constexpr int NT = NT_, MINB = MINB_, YPTS = YPTS_, RMAX = RMAX_;
+  static constexpr bool OUTLINE = OUTLINE_;
+  static constexpr int WARPS = NT_ / 32;
+  static constexpr int ptile(int n) { return YPTS_ / n > 16 ? 16 : (YPTS_ / n < 1 ? 1 : YPTS_ / n); }
+  // dynamic shared memory (complex elements): a y tile and the y-forward
+  // accumulator slots, or per warp the x-pass transpose buffer and w row of
+  // the largest row length
+  static constexpr int smem_elems() {
+    return (OUTLINE_ ? 2 : 1) * YPTS_ > WARPS * (544 + 512) ? (OUTLINE_ ? 2 : 1) * YPTS_ : WARPS * (544 + 512);
+  }
+};
 
-template <typename T, int LOGN> struct EnsY {
+template <typename T, class SH, int LOGN> struct EnsY {
   static constexpr int N = 1 << LOGN;
-  // tile width: 4096 points per tile (2 radix-8 jobs per thread), at most 16
-  static constexpr int P = (4096 / N) > 16 ? 16 : (4096 / N);
-  using E = FFTEngine<T, LOGN, P, P, kEnsNT, true>;
+  static constexpr int P = SH::ptile(N);
+  using E = FFTEngine<T, LOGN, P, P, SH::NT, true, 0, false, SH::RMAX>;
 };
 
 // Bounded grid-wide barrier for a cooperative launch.
@@ -97,9 +112,9 @@ __device__ __forceinline__ int ens_member_of(const EnsArgs<T>& ea, int item, boo
 }
 
 // P1: y-inverse of u^, v^, w^ generated from the stage input
-template <typename T, int LOGN>
-__device__ void ens_yinv(const EnsMember<T>& mb, int tile, C2<T>* sm, const C2<T>* __restrict__ tw) {
-  using Y = EnsY<T, LOGN>;
+template <typename T, class SH, int LOGN>
+__device__ __forceinline__ void ens_yinv(const EnsMember<T>& mb, int tile, C2<T>* sm, const C2<T>* __restrict__ tw) {
+  using Y = EnsY<T, SH, LOGN>;
   using E = typename Y::E;
   using C = C2<T>;
   constexpr int P = Y::P;
@@ -133,7 +148,7 @@ __device__ void ens_yinv(const EnsMember<T>& mb, int tile, C2<T>* sm, const C2<T
 
 // P2: one warp per row: c2r of u, v, w; products; r2c into work fields 0, 1
 template <typename T, int LOGM>
-__device__ void ens_xrow(const EnsMember<T>& mb, int row, C2<T>* smw, const C2<T>* __restrict__ tw) {
+__device__ __forceinline__ void ens_xrow(const EnsMember<T>& mb, int row, C2<T>* smw, const C2<T>* __restrict__ tw) {
   using WF = WarpFFT<T, LOGM>;
   using C = C2<T>;
   constexpr int M = WF::M, E = WF::E;
@@ -190,16 +205,20 @@ __device__ void ens_xrow(const EnsMember<T>& mb, int row, C2<T>* smw, const C2<T
   }
 }
 
-// P3: y-forward of the products, N^, symmetrize2d, mask, RK stage
-template <typename T, int LOGN>
-__device__ void ens_yfwd(const EnsMember<T>& mb, int tile, int stage, C2<T>* sm, const C2<T>* __restrict__ tw) {
-  using Y = EnsY<T, LOGN>;
+// P3: y-forward of the products, N^, symmetrize2d, mask, RK stage.  With
+// SH::OUTLINE the first product's contribution waits in thread-private
+// shared-memory slots above the tile (sm[YPTS ...]) instead of registers.
+template <typename T, class SH, int LOGN>
+__device__ __forceinline__ void ens_yfwd(const EnsMember<T>& mb, int tile, int stage, C2<T>* sm,
+                                      const C2<T>* __restrict__ tw) {
+  using Y = EnsY<T, SH, LOGN>;
   using E = typename Y::E;
   using C = C2<T>;
   constexpr int P = Y::P, N = Y::N;
   const int kx0 = tile * P;
   const int nvalid = min(P, mb.nxh - kx0);
-  C nl[E::JL][E::RL];
+  C* nlbuf = sm + SH::YPTS;
+  C nl[E::JL][E::RL], nl0[E::JL][E::RL];
   for (int f = 0; f < 2; ++f) {
     C in[E::J1][E::R1], o[E::JL][E::RL];
 #pragma unroll
@@ -219,7 +238,14 @@ __device__ void ens_yfwd(const EnsMember<T>& mb, int tile, int stage, C2<T>* sm,
         E::out_pos(a, r, p, n);
         const T k = f == 0 ? (T)(kx0 + p) : (T)wavenum(n, N);
         const C t = cmulmi(cscale(o[a][r], k));   // -i k X
-        nl[a][r] = f == 0 ? t : cadd(nl[a][r], t);
+        if constexpr (SH::OUTLINE) {
+          C* slot = nlbuf + (a * E::RL + r) * SH::NT + threadIdx.x;
+          if (f == 0) *slot = t;
+          else nl[a][r] = cadd(*slot, t);
+        } else {
+          if (f == 0) nl0[a][r] = t;
+          else nl[a][r] = cadd(nl0[a][r], t);
+        }
       }
   }
   // symmetrize2d: zero ky = -N/2, kx = N/2 and the mean; kx = 0 copies
@@ -280,15 +306,39 @@ __device__ void ens_yfwd(const EnsMember<T>& mb, int tile, int stage, C2<T>* sm,
     }
 }
 
-// dynamic shared memory of ens_stage_kernel (complex elements)
-constexpr int ens_smem_elems() {
-  return 4096 > kEnsWarps * (544 + 512) ? 4096 : kEnsWarps * (544 + 512);
+// Out-of-line entry points of the phases (SH::OUTLINE).
+template <typename T, class SH, int LOGN>
+__device__ __noinline__ void ens_yinv_call(const EnsMember<T>& mb, int tile, C2<T>* sm, const C2<T>* tw) {
+  ens_yinv<T, SH, LOGN>(mb, tile, sm, tw);
+}
+template <typename T, int LOGM>
+__device__ __noinline__ void ens_xrow_call(const EnsMember<T>& mb, int row, C2<T>* smw, const C2<T>* tw) {
+  ens_xrow<T, LOGM>(mb, row, smw, tw);
+}
+template <typename T, class SH, int LOGN>
+__device__ __noinline__ void ens_yfwd_call(const EnsMember<T>& mb, int tile, int stage, C2<T>* sm,
+                                           const C2<T>* tw) {
+  ens_yfwd<T, SH, LOGN>(mb, tile, stage, sm, tw);
+}
+template <typename T, class SH, int LOGN>
+__device__ __forceinline__ void ens_p1(const EnsMember<T>& mb, int t, C2<T>* sm, const C2<T>* tw) {
+  if constexpr (SH::OUTLINE) ens_yinv_call<T, SH, LOGN>(mb, t, sm, tw);
+  else ens_yinv<T, SH, LOGN>(mb, t, sm, tw);
+}
+template <typename T, class SH, int LOGM>
+__device__ __forceinline__ void ens_p2(const EnsMember<T>& mb, int row, C2<T>* smw, const C2<T>* tw) {
+  if constexpr (SH::OUTLINE) ens_xrow_call<T, LOGM>(mb, row, smw, tw);
+  else ens_xrow<T, LOGM>(mb, row, smw, tw);
+}
+template <typename T, class SH, int LOGN>
+__device__ __forceinline__ void ens_p3(const EnsMember<T>& mb, int t, int stage, C2<T>* sm, const C2<T>* tw) {
+  if constexpr (SH::OUTLINE) ens_yfwd_call<T, SH, LOGN>(mb, t, stage, sm, tw);
+  else ens_yfwd<T, SH, LOGN>(mb, t, stage, sm, tw);
 }
 
-// One RK stage for every member.  Stage 1 reads the state as its input (the
-// host points s at w for that stage through `stage_input_is_state`).
-template <typename T>
-__global__ void __launch_bounds__(kEnsNT, 2) ens_stage_kernel(EnsArgs<T> ea) {
+// One RK stage for every member.  Stage 1 reads the state as its input.
+template <typename T, class SH>
+__global__ void __launch_bounds__(SH::NT, SH::MINB) ens_stage_kernel(EnsArgs<T> ea) {
   using C = C2<T>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -299,32 +349,30 @@ __global__ void __launch_bounds__(kEnsNT, 2) ens_stage_kernel(EnsArgs<T> ea) {
     if (ea.stage == 1) mb.s = mb.w;
     const int t = item - mb.item_y0;
     switch (mb.logn) {
-      case 4: ens_yinv<T, 4>(mb, t, sm, ea.tw); break;
-      case 5: ens_yinv<T, 5>(mb, t, sm, ea.tw); break;
-      case 6: ens_yinv<T, 6>(mb, t, sm, ea.tw); break;
-      case 7: ens_yinv<T, 7>(mb, t, sm, ea.tw); break;
-      case 8: ens_yinv<T, 8>(mb, t, sm, ea.tw); break;
-      case 9: ens_yinv<T, 9>(mb, t, sm, ea.tw); break;
-      default: ens_yinv<T, 10>(mb, t, sm, ea.tw); break;
+      case 6: ens_p1<T, SH, 6>(mb, t, sm, ea.tw); break;
+      case 7: ens_p1<T, SH, 7>(mb, t, sm, ea.tw); break;
+      case 8: ens_p1<T, SH, 8>(mb, t, sm, ea.tw); break;
+      case 9: ens_p1<T, SH, 9>(mb, t, sm, ea.tw); break;
+      default: ens_p1<T, SH, 10>(mb, t, sm, ea.tw); break;
     }
   }
   if (!ens_grid_sync(ea.bar, ea.err)) return;
-  // P2: kEnsWarps rows per item
+  // P2: SH::WARPS rows per item
   {
     const int warp = threadIdx.x >> 5;
     for (int item = blockIdx.x; item < ea.items_x; item += gridDim.x) {
       const int mi = ens_member_of(ea, item, true);
       const EnsMember<T>& mb = ea.m[mi];
-      const int row = (item - mb.item_x0) * kEnsWarps + warp;
+      const int row = (item - mb.item_x0) * SH::WARPS + warp;
       if (row >= mb.n) continue;
       C* smw = sm + warp * (WarpFFT<T, 9>::SMEM + 512);   // transpose buffer + w row, largest size
       const C* tw = ea.tw;   // WarpFFT needs the tables of M and N = 2M at tw + M, tw + 2M
       switch (mb.logn - 1) {
-        case 5: ens_xrow<T, 5>(mb, row, smw, tw); break;
-        case 6: ens_xrow<T, 6>(mb, row, smw, tw); break;
-        case 7: ens_xrow<T, 7>(mb, row, smw, tw); break;
-        case 8: ens_xrow<T, 8>(mb, row, smw, tw); break;
-        default: ens_xrow<T, 9>(mb, row, smw, tw); break;
+        case 5: ens_p2<T, SH, 5>(mb, row, smw, tw); break;
+        case 6: ens_p2<T, SH, 6>(mb, row, smw, tw); break;
+        case 7: ens_p2<T, SH, 7>(mb, row, smw, tw); break;
+        case 8: ens_p2<T, SH, 8>(mb, row, smw, tw); break;
+        default: ens_p2<T, SH, 9>(mb, row, smw, tw); break;
       }
     }
   }
@@ -335,16 +383,37 @@ __global__ void __launch_bounds__(kEnsNT, 2) ens_stage_kernel(EnsArgs<T> ea) {
     EnsMember<T> mb = ea.m[mi];
     const int t = item - mb.item_y0;
     switch (mb.logn) {
-      case 4: ens_yfwd<T, 4>(mb, t, ea.stage, sm, ea.tw); break;
-      case 5: ens_yfwd<T, 5>(mb, t, ea.stage, sm, ea.tw); break;
-      case 6: ens_yfwd<T, 6>(mb, t, ea.stage, sm, ea.tw); break;
-      case 7: ens_yfwd<T, 7>(mb, t, ea.stage, sm, ea.tw); break;
-      case 8: ens_yfwd<T, 8>(mb, t, ea.stage, sm, ea.tw); break;
-      case 9: ens_yfwd<T, 9>(mb, t, ea.stage, sm, ea.tw); break;
-      default: ens_yfwd<T, 10>(mb, t, ea.stage, sm, ea.tw); break;
+      case 6: ens_p3<T, SH, 6>(mb, t, ea.stage, sm, ea.tw); break;
+      case 7: ens_p3<T, SH, 7>(mb, t, ea.stage, sm, ea.tw); break;
+      case 8: ens_p3<T, SH, 8>(mb, t, ea.stage, sm, ea.tw); break;
+      case 9: ens_p3<T, SH, 9>(mb, t, ea.stage, sm, ea.tw); break;
+      default: ens_p3<T, SH, 10>(mb, t, ea.stage, sm, ea.tw); break;
     }
     __syncthreads();
   }
 }
+
+// The compiled shapes (sc_ens_k_*.cu, one translation unit each), by variant
+// number, <threads, CTAs per SM, tile points, radix, out of line>.  FP32:
+// 0 <256, 2, 4096, 8, no>, 1 <256, 2, 4096, 8, yes>, 2 <512, 1, 8192, 8, no>,
+// 3 <512, 1, 8192, 8, yes>, 4 <256, 2, 4096, 4, no>, 5 <512, 1, 4096, 8, no>.
+// FP64: 0 <256, 2, 4096, 8, no>, 1 <256, 2, 4096, 8, yes>.
+
+// A compiled variant as the host sees it.
+struct EnsVariant {
+  const void* kernel;   // ens_stage_kernel<T, Shape>
+  int nt, minb, ypts, rmax, outline, smem_elems;
+};
+
+template <class SH, typename T> EnsVariant ens_variant_of() {
+  return EnsVariant{reinterpret_cast<const void*>(&ens_stage_kernel<T, SH>), SH::NT, SH::MINB, SH::YPTS, SH::RMAX,
+                    SH::OUTLINE ? 1 : 0, SH::smem_elems()};
+}
+
+// defined in sc_ens_variants.cu
+EnsVariant ens_variant_f32(int v);
+EnsVariant ens_variant_f64(int v);
+constexpr int kEnsVariantsF32 = 6;
+constexpr int kEnsVariantsF64 = 2;
 
 }  // namespace sc

@@ -24,20 +24,23 @@
 
 namespace sc {
 
-// Radix plan: as many radix-8 stages as possible, finished by one radix-4
-// (LOGN % 3 == 2), two radix-4 (LOGN % 3 == 1) or a lone radix-2 (N = 2).
-__host__ __device__ constexpr int fft_nstages(int logn) {
-  return logn <= 3 ? 1 : (logn % 3 == 0 ? logn / 3 : logn / 3 + 1);
+// Radix plan.  rmax = 8: as many radix-8 stages as possible, finished by one
+// radix-4 (LOGN % 3 == 2), two radix-4 (LOGN % 3 == 1) or a lone radix-2
+// (N = 2).  rmax = 4: radix-4 stages, the last one radix-2 for odd LOGN
+// (half the registers per butterfly job, one more pass over shared memory).
+__host__ __device__ constexpr int fft_nstages(int logn, int rmax = 8) {
+  return rmax == 4 ? (logn + 1) / 2 : (logn <= 3 ? 1 : (logn % 3 == 0 ? logn / 3 : logn / 3 + 1));
 }
-__host__ __device__ constexpr int fft_radix(int logn, int s) {
-  return logn == 1 ? 2
+__host__ __device__ constexpr int fft_radix(int logn, int s, int rmax = 8) {
+  return rmax == 4 ? ((logn & 1) && s == fft_nstages(logn, 4) - 1 ? 2 : 4)
+       : logn == 1 ? 2
        : logn == 2 ? 4
        : logn % 3 == 0 ? 8
        : logn % 3 == 2 ? (s < logn / 3 ? 8 : 4)
        : (s < logn / 3 - 1 ? 8 : 4);
 }
-__host__ __device__ constexpr int fft_ns(int logn, int s) {
-  return s == 0 ? 1 : fft_ns(logn, s - 1) * fft_radix(logn, s - 1);
+__host__ __device__ constexpr int fft_ns(int logn, int s, int rmax = 8) {
+  return s == 0 ? 1 : fft_ns(logn, s - 1, rmax) * fft_radix(logn, s - 1, rmax);
 }
 
 template <typename T> struct Consts;
@@ -90,13 +93,14 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C* v)
   else dft8<INV>(v);
 }
 
-template <typename T, int LOGN, int P, int PS, int NT, bool PFAST, int PADSHIFT = 0, bool ROTATE = false>
+template <typename T, int LOGN, int P, int PS, int NT, bool PFAST, int PADSHIFT = 0, bool ROTATE = false,
+          int RMAX = 8>
 struct FFTEngine {
   using C = C2<T>;
   static constexpr int N = 1 << LOGN;
-  static constexpr int NS = fft_nstages(LOGN);
-  static constexpr int R1 = fft_radix(LOGN, 0);
-  static constexpr int RL = fft_radix(LOGN, NS - 1);
+  static constexpr int NS = fft_nstages(LOGN, RMAX);
+  static constexpr int R1 = fft_radix(LOGN, 0, RMAX);
+  static constexpr int RL = fft_radix(LOGN, NS - 1, RMAX);
   static constexpr int TOT1 = P * (N / R1);
   static constexpr int TOTL = P * (N / RL);
   static constexpr int J1 = (TOT1 + NT - 1) / NT;
@@ -185,9 +189,9 @@ struct FFTEngine {
   // Stage S (0 < S < NS-1): shared -> shared.
   template <int S, bool INV>
   __device__ static __forceinline__ void mid_stage(C* sm, const C* __restrict__ tw) {
-    constexpr int R = fft_radix(LOGN, S);
+    constexpr int R = fft_radix(LOGN, S, RMAX);
     constexpr int NR = N / R;
-    constexpr int NSV = fft_ns(LOGN, S);
+    constexpr int NSV = fft_ns(LOGN, S, RMAX);
     constexpr int TOT = P * NR;
     constexpr int J = (TOT + NT - 1) / NT;
     C v[J][R];
@@ -241,7 +245,7 @@ struct FFTEngine {
   template <bool INV>
   __device__ static __forceinline__ void last_stage(C (&out)[JL][RL], C* sm, const C* __restrict__ tw) {
     constexpr int NR = N / RL;
-    constexpr int NSV = fft_ns(LOGN, NS - 1);
+    constexpr int NSV = fft_ns(LOGN, NS - 1, RMAX);
     static_assert(NSV == NR, "last stage spans the pencil");
 #pragma unroll
     for (int a = 0; a < JL; ++a) {
@@ -305,7 +309,7 @@ struct FFTEngine {
       mid_stages<1, INV>(sm, tw);
       // last stage: shared -> registers
       constexpr int NR = N / RL;
-      constexpr int NSV = fft_ns(LOGN, NS - 1);
+      constexpr int NSV = fft_ns(LOGN, NS - 1, RMAX);
       static_assert(NSV == NR, "last stage spans the pencil");
 #pragma unroll
       for (int a = 0; a < JL; ++a) {

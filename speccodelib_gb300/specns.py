@@ -335,5 +335,25 @@ class Ensemble2D:
     def uses_graph(self):
         return bool(lib().sc_ens_uses_graph(self.h))
 
+    def tune(self, trial_steps=3):
+        """Time every compiled launch shape on this ensemble; keep the fastest."""
+        v = C.c_int(0)
+        _check(lib().sc_ens_tune(self.h, trial_steps, C.byref(v)))
+        return v.value
+
+    def set_variant(self, v):
+        _check(lib().sc_ens_set_variant(self.h, v))
+
+    def variant(self):
+        """(variant, {"threads", "ctas_per_sm", "tile_points", "radix", "outline"},
+        ms per step of each variant in the last tuning, -1 = not timed)"""
+        v, cnt = C.c_int(0), C.c_int(0)
+        _check(lib().sc_ens_variant(self.h, C.byref(v), C.byref(cnt), None, None))
+        ms = (C.c_double * cnt.value)()
+        shape = (C.c_int * 5)()
+        _check(lib().sc_ens_variant(self.h, C.byref(v), C.byref(cnt), ms, shape))
+        keys = ("threads", "ctas_per_sm", "tile_points", "radix", "outline")
+        return v.value, dict(zip(keys, list(shape))), list(ms)
+
     def set_stream(self, stream_ptr):
         _check(lib().sc_ens_set_stream(self.h, C.c_void_p(stream_ptr)))
