@@ -40,6 +40,14 @@ METRIC = "RK4 steps/s, 512^3 forced DNS (FP32 bulk; plain FP64 alongside)"
 UNIT = "steps/s"
 
 
+def workload_config(n, world):
+    """The workload both arms report (the reference arm samples it on the CPU)."""
+    return {"workload": "forced DNS %d^3 IF-RK4, FP32 bulk" % n, "grid": n,
+            "nu": NU, "dt": DT, "eps": EPS, "fkmax": FKMAX,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (%d MB per field)" % round((n // 2 + 1) * n * n * 8 / 1e6)}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -182,7 +190,7 @@ def run_reference(a):
            "warmup": a.warmup, "ms_per_step": 4000.0 * t_rhs, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
            "impl": "reference",
-           "config": {"workload": "forced DNS %d^3 IF-RK4 (one RHS per sample)" % n, "grid": n},
+           "config": workload_config(n, world),
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
                             "sample": sample},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -430,10 +438,7 @@ def run_ours(a):
                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (ran1 seed 1 initial field, as the reference generates it)",
-               "config": {"workload": "forced DNS %d^3 IF-RK4, FP32 bulk" % n, "grid": n,
-                          "nu": NU, "dt": DT, "eps": EPS, "fkmax": FKMAX,
-                          "parallelism": "replicas" if world > 1 else "single GPU",
-                          "l2": "inputs larger than L2 (539 MB per field)"},
+               "config": workload_config(n, world),
                "gpu_launches": launches,
                "roofline": roofline,
                "step_model_bytes": step_bytes,
