@@ -437,11 +437,16 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
 #define SC_ZINV5_CASE_double(L) case L: return sc::launch_zinv5<double, L>(vmap, za, out, g, tw, err, s);
 #define SC_ZPHI_CASE_float(L) case L: return sc::launch_zinv_phi<float, L>(lmap, za, out, g, tw, err, s);
 #define SC_ZPHI_CASE_double(L) case L: return sc::launch_zinv_phi<double, L>(lmap, za, out, g, tw, err, s);
+#define SC_ZI_P_CASE_float(L) case L: return sc::ZiCfg<float, L>::P;
+#define SC_ZI_P_CASE_double(L) case L: return sc::ZiCfg<double, L>::P;
 #define SC_ZI_OK_CASE_float(L) case L: return sc::ZiCfg<float, L>::SUPPORTED;
 #define SC_ZI_OK_CASE_double(L) case L: return sc::ZiCfg<double, L>::SUPPORTED;
 #define SC_DEFINE_FUSED(T)                                                                       \
   template <> bool sc::Launch<T>::zinv5_supported(int logn) {                                   \
     switch (logn) { SC_LOGN_CASES(SC_ZI_OK_CASE_##T) default: return false; }                    \
+  }                                                                                              \
+  template <> int sc::Launch<T>::zinv5_tile(int logn) {                                          \
+    switch (logn) { SC_LOGN_CASES(SC_ZI_P_CASE_##T) default: return 0; }                         \
   }                                                                                              \
   template <>                                                                                    \
   cudaError_t sc::Launch<T>::zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, \

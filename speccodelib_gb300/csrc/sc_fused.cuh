@@ -41,6 +41,8 @@ template <typename T> struct FusedArgs {
 
 template <typename T, int LOGN> struct ZiCfg {
   using Cfg = TmaCfg<T, LOGN>;
+  // tile width: the strided passes' width (halving it, for more CTAs per SM,
+  // measured slower: 32-byte row segments)
   static constexpr int P = Cfg::P;
   static constexpr int N = Cfg::N;
   // two points per thread and radix-8 job at most 256 threads (ZI_DIV 16,
@@ -50,9 +52,12 @@ template <typename T, int LOGN> struct ZiCfg {
   static constexpr int EB = NT >= 512 ? 2 : 4;   // epilogue batch
   using EngF = FFTEngine<T, LOGN, P, P, NT, true, 0, true>;           // whole tile, in place
   using EngH = FFTEngine<T, LOGN, P / 2, P / 2, NT, true, 0, true>;   // half tile
-  static constexpr size_t TILE = Cfg::TILE_BYTES;
+  static constexpr size_t TILE = sizeof(C2<T>) * (size_t)N * P;
   static constexpr size_t SMEM = 3 * TILE + TILE / 2 + kSmemAlignPad;
   static constexpr bool SUPPORTED = P >= 2 && SMEM <= 113 * 1024;
+  // CTAs per SM that the shared memory allows (228 KB, 1 KB reserved per CTA)
+  static constexpr int MINB_RAW = (int)(233472 / (SMEM + 1024));
+  static constexpr int MINB = MINB_RAW > 4 ? 4 : (MINB_RAW < 1 ? 1 : MINB_RAW);
 };
 
 // Steps after the stage input s of tile (kx0, iy) is in the three tiles rt
@@ -117,7 +122,7 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
 // Standalone z-inverse (DNS): the stage input tile by TMA, K_f partial sums,
 // then zinv_from_tiles.  grid = (kx tiles or za.tiles_x, ny).
 template <typename T, int LOGN>
-__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, 2)
+__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
 zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldList<T> out, Geom g,
                  const C2<T>* __restrict__ tw, int* err) {
   using Z = ZiCfg<T, LOGN>;
@@ -177,7 +182,7 @@ zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldLi
 // c = sum Re(conj(mu) v) of the stage input v.  lam tiles by TMA, mu formed
 // in shared memory, three in-place transforms.  grid = (kx tiles, ny).
 template <typename T, int LOGN>
-__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, 2)
+__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
 zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, FieldList<T> out, Geom g,
                     const C2<T>* __restrict__ tw, int* err) {
   using Z = ZiCfg<T, LOGN>;
@@ -255,7 +260,7 @@ zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, Fiel
 // z-forward pass of RK stages 1-3 fused with the next stage's z-inverse.
 // grid = (kx tiles, ny).
 template <typename T, int LOGN>
-__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, 2)
+__global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
 zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, FusedArgs<T> fa, Geom g,
                      const C2<T>* __restrict__ tw, int* err) {
   using Z = ZiCfg<T, LOGN>;

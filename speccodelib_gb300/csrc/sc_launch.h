@@ -55,9 +55,10 @@ template <typename T> struct Launch {
                               const C2<T>* tw, int* err, cudaStream_t s);
   // z-inverse of the DNS operands with five transforms from TMA-loaded stage
   // input tiles, and the z-forward pass of RK stages 1-3 fused with it
-  // (sc_fused.cuh); both use the tma_tile width.  zinv5_supported: whether the
+  // (sc_fused.cuh), tile width zinv5_tile.  zinv5_supported: whether the
   // tiles fit shared memory for this length (else cudaErrorNotSupported).
   static bool zinv5_supported(int logn);
+  static int zinv5_tile(int logn);     // tile width of zinv5 / zinv_phi / zfwd_zinv
   static cudaError_t zinv5_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,
                                const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                                cudaStream_t s);

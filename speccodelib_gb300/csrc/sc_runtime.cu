@@ -361,7 +361,9 @@ template <typename T> struct Impl {
     st.eps = h->p.eps;
     st.kf_partial = h->kf_partial;
     // tiles of the zinv kernel that writes the K_f partial sums
-    const int pt = (h->tma && h->tma_zinv && h->p.sgs == SC_SGS_NONE) ? L::tma_ztile(h->logz) : pencil_tile(h->logz);
+    const int pt = use_zinv5(h) ? L::zinv5_tile(h->logz)
+                   : (h->tma && h->tma_zinv && h->p.sgs == SC_SGS_NONE) ? L::tma_ztile(h->logz)
+                                                                        : pencil_tile(h->logz);
     int nt = 0;
     const int ntiles = (h->g.nxh + pt - 1) / pt;
     while (nt < ntiles && (double)(nt * pt) * (nt * pt) < h->p.fkmax * h->p.fkmax) ++nt;
@@ -486,8 +488,7 @@ template <typename T> struct Impl {
   // (sc_fused.cuh): DNS, TMA passes, the fused kernel compiled for this
   // length, and its tile equal to zinv's so the K_f partial sums line up.
   static bool use_zinv5(sc_handle* h) {
-    return h->zinv5 && h->tma && !h->tma_zinv && h->p.sgs == SC_SGS_NONE && L::zinv5_supported(h->logz) &&
-           L::tma_tile(h->logz) == pencil_tile(h->logz);
+    return h->zinv5 && h->tma && !h->tma_zinv && h->p.sgs == SC_SGS_NONE && L::zinv5_supported(h->logz);
   }
   static bool can_fuse(sc_handle* h) { return h->fuse && use_zinv5(h); }
 
@@ -514,9 +515,11 @@ template <typename T> struct Impl {
     if (h->tma && !les && sin_spaced) {
       CUtensorMap vmap, lmap;
       const bool z5 = use_zinv5(h);
-      const int PZ = L::tma_ztile(h->logz), P = L::tma_tile(h->logz);
-      SC_TRY(encode_fields(h, sin[0], 3, 2, z5 ? P : PZ, g->nz, &vmap));
+      const int PZ = L::tma_ztile(h->logz), P = L::tma_tile(h->logz), P5 = L::zinv5_tile(h->logz);
+      SC_TRY(encode_fields(h, sin[0], 3, 2, z5 ? P5 : PZ, g->nz, &vmap));
       SC_TRY(encode_fields(h, wl.f[0], 3, 2, P, g->nz, &lmap));
+      CUtensorMap lmap5 = lmap;   // the Lamb vector as the fused kernel tiles it
+      if (z5 && P5 != P) SC_TRY(encode_fields(h, wl.f[0], 3, 2, P5, g->nz, &lmap5));
       if (fuse & FUSE_IN) {
         // produced by the previous stage
       } else if (z5) {
@@ -534,11 +537,11 @@ template <typename T> struct Impl {
         fa.out = wl;
         fa.kf_next = kf_next;
         fa.store_all = store_all;
-        SC_TRY(launch(h, "zfwd_zinv", [&] { return L::zfwd_zinv_tma(h->logz, lmap, st, fa, *g, tw(h, g->nz), h->derr, h->stream); }));
+        SC_TRY(launch(h, "zfwd_zinv", [&] { return L::zfwd_zinv_tma(h->logz, lmap5, st, fa, *g, tw(h, g->nz), h->derr, h->stream); }));
         SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));
         // the kx = 0 tile of the next stage's zinv, after the fix-up
         CUtensorMap smap;
-        SC_TRY(encode_fields(h, st.sout[0], 3, 2, P, g->nz, &smap));
+        SC_TRY(encode_fields(h, st.sout[0], 3, 2, P5, g->nz, &smap));
         sc::ZvArgs<T> z0 = za;
         for (int c = 0; c < 3; ++c) z0.v[c] = st.sout[c];
         z0.fs.partial = kf_next;
@@ -653,9 +656,10 @@ template <typename T> struct Impl {
     for (int i = 0; i < 9; ++i) w9.f[i] = AF(h, i);
     const bool spaced3 = aa.s[1] == aa.s[0] + g->field && aa.s[2] == aa.s[0] + 2 * g->field &&
                          aa.lw[1] == aa.lw[0] + g->field && aa.lw[2] == aa.lw[0] + 2 * g->field;
-    if (use_zinv5(h) && spaced3) {
+    const bool split5 = use_zinv5(h) && spaced3;
+    if (split5) {
       // u, w of the stage input (five transforms) and phi from lam, both TMA-fed
-      const int P = L::tma_tile(h->logz);
+      const int P = L::zinv5_tile(h->logz);
       CUtensorMap smap, lmap;
       SC_TRY(encode_fields(h, aa.s[0], 3, 2, P, g->nz, &smap));
       SC_TRY(encode_fields(h, aa.lw[0], 3, 2, P, g->nz, &lmap));
@@ -692,7 +696,8 @@ template <typename T> struct Impl {
     else SC_TRY(launch(h, "adj_ypass_fwd", [&] { return L::plain(h->logy, false, yf, ypass_args(h, 6), *g, g->nz, tw(h, g->ny), h->stream); }));
     aa.kf_partial = h->kf_partial;
     aa.c_partial = h->cpart;
-    const int pt = pencil_tile(h->logz);
+    // tile width of the kernels that wrote the band sums
+    const int pt = split5 ? L::zinv5_tile(h->logz) : pencil_tile(h->logz);
     int nt = 0;
     const int ntiles = (g->nxh + pt - 1) / pt;
     while (nt < ntiles && (double)(nt * pt) * (nt * pt) < h->p.fkmax * h->p.fkmax) ++nt;

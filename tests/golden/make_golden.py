@@ -5,7 +5,11 @@
 Fixtures (NumPy .npz, complex128 spectral fields in the reference layout
 (nz, ny, nx/2+1)): the seeded 16^3 initial field (ran1 seed 1, akp = 4,
 E = 0.5), its right-hand side, the state after 1 and 10 IF-RK4 steps, after
-3 IF-AB2 passes, and the Smagorinsky / dynamic-Smagorinsky stresses.  The
+3 IF-AB2 passes, and the Smagorinsky / dynamic-Smagorinsky stresses.  c1_128:
+the forced-DNS configuration at 128^3 in FP64 (nu = 0.01, dt = 2e-3, the same
+seeded field) after 1, 10 and 100 steps, stored compactly as the block of
+wavenumbers |kx|, |ky|, |kz| <= 6 plus, after 100 steps, the shell spectrum,
+energy and dissipation (python tests/golden/make_golden.py c1; a few minutes).  The
 reference itself cannot be run here; these fixtures freeze the oracle's
 outputs so that both the oracle and the CUDA library are checked against the
 same committed numbers.
@@ -43,5 +47,35 @@ def main():
                         seq_m7=R.ran1_sequence(-7, 4096))
 
 
+C1_N, C1_K = 128, 6
+
+
+def c1_block(v):
+    """Wavenumbers |kx|, |ky|, |kz| <= C1_K of three (nz, ny, nx/2+1) fields."""
+    idx = np.r_[0:C1_K + 1, C1_N - C1_K:C1_N]
+    return np.stack([a[np.ix_(idx, idx, np.arange(C1_K + 1))] for a in v])
+
+
+def c1():
+    n = C1_N
+    kcut = 2.0 * (n // 2) / 3.0
+    v = R.initialize_dealiased(n, n, n, 1, 4.0, 1.0 / np.sqrt(3.0), kcut)
+    g = R.Grid(R.Params(nx=n, nu=NU, dt=DT))
+    out = {}
+    done = 0
+    for target in (1, 10, 100):
+        v = R.rk4_run(v, g, target - done)
+        done = target
+        out["v%d" % target] = c1_block(v)
+    _, _, _, k2 = R.wavenumber(n, n, n)
+    out["ek100"] = R.spectrum(v, k2, n)
+    out["energy100"] = R.energy(v)
+    out["diss100"] = R.dissipation(v, k2, NU)
+    np.savez_compressed(os.path.join(HERE, "c1_128.npz"), n=n, kmax=C1_K, nu=NU, dt=DT, **out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["c1"]:
+        c1()
+    else:
+        main()

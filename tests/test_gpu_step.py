@@ -256,3 +256,58 @@ def test_graph_replay_matches_eager(specns_lib, prec, monkeypatch):
             h.rk4_steps(2)
             outs.append(h.get_state())
     assert rel_l2(outs[0], outs[1]) == 0.0
+
+
+@pytest.mark.parametrize("prec,tol", [(S.SC_FP64, (1e-12, 1e-12, 1e-11)), (S.SC_FP32, (1e-5, 1e-5, 1e-4))])
+def test_c1_forced_dns_128_against_fixture(specns_lib, prec, tol):
+    """Forced DNS at 128^3 (nu = 0.01, dt = 2e-3, the seeded ran1 field)
+    after 1, 10 and 100 steps against the oracle's committed results
+    (tests/golden/c1_128.npz): the wavenumbers |k| <= 6 per axis, and the
+    shell spectrum, energy and dissipation (FP64 diagnostics) at step 100."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "c1_128.npz"))
+    n, km = int(d["n"]), int(d["kmax"])
+    idx = np.r_[0:km + 1, n - km:n]
+
+    def block(v):
+        return np.stack([a[np.ix_(idx, idx, np.arange(km + 1))] for a in v])
+
+    with handle(n, prec, nu=float(d["nu"]), dt=float(d["dt"])) as h:
+        h.init_field(seed=1, akp=4.0, u0=1 / np.sqrt(3))
+        done = 0
+        for i, target in enumerate((1, 10, 100)):
+            h.rk4_steps(target - done)
+            done = target
+            assert rel_l2(block(h.get_state()), d["v%d" % target]) < tol[i], target
+        diag, eks = h.diagnostics()
+    ek = d["ek100"]
+    m = ek > 1e-10 * ek.sum()
+    assert np.max(np.abs(eks[m] - ek[m]) / ek[m]) < 10 * tol[2]
+    assert abs(diag["energy"] - float(d["energy100"])) < tol[2] * float(d["energy100"])
+    assert abs(diag["dissipation"] - float(d["diss100"])) < tol[2] * float(d["diss100"])
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_fused_stage_passes_long_z(specns_lib, prec, monkeypatch):
+    """nz = 512 with a small (nx, ny): the 512-point z-passes of the fused
+    step (FP64 tiles of 4 pencils, FP32 of 8) against the oracle, in all three
+    z-pass arrangements, forcing band wide enough to reach kx tiles past the
+    first."""
+    nx, ny, nz = 32, 16, 512
+    v = hermitian_fields((nx, ny, nz), 5, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.02, fkmax=6.0))
+    ref = R.rk4_run(tuple(v), g, 2)
+    outs = []
+    for nofuse, noz5 in (("0", "0"), ("1", "0"), ("1", "1")):
+        monkeypatch.setenv("SPECNS_NO_FUSE", nofuse)
+        monkeypatch.setenv("SPECNS_NO_ZINV5", noz5)
+        with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.02, fkmax=6.0)) as h:
+            h.set_state(*v)
+            h.rk4_steps(2)
+            outs.append(h.get_state())
+    for o in outs:
+        assert rel_l2(o, ref) < TOL[prec]
+    for o in outs[1:]:
+        assert rel_l2(outs[0], o) < (1e-13 if prec == S.SC_FP64 else 2e-6)
