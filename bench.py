@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-les", action="store_true")
     return ap.parse_args()
 
 
@@ -385,6 +386,25 @@ def run_ours(a):
                            "K steps and each segment recomputed"}
         torch.cuda.empty_cache()
 
+    # ---- LES at 256^3 FP32: Smagorinsky (c1 = 0.17^2) and dynamic (update every 10) ----
+    les = None
+    if not a.no_les:
+        les = {"grid": 256, "nu": 1e-4, "dt": 1e-3, "init": "E(k) ~ k^-5/3 on 2 <= k <= 85, E = 0.5"}
+        for sgs, name in ((S.SC_SGS_SMAG, "smagorinsky"), (S.SC_SGS_DYNSMAG, "dynamic")):
+            p = S.default_params(256, S.SC_FP32, nu=1e-4, dt=1e-3, sgs=sgs, c1=0.17 ** 2)
+            hl = S.SpectralNS(p)
+            hl.set_stream(stream.cuda_stream)
+            hl.init_field(seed=SEED, kind=1, u0=U0, kmin=2.0, kmax=85.0)
+            hl.rk4_steps(3)
+            kl = 20   # two dynamic-coefficient updates
+            ms_l = time_steps(hl, kl)
+            d_l, _ = hl.diagnostics()
+            hl.close()
+            del hl
+            les[name] = {"steps_per_s": kl / (ms_l / 1e3), "ms_per_step": ms_l / kl,
+                         "energy_after": d_l["energy"], "cs2": d_l["cs2"]}
+        torch.cuda.empty_cache()
+
     # ---- batched 2D ensemble: 24 x 256^2, 24 x 512^2, 16 x 1024^2 ----
     ensemble = None
     if not a.no_ensemble:
@@ -448,6 +468,7 @@ def run_ours(a):
                "e2e": e2e,
                "fp64": fp64,
                "adjoint": adjoint,
+               "les256": les,
                "ensemble2d": ensemble,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)

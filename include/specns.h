@@ -30,6 +30,7 @@ extern "C" {
 #define SC_ERR_NONFINITE 3   /* NaN/Inf found in the state */
 #define SC_ERR_TIMEOUT 4     /* a bounded device wait gave up */
 #define SC_ERR_NOMEM 5       /* device allocation failed */
+#define SC_ERR_IO 6          /* a file could not be read or written, or its records do not match */
 
 #define SC_FP32 0            /* FP32 bulk (twiddles rounded from FP64, FP64 reductions) */
 #define SC_FP64 1            /* plain FP64 */
@@ -91,6 +92,9 @@ int sc_set_stream(sc_handle* h, void* stream);
 /* Change dt (recomputes the integrating-factor tables). */
 int sc_set_dt(sc_handle* h, double dt);
 
+/* The handle's parameters (after defaults were filled in at sc_create). */
+int sc_get_params(sc_handle* h, sc_params* out);
+
 /* State upload / download in the reference layout (host pointers).
  * Replaces input / output of input.f90:106-136, output.f90:103-132. */
 int sc_set_state(sc_handle* h, const void* vx, const void* vy, const void* vz);
@@ -149,6 +153,26 @@ int sc_adjoint_kept_segments(sc_handle* h, int* kept);
  * in place.  Same checkpointing as sc_adjoint_rk4.  No reference counterpart. */
 int sc_adjoint_rk4_vjp(sc_handle* h, int nsteps, int checkpoint_every, const void* lx, const void* ly,
                        const void* lz, void* gx, void* gy, void* gz);
+
+/* Fortran unformatted field files, as the reference's output3d / input3d
+ * write and read them (output.f90:103-132, input.f90:106-136): the state goes
+ * to <dir>/ux<idump>.dat, uy<idump>.dat, uz<idump>.dat ("./out" in the
+ * reference), one sequential unformatted record each holding the
+ * complex(sp) (nx/2+1, ny, nz) array in Fortran order.  file_precision
+ * (SC_FP32 / SC_FP64) is the sp of the reference build that writes or reads
+ * the files; values convert to and from the handle's precision.  sc_input3d
+ * loads the state as sc_set_state does. */
+int sc_output3d(sc_handle* h, const char* dir, int idump, int file_precision);
+int sc_input3d(sc_handle* h, const char* dir, int idump, int file_precision);
+
+/* One record of a gfortran sequential unformatted file, host memory only: a
+ * 4-byte little-endian length marker, the bytes, the marker again; records
+ * longer than max_subrecord bytes (0 = gfortran's 2147483639) are split into
+ * subrecords, a leading marker negative when more follow and a trailing
+ * marker negative when one precedes.  The reader follows the markers and
+ * requires exactly nbytes of data. */
+int sc_fortran_record_write(const char* path, const void* data, long long nbytes, long long max_subrecord);
+int sc_fortran_record_read(const char* path, void* data, long long nbytes);
 
 /* FP64 diagnostics of the current state; eks (may be NULL) receives the
  * shell spectrum E(k), k = 1..nx/2 (specdns-forced-omp-ft.f90:159-176). */

@@ -19,6 +19,8 @@ _LIB = None
 _P = C.c_void_p
 _I = C.c_int
 _D = C.c_double
+_LL = C.c_longlong
+_CS = C.c_char_p
 
 # argument types of every function declared in include/specns.h
 SIGNATURES = {
@@ -38,6 +40,11 @@ SIGNATURES = {
     "sc_rk4_steps": ([_P, _I], _I),
     "sc_ab2_steps": ([_P, _I], _I),
     "sc_diagnostics": ([_P, _P, _P], _I),
+    "sc_get_params": ([_P, _P], _I),
+    "sc_output3d": ([_P, _CS, _I, _I], _I),
+    "sc_input3d": ([_P, _CS, _I, _I], _I),
+    "sc_fortran_record_write": ([_CS, _P, _LL, _LL], _I),
+    "sc_fortran_record_read": ([_CS, _P, _LL], _I),
     "sc_adjoint_rk4": ([_P, _I, _I, _I, _I, _P, _P, _P, _P], _I),
     "sc_adjoint_rk4_vjp": ([_P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
     "sc_set_adjoint_budget": ([_P, _D], _I),

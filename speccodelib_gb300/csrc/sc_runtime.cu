@@ -1258,6 +1258,12 @@ int sc_set_stream(sc_handle* h, void* stream) {
   return SC_OK;
 }
 
+int sc_get_params(sc_handle* h, sc_params* out) {
+  if (!h || !out) return fail(SC_ERR_INVALID, "null argument");
+  *out = h->p;
+  return SC_OK;
+}
+
 int sc_set_dt(sc_handle* h, double dt) {
   if (!h || !(dt > 0)) return fail(SC_ERR_INVALID, "need a handle and dt > 0");
   return h->p.precision == SC_FP32 ? Impl<float>::set_dt(h, dt) : Impl<double>::set_dt(h, dt);

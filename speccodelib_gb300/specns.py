@@ -250,6 +250,17 @@ class SpectralNS:
                                     *[_ptr(a, True) for a in g], C.byref(J)))
         return J.value, tuple(g)
 
+    def output3d(self, directory, idump, file_precision=None):
+        """Write the state as the reference's output3d does:
+        <directory>/u{x,y,z}<idump>.dat, Fortran unformatted records."""
+        fp = self.p.precision if file_precision is None else file_precision
+        _check(lib().sc_output3d(self.h, str(directory).encode(), int(idump), fp))
+
+    def input3d(self, directory, idump, file_precision=None):
+        """Load the state from the reference's output3d files."""
+        fp = self.p.precision if file_precision is None else file_precision
+        _check(lib().sc_input3d(self.h, str(directory).encode(), int(idump), fp))
+
     def set_adjoint_budget(self, nbytes):
         """Bytes for the adjoint's stage-input store (< 0: 90% of free memory,
         0: pure checkpointing with recomputation)."""

@@ -1,0 +1,39 @@
+"""sc_output3d / sc_input3d: the state as the reference's output3d writes it
+(u{x,y,z}<n>.dat, one Fortran unformatted record of complex(sp)
+(nx/2+1, ny, nz) each) and back."""
+import os
+
+import numpy as np
+import pytest
+
+import speccodelib_gb300 as S
+from oracle import fortran_record as FR
+from _util import rel_l2, solenoidal_init
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", [S.SC_FP64, S.SC_FP32])
+def test_output3d_files_and_round_trip(specns_lib, prec, tmp_path):
+    n = 32
+    v = solenoidal_init(n)
+    dt = np.complex128 if prec == S.SC_FP64 else np.complex64
+    with S.SpectralNS(S.default_params(n, prec)) as h:
+        h.set_state(*v)
+        h.rk4_steps(2)
+        state = h.get_state()
+        h.output3d(tmp_path, 7)
+        for c, name in enumerate(("ux", "uy", "uz")):
+            raw = open(os.path.join(tmp_path, "%s7.dat" % name), "rb").read()
+            arr = np.frombuffer(FR.read_record(raw), dtype=dt).reshape(state[c].shape)
+            assert np.array_equal(arr, state[c])          # Fortran order == (nz, ny, nx/2+1) C order
+        h.rk4_steps(1)
+        h.input3d(tmp_path, 7)
+        assert all(np.array_equal(a, b) for a, b in zip(h.get_state(), state))
+        # a reference build of the other precision: converted on the way out and in
+        other = S.SC_FP32 if prec == S.SC_FP64 else S.SC_FP64
+        h.output3d(tmp_path, 8, file_precision=other)
+        h.input3d(tmp_path, 8, file_precision=other)
+        assert rel_l2(h.get_state(), state) < (1e-7 if prec == S.SC_FP64 else 1e-15)
+        with pytest.raises(S.SpecNSError):
+            h.input3d(tmp_path, 99)                        # no such files
