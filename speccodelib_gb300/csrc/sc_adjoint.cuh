@@ -39,6 +39,11 @@ template <typename T> struct AdjArgs {
   int kf_tiles, kf_ptile;
   int mask_rhs;
   double kcut2;
+  // stage 1 only: chain = also start the previous step's adjoint (its masked
+  // lam into lt_next, dt/6 of it into lw, what a separate init pass would
+  // write); write_lam = store lam itself (the last step: the gradient)
+  C2<T>* lt_next[3];
+  int chain, write_lam;
 };
 
 // Add transformed product field f (0-2: w x phi, 3-5: phi x u), in the
@@ -162,10 +167,22 @@ __device__ __forceinline__ void adj_epilogue(C2<T> (&l)[E::JL][E::RL][3], const 
             lw[c][idx[b]] = cadd(cscale(ltv[b][c], Ef * Ef * dt / T(6)), cscale(ls[c], T(0.5) * Ef * dt));
           }
           break;
-        default:     // stage 1: lam = lv + ls
+        default: {   // stage 1: lam = lv + ls
+          const double kz = wavenum(iz, g.nz), ky = wavenum(iy, g.ny);
+          const double k2 = (double)ix * ix + ky * ky + kz * kz;
+          const bool cut = k2 >= aa.kcut2 && k2 > 0.0;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) lam[c][idx[b]] = cadd(lvv[b][c], ls[c]);
+          for (int c = 0; c < 3; ++c) {
+            const C lm = cadd(lvv[b][c], ls[c]);
+            if (aa.write_lam) lam[c][idx[b]] = lm;
+            if (aa.chain) {
+              const C l0 = cut ? czero<C>() : lm;
+              aa.lt_next[c][idx[b]] = l0;
+              lw[c][idx[b]] = cscale(l0, dt / T(6));
+            }
+          }
           break;
+        }
       }
     }
   }

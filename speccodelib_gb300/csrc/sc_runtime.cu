@@ -715,21 +715,29 @@ template <typename T> struct Impl {
   }
 
   // lam_n = S'(v_n)^T lam_{n+1}; st = the step's stage inputs; lam in slots 9..11
-  static int adj_step(sc_handle* h, C* const st[4][3]) {
+  // init: lt, lw from lam by a separate pass (the first backward step; later
+  // steps get them from the previous step's stage 1, `chain`); write_lam:
+  // store lam = the adjoint of v_n (the last backward step)
+  static int adj_step(sc_handle* h, C* const st[4][3], bool init, bool chain, bool write_lam) {
     auto* g = &h->g;
-    sc::AdjOpArgs<T> ao{};
-    ao.op = sc::AO_INIT;
-    for (int c = 0; c < 3; ++c) { ao.in[c] = AF(h, 9 + c); ao.out1[c] = AF(h, 12 + c); ao.out2[c] = AF(h, 18 + c); }
-    ao.dt = (T)h->p.dt;
-    ao.kcut2 = kcut2(h);
-    SC_TRY(launch(h, "adj_init", [&] { return L::adj_op(ao, *g, h->stream); }));
+    if (init) {
+      sc::AdjOpArgs<T> ao{};
+      ao.op = sc::AO_INIT;
+      for (int c = 0; c < 3; ++c) { ao.in[c] = AF(h, 9 + c); ao.out1[c] = AF(h, 12 + c); ao.out2[c] = AF(h, 18 + c); }
+      ao.dt = (T)h->p.dt;
+      ao.kcut2 = kcut2(h);
+      SC_TRY(launch(h, "adj_init", [&] { return L::adj_op(ao, *g, h->stream); }));
+    }
     sc::AdjArgs<T> aa{};
     for (int c = 0; c < 3; ++c) {
       aa.lam[c] = AF(h, 9 + c);
       aa.lt[c] = AF(h, 12 + c);
+      aa.lt_next[c] = AF(h, 12 + c);
       aa.lv[c] = AF(h, 15 + c);
       aa.lw[c] = AF(h, 18 + c);
     }
+    aa.chain = chain;
+    aa.write_lam = write_lam;
     aa.ex = reinterpret_cast<const T*>(h->ex);
     aa.ey = reinterpret_cast<const T*>(h->ey);
     aa.ez = reinterpret_cast<const T*>(h->ez);
@@ -905,7 +913,8 @@ template <typename T> struct Impl {
         C* st[4][3];
         for (int k = 0; k < 4; ++k)
           for (int c = 0; c < 3; ++c) st[k][c] = slot(base, i, k, c);
-        SC_TRY(adj_step(h, st));
+        const bool first = sg == ncp - 1 && i == len - 1, last = sg == 0 && i == 0;
+        SC_TRY(adj_step(h, st, first, !last, last));
       }
     }
     // restore the state v_0
