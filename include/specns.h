@@ -274,6 +274,28 @@ int sc_projection(int precision, void* vx, void* vy, void* vz, int lx1, int ly, 
 int sc_force(int precision, void* wx, void* wy, void* wz, const void* vx, const void* vy,
              const void* vz, int lx1, int ly, int lz, double fkmax, double eps);
 
+/* force_rot(wx,wy,wz,vx,vy,vz,k2,lx1,ly,lz,fk12,fk22,eps), force_rot.f90:3:
+ * w += eps/(2 K + tiny) v on the shell band fk12 <= k^2 < fk22 (squared
+ * bounds, as the reference passes them), K the band energy (FP64). */
+int sc_force_rot(int precision, void* wx, void* wy, void* wz, const void* vx, const void* vy,
+                 const void* vz, int lx1, int ly, int lz, double fk12, double fk22, double eps);
+
+/* convecphi_dns(vx,vy,vz,phi,wphi,kx,ky,kz,lx1,ly,lz,nx,ny,nz),
+ * convecphi_dns.f90:1: wphi <- i k . (u phi)^ / N^3, the spectral flux
+ * divergence of a passive scalar phi (kx, ky, kz implied). */
+int sc_convecphi_dns(int precision, const void* vx, const void* vy, const void* vz, const void* phi,
+                     void* wphi, int lx1, int ly, int lz, int nx, int ny, int nz);
+
+/* skewness(ux,kx,s,nx,ny,nz), skewness.f90:1: S = <d^3> / <d^2>^(3/2) of
+ * d = du_x/dx over the physical grid (moments summed in FP64). */
+int sc_skewness(int precision, const void* ux, int nx, int ny, int nz, double* s);
+
+/* enstrophy(ux,uy,uz,kx,ky,kz,enstr,lx1,ly,lz,lx,nx,ny,nz), enstrophy.f90:1:
+ * enstr = 1/2 |w|^2, w = curl u, at every physical point; enstr is real(dp)
+ * (nx, ny, nz) in Fortran order. */
+int sc_enstrophy(int precision, const void* ux, const void* uy, const void* uz, double* enstr, int lx1,
+                 int ly, int lz, int nx, int ny, int nz);
+
 /* symmetrize(c,lx1,ly,lz), symmetrize.f90:32 (3D). */
 int sc_symmetrize(int precision, void* c, int lx1, int ly, int lz);
 

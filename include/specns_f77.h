@@ -34,6 +34,27 @@ void force_(void* wx, void* wy, void* wz, const void* vx, const void* vy, const 
             const sc_f77_real* k2, const int* lx1, const int* ly, const int* lz,
             const sc_f77_real* fkmax, const sc_f77_real* eps);
 
+/* force_rot.f90:3 (k2 accepted and ignored; fk12, fk22 squared band bounds) */
+void force_rot_(void* wx, void* wy, void* wz, const void* vx, const void* vy, const void* vz,
+                const sc_f77_real* k2, const int* lx1, const int* ly, const int* lz,
+                const sc_f77_real* fk12, const sc_f77_real* fk22, const sc_f77_real* eps);
+
+/* convecphi_dns.f90:1 (kx, ky, kz accepted and ignored) */
+void convecphi_dns_(const void* vx, const void* vy, const void* vz, const void* phi, void* wphi,
+                    const sc_f77_real* kx, const sc_f77_real* ky, const sc_f77_real* kz,
+                    const int* lx1, const int* ly, const int* lz, const int* nx, const int* ny,
+                    const int* nz);
+
+/* skewness.f90:1 (kx accepted and ignored; s is real(sp)) */
+void skewness_(const void* ux, const sc_f77_real* kx, sc_f77_real* s, const int* nx, const int* ny,
+               const int* nz);
+
+/* enstrophy.f90:1 (double precision in both builds, as the reference declares
+ * it; kx, ky, kz accepted and ignored) */
+void enstrophy_(const void* ux, const void* uy, const void* uz, const double* kx, const double* ky,
+                const double* kz, double* enstr, const int* lx1, const int* ly, const int* lz, const int* lx,
+                const int* nx, const int* ny, const int* nz);
+
 /* projection.f90:2 (kx, ky, kz accepted and ignored) */
 void projection_(void* vx, void* vy, void* vz, const sc_f77_real* kx, const sc_f77_real* ky,
                  const sc_f77_real* kz, const int* lx1, const int* ly, const int* lz);

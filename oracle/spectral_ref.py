@@ -189,6 +189,49 @@ def force(wx, wy, wz, vx, vy, vz, k2, fkmax, eps):
             np.where(m, wz + a * vz, wz))
 
 
+def force_rot(wx, wy, wz, vx, vy, vz, k2, fk12, fk22, eps, tiny):
+    """force_rot.f90:3-29: w += a v on fk12 <= k2 < fk22 (squared bounds),
+    a = eps / (2 kinet + tiny), kinet the 1/2-weighted band energy; tiny is
+    the build's mytiny (constant.f90:11 / constant_sp.f90:14)."""
+    m = (k2 < fk22) & (k2 >= fk12)
+    tmp = np.where(m, (vx * np.conj(vx) + vy * np.conj(vy) + vz * np.conj(vz)).real, 0.0)
+    tmp[:, :, 0] *= 0.5
+    a = eps / (2.0 * float(np.sum(tmp)) + tiny)
+    return (np.where(m, wx + a * vx, wx), np.where(m, wy + a * vy, wy),
+            np.where(m, wz + a * vz, wz))
+
+
+def convecphi_dns(vx, vy, vz, phi, nx):
+    """convecphi_dns.f90:1-49: wphi = i k . (u phi)^, times 1/(nx ny nz)
+    after the transforms (:47)."""
+    ny, nz = vx.shape[1], vx.shape[0]
+    const = 1.0 / float(nx * ny * nz)
+    kx, ky, kz, _ = wavenumber(nx, ny, nz)
+    p = c2r(phi, nx)
+    fx, fy, fz = (r2c(c2r(a, nx) * p) for a in (vx, vy, vz))
+    w = 1j * kx[None, None, :] * fx + 1j * ky[None, :, None] * fy + 1j * kz[:, None, None] * fz
+    return w * const
+
+
+def skewness(ux, nx):
+    """skewness.f90:1-48: <d^3> / <d^2>^(3/2) of d = du_x/dx in physical
+    space (the mean over the nx ny nz points)."""
+    ny, nz = ux.shape[1], ux.shape[0]
+    kx, _, _, _ = wavenumber(nx, ny, nz)
+    d = c2r(1j * kx[None, None, :] * ux, nx)
+    c = 1.0 / float(nx * ny * nz)
+    return float(np.sum(d ** 3) * c / (np.sum(d ** 2) * c) ** 1.5)
+
+
+def enstrophy_field(ux, uy, uz, nx):
+    """enstrophy.f90:1-36: 1/2 |curl u|^2 at every physical point, returned
+    (nz, ny, nx) (the memory of the reference's real(dp) enstr(nx,ny,nz))."""
+    ny, nz = ux.shape[1], ux.shape[0]
+    kx, ky, kz, _ = wavenumber(nx, ny, nz)
+    w = vorticity(ux, uy, uz, kx, ky, kz)
+    return 0.5 * sum(c2r(a, nx) ** 2 for a in w)
+
+
 def vorticity(vx, vy, vz, kx, ky, kz):
     """w = i k x v (dns-deform.f90:265-273)."""
     KX = kx[None, None, :]

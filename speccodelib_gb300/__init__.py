@@ -7,4 +7,5 @@ reference's subroutine interface over it (`specns`).
 from .specns import (SC_FP32, SC_FP64, SC_SGS_DYNSMAG, SC_SGS_NONE, SC_SGS_SMAG,  # noqa: F401
                      SC_MASK_AFTER_STEP, SC_MASK_RHS_AND_STEP, SpecNSError, SpectralNS,
                      convec_dns, dealiasing, default_params, dynsmag, force, projection,
-                     smag, symmetrize, Ensemble2D)
+                     smag, symmetrize, Ensemble2D, force_rot, convecphi_dns,
+                     skewness, enstrophy)

@@ -67,6 +67,10 @@ SIGNATURES = {
     "sc_convec_dns": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
     "sc_projection": ([_I, _P, _P, _P, _I, _I, _I], _I),
     "sc_force": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _D], _I),
+    "sc_force_rot": ([_I, _P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _D, _D], _I),
+    "sc_convecphi_dns": ([_I, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
+    "sc_skewness": ([_I, _P, _I, _I, _I, _P], _I),
+    "sc_enstrophy": ([_I, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I], _I),
     "sc_symmetrize": ([_I, _P, _I, _I, _I], _I),
     "sc_dealiasing": ([_I, _P, _I, _I, _I], _I),
     "sc_smag": ([_I, _P, _P, _P] + [_P] * 6 + [_I] * 6 + [_D, _D], _I),

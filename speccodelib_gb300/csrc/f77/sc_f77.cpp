@@ -41,6 +41,31 @@ void force_(void* wx, void* wy, void* wz, const void* vx, const void* vy, const 
   check(sc_force(kPrec, wx, wy, wz, vx, vy, vz, *lx1, *ly, *lz, (double)*fkmax, (double)*eps), "force");
 }
 
+void force_rot_(void* wx, void* wy, void* wz, const void* vx, const void* vy, const void* vz,
+                const sc_f77_real*, const int* lx1, const int* ly, const int* lz, const sc_f77_real* fk12,
+                const sc_f77_real* fk22, const sc_f77_real* eps) {
+  check(sc_force_rot(kPrec, wx, wy, wz, vx, vy, vz, *lx1, *ly, *lz, (double)*fk12, (double)*fk22, (double)*eps),
+        "force_rot");
+}
+
+void convecphi_dns_(const void* vx, const void* vy, const void* vz, const void* phi, void* wphi,
+                    const sc_f77_real*, const sc_f77_real*, const sc_f77_real*, const int* lx1, const int* ly,
+                    const int* lz, const int* nx, const int* ny, const int* nz) {
+  check(sc_convecphi_dns(kPrec, vx, vy, vz, phi, wphi, *lx1, *ly, *lz, *nx, *ny, *nz), "convecphi_dns");
+}
+
+void skewness_(const void* ux, const sc_f77_real*, sc_f77_real* s, const int* nx, const int* ny, const int* nz) {
+  double v = 0.0;
+  check(sc_skewness(kPrec, ux, *nx, *ny, *nz, &v), "skewness");
+  *s = (sc_f77_real)v;
+}
+
+void enstrophy_(const void* ux, const void* uy, const void* uz, const double*, const double*, const double*,
+                double* enstr, const int* lx1, const int* ly, const int* lz, const int*, const int* nx,
+                const int* ny, const int* nz) {
+  check(sc_enstrophy(SC_FP64, ux, uy, uz, enstr, *lx1, *ly, *lz, *nx, *ny, *nz), "enstrophy");
+}
+
 void projection_(void* vx, void* vy, void* vz, const sc_f77_real*, const sc_f77_real*,
                  const sc_f77_real*, const int* lx1, const int* ly, const int* lz) {
   check(sc_projection(kPrec, vx, vy, vz, *lx1, *ly, *lz), "projection");

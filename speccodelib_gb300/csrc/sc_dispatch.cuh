@@ -375,6 +375,27 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     return cudaGetLastError();                                                                   \
   }                                                                                              \
   template <>                                                                                    \
+  cudaError_t sc::Launch<T>::moments(const C2<T>* d, const Geom& g, double* partial, int nblocks, \
+                                     double* out, cudaStream_t s) {                              \
+    const long long rows = (long long)g.ny * g.nz;                                               \
+    const int rpb = (int)((rows + nblocks - 1) / nblocks);                                       \
+    const int nb = (int)((rows + rpb - 1) / rpb);                                                \
+    sc::moments_kernel<T><<<nb, 256, 0, s>>>(d, g, rpb, partial);                                \
+    cudaError_t e = cudaGetLastError();                                                          \
+    if (e != cudaSuccess) return e;                                                              \
+    sc::moments_final_kernel<<<1, 32, 0, s>>>(partial, nb, out);                                 \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::enstrophy(const C2<T>* const w[3], const Geom& g, double* out,       \
+                                       cudaStream_t s) {                                         \
+    long long n = (long long)g.ny * g.nz * (g.nx / 2);                                           \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 152 * 16) nb = 152 * 16;                                                            \
+    sc::enstrophy_kernel<T><<<nb, 256, 0, s>>>(w[0], w[1], w[2], g, out);                        \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
   cudaError_t sc::Launch<T>::strain(const StrainArgs<T>& sa, const Geom& g, cudaStream_t s) {    \
     long long n = (long long)g.ny * g.nz * g.nxh;                                                \
     int nb = (int)((n + 255) / 256);                                                             \

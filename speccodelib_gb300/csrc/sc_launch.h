@@ -39,6 +39,12 @@ template <typename T> struct Launch {
   static cudaError_t diag(const DiagArgs<T>& da, const Geom& g, cudaStream_t s);
   static cudaError_t specop(const SpecOpArgs<T>& oa, const Geom& g, cudaStream_t s);
   static cudaError_t strain(const StrainArgs<T>& sa, const Geom& g, cudaStream_t s);
+  // post-processing of physical packed rows: sums of d^2, d^3 into out[0..1]
+  // (partial holds 2 doubles per block, nblocks at most); enstrophy density
+  // 1/2 |w|^2 into a real (nz, ny, nx) array
+  static cudaError_t moments(const C2<T>* d, const Geom& g, double* partial, int nblocks, double* out,
+                             cudaStream_t s);
+  static cudaError_t enstrophy(const C2<T>* const w[3], const Geom& g, double* out, cudaStream_t s);
   // physical-space pointwise op; PH_DYN2 also finishes cs2 into *c1_out
   static cudaError_t phys(const PhysArgs<T>& pa, int nblocks, const Geom& g, double* c1_out,
                           double* lm_mm, cudaStream_t s);

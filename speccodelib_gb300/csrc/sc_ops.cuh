@@ -130,7 +130,12 @@ enum SpecOp {
   OP_INIT_SHAPE = 5,    // initialize.f90:328-332 projection with +tiny
   OP_INIT_AMP = 6,      // initialize.f90:349-360 amplitude (akp) or k^(-11/6) band
   OP_SCALE = 7,         // f *= scalar (scalar from device or host value)
-  OP_AXPBY = 8          // f[c] = alpha f[c] + beta g[c]
+  OP_AXPBY = 8,         // f[c] = alpha f[c] + beta g[c]
+  OP_PMUL = 9,          // packed physical rows: f[c] = (f[c].x g0.x, f[c].y g0.y) (convecphi_dns.f90:23)
+  OP_IDIV = 10,         // f[0] = a i (kx f0 + ky f1 + kz f2) (convecphi_dns.f90:25-45)
+  OP_FORCE_BAND = 11,   // force_rot.f90:24-28: f += a g on b <= k2 < kcut2
+  OP_DX = 12,           // f[0] = i kx f[0] (skewness.f90:17-21)
+  OP_CURL = 13          // f[0..2] = i k x f[0..2] (enstrophy.f90:16-18)
 };
 
 template <typename T> struct SpecOpArgs {
@@ -220,12 +225,97 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
         for (int c = 0; c < oa.nfields; ++c)
           oa.f[c][idx] = cadd(cscale(oa.f[c][idx], (T)oa.a), cscale(oa.gsrc[c][idx], (T)oa.b));
         break;
+      case OP_PMUL: {
+        const C gp = oa.gsrc[0][idx];
+        for (int c = 0; c < oa.nfields; ++c) {
+          const C fp = oa.f[c][idx];
+          oa.f[c][idx] = mk<C>(fp.x * gp.x, fp.y * gp.y);
+        }
+        break;
+      }
+      case OP_IDIV: {
+        const C d = cadd(cadd(cscale(oa.f[0][idx], kx), cscale(oa.f[1][idx], ky)), cscale(oa.f[2][idx], kz));
+        oa.f[0][idx] = cmuli(cscale(d, (T)oa.a));
+        break;
+      }
+      case OP_DX:
+        oa.f[0][idx] = cmuli(cscale(oa.f[0][idx], kx));
+        break;
+      case OP_CURL: {
+        const C u0 = oa.f[0][idx], u1 = oa.f[1][idx], u2 = oa.f[2][idx];
+        oa.f[0][idx] = cmuli(csub(cscale(u2, ky), cscale(u1, kz)));
+        oa.f[1][idx] = cmuli(csub(cscale(u0, kz), cscale(u2, kx)));
+        oa.f[2][idx] = cmuli(csub(cscale(u1, kx), cscale(u0, ky)));
+        break;
+      }
+      case OP_FORCE_BAND:
+        if (k2d < oa.kcut2 && k2d >= oa.b) {
+          const T a = (T)oa.a;
+          for (int c = 0; c < 3; ++c) oa.f[c][idx] = cadd(oa.f[c][idx], cscale(oa.gsrc[c][idx], a));
+        }
+        break;
       default:
         break;
     }
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// post-processing on physical fields held as packed rows (x = 2m in .x,
+// x = 2m+1 in .y, m < nx/2)
+// ---------------------------------------------------------------------------
+// Sums of d^2 and d^3 over the real points, FP64, block partials
+// partial[b*2 + {0, 1}] (skewness.f90:22-45).
+template <typename T>
+__global__ void __launch_bounds__(256) moments_kernel(const C2<T>* d, Geom g, int rows_per_block, double* partial) {
+  __shared__ double red[256 / 32 + 1];
+  const long long rows = (long long)g.ny * g.nz;
+  const long long r0 = (long long)blockIdx.x * rows_per_block;
+  const long long r1 = r0 + rows_per_block < rows ? r0 + rows_per_block : rows;
+  const int m = g.nx / 2;
+  double s2 = 0.0, s3 = 0.0;
+  for (long long t = r0 * m + threadIdx.x; t < r1 * m; t += blockDim.x) {
+    const long long row = t / m;
+    const C2<T> v = d[row * g.nxp + (t % m)];
+    const double a = v.x, b = v.y;
+    s2 += a * a + b * b;
+    s3 += a * a * a + b * b * b;
+  }
+  s2 = block_sum<256>(s2, red);
+  s3 = block_sum<256>(s3, red);
+  if (threadIdx.x == 0) {
+    partial[2 * (long long)blockIdx.x] = s2;
+    partial[2 * (long long)blockIdx.x + 1] = s3;
+  }
+}
+
+// Block partials summed in block order (deterministic): out[0..1].
+static __global__ void moments_final_kernel(const double* partial, int nblocks, double* out) {
+  if (threadIdx.x < 2) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[2 * (long long)b + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+// Enstrophy density 1/2 |w|^2 of three physical vorticity fields into a real
+// (nz, ny, nx) array, FP64 (enstrophy.f90:24-34).
+template <typename T>
+__global__ void __launch_bounds__(256) enstrophy_kernel(const C2<T>* w0, const C2<T>* w1, const C2<T>* w2, Geom g,
+                                                        double* out) {
+  const int m = g.nx / 2;
+  const long long total = (long long)g.ny * g.nz * m;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long row = t / m;
+    const int i = (int)(t % m);
+    const long long idx = row * g.nxp + i;
+    const C2<T> a = w0[idx], b = w1[idx], c = w2[idx];
+    out[row * g.nx + 2 * i] = 0.5 * ((double)a.x * a.x + (double)b.x * b.x + (double)c.x * c.x);
+    out[row * g.nx + 2 * i + 1] = 0.5 * ((double)a.y * a.y + (double)b.y * b.y + (double)c.y * c.y);
+  }
+}
 
 // ---------------------------------------------------------------------------
 // strain rate in spectral space: S_ij = i (k_i v_j + k_j v_i)/2, order

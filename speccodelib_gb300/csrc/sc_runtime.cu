@@ -1501,7 +1501,7 @@ int sc_convec_dns(int precision, const void* vx, const void* vy, const void* vz,
 }  // extern "C"
 
 template <typename T> static int specop_host(sc_handle* h, int op, int nf, void* const io[], double a, double kc2,
-                                             const void* const extra[3]) {
+                                             const void* const extra[3], double b = 0.0) {
   using I = Impl<T>;
   for (int c = 0; c < nf; ++c) SC_TRY(copy_in(h, slot(h, S_W + c), io[c]));
   if (extra)
@@ -1511,6 +1511,7 @@ template <typename T> static int specop_host(sc_handle* h, int op, int nf, void*
   for (int c = 0; c < 3; ++c) oa.gsrc[c] = I::F(h, S_W + 3 + c);
   oa.nfields = nf;
   oa.a = a;
+  oa.b = b;
   oa.kcut2 = kc2;
   if (op == sc::OP_ZERO_PLANES) {
     oa.op = sc::OP_ZERO_PLANES;
@@ -1587,7 +1588,140 @@ int sc_force(int precision, void* wx, void* wy, void* wz, const void* vx, const 
                               : specop_host<double>(h, sc::OP_FORCE_ADD, 3, io, a, fkmax * fkmax, v);
 }
 
+// force_rot(wx,wy,wz,vx,vy,vz,k2,lx1,ly,lz,fk12,fk22,eps), force_rot.f90:3-29:
+// band fk12 <= k2 < fk22 (squared bounds), a = eps/(2 kinet + tiny).
+int sc_force_rot(int precision, void* wx, void* wy, void* wz, const void* vx, const void* vy, const void* vz,
+                 int lx1, int ly, int lz, double fk12, double fk22, double eps) {
+  if (!wx || !wy || !wz || !vx || !vy || !vz) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  const void* v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_V + c), v[c]));
+  // kinet = E(k2 < fk22) - E(k2 < fk12), FP64 (force_rot.f90:15-21)
+  double hi[sc::DQ_N], lo[sc::DQ_N];
+  int r;
+  if (precision == SC_FP32) {
+    const sc::C2<float>* vv[3] = {Impl<float>::F(h, S_V), Impl<float>::F(h, S_V + 1), Impl<float>::F(h, S_V + 2)};
+    r = Impl<float>::diag_run(h, vv, 0, fk22, 0, hi);
+    if (r == SC_OK) r = Impl<float>::diag_run(h, vv, 0, fk12, 0, lo);
+  } else {
+    const sc::C2<double>* vv[3] = {Impl<double>::F(h, S_V), Impl<double>::F(h, S_V + 1), Impl<double>::F(h, S_V + 2)};
+    r = Impl<double>::diag_run(h, vv, 0, fk22, 0, hi);
+    if (r == SC_OK) r = Impl<double>::diag_run(h, vv, 0, fk12, 0, lo);
+  }
+  if (r != SC_OK) return r;
+  // mytiny: tiny() of the build's real kind (constant.f90:11, constant_sp.f90:14)
+  const double tiny = precision == SC_FP32 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+  const double kinet = (fk12 > 0.0 ? hi[sc::DQ_ENERGY] - lo[sc::DQ_ENERGY] : hi[sc::DQ_ENERGY]);
+  const double a = eps / (2.0 * kinet + tiny);
+  void* io[3] = {wx, wy, wz};
+  return precision == SC_FP32 ? specop_host<float>(h, sc::OP_FORCE_BAND, 3, io, a, fk22, v, fk12)
+                              : specop_host<double>(h, sc::OP_FORCE_BAND, 3, io, a, fk22, v, fk12);
+}
+
 // tau_ij of the current slots S_V (velocity) with coefficient *dscal.
+}  // extern "C"
+
+// convecphi_dns(vx,vy,vz,phi,wphi,kx,ky,kz,lx1,ly,lz,nx,ny,nz),
+// convecphi_dns.f90:1-49: wphi = i k . (u phi)^ / N^3.
+template <typename T> static int convecphi_impl(sc_handle* h, const void* const v[3], const void* phi, void* wphi) {
+  using I = Impl<T>;
+  auto* g = &h->g;
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_W + c), v[c]));
+  SC_TRY(copy_in(h, slot(h, S_W + 3), phi));
+  SC_CUDA(cudaMemsetAsync(slot(h, S_W + 4), 0, 2 * h->csize * g->field, h->stream));
+  auto w6 = I::range(h, S_W, 6);
+  SC_TRY(I::inverse(h, w6, 6));   // u (0-2) and phi (3) in physical space
+  sc::SpecOpArgs<T> oa{};
+  for (int c = 0; c < 3; ++c) oa.f[c] = I::F(h, S_W + c);
+  oa.gsrc[0] = I::F(h, S_W + 3);
+  oa.nfields = 3;
+  oa.op = sc::OP_PMUL;
+  SC_TRY(I::specop(h, oa));
+  auto w3 = I::range(h, S_W, 3);
+  SC_TRY(I::forward(h, w3, 3));
+  oa.op = sc::OP_IDIV;
+  oa.a = 1.0 / ((double)g->nx * g->ny * g->nz);
+  SC_TRY(I::specop(h, oa));
+  SC_TRY(copy_out(h, wphi, slot(h, S_W)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+// skewness(ux,kx,s,nx,ny,nz), skewness.f90:1-48: S = <d^3> / <d^2>^(3/2),
+// d = du_x/dx in physical space, moments summed in FP64.
+template <typename T> static int skewness_impl(sc_handle* h, const void* ux, double* s) {
+  using I = Impl<T>;
+  auto* g = &h->g;
+  SC_TRY(copy_in(h, slot(h, S_W), ux));
+  SC_CUDA(cudaMemsetAsync(slot(h, S_W + 1), 0, 2 * h->csize * g->field, h->stream));
+  sc::SpecOpArgs<T> oa{};
+  oa.f[0] = I::F(h, S_W);
+  oa.nfields = 1;
+  oa.op = sc::OP_DX;
+  SC_TRY(I::specop(h, oa));
+  SC_TRY(I::inverse(h, I::range(h, S_W, 3), 3));
+  SC_TRY(launch(h, "moments", [&] { return sc::Launch<T>::moments(I::F(h, S_W), *g, h->dpart, 1024, h->dout, h->stream); }));
+  double m[2];
+  SC_CUDA(cudaMemcpyAsync(m, h->dout, sizeof m, cudaMemcpyDeviceToHost, h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  const double c = 1.0 / ((double)g->nx * g->ny * g->nz);
+  *s = (m[1] * c) / std::pow(m[0] * c, 1.5);
+  return SC_OK;
+}
+
+// enstrophy(ux,uy,uz,kx,ky,kz,enstr,lx1,ly,lz,lx,nx,ny,nz), enstrophy.f90:1-36:
+// 1/2 |i k x u|^2 at every physical point, (nx, ny, nz) real(dp).
+template <typename T> static int enstrophy_impl(sc_handle* h, const void* const u[3], double* enstr) {
+  using I = Impl<T>;
+  auto* g = &h->g;
+  for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_W + c), u[c]));
+  sc::SpecOpArgs<T> oa{};
+  for (int c = 0; c < 3; ++c) oa.f[c] = I::F(h, S_W + c);
+  oa.nfields = 3;
+  oa.op = sc::OP_CURL;
+  SC_TRY(I::specop(h, oa));
+  SC_TRY(I::inverse(h, I::range(h, S_W, 3), 3));
+  // the real (nz, ny, nx) output fits in the three work fields after S_W + 2
+  double* dev = reinterpret_cast<double*>(slot(h, S_W + 3));
+  const sc::C2<T>* w[3] = {I::F(h, S_W), I::F(h, S_W + 1), I::F(h, S_W + 2)};
+  SC_TRY(launch(h, "enstrophy", [&] { return sc::Launch<T>::enstrophy(w, *g, dev, h->stream); }));
+  SC_CUDA(cudaMemcpyAsync(enstr, dev, sizeof(double) * (size_t)g->nx * g->ny * g->nz, cudaMemcpyDeviceToHost,
+                          h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+extern "C" {
+
+int sc_skewness(int precision, const void* ux, int nx, int ny, int nz, double* s) {
+  if (!ux || !s) return fail(SC_ERR_INVALID, "null argument");
+  SC_TRY(shape_check(nx / 2 + 1, ny, nz, nx, ny, nz));
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, nx, ny, nz, SC_SGS_NONE, &h));
+  return precision == SC_FP32 ? skewness_impl<float>(h, ux, s) : skewness_impl<double>(h, ux, s);
+}
+
+int sc_enstrophy(int precision, const void* ux, const void* uy, const void* uz, double* enstr, int lx1, int ly,
+                 int lz, int nx, int ny, int nz) {
+  if (!ux || !uy || !uz || !enstr) return fail(SC_ERR_INVALID, "null argument");
+  SC_TRY(shape_check(lx1, ly, lz, nx, ny, nz));
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, nx, ny, nz, SC_SGS_NONE, &h));
+  const void* u[3] = {ux, uy, uz};
+  return precision == SC_FP32 ? enstrophy_impl<float>(h, u, enstr) : enstrophy_impl<double>(h, u, enstr);
+}
+
+int sc_convecphi_dns(int precision, const void* vx, const void* vy, const void* vz, const void* phi, void* wphi,
+                     int lx1, int ly, int lz, int nx, int ny, int nz) {
+  if (!vx || !vy || !vz || !phi || !wphi) return fail(SC_ERR_INVALID, "null array");
+  SC_TRY(shape_check(lx1, ly, lz, nx, ny, nz));
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, nx, ny, nz, SC_SGS_NONE, &h));
+  const void* v[3] = {vx, vy, vz};
+  return precision == SC_FP32 ? convecphi_impl<float>(h, v, phi, wphi) : convecphi_impl<double>(h, v, phi, wphi);
+}
+
 }  // extern "C"
 
 template <typename T> static int tau_impl(sc_handle* h, void* const t[6]) {

@@ -112,6 +112,36 @@ def force(wx, wy, wz, vx, vy, vz, fkmax, eps):
                           _ptr(vz), lx1, ly, lz, C.c_double(fkmax), C.c_double(eps)))
 
 
+
+def force_rot(wx, wy, wz, vx, vy, vz, fk12, fk22, eps):
+    """force_rot.f90:3 -- w += eps/(2 K + tiny) v on fk12 <= k2 < fk22; in place on w."""
+    prec, lx1, ly, lz = _same(wx, wy, wz, vx, vy, vz)
+    _check(lib().sc_force_rot(prec, _ptr(wx, True), _ptr(wy, True), _ptr(wz, True), _ptr(vx), _ptr(vy),
+                              _ptr(vz), lx1, ly, lz, C.c_double(fk12), C.c_double(fk22), C.c_double(eps)))
+
+
+def skewness(ux, nx):
+    """skewness.f90:1 -- velocity-derivative skewness <d^3>/<d^2>^(3/2), d = du_x/dx."""
+    prec, lx1, ly, lz = _same(ux)
+    s = C.c_double(0)
+    _check(lib().sc_skewness(prec, _ptr(ux), nx, ly, lz, C.byref(s)))
+    return s.value
+
+
+def enstrophy(ux, uy, uz, nx):
+    """enstrophy.f90:1 -- 1/2 |curl u|^2 at every physical point, (nz, ny, nx) float64."""
+    prec, lx1, ly, lz = _same(ux, uy, uz)
+    out = np.zeros((lz, ly, nx), dtype=np.float64)
+    _check(lib().sc_enstrophy(prec, _ptr(ux), _ptr(uy), _ptr(uz), _ptr(out, True), lx1, ly, lz, nx, ly, lz))
+    return out
+
+
+def convecphi_dns(vx, vy, vz, phi, wphi, nx):
+    """convecphi_dns.f90:1 -- wphi <- i k . (u phi)^ / N^3; writes wphi."""
+    prec, lx1, ly, lz = _same(vx, vy, vz, phi, wphi)
+    _check(lib().sc_convecphi_dns(prec, _ptr(vx), _ptr(vy), _ptr(vz), _ptr(phi), _ptr(wphi, True),
+                                  lx1, ly, lz, nx, ly, lz))
+
 def symmetrize(c):
     """symmetrize.f90:32 (3D) -- in place."""
     prec, lx1, ly, lz = _same(c)

@@ -65,3 +65,51 @@ def test_f77_dynsmag_recovers_test_filter(specns_lib, prec, dtype, real, tol):
                *[C.byref(o) for o in out], C.byref(C.c_int(1)))
     assert abs(out[2].value - cs2) < tol * abs(cs2) * 10
     assert rel_l2(t, ref) < tol * 10
+
+
+@pytest.mark.parametrize("prec,dtype,real,tol", [("dp", np.complex128, C.c_double, 1e-12),
+                                                  ("sp", np.complex64, C.c_float, 1e-5)])
+def test_f77_convecphi_and_force_rot(specns_lib, prec, dtype, real, tol):
+    """convecphi_dns_(vx,vy,vz,phi,wphi,kx,ky,kz,lx1,ly,lz,nx,ny,nz) and
+    force_rot_(wx,wy,wz,vx,vy,vz,k2,lx1,ly,lz,fk12,fk22,eps)."""
+    f = _lib.load_f77(prec)
+    n = 16
+    v = hermitian_fields((n, n, n), 41)
+    phi = hermitian_fields((n, n, n), 42, ncomp=1)[0]
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    rdt = np.float64 if prec == "dp" else np.float32
+    vv = [np.ascontiguousarray(a, dtype) for a in v]
+    pp = np.ascontiguousarray(phi, dtype)
+    out = np.zeros_like(pp)
+    kr = [np.ascontiguousarray(a, rdt) for a in (kx, ky, kz)]
+    f.convecphi_dns_(*[a.ctypes.data_as(C.c_void_p) for a in vv + [pp, out] + kr], *ref_int(n // 2 + 1, n, n, n, n, n))
+    assert rel_l2(out, R.convecphi_dns(*v, phi, n)) < tol
+    w = [np.ascontiguousarray(a, dtype) for a in hermitian_fields((n, n, n), 43)]
+    tiny = R.MYTINY_DP if prec == "dp" else R.MYTINY_SP
+    ref = R.force_rot(*[a.astype(np.complex128) for a in w], *v, k2, 4.0, 16.0, 0.1, tiny)
+    k2r = np.ascontiguousarray(k2, rdt)
+    f.force_rot_(*[a.ctypes.data_as(C.c_void_p) for a in w + vv], k2r.ctypes.data_as(C.c_void_p),
+                 *ref_int(n // 2 + 1, n, n), C.byref(real(4.0)), C.byref(real(16.0)), C.byref(real(0.1)))
+    assert rel_l2(w, ref) < tol
+
+
+@pytest.mark.parametrize("prec,dtype,real,tol", [("dp", np.complex128, C.c_double, 1e-11),
+                                                  ("sp", np.complex64, C.c_float, 1e-4)])
+def test_f77_skewness_and_enstrophy(specns_lib, prec, dtype, real, tol):
+    """skewness_(ux,kx,s,nx,ny,nz) (s real(sp)) and enstrophy_(...) (always
+    double precision, as the reference declares it)."""
+    f = _lib.load_f77(prec)
+    n = 16
+    v = hermitian_fields((n, n, n), 61, kcut=2 * (n // 2) / 3)
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    u = np.ascontiguousarray(v[0], dtype)
+    kr = np.ascontiguousarray(kx, np.float64 if prec == "dp" else np.float32)
+    s = real(0)
+    f.skewness_(u.ctypes.data_as(C.c_void_p), kr.ctypes.data_as(C.c_void_p), C.byref(s), *ref_int(n, n, n))
+    assert abs(s.value - R.skewness(v[0], n)) < tol * 10
+    uu = [np.ascontiguousarray(a, np.complex128) for a in v]
+    kd = [np.zeros((n, n, n // 2 + 1)) for _ in range(3)]
+    e = np.zeros((n, n, n))
+    f.enstrophy_(*[a.ctypes.data_as(C.c_void_p) for a in uu + kd + [e]], *ref_int(n // 2 + 1, n, n, n // 2, n, n, n))
+    e_ref = R.enstrophy_field(*v, n)
+    assert np.sqrt(np.sum((e - e_ref) ** 2) / np.sum(e_ref ** 2)) < 1e-12

@@ -124,3 +124,52 @@ def test_dynsmag(specns_lib, prec):
     ref2, _, _, _ = R.dynsmag(*v, kx, ky, kz, g, n, delta, 2 * delta, False, 0.05)
     t2, _, _, c2 = S.dynsmag(*cast(v, prec), k_test, delta, 2 * delta, False, 0.05)
     assert c2 == 0.05 and rel_l2(t2, ref2) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 16, 8), (128, 32, 16)])
+def test_convecphi_dns(specns_lib, prec, shape):
+    """Passive-scalar flux divergence i k . (u phi)^ / N^3 (convecphi_dns.f90)
+    against the oracle; (128, 32, 16) takes the warp x-pass for the c2r."""
+    nx, ny, nz = shape
+    v = hermitian_fields(shape, 21)
+    phi = hermitian_fields(shape, 22, ncomp=1)[0]
+    ref = R.convecphi_dns(*v, phi, nx)
+    vv = cast(v, prec)
+    pp = cast([phi], prec)[0]
+    out = np.zeros_like(pp)
+    S.convecphi_dns(*vv, pp, out, nx)
+    assert rel_l2(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("fk12,fk22", [(0.0, 6.25), (4.0, 16.0), (9.0, 40.0)])
+def test_force_rot(specns_lib, prec, fk12, fk22):
+    """Shell-band forcing of the rotating solver (force_rot.f90) against the
+    oracle, with the build's tiny (single or double) in the normalisation."""
+    shape = (16, 16, 16)
+    v = hermitian_fields(shape, 5)
+    w = complex_noise(shape, 6)
+    _, _, _, k2 = R.wavenumber(*shape)
+    tiny = R.MYTINY_SP if prec == S.SC_FP32 else R.MYTINY_DP
+    ref = R.force_rot(*w, *v, k2, fk12, fk22, 0.1, tiny)
+    ww, vv = cast(w, prec), cast(v, prec)
+    S.force_rot(*ww, *vv, fk12, fk22, 0.1)
+    assert rel_l2(ww, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec,tol", [(S.SC_FP64, 1e-12), (S.SC_FP32, 1e-5)])
+@pytest.mark.parametrize("shape", [(32, 32, 32), (128, 16, 32)])
+def test_skewness_and_enstrophy(specns_lib, prec, tol, shape):
+    """Post-processing of skewness.f90 and enstrophy.f90 against the oracle:
+    the derivative skewness (a scalar) and the physical enstrophy density."""
+    nx = shape[0]
+    v = hermitian_fields(shape, 51, kcut=2 * (nx // 2) / 3)
+    vv = cast(v, prec)
+    s = S.skewness(vv[0], nx)
+    s_ref = R.skewness(v[0], nx)
+    assert abs(s - s_ref) < tol * max(1.0, abs(s_ref)) * 10
+    e = S.enstrophy(*vv, nx)
+    e_ref = R.enstrophy_field(*v, nx)
+    assert e.shape == e_ref.shape
+    assert np.sqrt(np.sum((e - e_ref) ** 2) / np.sum(e_ref ** 2)) < tol * 10
