@@ -7,7 +7,11 @@
 //   twiddles W_M^{lane k1},
 //   transpose through a padded warp-private shared buffer,
 //   radix-E DFT in registers, twiddles W_32^{q u},
-//   (32/E)-point DFT across lanes by radix-2 warp-shuffle butterflies.
+//   (32/E)-point DFT across each group of 32/E lanes: radix-2 warp-shuffle
+//   butterflies down to groups of min(E, 32/E) lanes, then an all-to-all
+//   shuffle exchange of register blocks inside each group and the rest of
+//   the DFT in registers.
+// The per-lane twiddles of each level are powers of one table entry.
 // The inverse (natural in, digit-scrambled out) leaves every field in the
 // same scrambled order, so the Lamb product u x w is formed in registers; the
 // forward transform is the transposed network (scrambled in, natural out).
@@ -17,6 +21,8 @@
 // Z_k = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) e^{+2 pi i k/N}, and
 // X_k = ((Z_k + conj Z_{M-k}) - i e^{-2 pi i k/N} (Z_k - conj Z_{M-k}))/2.
 #pragma once
+#include <utility>
+
 #include "sc_passes.cuh"
 
 namespace sc {
@@ -78,11 +84,54 @@ template <int E, bool INV, typename C> __device__ __forceinline__ void dftE(C* v
   else if constexpr (E == 16) dft16<INV>(v);
 }
 
+// cos and sin of 2 pi j / n at compile time, for the constant twiddles of
+// the half-length c2r / r2c: quadrant and octant reduction to |x| <= pi/4,
+// then the Maclaurin series of sin and cos (14 terms: far below double
+// rounding on that interval).
+namespace roots {
+constexpr double kPi = 3.14159265358979323846264338327950288;
+__host__ __device__ constexpr double mac_sin(double x) {
+  double t = x, s = x;
+  for (int k = 1; k < 14; ++k) { t *= -x * x / ((2.0 * k) * (2.0 * k + 1)); s += t; }
+  return s;
+}
+__host__ __device__ constexpr double mac_cos(double x) {
+  double t = 1, s = 1;
+  for (int k = 1; k < 14; ++k) { t *= -x * x / ((2.0 * k - 1) * (2.0 * k)); s += t; }
+  return s;
+}
+// n a multiple of 8; j in [0, n)
+__host__ __device__ constexpr double cos2pi(int j, int n, bool want_sin) {
+  const int quad = (4 * j) / n, jr = j - quad * (n / 4);          // angle = quad pi/2 + 2 pi jr/n
+  const bool hi = 8 * jr > n;                                     // past pi/4: use the complement
+  const double x = 2 * kPi * (hi ? n / 4 - jr : jr) / n;
+  const double c0 = hi ? mac_sin(x) : mac_cos(x), s0 = hi ? mac_cos(x) : mac_sin(x);
+  const double c = quad == 0 ? c0 : quad == 1 ? -s0 : quad == 2 ? -c0 : s0;
+  const double s = quad == 0 ? s0 : quad == 1 ? c0 : quad == 2 ? -s0 : -c0;
+  return want_sin ? s : c;
+}
+template <typename C, int N, int J> __device__ __forceinline__ C w_root() {   // W_N^J = e^{-2 pi i J/N}
+  constexpr double c = cos2pi(J, N, false), s = cos2pi(J, N, true);
+  return mk<C>(decltype(C::x)(c), decltype(C::x)(-s));
+}
+template <typename C, int N, int... J> __device__ __forceinline__ void fill(C* w, std::integer_sequence<int, J...>) {
+  ((w[J] = w_root<C, N, J>()), ...);
+}
+}  // namespace roots
+
 template <typename T, int LOGM> struct WarpFFT {
   using C = C2<T>;
   static constexpr int M = 1 << LOGM;
   static constexpr int E = M / 32;          // points per lane
   static constexpr int Q = 32 / E;          // lanes per row of the second level
+  // The Q-point DFT across each group of Q lanes: radix-2 shuffle
+  // butterflies on the lane bits h >= Q2 = min(Q, E), then an all-to-all
+  // exchange of (E/Q2)-register blocks inside each group of Q2 lanes and a
+  // Q2-point DFT in registers.
+  static constexpr int Q2 = Q < E ? Q : E;
+  static constexpr bool XCH = Q2 > 1;
+  static constexpr int B = E / Q2;
+  static constexpr int HMIN = XCH ? Q2 : 1;   // smallest butterfly lane bit
   static constexpr int ROW = 32 + Q;        // padded shared row: conflict-free transpose
   static constexpr int SMEM = E * ROW;      // complex elements per warp
 
@@ -91,13 +140,77 @@ template <typename T, int LOGM> struct WarpFFT {
     return inv ? cconj(w) : w;
   }
 
-  // natural (x[r] = point lane + 32 r) -> scrambled
-  // (x[u] = point k1 + E u + E^2 bitrev(q), k1 = lane / Q, q = lane % Q)
+  // x[j] *= w^j, j = 1 .. E-1, with w = tw[m] (conjugated for INV): one table
+  // load, then the powers by squarings and one product per other power
+  // (SC_XW_TWLOAD: one table load per power instead)
+  template <bool INV>
+  __device__ static __forceinline__ void twiddle_powers(C (&x)[E], const C* __restrict__ tw, int m) {
+    if constexpr (E > 1) {
+#ifdef SC_XW_TWLOAD
+#pragma unroll
+      for (int j = 1; j < E; ++j) x[j] = cmul(x[j], twid(tw, m * j, INV));
+#else
+      C w[E];
+      w[1] = twid(tw, m, INV);
+#pragma unroll
+      for (int j = 2; j < E; ++j) {
+        const int hb = 1 << (31 - __clz(j));
+        w[j] = hb == j ? mk<C>(w[j / 2].x * w[j / 2].x - w[j / 2].y * w[j / 2].y, T(2) * w[j / 2].x * w[j / 2].y)
+                       : cmul(w[hb], w[j - hb]);
+      }
+#pragma unroll
+      for (int j = 1; j < E; ++j) x[j] = cmul(x[j], w[j]);
+#endif
+    }
+  }
+
+  // all-to-all inside each group of Q2 lanes: afterwards lane q holds at
+  // block p (registers p B .. p B + B-1) what lane p held at block q (q, p
+  // the lane's index in its group).  One stage per lane bit h: the lane with
+  // bit h clear keeps its blocks with bit h clear and trades the others with
+  // lane q ^ h.  An involution.
+  __device__ static __forceinline__ void exchange(C (&x)[E], int q) {
+#pragma unroll
+    for (int h = Q2 / 2; h >= 1; h >>= 1) {
+      const bool up = (q & h) != 0;
+#pragma unroll
+      for (int b = 0; b < Q2; ++b) {
+        if (b & h) continue;
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+          C& lo = x[b * B + i];
+          C& hi = x[(b | h) * B + i];
+          const C s = up ? lo : hi;
+          C r;
+          r.x = __shfl_xor_sync(0xffffffffu, s.x, h);
+          r.y = __shfl_xor_sync(0xffffffffu, s.y, h);
+          if (up) lo = r;
+          else hi = r;
+        }
+      }
+    }
+  }
+
+  // Q2-point DFT over registers p B + i (p = 0..Q2-1) for each i, in place
+  template <bool INV> __device__ static __forceinline__ void dft_cols(C (&x)[E]) {
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      C t[Q2];
+#pragma unroll
+      for (int p = 0; p < Q2; ++p) t[p] = x[p * B + i];
+      dftE<Q2, INV>(t);
+#pragma unroll
+      for (int p = 0; p < Q2; ++p) x[p * B + i] = t[p];
+    }
+  }
+
+  // natural (x[r] = point lane + 32 r) -> a digit-scrambled order, the same
+  // for every row and field (E >= Q: x[v B + i] = point k1 + E (q B + i) +
+  // E^2 v, with k1 = lane / Q, q = lane % Q)
   template <bool INV>
   __device__ static __forceinline__ void nat_to_scr(C (&x)[E], C* sm, const C* __restrict__ tw, int lane) {
     dftE<E, INV>(x);
-#pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) x[k1] = cmul(x[k1], twid(tw, lane * k1, INV));
+    twiddle_powers<INV>(x, tw, lane);
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) sm[k1 * ROW + lane] = x[k1];
     __syncwarp();
@@ -106,10 +219,9 @@ template <typename T, int LOGM> struct WarpFFT {
     for (int t = 0; t < E; ++t) x[t] = sm[k1 * ROW + q + Q * t];
     __syncwarp();
     dftE<E, INV>(x);
+    twiddle_powers<INV>(x, tw, q * E);
 #pragma unroll
-    for (int u = 1; u < E; ++u) x[u] = cmul(x[u], twid(tw, q * u * E, INV));
-#pragma unroll
-    for (int h = Q / 2; h >= 1; h >>= 1) {
+    for (int h = Q / 2; h >= HMIN; h >>= 1) {
       const C w = twid(tw, (q & (h - 1)) * (M / (2 * h)), INV);
       const bool up = (q & h) != 0;
 #pragma unroll
@@ -120,14 +232,22 @@ template <typename T, int LOGM> struct WarpFFT {
         x[u] = up ? cmul(csub(p, x[u]), w) : cadd(x[u], p);
       }
     }
+    if constexpr (XCH) {
+      exchange(x, q);
+      dft_cols<INV>(x);
+    }
   }
 
   // scrambled -> natural (the transposed network of nat_to_scr)
   template <bool INV>
   __device__ static __forceinline__ void scr_to_nat(C (&x)[E], C* sm, const C* __restrict__ tw, int lane) {
     const int k1 = lane / Q, q = lane % Q;
+    if constexpr (XCH) {
+      dft_cols<INV>(x);
+      exchange(x, q);
+    }
 #pragma unroll
-    for (int h = 1; h <= Q / 2; h <<= 1) {
+    for (int h = HMIN; h <= Q / 2; h <<= 1) {
       const C w = twid(tw, (q & (h - 1)) * (M / (2 * h)), INV);
       const bool up = (q & h) != 0;
 #pragma unroll
@@ -138,8 +258,7 @@ template <typename T, int LOGM> struct WarpFFT {
         x[u] = up ? csub(p, cmul(w, x[u])) : cadd(x[u], cmul(w, p));
       }
     }
-#pragma unroll
-    for (int u = 1; u < E; ++u) x[u] = cmul(x[u], twid(tw, q * u * E, INV));
+    twiddle_powers<INV>(x, tw, q * E);
     dftE<E, INV>(x);
 #pragma unroll
     for (int t = 0; t < E; ++t) sm[k1 * ROW + q + Q * t] = x[t];
@@ -147,9 +266,19 @@ template <typename T, int LOGM> struct WarpFFT {
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = sm[j * ROW + lane];
     __syncwarp();
-#pragma unroll
-    for (int j = 1; j < E; ++j) x[j] = cmul(x[j], twid(tw, lane * j, INV));
+    twiddle_powers<INV>(x, tw, lane);
     dftE<E, INV>(x);
+  }
+
+  // w[r] = W_N^{lane + 32 r} (N = 2M), r = 0..E-1: one table load times the
+  // compile-time roots W_{2E}^r
+  __device__ static __forceinline__ void half_twiddles(C (&w)[E], const C* __restrict__ twN, int lane) {
+    C cr[E];
+    roots::fill<C, 2 * E>(cr, std::make_integer_sequence<int, E>{});
+    const C wl = __ldg(&twN[lane]);
+    w[0] = wl;
+#pragma unroll
+    for (int r = 1; r < E; ++r) w[r] = cmul(wl, cr[r]);
   }
 };
 
@@ -173,16 +302,28 @@ template <typename T, int LOGM> struct XwRow {
   long long off;
   int lane;
 
+  // wn[r] = W_N^{lane + 32 r}, N = 2M
+  __device__ __forceinline__ void half_twiddles(C (&wn)[E]) const {
+#ifdef SC_XW_TWLOAD
+#pragma unroll
+    for (int r = 0; r < E; ++r) wn[r] = __ldg(&twN[lane + 32 * r]);
+#else
+    WF::half_twiddles(wn, twN, lane);
+#endif
+  }
+
   // half-length c2r pre-processing of a row into natural-order Z
   __device__ __forceinline__ void load_z(const C* __restrict__ fp, C (&x)[E]) const {
     const C* __restrict__ rp = fp + off;
+    C wn[E];
+    half_twiddles(wn);
 #pragma unroll
     for (int r = 0; r < E; ++r) {
       const int k = lane + 32 * r;
       C xk = rp[k], xm = rp[M - k];
       if (k == 0) { xk.y = 0; xm.y = 0; }   // DC and Nyquist are real
       const C e = cadd(xk, cconj(xm));
-      const C o = cmulc(csub(xk, cconj(xm)), __ldg(&twN[k]));
+      const C o = cmulc(csub(xk, cconj(xm)), wn[r]);
       x[r] = cadd(e, cmuli(o));
     }
   }
@@ -242,6 +383,8 @@ template <typename T, int LOGM> struct XwRow {
       // (32 - lane) % 32, register E-1-r (lane 0: its own register (E - r) % E)
       C* __restrict__ op = of[c] + off;
       const int src = (32 - lane) & 31;
+      C wn[E];
+      half_twiddles(wn);
 #pragma unroll
       for (int r = 0; r < E; ++r) {
         C zm;
@@ -252,7 +395,7 @@ template <typename T, int LOGM> struct XwRow {
         const C zk = x[r];
         const C zmc = cconj(zm);
         const C e = cadd(zk, zmc);
-        const C d = cmul(csub(zk, zmc), __ldg(&twN[k]));
+        const C d = cmul(csub(zk, zmc), wn[r]);
         op[k] = cscale(csub(e, cmuli(d)), T(0.5));
         if (k == 0) {   // X_M from Z_0
           const C d0 = cmul(csub(zk, zmc), __ldg(&twN[M]));
