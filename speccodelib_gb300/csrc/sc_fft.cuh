@@ -186,6 +186,30 @@ struct FFTEngine {
     }
   }
 
+  // The same in two steps: the table loads are issued with the stage's
+  // shared-memory reads, before its barrier, so their latency overlaps the
+  // barrier wait (SC_TW_LATE: loads after the barrier, as `twiddle`).
+#ifdef SC_TW_LATE
+  static constexpr bool TW_EARLY = false;
+#else
+  static constexpr bool TW_EARLY = true;
+#endif
+  template <int R, int NSV>
+  __device__ static __forceinline__ void twiddle_load(C* w, int k, const C* __restrict__ tw) {
+    if constexpr (NSV > 1) {
+      constexpr int STRIDE = N / (NSV * R);
+#pragma unroll
+      for (int r = 1; r < R; ++r) w[r] = __ldg(&tw[k * r * STRIDE]);
+    }
+  }
+  template <int R, int NSV, bool INV>
+  __device__ static __forceinline__ void twiddle_apply(C* v, const C* w) {
+    if constexpr (NSV > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = INV ? cmulc(v[r], w[r]) : cmul(v[r], w[r]);
+    }
+  }
+
   // Stage S (0 < S < NS-1): shared -> shared.
   template <int S, bool INV>
   __device__ static __forceinline__ void mid_stage(C* sm, const C* __restrict__ tw) {
@@ -194,7 +218,7 @@ struct FFTEngine {
     constexpr int NSV = fft_ns(LOGN, S, RMAX);
     constexpr int TOT = P * NR;
     constexpr int J = (TOT + NT - 1) / NT;
-    C v[J][R];
+    C v[J][R], w[TW_EARLY && NSV > 1 ? J : 1][R];
 #pragma unroll
     for (int a = 0; a < J; ++a) {
       int job = threadIdx.x + a * NT, p, j;
@@ -202,6 +226,7 @@ struct FFTEngine {
       if ((TOT % NT == 0) || job < TOT) {
 #pragma unroll
         for (int r = 0; r < R; ++r) v[a][r] = sm[sidx(j + r * NR) * PS + p];
+        if constexpr (TW_EARLY && NSV > 1) twiddle_load<R, NSV>(w[a], j % NSV, tw);
       }
     }
     __syncthreads();
@@ -211,7 +236,8 @@ struct FFTEngine {
       decode<R>(job, p, j);
       if ((TOT % NT == 0) || job < TOT) {
         const int k = j % NSV;
-        twiddle<R, NSV, INV>(v[a], k, tw);
+        if constexpr (TW_EARLY && NSV > 1) twiddle_apply<R, NSV, INV>(v[a], w[a]);
+        else twiddle<R, NSV, INV>(v[a], k, tw);
         dft<R, INV>(v[a]);
         if constexpr (S == 0) {
           store_stage0<R>(v[a], sm, j, p);
@@ -247,6 +273,7 @@ struct FFTEngine {
     constexpr int NR = N / RL;
     constexpr int NSV = fft_ns(LOGN, NS - 1, RMAX);
     static_assert(NSV == NR, "last stage spans the pencil");
+    C w[TW_EARLY && NSV > 1 ? JL : 1][RL];
 #pragma unroll
     for (int a = 0; a < JL; ++a) {
       int job = threadIdx.x + a * NT, p, j;
@@ -254,6 +281,7 @@ struct FFTEngine {
       if ((TOTL % NT == 0) || job < TOTL) {
 #pragma unroll
         for (int r = 0; r < RL; ++r) out[a][r] = sm[sidx(j + r * NR) * PS + p];
+        if constexpr (TW_EARLY && NSV > 1) twiddle_load<RL, NSV>(w[a], j, tw);
       }
     }
     __syncthreads();
@@ -262,7 +290,8 @@ struct FFTEngine {
       int job = threadIdx.x + a * NT, p, j;
       decode<RL>(job, p, j);
       if ((TOTL % NT == 0) || job < TOTL) {
-        twiddle<RL, NSV, INV>(out[a], j, tw);
+        if constexpr (TW_EARLY && NSV > 1) twiddle_apply<RL, NSV, INV>(out[a], w[a]);
+        else twiddle<RL, NSV, INV>(out[a], j, tw);
         dft<RL, INV>(out[a]);
       }
     }
@@ -307,29 +336,7 @@ struct FFTEngine {
       }
       __syncthreads();
       mid_stages<1, INV>(sm, tw);
-      // last stage: shared -> registers
-      constexpr int NR = N / RL;
-      constexpr int NSV = fft_ns(LOGN, NS - 1, RMAX);
-      static_assert(NSV == NR, "last stage spans the pencil");
-#pragma unroll
-      for (int a = 0; a < JL; ++a) {
-        int job = threadIdx.x + a * NT, p, j;
-        decode<RL>(job, p, j);
-        if ((TOTL % NT == 0) || job < TOTL) {
-#pragma unroll
-          for (int r = 0; r < RL; ++r) out[a][r] = sm[sidx(j + r * NR) * PS + p];
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int a = 0; a < JL; ++a) {
-        int job = threadIdx.x + a * NT, p, j;
-        decode<RL>(job, p, j);
-        if ((TOTL % NT == 0) || job < TOTL) {
-          twiddle<RL, NSV, INV>(out[a], j, tw);
-          dft<RL, INV>(out[a]);
-        }
-      }
+      last_stage<INV>(out, sm, tw);
     }
   }
 };

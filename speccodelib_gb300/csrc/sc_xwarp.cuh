@@ -11,7 +11,6 @@
 //   butterflies down to groups of min(E, 32/E) lanes, then an all-to-all
 //   shuffle exchange of register blocks inside each group and the rest of
 //   the DFT in registers.
-// The per-lane twiddles of each level are powers of one table entry.
 // The inverse (natural in, digit-scrambled out) leaves every field in the
 // same scrambled order, so the Lamb product u x w is formed in registers; the
 // forward transform is the transposed network (scrambled in, natural out).
@@ -140,13 +139,13 @@ template <typename T, int LOGM> struct WarpFFT {
     return inv ? cconj(w) : w;
   }
 
-  // x[j] *= w^j, j = 1 .. E-1, with w = tw[m] (conjugated for INV): one table
-  // load, then the powers by squarings and one product per other power
-  // (SC_XW_TWLOAD: one table load per power instead)
+  // x[j] *= w^j, j = 1 .. E-1, with w = tw[m] (conjugated for INV): one
+  // table load per power (measured faster than forming the powers by
+  // squarings and products from one load, SC_XW_TWPOW)
   template <bool INV>
   __device__ static __forceinline__ void twiddle_powers(C (&x)[E], const C* __restrict__ tw, int m) {
     if constexpr (E > 1) {
-#ifdef SC_XW_TWLOAD
+#ifndef SC_XW_TWPOW
 #pragma unroll
       for (int j = 1; j < E; ++j) x[j] = cmul(x[j], twid(tw, m * j, INV));
 #else
@@ -302,9 +301,10 @@ template <typename T, int LOGM> struct XwRow {
   long long off;
   int lane;
 
-  // wn[r] = W_N^{lane + 32 r}, N = 2M
+  // wn[r] = W_N^{lane + 32 r}, N = 2M: one table load times compile-time
+  // roots (SC_XW_HALFLOAD: one table load each)
   __device__ __forceinline__ void half_twiddles(C (&wn)[E]) const {
-#ifdef SC_XW_TWLOAD
+#ifdef SC_XW_HALFLOAD
 #pragma unroll
     for (int r = 0; r < E; ++r) wn[r] = __ldg(&twN[lane + 32 * r]);
 #else
