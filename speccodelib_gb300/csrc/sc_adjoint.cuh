@@ -106,6 +106,7 @@ __device__ __forceinline__ void adj_epilogue(C2<T> (&l)[E::JL][E::RL][3], const 
   C* __restrict__ lam[3] = {aa.lam[0], aa.lam[1], aa.lam[2]};
   const int stage = aa.stage;
   const T dt = aa.dt;
+  const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(aa.fkmax2), kc_b = k2_lt(aa.kcut2);
 #pragma unroll
   for (int q0 = 0; q0 < NP; q0 += B) {
     long long idx[B];
@@ -133,11 +134,12 @@ __device__ __forceinline__ void adj_epilogue(C2<T> (&l)[E::JL][E::RL][3], const 
       const int q = q0 + b;
       C* ls = l[q / E::RL][q % E::RL];
       const int ix = ixs[b], iz = izs[b];
+      const int kzi = wavenum(iz, g.nz);
+      const int k2i = ix * ix + kyi * kyi + kzi * kzi;
       if (fblock) {
-        const double kz = wavenum(iz, g.nz), ky = wavenum(iy, g.ny);
-        if ((double)ix * ix + ky * ky + kz * kz < aa.fkmax2) {
+        if (k2i < fk_b) {
           C m[3] = {lw[0][idx[b]], lw[1][idx[b]], lw[2][idx[b]]};
-          adj_mu<C, T>(m, ix, iy, iz, g, aa.mask_rhs, aa.kcut2);
+          adj_mu<C, T>(m, ix, iy, iz, g, aa.mask_rhs, kc_b);
           const T sa = (T)s_a, sb = (T)(ix == 0 ? 0.5 * s_b : s_b);
 #pragma unroll
           for (int c = 0; c < 3; ++c)
@@ -168,9 +170,7 @@ __device__ __forceinline__ void adj_epilogue(C2<T> (&l)[E::JL][E::RL][3], const 
           }
           break;
         default: {   // stage 1: lam = lv + ls
-          const double kz = wavenum(iz, g.nz), ky = wavenum(iy, g.ny);
-          const double k2 = (double)ix * ix + ky * ky + kz * kz;
-          const bool cut = k2 >= aa.kcut2 && k2 > 0.0;
+          const bool cut = k2i >= kc_b && k2i > 0;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const C lm = cadd(lvv[b][c], ls[c]);

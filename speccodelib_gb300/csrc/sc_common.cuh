@@ -75,6 +75,17 @@ template <> __device__ __forceinline__ float2 cscale<float2, float>(float2 a, fl
 // (the FFTW ordering, wavenumber.f90:109,115).
 __device__ __forceinline__ int wavenum(int i, int n) { return i < n / 2 ? i : i - n; }
 
+// Integer forms of a real bound t on an integer k^2 (exact in int: 3 (n/2)^2
+// < 2^31 for every supported n):  k2 < t  <=>  k2 < k2_lt(t),  and
+// k2 <= t  <=>  k2 < k2_le(t).  Computed once per kernel, they keep the
+// per-point wavenumber tests in integer arithmetic (double-precision
+// throughput on this part is a small fraction of single precision).
+__host__ __device__ inline int k2_clamp(double b) {
+  return b >= 2147483647.0 ? 2147483647 : (b <= -2147483647.0 ? -2147483647 : (int)b);
+}
+__host__ __device__ inline int k2_lt(double t) { return k2_clamp(ceil(t)); }
+__host__ __device__ inline int k2_le(double t) { return k2_clamp(floor(t) + 1.0); }
+
 // Grid geometry shared by all passes.
 struct Geom {
   int nx, ny, nz;      // physical grid

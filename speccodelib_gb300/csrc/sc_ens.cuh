@@ -250,6 +250,7 @@ __device__ __forceinline__ void ens_yfwd(const EnsMember<T>& mb, int tile, int s
   }
   // symmetrize2d: zero ky = -N/2, kx = N/2 and the mean; kx = 0 copies
   const double kc = 2.0 * (N / 2) / 3.0;
+  const int kc_b = k2_lt(kc * kc);
   if (kx0 == 0) {
 #pragma unroll
     for (int a = 0; a < E::JL; ++a)
@@ -275,11 +276,12 @@ __device__ __forceinline__ void ens_yfwd(const EnsMember<T>& mb, int tile, int s
       int p, n;
       if (!(E::out_pos(a, r, p, n) && p < nvalid)) continue;
       const int ix = kx0 + p;
-      const double ky = wavenum(n, N);
-      const double k2 = (double)ix * ix + ky * ky;
+      const int ky = wavenum(n, N);
+      const int k2i = ix * ix + ky * ky;
       C w = nl[a][r];
-      if (n == N / 2 || ix == mb.nxh - 1 || (ix == 0 && n == 0) || k2 >= kc * kc) w = czero<C>();
-      const T arg = (T)((double)mb.alpha + (double)mb.nu8 * k2 * k2 * k2 * k2) * mb.dt * T(0.5);
+      if (n == N / 2 || ix == mb.nxh - 1 || (ix == 0 && n == 0) || k2i >= kc_b) w = czero<C>();
+      const T k2 = (T)k2i, k4 = k2 * k2;   // exact: k2 < 2^24
+      const T arg = (mb.alpha + mb.nu8 * (k4 * k4)) * mb.dt * T(0.5);
       const T Ef = exp(-arg);
       const T E2 = Ef * Ef, dt = mb.dt, hdt = T(0.5) * mb.dt;
       const long long idx = (long long)n * mb.nxp + ix;

@@ -160,11 +160,11 @@ zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldLi
   // forcing band energy of the stage input (force.f90:16-22), FP64
   if (za.fs.enabled && ((double)kx0 * kx0 + (double)ky * ky < za.fs.fkmax2)) {
     double q = 0.0;
+    const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(za.fs.fkmax2);
     for (int e = threadIdx.x; e < P * N; e += NT) {
       const int p = e % P, n = e / P;
-      const double kx = kx0 + p, kz = wavenum(n, g.nz);
-      const double k2 = kx * kx + (double)ky * ky + kz * kz;
-      if (p < nvalid && k2 < za.fs.fkmax2) {
+      const int kx = kx0 + p, kz = wavenum(n, g.nz);
+      if (p < nvalid && kx * kx + kyi * kyi + kz * kz < fk_b) {
         double s = 0.0;
         for (int c = 0; c < 3; ++c) s += (double)rt[c][e].x * rt[c][e].x + (double)rt[c][e].y * rt[c][e].y;
         q += (kx0 + p == 0) ? 0.5 * s : s;
@@ -218,16 +218,17 @@ zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, Fiel
   __syncthreads();
   if (!mbar_wait_bounded(&bar, 0, err)) return;
   const bool fsum = za.fs.enabled && ((double)kx0 * kx0 + ky * ky < za.fs.fkmax2);
+  const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(za.fs.fkmax2), kc_b = k2_lt(za.kcut2);
   double q = 0.0;
   for (int e = threadIdx.x; e < P * N; e += NT) {
     const int p = e % P, n = e / P;
     if (p >= nvalid) continue;   // columns beyond nx/2: zeros, never stored
     const int ix = kx0 + p;
     C m[3] = {rt[0][e], rt[1][e], rt[2][e]};
-    adj_mu<C, T>(m, ix, iy, n, g, za.mask_rhs, za.kcut2);
+    adj_mu<C, T>(m, ix, iy, n, g, za.mask_rhs, kc_b);
     if (fsum) {
-      const double kz = wavenum(n, g.nz);
-      if ((double)ix * ix + ky * ky + kz * kz < za.fs.fkmax2)
+      const int kz = wavenum(n, g.nz);
+      if (ix * ix + kyi * kyi + kz * kz < fk_b)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const C sv = za.v[c][base + n * zstride + p];
@@ -286,6 +287,7 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, 
   const T ky = (T)wavenum(iy, g.ny);
   const bool tile0 = kx0 == 0;
   const bool band = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
+  const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(st.fkmax2), kc_b = k2_lt(st.kcut2);
   if (launch_failed(err)) return;
   if (threadIdx.x == 0) {
     for (int c = 0; c < 3; ++c) mbar_init(&bars[c], 1);
@@ -332,9 +334,9 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, 
       const int ix = kx0 + p;
       const long long idx = base + iz * zstride + p;
       C* wp = wv[i];
-      const double kz = wavenum(iz, g.nz);
-      const double k2 = (double)ix * ix + (double)ky * ky + kz * kz;
-      if (band && k2 < st.fkmax2) {
+      const int kz = wavenum(iz, g.nz);
+      const int k2 = ix * ix + kyi * kyi + kz * kz;
+      if (band && k2 < fk_b) {
         const T ac = (T)s_coef;
 #pragma unroll
         for (int c = 0; c < 3; ++c) wp[c] = cadd(wp[c], cscale(st.sin[c][idx], ac));
@@ -348,7 +350,7 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, 
       if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
         wp[0] = wp[1] = wp[2] = czero<C>();
       C sn[3];
-      finish_point_pre<T>(st, g, idx, ix, iy, iz, wp, vv[i], av[i], sn);
+      finish_point_pre<T>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i], sn);
       if (tile0 || band || fa.store_all) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) st.sout[c][idx] = sn[c];
@@ -356,7 +358,7 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, 
       if (!tile0) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) rt[c][e] = sn[c];
-        if (band && k2 < st.fkmax2) {
+        if (band && k2 < fk_b) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) q += (double)sn[c].x * sn[c].x + (double)sn[c].y * sn[c].y;
         }

@@ -91,6 +91,7 @@ pencil_plain_kernel(FieldList<T> fl, PlainArgs<T> pa, Geom g, const C2<T>* __res
   const int nvalid = min(P, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * pa.outer_stride + kx0;
   const int kyv = wavenum(blockIdx.y, g.ny);
+  const int kmax_b = k2_le(pa.kmax2);
   for (int f = 0; f < pa.nfields; ++f) {
     C* __restrict__ fp = fl.f[f] + base;
     C in[E::J1][E::R1], out[E::JL][E::RL];
@@ -103,8 +104,7 @@ pencil_plain_kernel(FieldList<T> fl, PlainArgs<T> pa, Geom g, const C2<T>* __res
         C x = ok ? fp[n * pa.axis_stride + p] : czero<C>();
         if (pa.filter) {
           const int kx = kx0 + p, kz = wavenum(n, g.nz);
-          const double k2 = (double)kx * kx + (double)kyv * kyv + (double)kz * kz;
-          x = (k2 <= pa.kmax2) ? cscale(x, pa.scale) : czero<C>();
+          x = (kx * kx + kyv * kyv + kz * kz < kmax_b) ? cscale(x, pa.scale) : czero<C>();
         }
         in[a][r] = x;
       }
@@ -151,21 +151,23 @@ template <typename T> struct ZvArgs {
 };
 
 // zero (symmetrize's planes and mean), optional RHS mask, then projection:
-// mu = zero P lam at wavenumber (ix, ky, kz).
+// mu = zero P lam at wavenumber (ix, ky, kz); kcut_b = k2_lt(kcut2).
 template <typename C, typename R>
 __device__ __forceinline__ void adj_mu(C* m, int ix, int iy, int iz, const Geom& g, int mask_rhs,
-                                       double kcut2) {
-  const R kx = (R)ix, ky = (R)wavenum(iy, g.ny), kz = (R)wavenum(iz, g.nz);
-  const R k2 = kx * kx + ky * ky + kz * kz;
+                                       int kcut_b) {
+  const int kyi = wavenum(iy, g.ny), kzi = wavenum(iz, g.nz);
+  const int k2i = ix * ix + kyi * kyi + kzi * kzi;
+  const R kx = (R)ix, ky = (R)kyi, kz = (R)kzi;
+  const R k2 = (R)k2i;
   const bool zero = iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0) ||
-                    (mask_rhs && (double)k2 >= kcut2);
+                    (mask_rhs && k2i >= kcut_b);
   if (zero) {
     m[0] = m[1] = m[2] = czero<C>();
     return;
   }
   if (k2 > R(0)) {
     C t = cadd(cadd(cscale(m[0], kx), cscale(m[1], ky)), cscale(m[2], kz));
-    t = mk<C>(t.x / k2, t.y / k2);
+    t = cscale(t, R(1) / k2);
     m[0] = csub(m[0], cscale(t, kx));
     m[1] = csub(m[1], cscale(t, ky));
     m[2] = csub(m[2], cscale(t, kz));
@@ -225,6 +227,8 @@ zinv_vel_kernel(ZvArgs<T> za, FieldList<T> out, Geom g, const C2<T>* __restrict_
   const long long zstride = (long long)g.ny * g.nxp;
   const long long base = (long long)iy * g.nxp + kx0;
   const T ky = (T)wavenum(iy, g.ny);
+  const int kyi = wavenum(iy, g.ny);
+  const int fk_b = k2_lt(za.fs.fkmax2), kt_b = k2_le(za.ktest2), kc_b = k2_lt(za.kcut2);
 
   C vr[E::J1][E::R1][3];
   double q = 0.0;
@@ -238,9 +242,8 @@ zinv_vel_kernel(ZvArgs<T> za, FieldList<T> out, Geom g, const C2<T>* __restrict_
 #pragma unroll
       for (int c = 0; c < 3; ++c) vr[a][r][c] = ok ? za.v[c][base + n * zstride + p] : czero<C>();
       if (fsum && ok) {
-        const double kx = kx0 + p, kz = wavenum(n, g.nz);
-        const double k2 = kx * kx + (double)ky * ky + kz * kz;
-        if (k2 < za.fs.fkmax2) {
+        const int kx = kx0 + p, kz = wavenum(n, g.nz);
+        if (kx * kx + kyi * kyi + kz * kz < fk_b) {
           double e = 0.0;
 #pragma unroll
           for (int c = 0; c < 3; ++c)
@@ -261,12 +264,10 @@ zinv_vel_kernel(ZvArgs<T> za, FieldList<T> out, Geom g, const C2<T>* __restrict_
       for (int r = 0; r < E::R1; ++r) {
         int p, n;
         E::in_pos(a, r, p, n);
-        const T kx = (T)(kx0 + p), kz = (T)wavenum(n, g.nz);
+        const int kzi = wavenum(n, g.nz);
+        const T kx = (T)(kx0 + p), kz = (T)kzi;
         bool gin = true;
-        if (MODE == ZV_DYN) {
-          const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
-          gin = k2 <= za.ktest2;
-        }
+        if (MODE == ZV_DYN) gin = (kx0 + p) * (kx0 + p) + kyi * kyi + kzi * kzi < kt_b;
         in[a][r] = zv_gen<MODE == ZV_ADJ ? ZV_DNS : MODE>(f, vr[a][r][0], vr[a][r][1], vr[a][r][2], kx, ky, kz, gin);
       }
     E::template run<true>(in, o, sm, tw);
@@ -292,10 +293,10 @@ zinv_vel_kernel(ZvArgs<T> za, FieldList<T> out, Geom g, const C2<T>* __restrict_
         C m[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) m[c] = ok ? za.lam[c][base + n * zstride + p] : czero<C>();
-        if (ok) adj_mu<C, T>(m, kx0 + p, iy, n, g, za.mask_rhs, za.kcut2);
+        if (ok) adj_mu<C, T>(m, kx0 + p, iy, n, g, za.mask_rhs, kc_b);
         if (fsum && ok) {
-          const double kx = kx0 + p, kz = wavenum(n, g.nz);
-          if (kx * kx + (double)ky * ky + kz * kz < za.fs.fkmax2)
+          const int kx = kx0 + p, kz = wavenum(n, g.nz);
+          if (kx * kx + kyi * kyi + kz * kz < fk_b)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const C sv = za.v[c][base + n * zstride + p];
@@ -380,21 +381,23 @@ __host__ __device__ constexpr bool mode_reads_acc(int m) {
 // `snext` given, RK stages 1-3 return the next stage input there instead of
 // storing it to st.sout.
 template <typename T>
+// kcut_b = k2_lt(st.kcut2), computed once per kernel.
 __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const Geom& g, long long idx,
-                                                 int ix, int iy, int iz, C2<T>* w, const C2<T>* vv,
+                                                 int ix, int iy, int iz, int kcut_b, C2<T>* w, const C2<T>* vv,
                                                  const C2<T>* av, C2<T>* snext = nullptr) {
   using C = C2<T>;
-  const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
-  const T k2 = kx * kx + ky * ky + kz * kz;
-  if (st.project && k2 > T(0)) {
+  const int kyi = wavenum(iy, g.ny), kzi = wavenum(iz, g.nz);
+  const int k2i = ix * ix + kyi * kyi + kzi * kzi;
+  const T kx = (T)ix, ky = (T)kyi, kz = (T)kzi;
+  if (st.project && k2i > 0) {
     // projection.f90:24-28: w -= k (k.w)/(k^2 + tiny)
     C t = cadd(cadd(cscale(w[0], kx), cscale(w[1], ky)), cscale(w[2], kz));
-    t = mk<C>(t.x / k2, t.y / k2);
+    t = cscale(t, T(1) / (T)k2i);
     w[0] = csub(w[0], cscale(t, kx));
     w[1] = csub(w[1], cscale(t, ky));
     w[2] = csub(w[2], cscale(t, kz));
   }
-  const bool cut = (double)k2 >= st.kcut2 && !(ix == 0 && iy == 0 && iz == 0);
+  const bool cut = k2i >= kcut_b && !(ix == 0 && iy == 0 && iz == 0);
   if (st.mask_rhs && cut) w[0] = w[1] = w[2] = czero<C>();
   if (st.mode == SM_RHS || st.mode == SM_LAMB) {
 #pragma unroll
@@ -482,10 +485,10 @@ __device__ __forceinline__ void load_state(const StageArgs<T>& st, long long idx
 
 template <typename T>
 __device__ __forceinline__ void finish_point(const StageArgs<T>& st, const Geom& g, long long idx,
-                                             int ix, int iy, int iz, C2<T>* w) {
+                                             int ix, int iy, int iz, int kcut_b, C2<T>* w) {
   C2<T> vv[3], av[3];
   load_state<T>(st, idx, vv, av);
-  finish_point_pre<T>(st, g, idx, ix, iy, iz, w, vv, av);
+  finish_point_pre<T>(st, g, idx, ix, iy, iz, kcut_b, w, vv, av);
 }
 
 // K_f of force.f90:16-22 from the zinv partial sums, fixed order.
@@ -585,6 +588,7 @@ zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __rest
   }
   // forcing coefficient a = eps / (2 K_f) (force.f90:23)
   const bool fblock = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
+  const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(st.fkmax2), kc_b = k2_lt(st.kcut2);
   if (fblock) {
     if (threadIdx.x == 0) {
       const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
@@ -602,9 +606,8 @@ zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __rest
       const long long idx = base + n * zstride + p;
       C* wp = w[a][r];
       if (fblock) {
-        const double kz = wavenum(iz, g.nz);
-        const double k2 = (double)ix * ix + (double)ky * ky + kz * kz;
-        if (k2 < st.fkmax2) {
+        const int kz = wavenum(iz, g.nz);
+        if (ix * ix + kyi * kyi + kz * kz < fk_b) {
           const T ac = (T)s_coef;
 #pragma unroll
           for (int c = 0; c < 3; ++c) wp[c] = cadd(wp[c], cscale(st.sin[c][idx], ac));
@@ -621,7 +624,7 @@ zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __rest
         if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
           wp[0] = wp[1] = wp[2] = czero<C>();
       }
-      finish_point<T>(st, g, idx, ix, iy, iz, wp);
+      finish_point<T>(st, g, idx, ix, iy, iz, kc_b, wp);
     }
 }
 
@@ -631,6 +634,7 @@ template <typename T>
 __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
   using C = C2<T>;
   const long long total = (long long)g.ny * g.nz;
+  const int kc_b = k2_lt(st.kcut2);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int iy = (int)(t % g.ny), iz = (int)(t / g.ny);
@@ -641,7 +645,7 @@ __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) w[c] = (iy == g.ny / 2) ? czero<C>() : cconj(st.side[s + c]);
     const long long idx = ((long long)iz * g.ny + iy) * g.nxp;
-    finish_point<T>(st, g, idx, 0, iy, iz, w);
+    finish_point<T>(st, g, idx, 0, iy, iz, kc_b, w);
   }
 }
 

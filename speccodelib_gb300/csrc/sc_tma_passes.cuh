@@ -173,11 +173,11 @@ zinv_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldLis
   const bool fsum = za.fs.enabled && ((double)kx0 * kx0 + (double)ky * ky < za.fs.fkmax2);
   if (fsum) {
     double q = 0.0;
+    const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(za.fs.fkmax2);
     for (int e = threadIdx.x; e < P * N; e += NT) {
       const int p = e % P, n = e / P;
-      const double kx = kx0 + p, kz = wavenum(n, g.nz);
-      const double k2 = kx * kx + (double)ky * ky + kz * kz;
-      if (p < nvalid && k2 < za.fs.fkmax2) {
+      const int kx = kx0 + p, kz = wavenum(n, g.nz);
+      if (p < nvalid && kx * kx + kyi * kyi + kz * kz < fk_b) {
         double s = 0.0;
         for (int c = 0; c < 3; ++c) s += (double)in[c][e].x * in[c][e].x + (double)in[c][e].y * in[c][e].y;
         q += (kx0 + p == 0) ? 0.5 * s : s;
@@ -246,6 +246,7 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom 
     }
   }
   const bool fblock = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
+  const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(st.fkmax2), kc_b = k2_lt(st.kcut2);
   if (fblock && threadIdx.x == 0) {
     const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
     s_coef = st.eps / (2.0 * kf);
@@ -281,9 +282,8 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom 
       const long long idx = base + iz * zstride + p;
       C* wp = wv[i];
       if (fblock) {
-        const double kz = wavenum(iz, g.nz);
-        const double k2 = (double)ix * ix + (double)ky * ky + kz * kz;
-        if (k2 < st.fkmax2) {
+        const int kz = wavenum(iz, g.nz);
+        if (ix * ix + kyi * kyi + kz * kz < fk_b) {
           const T ac = (T)s_coef;
 #pragma unroll
           for (int c = 0; c < 3; ++c) wp[c] = cadd(wp[c], cscale(st.sin[c][idx], ac));
@@ -299,7 +299,7 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom 
         if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
           wp[0] = wp[1] = wp[2] = czero<C>();
       }
-      finish_point_pre<T>(st, g, idx, ix, iy, iz, wp, vv[i], av[i]);
+      finish_point_pre<T>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i]);
     }
   }
 }
