@@ -110,8 +110,8 @@ cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, con
 }
 
 template <typename T, int LOGN>
-cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const StageArgs<T>& st, const FusedArgs<T>& fa,
-                             const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
+cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const CUtensorMap& fmap, const StageArgs<T>& st,
+                             const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
   using Z = ZiCfg<T, LOGN>;
   if constexpr (!Z::SUPPORTED) {
     return cudaErrorNotSupported;
@@ -120,7 +120,7 @@ cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const StageArgs<T>& st, co
     static cudaError_t attr = smem_attr(k, Z::SMEM);
     if (attr != cudaSuccess) return attr;
     dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
-    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, st, fa, g, tw, err);
+    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, fmap, st, fa, g, tw, err);
     return cudaGetLastError();
   }
 }
@@ -451,9 +451,9 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
 #define SC_XPASS_CASE_double(L) SC_XPASS_BODY(double, L)
 
 #define SC_FUSED_CASE_float(L) \
-  case L: return sc::launch_zfwd_zinv<float, L>(lmap, st, fa, g, tw, err, s);
+  case L: return sc::launch_zfwd_zinv<float, L>(lmap, fmap, st, fa, g, tw, err, s);
 #define SC_FUSED_CASE_double(L) \
-  case L: return sc::launch_zfwd_zinv<double, L>(lmap, st, fa, g, tw, err, s);
+  case L: return sc::launch_zfwd_zinv<double, L>(lmap, fmap, st, fa, g, tw, err, s);
 #define SC_ZINV5_CASE_float(L) case L: return sc::launch_zinv5<float, L>(vmap, za, out, g, tw, err, s);
 #define SC_ZINV5_CASE_double(L) case L: return sc::launch_zinv5<double, L>(vmap, za, out, g, tw, err, s);
 #define SC_ZPHI_CASE_float(L) case L: return sc::launch_zinv_phi<float, L>(lmap, za, out, g, tw, err, s);
@@ -470,9 +470,10 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     switch (logn) { SC_LOGN_CASES(SC_ZI_P_CASE_##T) default: return 0; }                         \
   }                                                                                              \
   template <>                                                                                    \
-  cudaError_t sc::Launch<T>::zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, \
-                                           const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, \
-                                           int* err, cudaStream_t s) {                           \
+  cudaError_t sc::Launch<T>::zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const CUtensorMap& fmap, \
+                                           const StageArgs<T>& st, const FusedArgs<T>& fa,      \
+                                           const Geom& g, const C2<T>* tw, int* err,            \
+                                           cudaStream_t s) {                                    \
     switch (logn) {                                                                              \
       SC_LOGN_CASES(SC_FUSED_CASE_##T)                                                           \
       default: return cudaErrorInvalidValue;                                                     \

@@ -262,8 +262,8 @@ zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, Fiel
 // grid = (kx tiles, ny).
 template <typename T, int LOGN>
 __global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
-zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, FusedArgs<T> fa, Geom g,
-                     const C2<T>* __restrict__ tw, int* err) {
+zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap fmap,
+                     StageArgs<T> st, FusedArgs<T> fa, Geom g, const C2<T>* __restrict__ tw, int* err) {
   using Z = ZiCfg<T, LOGN>;
   using Cfg = TmaCfg<T, LOGN>;
   using EF = typename Z::EngF;
@@ -307,6 +307,9 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, 
   __syncthreads();
   for (int c = 0; c < 3; ++c) {
     if (!mbar_wait_bounded(&bars[c], 0, err)) return;
+    // the update's operands into L2 once the Lamb tiles are in (issued with
+    // them, the prefetch delays them)
+    if (c == 2 && threadIdx.x == 0) prefetch_update_tile<Cfg>(&fmap, st, kx0, iy);
     EF::template run_inplace<false>(rt[c], tw);
   }
   // spectral update; the next stage input goes back into the tiles

@@ -73,9 +73,11 @@ template <typename T> struct Launch {
   static cudaError_t zinv_phi_tma(int logn, const CUtensorMap& lmap, const ZvArgs<T>& za,
                                   const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                                   cudaStream_t s);
-  static cudaError_t zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st,
-                                   const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, int* err,
-                                   cudaStream_t s);
+  // fmap: the whole field slab, tiles as lmap, for the L2 prefetch of the
+  // update operands (StageArgs::pf_slot)
+  static cudaError_t zfwd_zinv_tma(int logn, const CUtensorMap& lmap, const CUtensorMap& fmap,
+                                   const StageArgs<T>& st, const FusedArgs<T>& fa, const Geom& g,
+                                   const C2<T>* tw, int* err, cudaStream_t s);
   // discrete adjoint (sc_adjoint.cuh)
   static cudaError_t zfwd_adj(int logn, const FieldList<T>& fin, const AdjArgs<T>& aa, const Geom& g,
                               const C2<T>* tw, cudaStream_t s);

@@ -364,7 +364,12 @@ template <typename T> struct StageArgs {
   int mask_rhs;         // also truncate the RHS (mask = rhs_and_step)
   int symmetrize;       // apply symmetrize.f90:32-64 to w
   int project;          // apply projection.f90 to w
+  // TMA z-forward kernels: slots (field indices of the slab map) of the
+  // fields the update reads, prefetched into L2 when a tile starts
+  int pf_n;
+  int pf_slot[6];
 };
+
 
 // What the update of a mode reads at each point besides w.
 __host__ __device__ constexpr bool mode_reads_v(int m) {

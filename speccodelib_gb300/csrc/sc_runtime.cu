@@ -93,6 +93,7 @@ struct sc_handle {
   bool zinv5 = true;              // TMA-fed five-transform zinv (DNS)
   bool fuse = true;               // RK stages 1-3: zfwd fused with the next zinv
   bool graph = true;              // replay captured CUDA graphs (steps, adjoint)
+  bool prefetch = true;           // L2 prefetch of the update operands in the fused z kernel
   cudaGraphExec_t step_exec = nullptr;   // one RK4 step
   cudaGraphExec_t adj_exec = nullptr;    // one adjoint call, for adj_key
   long long adj_key[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -499,6 +500,26 @@ template <typename T> struct Impl {
   //                  fused zfwd (no zinv here); st.kf_partial holds their K_f sums
   // fuse & FUSE_OUT: this stage's zfwd also runs the next stage's zinv,
   //                  writing that stage's K_f sums to kf_next
+  // The slots of the fields the update of `st` reads (v or v0, acc) in the
+  // field slab, and a map over the slab tiled P wide, for the fused z
+  // kernel's L2 prefetch (SPECNS_NO_PREFETCH=1 switches it off); no slots
+  // when a field lies outside the slab.
+  static int prefetch_slots(sc_handle* h, sc::StageArgs<T>& st, int P, CUtensorMap* fmap) {
+    const long long nslab = S_W + h->nwork, fe = h->g.field;
+    const C* f0 = static_cast<const C*>(h->fields);
+    st.pf_n = 0;
+    bool ok = h->prefetch;
+    auto add = [&](const C* p) {
+      const long long d = p - f0;
+      if (!p || d < 0 || d % fe != 0 || d / fe >= nslab) ok = false;
+      else st.pf_slot[st.pf_n++] = (int)(d / fe);
+    };
+    for (int c = 0; c < 3 && sc::mode_reads_v(st.mode); ++c) add(st.mode == sc::SM_AB2_MID ? st.v0[c] : st.v[c]);
+    for (int c = 0; c < 3 && sc::mode_reads_acc(st.mode); ++c) add(st.acc[c]);
+    if (!ok) st.pf_n = 0;
+    return encode_fields(h, h->fields, (int)nslab, 2, P, h->g.nz, fmap);
+  }
+
   static int rhs_pipeline(sc_handle* h, const C* sin[3], sc::StageArgs<T> st, int fuse = 0,
                           double* kf_next = nullptr, bool store_all = false) {
     auto* g = &h->g;
@@ -537,7 +558,9 @@ template <typename T> struct Impl {
         fa.out = wl;
         fa.kf_next = kf_next;
         fa.store_all = store_all;
-        SC_TRY(launch(h, "zfwd_zinv", [&] { return L::zfwd_zinv_tma(h->logz, lmap5, st, fa, *g, tw(h, g->nz), h->derr, h->stream); }));
+        CUtensorMap fmap5;
+        SC_TRY(prefetch_slots(h, st, P5, &fmap5));
+        SC_TRY(launch(h, "zfwd_zinv", [&] { return L::zfwd_zinv_tma(h->logz, lmap5, fmap5, st, fa, *g, tw(h, g->nz), h->derr, h->stream); }));
         SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));
         // the kx = 0 tile of the next stage's zinv, after the fix-up
         CUtensorMap smap;
@@ -1197,6 +1220,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
     h->zinv5 = !(z5 && z5[0] == '1');
     const char* gr = std::getenv("SPECNS_NO_GRAPH");
     h->graph = !(gr && gr[0] == '1');
+    const char* pf = std::getenv("SPECNS_NO_PREFETCH");
+    h->prefetch = !(pf && pf[0] == '1');
   }
   {
     int dev = 0;

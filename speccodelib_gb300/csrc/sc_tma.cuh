@@ -87,6 +87,15 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+// L2 prefetch of one box of a tensor map (the copy engine fetches it; no
+// completion to wait for, boxes outside the tensor fetch nothing).
+__device__ __forceinline__ void tma_prefetch_4d(const CUtensorMap* map, int c0, int c1, int c2, int c3) {
+  asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+               : "memory");
+}
+
 // Tensor view of `nf` equally spaced fields for the strided-axis passes:
 // dims (x: nxh complex in 8-byte units, y: ny, z: nz, field), rows of pitch
 // nxp.  Columns beyond nxh are outside the tensor and load as zero.

@@ -43,6 +43,17 @@ template <typename T, int LOGN> struct TmaCfg {
   static constexpr size_t WORKZ_BYTES = sizeof(C2<T>) * EngineZ::SMEM_ELEMS;
 };
 
+// L2 prefetch of the update's operands for a z tile (thread 0; `fmap` is the
+// whole field slab with tiles P wide and BOX long in z).
+template <typename Cfg, typename T>
+__device__ __forceinline__ void prefetch_update_tile(const CUtensorMap* fmap, const StageArgs<T>& st, int kx0,
+                                                     int iy) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    if (i < st.pf_n)
+      for (int h = 0; h < Cfg::NBOX; ++h) tma_prefetch_4d(fmap, kx0 * Cfg::U, iy, h * Cfg::BOX, st.pf_slot[i]);
+}
+
 // Where a pencil lies: element (p, n) of tile (kx0, outer) of field f is
 // base + f*field + outer*outer_stride + n*axis_stride + kx0 + p.
 template <typename T> struct TmaPass {
@@ -89,9 +100,13 @@ pencil_tma_kernel(const __grid_constant__ CUtensorMap map, TmaPass<T> tp, Geom g
   }
   __syncthreads();
   auto buf = [&](int b) { return reinterpret_cast<C*>(smraw + (size_t)b * Cfg::TILE_BYTES); };
+  // field slowest: the CTAs in flight work on neighbouring tiles of one
+  // field (field fastest, six fields at the same offset, measured 12%
+  // slower for the six-field inverse y-pass)
   auto decode = [&](long long job, int& kx0, int& outer, int& f) {
-    f = (int)(job % tp.nf);
-    const long long t = job / tp.nf;
+    const long long per = (long long)tp.ntx * tp.nouter;
+    f = (int)(job / per);
+    const long long t = job % per;
     kx0 = (int)(t % tp.ntx) * P;
     outer = (int)(t / tp.ntx);
   };
