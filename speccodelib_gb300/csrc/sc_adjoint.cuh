@@ -364,16 +364,16 @@ template <typename T>
 __global__ void __launch_bounds__(256) adj_op_kernel(AdjOpArgs<T> ao, Geom g) {
   using C = C2<T>;
   const long long total = (long long)g.ny * g.nz * g.nxh;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long row = t / g.nxh;
-    const int ix = (int)(t % g.nxh);
-    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
-    const long long idx = row * g.nxp + ix;
-    const double ky = wavenum(iy, g.ny), kz = wavenum(iz, g.nz);
-    const double k2 = (double)ix * ix + ky * ky + kz * kz;
+  const int kc_b = k2_lt(ao.kcut2);
+  for (Walk3 w(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, total, g.nxh,
+               g.ny);
+       w.ok(); w.next()) {
+    const int ix = w.ix;
+    const long long idx = w.row() * g.nxp + ix;
+    const int kyi = wavenum(w.iy, g.ny), kzi = wavenum(w.iz, g.nz);
+    const int k2 = ix * ix + kyi * kyi + kzi * kzi;
     if (ao.op == AO_INIT) {
-      const bool cut = k2 >= ao.kcut2 && k2 > 0.0;
+      const bool cut = k2 >= kc_b && k2 > 0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const C l = cut ? czero<C>() : ao.in[c][idx];
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(256) adj_op_kernel(AdjOpArgs<T> ao, Geom g) {
         ao.out2[c][idx] = cscale(l, ao.dt / T(6));
       }
     } else {
-      const int ll = (int)floor(sqrt(k2) + 0.5);
+      const int ll = shell_index(k2);
       const bool in = ll >= ao.kmin && ll <= ao.kmax;
       const T f = in ? (T)(2.0 * k2 * (ix == 0 ? 0.5 : 1.0)) : T(0);
 #pragma unroll

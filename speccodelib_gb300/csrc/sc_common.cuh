@@ -84,6 +84,48 @@ __host__ __device__ inline int k2_clamp(double b) {
   return b >= 2147483647.0 ? 2147483647 : (b <= -2147483647.0 ? -2147483647 : (int)b);
 }
 __host__ __device__ inline int k2_lt(double t) { return k2_clamp(ceil(t)); }
+
+// floor(sqrt(k2) + 1/2) for an integer k2 >= 0, exactly: the n with
+// n^2 - n < k2 <= n^2 + n (a float root is within one of it).
+__device__ __forceinline__ int shell_index(int k2) {
+  int n = (int)(sqrtf((float)k2) + 0.5f);
+  const long long nn = (long long)n * n;
+  if (nn + n < k2) ++n;
+  else if (n > 0 && nn - n >= k2) --n;
+  return n;
+}
+
+// Grid-stride walk over the points (ix, iy, iz) of an index space of n x ny
+// x (any) points, ix fastest, from point t0 in steps of `stride` points: the
+// coordinates are carried from step to step (two 64-bit divisions per thread
+// instead of three per point).
+struct Walk3 {
+  long long t, total, stride;
+  int ix, iy, iz;
+  int n, ny, dix, diy, diz;
+  __device__ __forceinline__ Walk3(long long t0, long long stride_, long long total_, int n_, int ny_)
+      : t(t0), total(total_), stride(stride_), n(n_), ny(ny_) {
+    const long long r = t0 / n_, sr = stride_ / n_;
+    ix = (int)(t0 - r * n_);
+    iy = (int)(r % ny_);
+    iz = (int)(r / ny_);
+    dix = (int)(stride_ - sr * n_);
+    diy = (int)(sr % ny_);
+    diz = (int)(sr / ny_);
+  }
+  __device__ __forceinline__ bool ok() const { return t < total; }
+  __device__ __forceinline__ void next() {
+    t += stride;
+    ix += dix;
+    int c = ix >= n;
+    if (c) ix -= n;
+    iy += diy + c;
+    c = iy >= ny;
+    if (c) iy -= ny;
+    iz += diz + c;
+  }
+  __device__ __forceinline__ long long row() const { return (long long)iz * ny + iy; }
+};
 __host__ __device__ inline int k2_le(double t) { return k2_clamp(floor(t) + 1.0); }
 
 // Grid geometry shared by all passes.

@@ -36,44 +36,40 @@ __global__ void __launch_bounds__(256) diag_partial_kernel(DiagArgs<T> da, Geom 
   const int ns = da.nshell;
   for (int i = threadIdx.x; i < ns; i += blockDim.x) shells[i] = 0.0;
   __syncthreads();
-  double e = 0.0, k2q = 0.0, mdiv = 0.0, nf = 0.0, mu2 = 0.0;
+  // per-point products in the field's precision, sums in double
+  double e = 0.0, k2q = 0.0, nf = 0.0;
+  T mdiv = T(0), mu2 = T(0);
   const long long rows = (long long)g.ny * g.nz;
   const long long r0 = (long long)blockIdx.x * da.rows_per_block;
+  const long long r1 = r0 + da.rows_per_block < rows ? r0 + da.rows_per_block : rows;
   const int ncol = da.physical ? g.nx / 2 : g.nxh;
-  const long long tot = (long long)da.rows_per_block * ncol;
-  for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
-    const long long row = r0 + t / ncol;
-    const int ix = (int)(t % ncol);
-    if (row >= rows) break;
-    const long long idx = row * g.nxp + ix;
+  const bool kmax_on = da.kmax2 >= 0.0;
+  const int kmax_b = k2_lt(da.kmax2);
+  for (Walk3 w(r0 * ncol + threadIdx.x, blockDim.x, r1 * ncol, ncol, g.ny); w.ok(); w.next()) {
+    const int ix = w.ix;
+    const long long idx = w.row() * g.nxp + ix;
     const C a = da.v[0][idx], b = da.v[1][idx], c = da.v[2][idx];
     if (da.physical) {
-      const double ue = (double)a.x * a.x + (double)b.x * b.x + (double)c.x * c.x;
-      const double uo = (double)a.y * a.y + (double)b.y * b.y + (double)c.y * c.y;
+      const T ue = a.x * a.x + b.x * b.x + c.x * c.x;
+      const T uo = a.y * a.y + b.y * b.y + c.y * c.y;
       mu2 = fmax(mu2, fmax(ue, uo));
       if (!isfinite(ue) || !isfinite(uo)) nf += 1.0;
       continue;
     }
-    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
-    const double kx = ix, ky = wavenum(iy, g.ny), kz = wavenum(iz, g.nz);
-    const double k2 = kx * kx + ky * ky + kz * kz;
-    if (da.kmax2 >= 0.0 && !(k2 < da.kmax2)) continue;
-    if (da.shell_hi > 0) {
-      const int sh = (int)floor(sqrt(k2) + 0.5);
-      if (sh < da.shell_lo || sh > da.shell_hi) continue;
-    }
-    double q = (double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x + (double)b.y * b.y +
-               (double)c.x * c.x + (double)c.y * c.y;
+    const int kyi = wavenum(w.iy, g.ny), kzi = wavenum(w.iz, g.nz);
+    const int k2 = ix * ix + kyi * kyi + kzi * kzi;
+    if (kmax_on && !(k2 < kmax_b)) continue;
+    const int ll = (da.shell_hi > 0 || ns > 0) ? shell_index(k2) : 0;
+    if (da.shell_hi > 0 && (ll < da.shell_lo || ll > da.shell_hi)) continue;
+    T q = a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
     if (!isfinite(q)) nf += 1.0;
-    if (ix == 0) q *= 0.5;
-    e += q;
-    k2q += k2 * q;
-    const double dr = kx * a.x + ky * b.x + kz * c.x, di = kx * a.y + ky * b.y + kz * c.y;
+    if (ix == 0) q *= T(0.5);
+    e += (double)q;
+    k2q += (double)((T)k2 * q);
+    const T kx = (T)ix, ky = (T)kyi, kz = (T)kzi;
+    const T dr = kx * a.x + ky * b.x + kz * c.x, di = kx * a.y + ky * b.y + kz * c.y;
     mdiv = fmax(mdiv, sqrt(dr * dr + di * di));
-    if (ns > 0) {
-      const int ll = (int)floor(sqrt(k2) + 0.5);
-      if (ll >= 1 && ll <= ns) atomicAdd(&shells[ll - 1], q);
-    }
+    if (ns > 0 && ll >= 1 && ll <= ns) atomicAdd(&shells[ll - 1], (double)q);
   }
   double* out = da.partial + (long long)blockIdx.x * (DQ_N + ns);
   double s;
@@ -84,7 +80,7 @@ __global__ void __launch_bounds__(256) diag_partial_kernel(DiagArgs<T> da, Geom 
   s = block_sum<256>(nf, red);
   if (threadIdx.x == 0) out[DQ_NONFINITE] = s;
   // maxima: reuse the sum tree with max
-  double m1 = warp_max(mdiv), m2 = warp_max(mu2);
+  double m1 = warp_max((double)mdiv), m2 = warp_max((double)mu2);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = m1; }
   __syncthreads();
@@ -154,33 +150,34 @@ template <typename T>
 __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
   using C = C2<T>;
   const long long rows = (long long)g.ny * g.nz;
-  const long long total = (oa.op == OP_KX0_COPY) ? rows : rows * g.nxh;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tstride = (long long)gridDim.x * blockDim.x;
   T sfac = T(1);
   if (oa.op == OP_SCALE) sfac = oa.dscal ? (T)sqrt(oa.a / *oa.dscal) : (T)oa.a;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    if (oa.op == OP_KX0_COPY) {
+  if (oa.op == OP_KX0_COPY) {
+    for (long long t = t0; t < rows; t += tstride) {
       const int iy = (int)(t % g.ny), iz = (int)(t / g.ny);
       if (!(iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2))) continue;
       const int sy = (g.ny - iy) % g.ny, sz = (g.nz - iz) % g.nz;
       const long long d = ((long long)iz * g.ny + iy) * g.nxp, s = ((long long)sz * g.ny + sy) * g.nxp;
       for (int c = 0; c < oa.nfields; ++c) oa.f[c][d] = (iy == g.ny / 2) ? czero<C>() : cconj(oa.f[c][s]);
-      continue;
     }
-    const long long row = t / g.nxh;
-    const int ix = (int)(t % g.nxh);
-    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
-    const long long idx = row * g.nxp + ix;
-    const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
-    const double k2d = (double)ix * ix + (double)ky * ky + (double)kz * kz;
+    return;
+  }
+  const int kc_b = k2_lt(oa.kcut2), b_b = k2_lt(oa.b);
+  for (Walk3 w(t0, tstride, rows * g.nxh, g.nxh, g.ny); w.ok(); w.next()) {
+    const int ix = w.ix, iy = w.iy, iz = w.iz;
+    const long long idx = w.row() * g.nxp + ix;
+    const int kyi = wavenum(iy, g.ny), kzi = wavenum(iz, g.nz);
+    const int k2i = ix * ix + kyi * kyi + kzi * kzi;
+    const T kx = (T)ix, ky = (T)kyi, kz = (T)kzi;
     switch (oa.op) {
       case OP_PROJECT:
       case OP_INIT_SHAPE: {
         C w0 = oa.f[0][idx], w1 = oa.f[1][idx], w2 = oa.f[2][idx];
-        const T k2 = kx * kx + ky * ky + kz * kz;
-        if (k2 > T(0)) {
+        if (k2i > 0) {
           C tt = cadd(cadd(cscale(w0, kx), cscale(w1, ky)), cscale(w2, kz));
-          tt = mk<C>(tt.x / k2, tt.y / k2);
+          tt = cscale(tt, T(1) / (T)k2i);
           w0 = csub(w0, cscale(tt, kx));
           w1 = csub(w1, cscale(tt, ky));
           w2 = csub(w2, cscale(tt, kz));
@@ -193,19 +190,19 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
           for (int c = 0; c < oa.nfields; ++c) oa.f[c][idx] = czero<C>();
         break;
       case OP_MASK:
-        if (k2d >= oa.kcut2 && k2d > 0.0)
+        if (k2i >= kc_b && k2i > 0)
           for (int c = 0; c < oa.nfields; ++c) oa.f[c][idx] = czero<C>();
         break;
       case OP_FORCE_ADD:
         // k2(1,1,1) = tiny < fkmax^2: the mean mode is in the band too
-        if (k2d < oa.kcut2) {
+        if (k2i < kc_b) {
           const T a = (T)oa.a;
           for (int c = 0; c < 3; ++c) oa.f[c][idx] = cadd(oa.f[c][idx], cscale(oa.gsrc[c][idx], a));
         }
         break;
       case OP_INIT_AMP: {
         // k2 at the mean mode is tiny(1.0_sp) (wavenumber.f90:156)
-        const double k2r = (k2d == 0.0) ? 1.1754943508222875e-38 : k2d;
+        const double k2r = (k2i == 0) ? 1.1754943508222875e-38 : (double)k2i;
         double amp;
         if (oa.spectrum_kind == 0) {
           const double pi = 3.1415926536;
@@ -249,7 +246,7 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
         break;
       }
       case OP_FORCE_BAND:
-        if (k2d < oa.kcut2 && k2d >= oa.b) {
+        if (k2i < kc_b && !(k2i < b_b)) {
           const T a = (T)oa.a;
           for (int c = 0; c < 3; ++c) oa.f[c][idx] = cadd(oa.f[c][idx], cscale(oa.gsrc[c][idx], a));
         }
@@ -275,13 +272,13 @@ __global__ void __launch_bounds__(256) moments_kernel(const C2<T>* d, Geom g, in
   const long long r1 = r0 + rows_per_block < rows ? r0 + rows_per_block : rows;
   const int m = g.nx / 2;
   double s2 = 0.0, s3 = 0.0;
-  for (long long t = r0 * m + threadIdx.x; t < r1 * m; t += blockDim.x) {
-    const long long row = t / m;
-    const C2<T> v = d[row * g.nxp + (t % m)];
-    const double a = v.x, b = v.y;
-    s2 += a * a + b * b;
-    s3 += a * a * a + b * b * b;
-  }
+  for (long long row = r0; row < r1; ++row)
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      const C2<T> v = d[row * g.nxp + i];
+      const double a = v.x, b = v.y;
+      s2 += a * a + b * b;
+      s3 += a * a * a + b * b * b;
+    }
   s2 = block_sum<256>(s2, red);
   s3 = block_sum<256>(s3, red);
   if (threadIdx.x == 0) {
@@ -306,10 +303,10 @@ __global__ void __launch_bounds__(256) enstrophy_kernel(const C2<T>* w0, const C
                                                         double* out) {
   const int m = g.nx / 2;
   const long long total = (long long)g.ny * g.nz * m;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long row = t / m;
-    const int i = (int)(t % m);
+  for (Walk3 w(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, total, m, g.ny);
+       w.ok(); w.next()) {
+    const long long row = w.row();
+    const int i = w.ix;
     const long long idx = row * g.nxp + i;
     const C2<T> a = w0[idx], b = w1[idx], c = w2[idx];
     out[row * g.nx + 2 * i] = 0.5 * ((double)a.x * a.x + (double)b.x * b.x + (double)c.x * c.x);
@@ -331,13 +328,12 @@ __global__ void __launch_bounds__(256) strain_kernel(StrainArgs<T> sa, Geom g) {
   using C = C2<T>;
   const long long total = (long long)g.ny * g.nz * g.nxh;
   const T half = T(0.5);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long row = t / g.nxh;
-    const int ix = (int)(t % g.nxh);
-    const int iy = (int)(row % g.ny), iz = (int)(row / g.ny);
-    const long long idx = row * g.nxp + ix;
-    const T kx = (T)ix, ky = (T)wavenum(iy, g.ny), kz = (T)wavenum(iz, g.nz);
+  for (Walk3 w(blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, total, g.nxh,
+               g.ny);
+       w.ok(); w.next()) {
+    const int ix = w.ix;
+    const long long idx = w.row() * g.nxp + ix;
+    const T kx = (T)ix, ky = (T)wavenum(w.iy, g.ny), kz = (T)wavenum(w.iz, g.nz);
     const C v0 = sa.v[0][idx], v1 = sa.v[1][idx], v2 = sa.v[2][idx];
     sa.s[0][idx] = cmuli(cscale(v0, kx));
     sa.s[1][idx] = cmuli(cscale(cadd(cscale(v1, kx), cscale(v0, ky)), half));
@@ -379,14 +375,12 @@ __global__ void __launch_bounds__(256) phys_kernel(PhysArgs<T> pa, Geom g) {
   const long long rows = (long long)g.ny * g.nz;
   const int ncol = g.nx / 2;
   const long long r0 = (long long)blockIdx.x * pa.rows_per_block;
-  const long long tot = (long long)pa.rows_per_block * ncol;
+  const long long r1 = r0 + pa.rows_per_block < rows ? r0 + pa.rows_per_block : rows;
   double lm = 0.0, mm = 0.0;
   T coef = T(0);
   if (pa.op == PH_TAU) coef = (T)(-2.0 * (*pa.c1) * pa.delta2) * pa.scale;
-  for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
-    const long long row = r0 + t / ncol;
-    if (row >= rows) break;
-    const long long idx = row * g.nxp + (t % ncol);
+  for (Walk3 w(r0 * ncol + threadIdx.x, blockDim.x, r1 * ncol, ncol, g.ny); w.ok(); w.next()) {
+    const long long idx = w.row() * g.nxp + w.ix;
     if (pa.op == PH_TAU) {
       C s[6];
 #pragma unroll
@@ -420,14 +414,15 @@ __global__ void __launch_bounds__(256) phys_kernel(PhysArgs<T> pa, Geom g) {
       }
     } else {
       // slots: G 0-5, filt(s) 6-11, T 12-17, filt(D) 18-23
-      const T w[6] = {T(1), T(2), T(2), T(1), T(2), T(1)};
+      const T wq[6] = {T(1), T(2), T(2), T(1), T(2), T(1)};
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
         const C G = pa.f[q][idx], fs = pa.f[6 + q][idx], Tq = pa.f[12 + q][idx], fD = pa.f[18 + q][idx];
-        const double Lr = (double)fD.x - G.x, Li = (double)fD.y - G.y;
-        const double Mr = (double)fs.x + Tq.x, Mi = (double)fs.y + Tq.y;
-        lm += w[q] * (Lr * Mr + Li * Mi);
-        mm += w[q] * (Mr * Mr + Mi * Mi);
+        // products in the field's precision, sums in double
+        const T Lr = fD.x - G.x, Li = fD.y - G.y;
+        const T Mr = fs.x + Tq.x, Mi = fs.y + Tq.y;
+        lm += (double)(wq[q] * (Lr * Mr + Li * Mi));
+        mm += (double)(wq[q] * (Mr * Mr + Mi * Mi));
       }
     }
   }
