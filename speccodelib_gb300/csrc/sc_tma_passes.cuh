@@ -84,7 +84,9 @@ template <typename T, int LOGN, bool INV>
 __global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
 pencil_tma_kernel(const __grid_constant__ CUtensorMap map, TmaPass<T> tp, Geom g, const C2<T>* __restrict__ tw) {
   using Cfg = TmaCfg<T, LOGN>;
-  using E = typename Cfg::Engine;
+  // stage-0 writes XOR-rotated (conflict-free 64-byte rows) in the forward
+  // pass only: measured 4% faster there, 3% slower in the inverse pass
+  using E = FFTEngine<T, LOGN, Cfg::P, Cfg::P, Cfg::NT, true, 0, !INV>;
   using C = C2<T>;
   constexpr int P = Cfg::P;
   constexpr int NS = Cfg::STAGES;
