@@ -161,7 +161,7 @@ cudaError_t launch_zinv5(const CUtensorMap& vmap, const ZvArgs<T>& za, const Fie
 template <typename T, int LOGM, int MODE>
 cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, const Geom& g, const C2<T>* twM,
                          const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s) {
-  using Cfg = XwCfg<T, LOGM>;
+  using Cfg = XwCfg<T, LOGM, MODE>;
   auto k = xpass_warp_kernel<T, LOGM, MODE>;
   static cudaError_t attr = smem_attr(k, Cfg::SMEM);
   if (attr != cudaSuccess) return attr;
@@ -249,8 +249,9 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
 
 #define SC_XWARP_CASE(T, L)                                                                      \
   case L:                                                                                        \
-    return mode == sc::XW_ADJ ? sc::launch_xwarp<T, L, sc::XW_ADJ>(fin, fout, g, twM, twN, xa, s) \
-                              : sc::launch_xwarp<T, L, sc::XW_DNS>(fin, fout, g, twM, twN, xa, s);
+    return mode == sc::XW_ADJ    ? sc::launch_xwarp<T, L, sc::XW_ADJ>(fin, fout, g, twM, twN, xa, s)  \
+           : mode == sc::XW_SMAG ? sc::launch_xwarp<T, L, sc::XW_SMAG>(fin, fout, g, twM, twN, xa, s) \
+                                 : sc::launch_xwarp<T, L, sc::XW_DNS>(fin, fout, g, twM, twN, xa, s);
 
 #define SC_TMA_TILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::P;
 #define SC_TMA_ZTILE_CASE(L) case L: return sc::TmaCfg<TMA_T, L>::PZ;

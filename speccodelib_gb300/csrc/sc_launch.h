@@ -87,9 +87,9 @@ template <typename T> struct Launch {
                                   const Geom& g, const C2<T>* tw, int* err, cudaStream_t s);
   static cudaError_t adj_copyT(const FieldList<T>& lw, const Geom& g, cudaStream_t s);
   static cudaError_t adj_op(const AdjOpArgs<T>& ao, const Geom& g, cudaStream_t s);
-  // warp-per-row x-pass (sc_xwarp.cuh): mode XW_DNS (Lamb product) or
-  // XW_ADJ (its adjoint); cudaErrorNotSupported for lengths it has no
-  // instance for
+  // warp-per-row x-pass (sc_xwarp.cuh): mode XW_DNS (Lamb product), XW_ADJ
+  // (its adjoint) or XW_SMAG (Lamb product and Smagorinsky tau_ij);
+  // cudaErrorNotSupported for lengths it has no instance for
   static cudaError_t xpass_warp(int logm, int mode, const FieldList<T>& fin, const FieldList<T>& fout,
                                 const Geom& g, const C2<T>* twM, const C2<T>* twN, const XArgs<T>& xa,
                                 cudaStream_t s);

@@ -659,7 +659,7 @@ __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
 // ---------------------------------------------------------------------------
 enum XpMode { XP_DNS = 0, XP_SMAG = 1, XP_C2R3 = 2, XP_R2C3 = 3, XP_ADJ = 4 };
 // modes of the warp-per-row x-pass (sc_xwarp.cuh)
-enum XwMode { XW_DNS = 0, XW_ADJ = 1 };
+enum XwMode { XW_DNS = 0, XW_ADJ = 1, XW_SMAG = 2 };
 template <int MODE> struct XpIO;
 template <> struct XpIO<XP_DNS> { static constexpr int fin = 6, fout = 3; };
 template <> struct XpIO<XP_SMAG> { static constexpr int fin = 12, fout = 9; };

@@ -576,7 +576,13 @@ template <typename T> struct Impl {
       SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
       if (h->tma) SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
       else SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, wl, ypass_args(h, nw), *g, g->nz, tw(h, g->ny), h->stream); }));
-      if (les) SC_TRY(launch(h, "xpass", [&] { return L::xpass(h->logx - 1, sc::XP_SMAG, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream); }));
+      if (les) SC_TRY(launch(h, "xpass", [&] {
+        if (h->xwarp) {
+          cudaError_t e = L::xpass_warp(h->logx - 1, sc::XW_SMAG, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+          if (e != cudaErrorNotSupported) return e;
+        }
+        return L::xpass(h->logx - 1, sc::XP_SMAG, wl, wl, *g, tw(h, g->nx / 2), tw(h, g->nx), xargs(h), h->stream);
+      }));
       else SC_TRY(xpass_dns(h, wl));
       if (h->tma) SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
       else SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, wl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));

@@ -281,11 +281,14 @@ template <typename T, int LOGM> struct WarpFFT {
   }
 };
 
-template <typename T, int LOGM> struct XwCfg {
-  static constexpr int WARPS = 8;
+template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
+  // per warp: the transpose buffer + the rows kept in scrambled order (u;
+  // XW_SMAG also S_ij)
+  static constexpr int KEPT = MODE == XW_SMAG ? 9 : 3;
+  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M;
+  // 8 warps per CTA unless that passes 110 KB of shared memory
+  static constexpr int WARPS = sizeof(C2<T>) * PER_WARP * 8 <= 110 * 1024 ? 8 : 4;
   static constexpr int NT = 32 * WARPS;
-  // per warp: the transpose buffer + three rows kept in scrambled order
-  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + 3 * WarpFFT<T, LOGM>::M;
   static constexpr size_t SMEM = sizeof(C2<T>) * PER_WARP * WARPS;
 };
 
@@ -340,6 +343,32 @@ template <typename T, int LOGM> struct XwRow {
     }
   }
 
+  // r2c post-processing of natural-order Z into the half-complex row at op:
+  // needs Z_{M-k}; k = lane + 32 r pairs with lane (32 - lane) % 32,
+  // register E-1-r (lane 0: its own register (E - r) % E)
+  __device__ __forceinline__ void r2c_store(C (&x)[E], C* __restrict__ op) const {
+    const int src = (32 - lane) & 31;
+    C wn[E];
+    half_twiddles(wn);
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      C zm;
+      zm.x = __shfl_sync(0xffffffffu, x[E - 1 - r].x, src);
+      zm.y = __shfl_sync(0xffffffffu, x[E - 1 - r].y, src);
+      if (lane == 0) zm = x[(E - r) % E];
+      const int k = lane + 32 * r;
+      const C zk = x[r];
+      const C zmc = cconj(zm);
+      const C e = cadd(zk, zmc);
+      const C d = cmul(csub(zk, zmc), wn[r]);
+      op[k] = cscale(csub(e, cmuli(d)), T(0.5));
+      if (k == 0) {   // X_M from Z_0
+        const C d0 = cmul(csub(zk, zmc), __ldg(&twN[M]));
+        op[M] = cscale(csub(e, cmuli(d0)), T(0.5));
+      }
+    }
+  }
+
   // out = r2c(sc * (a x b)), b = c2r of rows bf[0..2]; the cross product is
   // accumulated as the b components arrive (convec_dns.f90:30-38: even
   // points in .x, odd points in .y)
@@ -379,49 +408,71 @@ template <typename T, int LOGM> struct XwRow {
 #pragma unroll
       for (int i = 0; i < E; ++i) x[i] = cscale(l[c][i], sc);
       WF::template scr_to_nat<false>(x, sm, twM, lane);
-      // r2c post-processing: needs Z_{M-k}; k = lane + 32 r pairs with lane
-      // (32 - lane) % 32, register E-1-r (lane 0: its own register (E - r) % E)
-      C* __restrict__ op = of[c] + off;
-      const int src = (32 - lane) & 31;
-      C wn[E];
-      half_twiddles(wn);
+      r2c_store(x, of[c] + off);
+    }
+  }
+
+  // S_ij rows sf[0..5] (order 11 12 13 22 23 33) -> c2r, kept in shared
+  // memory after the three a rows
+  __device__ __forceinline__ void load_s(const C* const sf[6]) const {
+#pragma unroll 1
+    for (int q = 0; q < 6; ++q) {
+      C x[E];
+      load_z(sf[q], x);
+      WF::template nat_to_scr<true>(x, sm, twM, lane);
 #pragma unroll
-      for (int r = 0; r < E; ++r) {
-        C zm;
-        zm.x = __shfl_sync(0xffffffffu, x[E - 1 - r].x, src);
-        zm.y = __shfl_sync(0xffffffffu, x[E - 1 - r].y, src);
-        if (lane == 0) zm = x[(E - r) % E];
-        const int k = lane + 32 * r;
-        const C zk = x[r];
-        const C zmc = cconj(zm);
-        const C e = cadd(zk, zmc);
-        const C d = cmul(csub(zk, zmc), wn[r]);
-        op[k] = cscale(csub(e, cmuli(d)), T(0.5));
-        if (k == 0) {   // X_M from Z_0
-          const C d0 = cmul(csub(zk, zmc), __ldg(&twN[M]));
-          op[M] = cscale(csub(e, cmuli(d0)), T(0.5));
-        }
+      for (int i = 0; i < E; ++i) as[((3 + q) * E + i) * 32 + lane] = x[i];
+    }
+  }
+
+  // tau_ij = tcoef |S| S_ij on every real point (smag.f90:41-64: even points
+  // in .x, odd in .y), |S| = sqrt(2 (S11^2 + S22^2 + S33^2 + 2 (S12^2 + S13^2
+  // + S23^2))); r2c into of[0..5]
+  __device__ __forceinline__ void tau_store(C* const of[6], T tcoef) const {
+    auto S = [&](int q, int i) { return as[((3 + q) * E + i) * 32 + lane]; };
+    T ar[E], ai[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const C s11 = S(0, i), s12 = S(1, i), s13 = S(2, i), s22 = S(3, i), s23 = S(4, i), s33 = S(5, i);
+      ar[i] = tcoef * sqrt(T(2) * (s11.x * s11.x + s22.x * s22.x + s33.x * s33.x +
+                                   T(2) * (s12.x * s12.x + s13.x * s13.x + s23.x * s23.x)));
+      ai[i] = tcoef * sqrt(T(2) * (s11.y * s11.y + s22.y * s22.y + s33.y * s33.y +
+                                   T(2) * (s12.y * s12.y + s13.y * s13.y + s23.y * s23.y)));
+    }
+#pragma unroll 1
+    for (int q = 0; q < 6; ++q) {
+      C x[E];
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const C s = S(q, i);
+        x[i] = mk<C>(ar[i] * s.x, ai[i] * s.y);
       }
+      WF::template scr_to_nat<false>(x, sm, twM, lane);
+      r2c_store(x, of[q] + off);
     }
   }
 };
 
 // XW_DNS: fin = (u, w) -> fout[0..2] = r2c(u x w / N^3), in place allowed.
+// XW_SMAG: fin = (u, w, S_ij) -> fout[0..2] = r2c(u x w / N^3) and
+//   fout[3..8] = r2c(tau_ij), tau_ij = -2 c1 D^2 |S| S_ij / N^3 (smag.f90:41-64),
+//   in place allowed: u and S are staged and w is read before any output.
 // XW_ADJ: fin = (u, w, phi) -> adjoint of the Lamb product (no scale):
 //   w x phi = -(phi x w) into fout[0..2], then phi x u into fout[3..5];
 //   fout must not alias u (read by the second product) -- the host passes
 //   the w and phi slots.
 template <typename T, int LOGM, int MODE>
-__global__ void __launch_bounds__(XwCfg<T, LOGM>::NT, 2)
+__global__ void __launch_bounds__(XwCfg<T, LOGM, MODE>::NT, 16 / XwCfg<T, LOGM, MODE>::WARPS)
 xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restrict__ twM,
                   const C2<T>* __restrict__ twN, XArgs<T> xa) {
   using C = C2<T>;
+  using Cfg = XwCfg<T, LOGM, MODE>;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long row = (long long)blockIdx.x * XwCfg<T, LOGM>::WARPS + warp;
+  const long long row = (long long)blockIdx.x * Cfg::WARPS + warp;
   if (row >= xa.rows) return;
   XwRow<T, LOGM> R;
-  R.sm = reinterpret_cast<C*>(smraw) + warp * XwCfg<T, LOGM>::PER_WARP;
+  R.sm = reinterpret_cast<C*>(smraw) + warp * Cfg::PER_WARP;
   R.as = R.sm + WarpFFT<T, LOGM>::SMEM;
   R.twM = twM;
   R.twN = twN;
@@ -433,6 +484,17 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
     C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
     R.load_a(a);
     R.cross_store(b, o, xa.scale);
+  } else if constexpr (MODE == XW_SMAG) {
+    const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
+    const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
+    const C* s[6] = {fin.f[6], fin.f[7], fin.f[8], fin.f[9], fin.f[10], fin.f[11]};
+    C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
+    C* ot[6] = {fout.f[3], fout.f[4], fout.f[5], fout.f[6], fout.f[7], fout.f[8]};
+    const T tcoef = (T)(-2.0 * (*xa.c1) * xa.delta2) * xa.scale;
+    R.load_a(a);
+    R.load_s(s);
+    R.cross_store(b, o, xa.scale);
+    R.tau_store(ot, tcoef);
   } else {
     const C* phi[3] = {fin.f[6], fin.f[7], fin.f[8]};
     const C* w[3] = {fin.f[3], fin.f[4], fin.f[5]};
