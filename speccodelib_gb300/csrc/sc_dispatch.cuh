@@ -109,6 +109,21 @@ cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, con
   return cudaGetLastError();
 }
 
+template <typename T, int LOGN, int MODE>
+cudaError_t launch_zfwd_zinv_mode(const CUtensorMap& lmap, const CUtensorMap& fmap, const StageArgs<T>& st,
+                                  const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, int* err,
+                                  cudaStream_t s) {
+  using Z = ZiCfg<T, LOGN>;
+  auto k = zfwd_zinv_tma_kernel<T, LOGN, MODE>;
+  static cudaError_t attr = smem_attr(k, Z::SMEM);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
+  k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, fmap, st, fa, g, tw, err);
+  return cudaGetLastError();
+}
+
+// one instance per RK stage (the update's mode a compile-time constant;
+// SC_FUSED_RUNTIME_MODE: one instance reading it at run time)
 template <typename T, int LOGN>
 cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const CUtensorMap& fmap, const StageArgs<T>& st,
                              const FusedArgs<T>& fa, const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
@@ -116,12 +131,16 @@ cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const CUtensorMap& fmap, c
   if constexpr (!Z::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
-    auto k = zfwd_zinv_tma_kernel<T, LOGN>;
-    static cudaError_t attr = smem_attr(k, Z::SMEM);
-    if (attr != cudaSuccess) return attr;
-    dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
-    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, fmap, st, fa, g, tw, err);
-    return cudaGetLastError();
+#ifdef SC_FUSED_RUNTIME_MODE
+    return launch_zfwd_zinv_mode<T, LOGN, -1>(lmap, fmap, st, fa, g, tw, err, s);
+#else
+    switch (st.mode) {
+      case SM_RK1: return launch_zfwd_zinv_mode<T, LOGN, SM_RK1>(lmap, fmap, st, fa, g, tw, err, s);
+      case SM_RK2: return launch_zfwd_zinv_mode<T, LOGN, SM_RK2>(lmap, fmap, st, fa, g, tw, err, s);
+      case SM_RK3: return launch_zfwd_zinv_mode<T, LOGN, SM_RK3>(lmap, fmap, st, fa, g, tw, err, s);
+      default: return cudaErrorNotSupported;
+    }
+#endif
   }
 }
 

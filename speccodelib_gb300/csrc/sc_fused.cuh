@@ -258,9 +258,10 @@ zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, Fiel
   }
 }
 
-// z-forward pass of RK stages 1-3 fused with the next stage's z-inverse.
+// z-forward pass of RK stages 1-3 fused with the next stage's z-inverse,
+// MODE the stage's update mode (SM_RK1..3; -1: st.mode at run time).
 // grid = (kx tiles, ny).
-template <typename T, int LOGN>
+template <typename T, int LOGN, int MODE>
 __global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
 zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap fmap,
                      StageArgs<T> st, FusedArgs<T> fa, Geom g, const C2<T>* __restrict__ tw, int* err) {
@@ -325,7 +326,7 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_cons
       act[i] = e < P * N && p < nvalid;
       if (!act[i]) continue;
       const long long idx = base + iz * zstride + p;
-      load_state<T>(st, idx, vv[i], av[i]);
+      load_state<T, MODE>(st, idx, vv[i], av[i]);
 #pragma unroll
       for (int c = 0; c < 3; ++c) wv[i][c] = rt[c][e];
     }
@@ -353,7 +354,7 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_cons
       if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
         wp[0] = wp[1] = wp[2] = czero<C>();
       C sn[3];
-      finish_point_pre<T>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i], sn);
+      finish_point_pre<T, MODE>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i], sn);
       if (tile0 || band || fa.store_all) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) st.sout[c][idx] = sn[c];

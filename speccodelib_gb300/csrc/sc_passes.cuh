@@ -384,9 +384,10 @@ __host__ __device__ constexpr bool mode_reads_acc(int m) {
 // state (v, or v0 for the AB2 midpoint pass) and accumulator values already
 // loaded.  w is the right-hand side after forcing and symmetrize.  With
 // `snext` given, RK stages 1-3 return the next stage input there instead of
-// storing it to st.sout.
-template <typename T>
-// kcut_b = k2_lt(st.kcut2), computed once per kernel.
+// storing it to st.sout.  kcut_b = k2_lt(st.kcut2), computed once per
+// kernel.  MODE >= 0: the update mode as a compile-time constant (st.mode
+// otherwise).
+template <typename T, int MODE = -1>
 __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const Geom& g, long long idx,
                                                  int ix, int iy, int iz, int kcut_b, C2<T>* w, const C2<T>* vv,
                                                  const C2<T>* av, C2<T>* snext = nullptr) {
@@ -404,7 +405,8 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
   }
   const bool cut = k2i >= kcut_b && !(ix == 0 && iy == 0 && iz == 0);
   if (st.mask_rhs && cut) w[0] = w[1] = w[2] = czero<C>();
-  if (st.mode == SM_RHS || st.mode == SM_LAMB) {
+  const int mode = MODE >= 0 ? MODE : st.mode;
+  if (mode == SM_RHS || mode == SM_LAMB) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) st.w[c][idx] = w[c];
     return;
@@ -413,7 +415,7 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
   const T E2 = E * E;
   const T dt = st.dt, hdt = T(0.5) * st.dt;
   const bool zero_mean_cut = cut || (ix == 0 && iy == 0 && iz == 0);
-  switch (st.mode) {
+  switch (mode) {
     case SM_RK1:  // acc = E^2 dt w1 ; s2 = E (v + dt w1/2)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -478,12 +480,13 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
   }
 }
 
-template <typename T>
+template <typename T, int MODE = -1>
 __device__ __forceinline__ void load_state(const StageArgs<T>& st, long long idx, C2<T>* vv, C2<T>* av) {
-  const bool rv = mode_reads_v(st.mode), ra = mode_reads_acc(st.mode);
+  const int mode = MODE >= 0 ? MODE : st.mode;
+  const bool rv = mode_reads_v(mode), ra = mode_reads_acc(mode);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    if (rv) vv[c] = st.mode == SM_AB2_MID ? st.v0[c][idx] : st.v[c][idx];
+    if (rv) vv[c] = mode == SM_AB2_MID ? st.v0[c][idx] : st.v[c][idx];
     if (ra) av[c] = st.acc[c][idx];
   }
 }

@@ -141,6 +141,31 @@ def test_diagnostics(specns_lib, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+def test_diagnostics_high_wavenumbers(specns_lib, prec):
+    """Diagnostics on a 1024 x 64 x 64 grid of white noise: shells up to
+    |k| ~ 514, with k^2 = n^2 + n (the last point of shell n) and n^2 + n + 1
+    (the first of shell n + 1) on the grid for large n, so the integer shell
+    index is checked at its boundaries; energy, dissipation, every shell,
+    max |k . v| and max |u| against the oracle."""
+    nx, ny, nz = 1024, 64, 64
+    v = hermitian_fields((nx, ny, nz), 83)
+    kx, ky, kz, k2 = R.wavenumber(nx, ny, nz)
+    with handle(nx, prec, ny=ny, nz=nz) as h:
+        nu = h.p.nu
+        h.set_state(*v)
+        d, eks = h.diagnostics()
+    tol = 1e-12 if prec == S.SC_FP64 else 1e-6
+    assert abs(d["energy"] - R.energy(v)) < tol * R.energy(v)
+    assert abs(d["dissipation"] - R.dissipation(v, k2, nu)) < tol * R.dissipation(v, k2, nu)
+    ref_eks = R.spectrum(v, k2, nx)
+    assert np.max(np.abs(eks - ref_eks)) < tol * np.max(ref_eks)
+    md = R.max_divergence(v, kx, ky, kz)
+    assert abs(d["max_div"] - md) < (1e-12 if prec == S.SC_FP64 else 1e-5) * md
+    mu = R.max_velocity(v, nx)
+    assert abs(d["max_u"] - mu) < (1e-12 if prec == S.SC_FP64 else 1e-5) * mu
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_ab2_matches_oracle(specns_lib, prec):
     n = 32
     v = solenoidal_init(n)
