@@ -64,10 +64,13 @@ template <typename T, int LOGN> struct ZiCfg {
 // (natural order, element (p, n) at n*P + p): transform w_x, w_y (half tiles
 // through `work`), then s in place, and store u and w.  Starts with the tiles
 // complete (caller's barrier); ends with a barrier.
+// umap: a map of out.f[0..2] tiled as rt (u leaves the tiles by bulk tensor
+// stores), or nullptr (element stores).
 template <typename T, int LOGN>
 __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work, int kx0, int iy, int nvalid,
                                                 long long base, long long zstride, const FieldList<T>& out,
-                                                const Geom& g, const C2<T>* __restrict__ tw) {
+                                                const Geom& g, const C2<T>* __restrict__ tw,
+                                                const CUtensorMap* umap) {
   using Z = ZiCfg<T, LOGN>;
   using EH = typename Z::EngH;
   using EF = typename Z::EngF;
@@ -104,6 +107,31 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
     }
   }
   for (int c = 0; c < 3; ++c) EF::template run_inplace<true>(rt[c], tw);
+#ifdef SC_NO_USTORE
+  umap = nullptr;
+#endif
+  if (umap) {
+    using Cfg = TmaCfg<T, LOGN>;
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int c = 0; c < 3; ++c)
+        for (int h = 0; h < Cfg::NBOX; ++h)
+          tma_store_4d(umap, rt[c] + (size_t)h * Cfg::BOX * P, kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+      tma_store_commit();
+    }
+    // w_z = i kx u_y - i ky u_x from the tiles (read only while they drain)
+    for (int e = threadIdx.x; e < P * N; e += NT) {
+      const int p = e % P, n = e / P;
+      if (p >= nvalid) continue;
+      const C ux = rt[0][e], uy = rt[1][e];
+      const T kx = (T)(kx0 + p);
+      out.f[5][base + n * zstride + p] = cmuli(csub(cscale(uy, kx), cscale(ux, ky)));
+    }
+    if (threadIdx.x == 0) tma_store_wait_read();
+    __syncthreads();
+    return;
+  }
   // u and w_z = i kx u_y - i ky u_x, 64-byte row segments
   for (int e = threadIdx.x; e < P * N; e += NT) {
     const int p = e % P, n = e / P;
@@ -123,8 +151,8 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
 // then zinv_from_tiles.  grid = (kx tiles or za.tiles_x, ny).
 template <typename T, int LOGN>
 __global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
-zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldList<T> out, Geom g,
-                 const C2<T>* __restrict__ tw, int* err) {
+zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, const __grid_constant__ CUtensorMap umap, ZvArgs<T> za,
+                 FieldList<T> out, Geom g, const C2<T>* __restrict__ tw, int* err) {
   using Z = ZiCfg<T, LOGN>;
   using Cfg = TmaCfg<T, LOGN>;
   using C = C2<T>;
@@ -173,7 +201,7 @@ zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldLi
     const double sum = block_sum<NT>(q, red);
     if (threadIdx.x == 0) za.fs.partial[(long long)blockIdx.x * g.ny + iy] = sum;
   }
-  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, out, g, tw);
+  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, out, g, tw, za.ustore ? &umap : nullptr);
 }
 
 // Third operand of the adjoint right-hand side along z:
@@ -376,7 +404,8 @@ zfwd_zinv_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_cons
     const double sum = block_sum<NT>(q, red);
     if (threadIdx.x == 0) fa.kf_next[(long long)blockIdx.x * g.ny + iy] = sum;
   }
-  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, fa.out, g, tw);
+  // fa.out[0..2] are the Lamb fields: lmap tiles them as rt
+  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, fa.out, g, tw, &lmap);
 }
 
 }  // namespace sc

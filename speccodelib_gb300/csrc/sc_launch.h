@@ -65,7 +65,9 @@ template <typename T> struct Launch {
   // tiles fit shared memory for this length (else cudaErrorNotSupported).
   static bool zinv5_supported(int logn);
   static int zinv5_tile(int logn);     // tile width of zinv5 / zinv_phi / zfwd_zinv
-  static cudaError_t zinv5_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,
+  // umap: a map of out.f[0..2] tiled zinv5_tile wide, used when
+  // za.ustore (u leaves by bulk tensor stores)
+  static cudaError_t zinv5_tma(int logn, const CUtensorMap& vmap, const CUtensorMap& umap, const ZvArgs<T>& za,
                                const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                                cudaStream_t s);
   // phi^ of the adjoint right-hand side from TMA-loaded lam tiles (za.lam is

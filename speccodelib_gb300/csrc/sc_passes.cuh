@@ -148,6 +148,7 @@ template <typename T> struct ZvArgs {
   double kcut2;
   double inv_n3;
   int tiles_x;       // > 0: only the first tiles_x kx tiles (grid.x)
+  int ustore;        // TMA z-inverse: u stored from its tiles by bulk tensor stores
 };
 
 // zero (symmetrize's planes and mean), optional RHS mask, then projection:

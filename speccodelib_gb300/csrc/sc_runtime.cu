@@ -546,7 +546,9 @@ template <typename T> struct Impl {
       if (fuse & FUSE_IN) {
         // produced by the previous stage
       } else if (z5) {
-        SC_TRY(launch(h, "zinv", [&] { return L::zinv5_tma(h->logz, vmap, za, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
+        sc::ZvArgs<T> zu = za;
+        zu.ustore = 1;   // lmap5 tiles the output fields wl[0..2] as zinv5 does
+        SC_TRY(launch(h, "zinv", [&] { return L::zinv5_tma(h->logz, vmap, lmap5, zu, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
       } else if (h->tma_zinv) {
         SC_TRY(launch(h, "zinv", [&] { return L::zinv_tma(h->logz, vmap, za, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
       } else {
@@ -571,7 +573,8 @@ template <typename T> struct Impl {
         for (int c = 0; c < 3; ++c) z0.v[c] = st.sout[c];
         z0.fs.partial = kf_next;
         z0.tiles_x = 1;
-        return launch(h, "zinv_kx0", [&] { return L::zinv5_tma(h->logz, smap, z0, wl, *g, tw(h, g->nz), h->derr, h->stream); });
+        z0.ustore = 1;
+        return launch(h, "zinv_kx0", [&] { return L::zinv5_tma(h->logz, smap, lmap5, z0, wl, *g, tw(h, g->nz), h->derr, h->stream); });
       }
       SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, st, *g, tw(h, g->nz), h->derr, h->stream); }));
     } else {
@@ -694,7 +697,7 @@ template <typename T> struct Impl {
       CUtensorMap smap, lmap;
       SC_TRY(encode_fields(h, aa.s[0], 3, 2, P, g->nz, &smap));
       SC_TRY(encode_fields(h, aa.lw[0], 3, 2, P, g->nz, &lmap));
-      SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv5_tma(h->logz, smap, za, w9, *g, tw(h, g->nz), h->derr, h->stream); }));
+      SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv5_tma(h->logz, smap, smap, za, w9, *g, tw(h, g->nz), h->derr, h->stream); }));
       sc::FieldList<T> phi{};
       for (int c = 0; c < 3; ++c) phi.f[c] = w9.f[6 + c];
       SC_TRY(launch(h, "adj_zphi", [&] { return L::zinv_phi_tma(h->logz, lmap, za, phi, *g, tw(h, g->nz), h->derr, h->stream); }));
