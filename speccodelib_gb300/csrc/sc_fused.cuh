@@ -64,8 +64,8 @@ template <typename T, int LOGN> struct ZiCfg {
 // (natural order, element (p, n) at n*P + p): transform w_x, w_y (half tiles
 // through `work`), then s in place, and store u and w.  Starts with the tiles
 // complete (caller's barrier); ends with a barrier.
-// umap: a map of out.f[0..2] tiled as rt (u leaves the tiles by bulk tensor
-// stores), or nullptr (element stores).
+// umap: a map of out.f[0..5] tiled as rt (u and w_z leave the tiles by bulk
+// tensor stores), or nullptr (element stores).
 template <typename T, int LOGN>
 __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work, int kx0, int iy, int nvalid,
                                                 long long base, long long zstride, const FieldList<T>& out,
@@ -112,23 +112,36 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
 #endif
   if (umap) {
     using Cfg = TmaCfg<T, LOGN>;
+    auto store = [&](int c, int f) {
+      for (int h = 0; h < Cfg::NBOX; ++h)
+        tma_store_4d(umap, rt[c] + (size_t)h * Cfg::BOX * P, kx0 * Cfg::U, iy, h * Cfg::BOX, f);
+    };
+    fence_proxy_async();
+    __syncthreads();
+    // u_z first, in a group of its own: its tile takes w_z once read out
+    if (threadIdx.x == 0) {
+      store(2, 2);
+      tma_store_commit();
+      store(0, 0);
+      store(1, 1);
+      tma_store_commit();
+      tma_store_wait_read<1>();
+    }
+    __syncthreads();
+    // w_z = i kx u_y - i ky u_x into the u_z tile (u_x, u_y read while they drain)
+    for (int e = threadIdx.x; e < P * N; e += NT) {
+      const int p = e % P;
+      const C ux = rt[0][e], uy = rt[1][e];
+      const T kx = (T)(kx0 + p);
+      rt[2][e] = cmuli(csub(cscale(uy, kx), cscale(ux, ky)));
+    }
     fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int c = 0; c < 3; ++c)
-        for (int h = 0; h < Cfg::NBOX; ++h)
-          tma_store_4d(umap, rt[c] + (size_t)h * Cfg::BOX * P, kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+      store(2, 5);
       tma_store_commit();
+      tma_store_wait_read<0>();
     }
-    // w_z = i kx u_y - i ky u_x from the tiles (read only while they drain)
-    for (int e = threadIdx.x; e < P * N; e += NT) {
-      const int p = e % P, n = e / P;
-      if (p >= nvalid) continue;
-      const C ux = rt[0][e], uy = rt[1][e];
-      const T kx = (T)(kx0 + p);
-      out.f[5][base + n * zstride + p] = cmuli(csub(cscale(uy, kx), cscale(ux, ky)));
-    }
-    if (threadIdx.x == 0) tma_store_wait_read();
     __syncthreads();
     return;
   }

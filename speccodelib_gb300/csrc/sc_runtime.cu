@@ -541,13 +541,15 @@ template <typename T> struct Impl {
       const int PZ = L::tma_ztile(h->logz), P = L::tma_tile(h->logz), P5 = L::zinv5_tile(h->logz);
       SC_TRY(encode_fields(h, sin[0], 3, 2, z5 ? P5 : PZ, g->nz, &vmap));
       SC_TRY(encode_fields(h, wl.f[0], 3, 2, P, g->nz, &lmap));
-      CUtensorMap lmap5 = lmap;   // the Lamb vector as the fused kernel tiles it
-      if (z5 && P5 != P) SC_TRY(encode_fields(h, wl.f[0], 3, 2, P5, g->nz, &lmap5));
+      // the Lamb vector (fields 0-2) and the z-inverse outputs u, w (0-5) as
+      // the fused and five-transform kernels tile them
+      CUtensorMap lmap5;
+      SC_TRY(encode_fields(h, wl.f[0], 6, 2, P5, g->nz, &lmap5));
       if (fuse & FUSE_IN) {
         // produced by the previous stage
       } else if (z5) {
         sc::ZvArgs<T> zu = za;
-        zu.ustore = 1;   // lmap5 tiles the output fields wl[0..2] as zinv5 does
+        zu.ustore = 1;   // lmap5 tiles the output fields wl[0..5] as zinv5 does
         SC_TRY(launch(h, "zinv", [&] { return L::zinv5_tma(h->logz, vmap, lmap5, zu, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
       } else if (h->tma_zinv) {
         SC_TRY(launch(h, "zinv", [&] { return L::zinv_tma(h->logz, vmap, za, wl, *g, tw(h, g->nz), h->derr, h->stream); }));
@@ -694,10 +696,13 @@ template <typename T> struct Impl {
     if (split5) {
       // u, w of the stage input (five transforms) and phi from lam, both TMA-fed
       const int P = L::zinv5_tile(h->logz);
-      CUtensorMap smap, lmap;
+      CUtensorMap smap, lmap, wmap;
       SC_TRY(encode_fields(h, aa.s[0], 3, 2, P, g->nz, &smap));
       SC_TRY(encode_fields(h, aa.lw[0], 3, 2, P, g->nz, &lmap));
-      SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv5_tma(h->logz, smap, smap, za, w9, *g, tw(h, g->nz), h->derr, h->stream); }));
+      SC_TRY(encode_fields(h, w9.f[0], 6, 2, P, g->nz, &wmap));   // u, w leave by bulk stores
+      sc::ZvArgs<T> zu = za;
+      zu.ustore = 1;
+      SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv5_tma(h->logz, smap, wmap, zu, w9, *g, tw(h, g->nz), h->derr, h->stream); }));
       sc::FieldList<T> phi{};
       for (int c = 0; c < 3; ++c) phi.f[c] = w9.f[6 + c];
       SC_TRY(launch(h, "adj_zphi", [&] { return L::zinv_phi_tma(h->logz, lmap, za, phi, *g, tw(h, g->nz), h->derr, h->stream); }));
