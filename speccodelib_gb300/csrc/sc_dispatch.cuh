@@ -96,6 +96,19 @@ cudaError_t launch_zinv_tma(const CUtensorMap& vmap, const ZvArgs<T>& za, const 
   return cudaGetLastError();
 }
 
+template <typename T, int LOGN, int NIN>
+cudaError_t launch_zfwd_fields_tma(const CUtensorMap& fmap, const StageArgs<T>& st, const Geom& g, const C2<T>* tw,
+                                   int* err, cudaStream_t s) {
+  using Cfg = TmaCfg<T, LOGN>;
+  auto k = zfwd_fields_tma_kernel<T, LOGN, NIN>;
+  constexpr size_t sm = 3 * Cfg::TILE_BYTES + kSmemAlignPad;
+  static cudaError_t attr = smem_attr(k, sm);
+  if (attr != cudaSuccess) return attr;
+  dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
+  k<<<grid, Cfg::NT, sm, s>>>(fmap, st, g, tw, err);
+  return cudaGetLastError();
+}
+
 template <typename T, int LOGN>
 cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
                             const C2<T>* tw, int* err, cudaStream_t s) {
@@ -301,6 +314,16 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     }                                                                                            \
   }                                                                                              \
   template <>                                                                                    \
+  cudaError_t sc::Launch<T>::zfwd_fields_tma(int logn, int nin, const CUtensorMap& fmap,         \
+                                             const StageArgs<T>& st, const Geom& g,              \
+                                             const C2<T>* tw, int* err, cudaStream_t s) {        \
+    if (nin != 9) return cudaErrorNotSupported;                                                  \
+    switch (logn) {                                                                              \
+      SC_LOGN_CASES(SC_ZFWDFIELDS_CASE_##T)                                                      \
+      default: return cudaErrorNotSupported;                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  template <>                                                                                    \
   cudaError_t sc::Launch<T>::zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, \
                                       const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) { \
     switch (logn) {                                                                              \
@@ -317,6 +340,8 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
                      : sc::launch_plain_tma<double, L, false>(map, tp, g, tw, nsm, s);
 #define SC_ZINVTMA_CASE_float(L) case L: return sc::launch_zinv_tma<float, L>(vmap, za, out, g, tw, err, s);
 #define SC_ZINVTMA_CASE_double(L) case L: return sc::launch_zinv_tma<double, L>(vmap, za, out, g, tw, err, s);
+#define SC_ZFWDFIELDS_CASE_float(L) case L: return sc::launch_zfwd_fields_tma<float, L, 9>(fmap, st, g, tw, err, s);
+#define SC_ZFWDFIELDS_CASE_double(L) case L: return sc::launch_zfwd_fields_tma<double, L, 9>(fmap, st, g, tw, err, s);
 #define SC_ZFWDTMA_CASE_float(L) case L: return sc::launch_zfwd_tma<float, L>(lmap, st, g, tw, err, s);
 #define SC_ZFWDTMA_CASE_double(L) case L: return sc::launch_zfwd_tma<double, L>(lmap, st, g, tw, err, s);
 

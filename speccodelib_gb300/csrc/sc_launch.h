@@ -59,6 +59,10 @@ template <typename T> struct Launch {
                               cudaStream_t s);
   static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
                               const C2<T>* tw, int* err, cudaStream_t s);
+  // z-forward of nin fields (9: the LES Lamb vector and tau_ij) through a
+  // TMA ring, fmap tiled tma_tile wide; cudaErrorNotSupported otherwise
+  static cudaError_t zfwd_fields_tma(int logn, int nin, const CUtensorMap& fmap, const StageArgs<T>& st,
+                                     const Geom& g, const C2<T>* tw, int* err, cudaStream_t s);
   // z-inverse of the DNS operands with five transforms from TMA-loaded stage
   // input tiles, and the z-forward pass of RK stages 1-3 fused with it
   // (sc_fused.cuh), tile width zinv5_tile.  zinv5_supported: whether the

@@ -517,70 +517,55 @@ __device__ __forceinline__ double forcing_energy(const double* partial, int tile
 // zfwd: z-axis forward pass + spectral update.  NIN = 3 (Lamb vector) or 9
 // (Lamb vector + tau_ij, order 11 12 13 22 23 33).
 // ---------------------------------------------------------------------------
-template <typename T, int LOGN, int NIN>
-__global__ void __launch_bounds__(PencilCfg<T, LOGN>::NT, PencilCfg<T, LOGN>::MINB_FUSED)
-zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __restrict__ tw) {
-  using Cfg = PencilCfg<T, LOGN>;
-  using E = typename Cfg::Engine;
-  using C = C2<T>;
-  constexpr int P = Cfg::P;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* sm = reinterpret_cast<C*>(smraw);
-  __shared__ double s_coef;
-  const int kx0 = blockIdx.x * P;
-  const int iy = blockIdx.y;
-  const int nvalid = min(P, g.nxh - kx0);
-  const long long zstride = (long long)g.ny * g.nxp;
-  const long long base = (long long)iy * g.nxp + kx0;
-  const T ky = (T)wavenum(iy, g.ny);
-
-  C w[E::JL][E::RL][3];
-  for (int f = 0; f < NIN; ++f) {
-    const C* __restrict__ fp = fin.f[f] + base;
-    C in[E::J1][E::R1], o[E::JL][E::RL];
+// w (the engine's output layout) += the z-transformed field f of the
+// right-hand side: the Lamb vector (f < 3) or tau_ij (f >= 3, order 11 12 13
+// 22 23 33: w_i -= i k_j tau_ij, spectral_les.f90:232-234).
+template <typename E, typename T>
+__device__ __forceinline__ void zfwd_accumulate(C2<T> (&w)[E::JL][E::RL][3], const C2<T> (&o)[E::JL][E::RL], int f,
+                                                int kx0, T ky, const Geom& g) {
 #pragma unroll
-    for (int a = 0; a < E::J1; ++a)
+  for (int a = 0; a < E::JL; ++a)
 #pragma unroll
-      for (int r = 0; r < E::R1; ++r) {
+    for (int r = 0; r < E::RL; ++r) {
+      if (f < 3) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (c == f) w[a][r][c] = o[a][r];
+      } else {
         int p, n;
-        bool ok = E::in_pos(a, r, p, n) && p < nvalid;
-        in[a][r] = ok ? fp[n * zstride + p] : czero<C>();
-      }
-    E::template run<false>(in, o, sm, tw);
-#pragma unroll
-    for (int a = 0; a < E::JL; ++a)
-#pragma unroll
-      for (int r = 0; r < E::RL; ++r) {
-        if (f < 3) {
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            if (c == f) w[a][r][c] = o[a][r];
-        } else {
-          // w_i -= i k_j tau_ij (spectral_les.f90:232-234)
-          int p, n;
-          E::out_pos(a, r, p, n);
-          const T kx = (T)(kx0 + p), kz = (T)wavenum(n, g.nz);
-          const C t = o[a][r];
-          switch (f - 3) {
-            case 0: w[a][r][0] = csub(w[a][r][0], cmuli(cscale(t, kx))); break;
-            case 1:
-              w[a][r][0] = csub(w[a][r][0], cmuli(cscale(t, ky)));
-              w[a][r][1] = csub(w[a][r][1], cmuli(cscale(t, kx)));
-              break;
-            case 2:
-              w[a][r][0] = csub(w[a][r][0], cmuli(cscale(t, kz)));
-              w[a][r][2] = csub(w[a][r][2], cmuli(cscale(t, kx)));
-              break;
-            case 3: w[a][r][1] = csub(w[a][r][1], cmuli(cscale(t, ky))); break;
-            case 4:
-              w[a][r][1] = csub(w[a][r][1], cmuli(cscale(t, kz)));
-              w[a][r][2] = csub(w[a][r][2], cmuli(cscale(t, ky)));
-              break;
-            default: w[a][r][2] = csub(w[a][r][2], cmuli(cscale(t, kz))); break;
-          }
+        E::out_pos(a, r, p, n);
+        const T kx = (T)(kx0 + p), kz = (T)wavenum(n, g.nz);
+        const C2<T> t = o[a][r];
+        switch (f - 3) {
+          case 0: w[a][r][0] = csub(w[a][r][0], cmuli(cscale(t, kx))); break;
+          case 1:
+            w[a][r][0] = csub(w[a][r][0], cmuli(cscale(t, ky)));
+            w[a][r][1] = csub(w[a][r][1], cmuli(cscale(t, kx)));
+            break;
+          case 2:
+            w[a][r][0] = csub(w[a][r][0], cmuli(cscale(t, kz)));
+            w[a][r][2] = csub(w[a][r][2], cmuli(cscale(t, kx)));
+            break;
+          case 3: w[a][r][1] = csub(w[a][r][1], cmuli(cscale(t, ky))); break;
+          case 4:
+            w[a][r][1] = csub(w[a][r][1], cmuli(cscale(t, kz)));
+            w[a][r][2] = csub(w[a][r][2], cmuli(cscale(t, ky)));
+            break;
+          default: w[a][r][2] = csub(w[a][r][2], cmuli(cscale(t, kz))); break;
         }
       }
-  }
+    }
+}
+
+// The z-forward pass's update of tile (kx0, iy) from w in the engine's
+// output layout: the RHS itself (SM_LAMB), else forcing, symmetrize and the
+// mode's update.  s_coef: a shared double of the block.
+template <typename E, typename T>
+__device__ __forceinline__ void zfwd_finish(C2<T> (&w)[E::JL][E::RL][3], const StageArgs<T>& st, const Geom& g,
+                                            int kx0, int iy, int nvalid, long long base, long long zstride,
+                                            double& s_coef) {
+  using C = C2<T>;
+  const T ky = (T)wavenum(iy, g.ny);
   if (st.mode == SM_LAMB) {
 #pragma unroll
     for (int a = 0; a < E::JL; ++a)
@@ -635,6 +620,41 @@ zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __rest
       }
       finish_point<T>(st, g, idx, ix, iy, iz, kc_b, wp);
     }
+}
+
+template <typename T, int LOGN, int NIN>
+__global__ void __launch_bounds__(PencilCfg<T, LOGN>::NT, PencilCfg<T, LOGN>::MINB_FUSED)
+zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __restrict__ tw) {
+  using Cfg = PencilCfg<T, LOGN>;
+  using E = typename Cfg::Engine;
+  using C = C2<T>;
+  constexpr int P = Cfg::P;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  __shared__ double s_coef;
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+
+  C w[E::JL][E::RL][3];
+  for (int f = 0; f < NIN; ++f) {
+    const C* __restrict__ fp = fin.f[f] + base;
+    C in[E::J1][E::R1], o[E::JL][E::RL];
+#pragma unroll
+    for (int a = 0; a < E::J1; ++a)
+#pragma unroll
+      for (int r = 0; r < E::R1; ++r) {
+        int p, n;
+        bool ok = E::in_pos(a, r, p, n) && p < nvalid;
+        in[a][r] = ok ? fp[n * zstride + p] : czero<C>();
+      }
+    E::template run<false>(in, o, sm, tw);
+    zfwd_accumulate<E, T>(w, o, f, kx0, ky, g);
+  }
+  zfwd_finish<E, T>(w, st, g, kx0, iy, nvalid, base, zstride, s_coef);
 }
 
 // Hermitian copy on the kx = 0 plane (symmetrize.f90:52-62):

@@ -593,7 +593,16 @@ template <typename T> struct Impl {
       else SC_TRY(xpass_dns(h, wl));
       if (h->tma) SC_TRY(plain_tma(h, "ypass_fwd", 1, false, wl.f[0], nf));
       else SC_TRY(launch(h, "ypass_fwd", [&] { return L::plain(h->logy, false, wl, ypass_args(h, nf), *g, g->nz, tw(h, g->ny), h->stream); }));
-      SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_stage(h->logz, nf, wl, st, *g, tw(h, g->nz), h->stream); }));
+      CUtensorMap fmap;
+      const bool fields_tma = h->tma && spaced(wl, nf, g->field);
+      if (fields_tma) SC_TRY(encode_fields(h, wl.f[0], nf, 2, L::tma_tile(h->logz), g->nz, &fmap));
+      SC_TRY(launch(h, "zfwd", [&] {
+        if (fields_tma) {
+          cudaError_t e = L::zfwd_fields_tma(h->logz, nf, fmap, st, *g, tw(h, g->nz), h->derr, h->stream);
+          if (e != cudaErrorNotSupported) return e;
+        }
+        return L::zfwd_stage(h->logz, nf, wl, st, *g, tw(h, g->nz), h->stream);
+      }));
     }
     if (st.symmetrize && st.mode != sc::SM_LAMB)
       SC_TRY(launch(h, "fixup", [&] { return L::fixup(st, *g, h->stream); }));

@@ -227,6 +227,55 @@ zinv_tma_kernel(const __grid_constant__ CUtensorMap vmap, ZvArgs<T> za, FieldLis
   }
 }
 
+// z-forward pass of NIN fields (LES: the Lamb vector and tau_ij, NIN = 9)
+// + the spectral update: the fields' tiles stream through a three-deep TMA
+// ring, each transformed from shared memory into registers and accumulated
+// into w (zfwd_accumulate); a buffer is refilled once its transform has read
+// it.  fmap: the NIN fields, tiles P wide along z.
+template <typename T, int LOGN, int NIN>
+__global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 1)
+zfwd_fields_tma_kernel(const __grid_constant__ CUtensorMap fmap, StageArgs<T> st, Geom g,
+                       const C2<T>* __restrict__ tw, int* err) {
+  using Cfg = TmaCfg<T, LOGN>;
+  using E = typename Cfg::Engine;
+  using C = C2<T>;
+  constexpr int P = Cfg::P;
+  constexpr int NB = 3;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = align128(smdyn);
+  __shared__ __align__(8) uint64_t bars[NB];
+  __shared__ double s_coef;
+  auto buf = [&](int b) { return reinterpret_cast<C*>(smraw + (size_t)b * Cfg::TILE_BYTES); };
+  const int kx0 = blockIdx.x * P;
+  const int iy = blockIdx.y;
+  const int nvalid = min(P, g.nxh - kx0);
+  const long long zstride = (long long)g.ny * g.nxp;
+  const long long base = (long long)iy * g.nxp + kx0;
+  const T ky = (T)wavenum(iy, g.ny);
+  if (launch_failed(err)) return;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NB; ++b) mbar_init(&bars[b], 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    for (int f = 0; f < NB && f < NIN; ++f)
+      tma_issue_tile<Cfg>(buf(f), &fmap, &bars[f], 2, kx0, iy, f, P, Cfg::TILE_BYTES);
+  }
+  __syncthreads();
+  C w[E::JL][E::RL][3];
+  for (int f = 0; f < NIN; ++f) {
+    const int b = f % NB;
+    if (!mbar_wait_bounded(&bars[b], (f / NB) & 1, err)) return;
+    C o[E::JL][E::RL];
+    E::template run_smem<false>(o, buf(b), tw);   // every read of buf(b) precedes its last barrier
+    if (threadIdx.x == 0 && f + NB < NIN) {
+      fence_proxy_async();
+      tma_issue_tile<Cfg>(buf(b), &fmap, &bars[b], 2, kx0, iy, f + NB, P, Cfg::TILE_BYTES);
+    }
+    zfwd_accumulate<E, T>(w, o, f, kx0, ky, g);
+  }
+  zfwd_finish<E, T>(w, st, g, kx0, iy, nvalid, base, zstride, s_coef);
+}
+
 // z-forward pass of the Lamb vector + the spectral update (DNS).
 template <typename T, int LOGN>
 __global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
