@@ -173,14 +173,14 @@ cudaError_t launch_zinv_phi(const CUtensorMap& lmap, const ZvArgs<T>& za, const 
   }
 }
 
-template <typename T, int LOGN>
+template <typename T, int LOGN, int MODE>
 cudaError_t launch_zinv5(const CUtensorMap& vmap, const CUtensorMap& umap, const ZvArgs<T>& za,
                          const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
   using Z = ZiCfg<T, LOGN>;
   if constexpr (!Z::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
-    auto k = zinv5_tma_kernel<T, LOGN>;
+    auto k = zinv5_tma_kernel<T, LOGN, MODE>;
     static cudaError_t attr = smem_attr(k, Z::SMEM);
     if (attr != cudaSuccess) return attr;
     dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
@@ -499,8 +499,14 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
   case L: return sc::launch_zfwd_zinv<float, L>(lmap, fmap, st, fa, g, tw, err, s);
 #define SC_FUSED_CASE_double(L) \
   case L: return sc::launch_zfwd_zinv<double, L>(lmap, fmap, st, fa, g, tw, err, s);
-#define SC_ZINV5_CASE_float(L) case L: return sc::launch_zinv5<float, L>(vmap, umap, za, out, g, tw, err, s);
-#define SC_ZINV5_CASE_double(L) case L: return sc::launch_zinv5<double, L>(vmap, umap, za, out, g, tw, err, s);
+#define SC_ZINV5_CASE_float(L)                                                                     \
+  case L:                                                                                          \
+    return mode == sc::ZV_SMAG ? sc::launch_zinv5<float, L, sc::ZV_SMAG>(vmap, umap, za, out, g, tw, err, s) \
+                               : sc::launch_zinv5<float, L, sc::ZV_DNS>(vmap, umap, za, out, g, tw, err, s);
+#define SC_ZINV5_CASE_double(L)                                                                    \
+  case L:                                                                                          \
+    return mode == sc::ZV_SMAG ? sc::launch_zinv5<double, L, sc::ZV_SMAG>(vmap, umap, za, out, g, tw, err, s) \
+                               : sc::launch_zinv5<double, L, sc::ZV_DNS>(vmap, umap, za, out, g, tw, err, s);
 #define SC_ZPHI_CASE_float(L) case L: return sc::launch_zinv_phi<float, L>(lmap, za, out, g, tw, err, s);
 #define SC_ZPHI_CASE_double(L) case L: return sc::launch_zinv_phi<double, L>(lmap, za, out, g, tw, err, s);
 #define SC_ZI_P_CASE_float(L) case L: return sc::ZiCfg<float, L>::P;
@@ -536,7 +542,7 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
   template <>                                                                                    \
   cudaError_t sc::Launch<T>::zinv5_tma(int logn, const CUtensorMap& vmap, const CUtensorMap& umap, \
                                        const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g, \
-                                       const C2<T>* tw, int* err, cudaStream_t s) {              \
+                                       const C2<T>* tw, int* err, cudaStream_t s, int mode) {    \
     switch (logn) {                                                                              \
       SC_LOGN_CASES(SC_ZINV5_CASE_##T)                                                           \
       default: return cudaErrorInvalidValue;                                                     \

@@ -60,13 +60,39 @@ template <typename T, int LOGN> struct ZiCfg {
   static constexpr int MINB = MINB_RAW > 4 ? 4 : (MINB_RAW < 1 ? 1 : MINB_RAW);
 };
 
+// The outputs of the z-inverse that carry kz, transformed half a tile at a
+// time: ZV_DNS w_x, w_y; ZV_SMAG also S13, S23, S33.  The others follow
+// pointwise from u (kx and ky are constant along a z pencil): w_z, and for
+// ZV_SMAG S11, S12, S22.
+template <int MODE> struct ZiFields;
+template <> struct ZiFields<ZV_DNS> {
+  static constexpr int NKZ = 2, NPW = 1;
+  __device__ static constexpr int kz_field(int q) { return 3 + q; }
+  __device__ static constexpr int pw_field(int) { return 5; }
+};
+template <> struct ZiFields<ZV_SMAG> {
+  static constexpr int NKZ = 5, NPW = 4;
+  __device__ static constexpr int kz_field(int q) { return q < 2 ? 3 + q : (q == 2 ? 8 : (q == 3 ? 10 : 11)); }
+  __device__ static constexpr int pw_field(int q) { return q == 0 ? 5 : (q == 1 ? 6 : (q == 2 ? 7 : 9)); }
+};
+// pointwise output f (5: w_z, 6: S11, 7: S12, 9: S22) from u at (kx, ky)
+template <typename C, typename R> __device__ __forceinline__ C zi_pointwise(int f, C ux, C uy, R kx, R ky) {
+  switch (f) {
+    case 5: return cmuli(csub(cscale(uy, kx), cscale(ux, ky)));
+    case 6: return cmuli(cscale(ux, kx));
+    case 7: return cmuli(cscale(cadd(cscale(uy, kx), cscale(ux, ky)), R(0.5)));
+    default: return cmuli(cscale(uy, ky));
+  }
+}
+
 // Steps after the stage input s of tile (kx0, iy) is in the three tiles rt
-// (natural order, element (p, n) at n*P + p): transform w_x, w_y (half tiles
-// through `work`), then s in place, and store u and w.  Starts with the tiles
-// complete (caller's barrier); ends with a barrier.
-// umap: a map of out.f[0..5] tiled as rt (u and w_z leave the tiles by bulk
-// tensor stores), or nullptr (element stores).
-template <typename T, int LOGN>
+// (natural order, element (p, n) at n*P + p): transform the outputs that
+// carry kz (half tiles through `work`), then s in place, and store u and the
+// pointwise outputs.  Starts with the tiles complete (caller's barrier);
+// ends with a barrier.
+// umap: a map of out.f[0..5] tiled as rt (u, and for ZV_DNS w_z, leave the
+// tiles by bulk tensor stores), or nullptr (element stores).
+template <typename T, int LOGN, int MODE = ZV_DNS>
 __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work, int kx0, int iy, int nvalid,
                                                 long long base, long long zstride, const FieldList<T>& out,
                                                 const Geom& g, const C2<T>* __restrict__ tw,
@@ -79,9 +105,11 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
   constexpr int N = Z::N;
   constexpr int NT = Z::NT;
   constexpr int PH = P / 2;
+  using ZF = ZiFields<MODE>;
   const T ky = (T)wavenum(iy, g.ny);
 #pragma unroll 1
-  for (int f = 3; f < 5; ++f) {
+  for (int q = 0; q < ZF::NKZ; ++q) {
+    const int f = ZF::kz_field(q);
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
       C x[EH::J1][EH::R1], o[EH::JL][EH::RL];
@@ -93,7 +121,7 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
           const bool ok = EH::in_pos(a, r, p, n);
           const int e = ok ? n * P + h * PH + p : 0;   // padding jobs (tiny N) read nothing
           const T kx = (T)(kx0 + h * PH + p), kz = (T)wavenum(n, g.nz);
-          x[a][r] = ok ? zv_gen<ZV_DNS>(f, rt[0][e], rt[1][e], rt[2][e], kx, ky, kz, true) : czero<C>();
+          x[a][r] = ok ? zv_gen<MODE>(f, rt[0][e], rt[1][e], rt[2][e], kx, ky, kz, true) : czero<C>();
         }
       EH::template run<true>(x, o, work, tw);
       C* __restrict__ fp = out.f[f] + base + h * PH;
@@ -110,6 +138,30 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
 #ifdef SC_NO_USTORE
   umap = nullptr;
 #endif
+  if (umap && MODE != ZV_DNS) {
+    // u by bulk stores; the pointwise outputs from the tiles while they drain
+    using Cfg = TmaCfg<T, LOGN>;
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int c = 0; c < 3; ++c)
+        for (int h = 0; h < Cfg::NBOX; ++h)
+          tma_store_4d(umap, rt[c] + (size_t)h * Cfg::BOX * P, kx0 * Cfg::U, iy, h * Cfg::BOX, c);
+      tma_store_commit();
+    }
+    for (int e = threadIdx.x; e < P * N; e += NT) {
+      const int p = e % P, n = e / P;
+      if (p >= nvalid) continue;
+      const C ux = rt[0][e], uy = rt[1][e];
+      const T kx = (T)(kx0 + p);
+      const long long idx = base + n * zstride + p;
+#pragma unroll
+      for (int q = 0; q < ZF::NPW; ++q) out.f[ZF::pw_field(q)][idx] = zi_pointwise(ZF::pw_field(q), ux, uy, kx, ky);
+    }
+    if (threadIdx.x == 0) tma_store_wait_read<0>();
+    __syncthreads();
+    return;
+  }
   if (umap) {
     using Cfg = TmaCfg<T, LOGN>;
     auto store = [&](int c, int f) {
@@ -145,7 +197,7 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
     __syncthreads();
     return;
   }
-  // u and w_z = i kx u_y - i ky u_x, 64-byte row segments
+  // u and the pointwise outputs, 64-byte row segments
   for (int e = threadIdx.x; e < P * N; e += NT) {
     const int p = e % P, n = e / P;
     if (p >= nvalid) continue;
@@ -155,14 +207,16 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
     out.f[1][idx] = uy;
     out.f[2][idx] = uz;
     const T kx = (T)(kx0 + p);
-    out.f[5][idx] = cmuli(csub(cscale(uy, kx), cscale(ux, ky)));
+#pragma unroll
+    for (int q = 0; q < ZF::NPW; ++q) out.f[ZF::pw_field(q)][idx] = zi_pointwise(ZF::pw_field(q), ux, uy, kx, ky);
   }
   __syncthreads();
 }
 
-// Standalone z-inverse (DNS): the stage input tile by TMA, K_f partial sums,
-// then zinv_from_tiles.  grid = (kx tiles or za.tiles_x, ny).
-template <typename T, int LOGN>
+// Standalone z-inverse (MODE ZV_DNS, or ZV_SMAG for the LES operands): the
+// stage input tile by TMA, K_f partial sums, then zinv_from_tiles.
+// grid = (kx tiles or za.tiles_x, ny).
+template <typename T, int LOGN, int MODE>
 __global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
 zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, const __grid_constant__ CUtensorMap umap, ZvArgs<T> za,
                  FieldList<T> out, Geom g, const C2<T>* __restrict__ tw, int* err) {
@@ -214,7 +268,7 @@ zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, const __grid_constant
     const double sum = block_sum<NT>(q, red);
     if (threadIdx.x == 0) za.fs.partial[(long long)blockIdx.x * g.ny + iy] = sum;
   }
-  zinv_from_tiles<T, LOGN>(rt, work, kx0, iy, nvalid, base, zstride, out, g, tw, za.ustore ? &umap : nullptr);
+  zinv_from_tiles<T, LOGN, MODE>(rt, work, kx0, iy, nvalid, base, zstride, out, g, tw, za.ustore ? &umap : nullptr);
 }
 
 // Third operand of the adjoint right-hand side along z:

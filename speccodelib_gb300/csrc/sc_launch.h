@@ -71,9 +71,10 @@ template <typename T> struct Launch {
   static int zinv5_tile(int logn);     // tile width of zinv5 / zinv_phi / zfwd_zinv
   // umap: a map of out.f[0..2] tiled zinv5_tile wide, used when
   // za.ustore (u leaves by bulk tensor stores)
+  // mode ZV_DNS = 0 (u, w) or ZV_SMAG (u, w, S_ij: eight transforms, not 12)
   static cudaError_t zinv5_tma(int logn, const CUtensorMap& vmap, const CUtensorMap& umap, const ZvArgs<T>& za,
                                const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
-                               cudaStream_t s);
+                               cudaStream_t s, int mode = 0);
   // phi^ of the adjoint right-hand side from TMA-loaded lam tiles (za.lam is
   // unused; the map covers lam), with the forcing-adjoint band sums
   static cudaError_t zinv_phi_tma(int logn, const CUtensorMap& lmap, const ZvArgs<T>& za,

@@ -580,7 +580,18 @@ template <typename T> struct Impl {
       }
       SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, st, *g, tw(h, g->nz), h->derr, h->stream); }));
     } else {
-      SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
+      if (les && h->tma && h->zinv5 && sin_spaced && L::zinv5_supported(h->logz)) {
+        // LES operands u, w, S_ij: TMA-fed, eight transforms (not 12), u by bulk stores
+        const int P5 = L::zinv5_tile(h->logz);
+        CUtensorMap vmap, umap;
+        SC_TRY(encode_fields(h, sin[0], 3, 2, P5, g->nz, &vmap));
+        SC_TRY(encode_fields(h, wl.f[0], 3, 2, P5, g->nz, &umap));
+        sc::ZvArgs<T> zu = za;
+        zu.ustore = 1;
+        SC_TRY(launch(h, "zinv", [&] { return L::zinv5_tma(h->logz, vmap, umap, zu, wl, *g, tw(h, g->nz), h->derr, h->stream, sc::ZV_SMAG); }));
+      } else {
+        SC_TRY(launch(h, "zinv", [&] { return L::zinv_vel(h->logz, les ? sc::ZV_SMAG : sc::ZV_DNS, za, wl, *g, tw(h, g->nz), h->stream); }));
+      }
       if (h->tma) SC_TRY(plain_tma(h, "ypass_inv", 1, true, wl.f[0], nw));
       else SC_TRY(launch(h, "ypass_inv", [&] { return L::plain(h->logy, true, wl, ypass_args(h, nw), *g, g->nz, tw(h, g->ny), h->stream); }));
       if (les) SC_TRY(launch(h, "xpass", [&] {
