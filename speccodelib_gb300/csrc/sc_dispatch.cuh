@@ -109,17 +109,26 @@ cudaError_t launch_zfwd_fields_tma(const CUtensorMap& fmap, const StageArgs<T>& 
   return cudaGetLastError();
 }
 
-template <typename T, int LOGN>
-cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
-                            const C2<T>* tw, int* err, cudaStream_t s) {
+template <typename T, int LOGN, int MODE>
+cudaError_t launch_zfwd_tma_mode(const CUtensorMap& lmap, const CUtensorMap& vmap, int vstore, const StageArgs<T>& st,
+                                 const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
   using Cfg = TmaCfg<T, LOGN>;
-  auto k = zfwd_tma_kernel<T, LOGN>;
+  auto k = zfwd_tma_kernel<T, LOGN, MODE>;
   constexpr size_t sm = 3 * Cfg::TILE_BYTES + kSmemAlignPad;
   static cudaError_t attr = smem_attr(k, sm);
   if (attr != cudaSuccess) return attr;
   dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
-  k<<<grid, Cfg::NT, sm, s>>>(lmap, st, g, tw, err);
+  k<<<grid, Cfg::NT, sm, s>>>(lmap, vmap, vstore, st, g, tw, err);
   return cudaGetLastError();
+}
+
+// RK stage 4 (the step's last) in its own instance, the state stored from the
+// tiles when vstore; other modes read st.mode at run time
+template <typename T, int LOGN>
+cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const CUtensorMap& vmap, int vstore, const StageArgs<T>& st,
+                            const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
+  if (st.mode == SM_RK4) return launch_zfwd_tma_mode<T, LOGN, SM_RK4>(lmap, vmap, vstore, st, g, tw, err, s);
+  return launch_zfwd_tma_mode<T, LOGN, -1>(lmap, vmap, 0, st, g, tw, err, s);
 }
 
 template <typename T, int LOGN, int MODE>
@@ -324,8 +333,9 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     }                                                                                            \
   }                                                                                              \
   template <>                                                                                    \
-  cudaError_t sc::Launch<T>::zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, \
-                                      const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) { \
+  cudaError_t sc::Launch<T>::zfwd_tma(int logn, const CUtensorMap& lmap, const CUtensorMap& vmap,  \
+                                      int vstore, const StageArgs<T>& st, const Geom& g,         \
+                                      const C2<T>* tw, int* err, cudaStream_t s) {               \
     switch (logn) {                                                                              \
       SC_LOGN_CASES(SC_ZFWDTMA_CASE_##T)                                                         \
       default: return cudaErrorInvalidValue;                                                     \
@@ -342,8 +352,8 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
 #define SC_ZINVTMA_CASE_double(L) case L: return sc::launch_zinv_tma<double, L>(vmap, za, out, g, tw, err, s);
 #define SC_ZFWDFIELDS_CASE_float(L) case L: return sc::launch_zfwd_fields_tma<float, L, 9>(fmap, st, g, tw, err, s);
 #define SC_ZFWDFIELDS_CASE_double(L) case L: return sc::launch_zfwd_fields_tma<double, L, 9>(fmap, st, g, tw, err, s);
-#define SC_ZFWDTMA_CASE_float(L) case L: return sc::launch_zfwd_tma<float, L>(lmap, st, g, tw, err, s);
-#define SC_ZFWDTMA_CASE_double(L) case L: return sc::launch_zfwd_tma<double, L>(lmap, st, g, tw, err, s);
+#define SC_ZFWDTMA_CASE_float(L) case L: return sc::launch_zfwd_tma<float, L>(lmap, vmap, vstore, st, g, tw, err, s);
+#define SC_ZFWDTMA_CASE_double(L) case L: return sc::launch_zfwd_tma<double, L>(lmap, vmap, vstore, st, g, tw, err, s);
 
 #define SC_DEFINE_TILE(T) \
   template <> int sc::Launch<T>::tile() { return sc::Tile<T>::P; }

@@ -57,8 +57,10 @@ template <typename T> struct Launch {
   static cudaError_t zinv_tma(int logn, const CUtensorMap& vmap, const ZvArgs<T>& za,
                               const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                               cudaStream_t s);
-  static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const StageArgs<T>& st, const Geom& g,
-                              const C2<T>* tw, int* err, cudaStream_t s);
+  // vstore (RK stage 4 only): the new state leaves by bulk tensor stores
+  // through vmap (st.vout[0..2], tiles as lmap)
+  static cudaError_t zfwd_tma(int logn, const CUtensorMap& lmap, const CUtensorMap& vmap, int vstore,
+                              const StageArgs<T>& st, const Geom& g, const C2<T>* tw, int* err, cudaStream_t s);
   // z-forward of nin fields (9: the LES Lamb vector and tau_ij) through a
   // TMA ring, fmap tiled tma_tile wide; cudaErrorNotSupported otherwise
   static cudaError_t zfwd_fields_tma(int logn, int nin, const CUtensorMap& fmap, const StageArgs<T>& st,

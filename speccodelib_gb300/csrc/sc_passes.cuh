@@ -449,7 +449,9 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
       for (int c = 0; c < 3; ++c) {
         const C a = cadd(av[c], cscale(w[c], dt));
         C vn = cadd(cscale(vv[c], E2), cscale(a, T(1) / T(6)));
-        st.vout[c][idx] = cut ? czero<C>() : vn;
+        if (cut) vn = czero<C>();
+        if (snext) snext[c] = vn;
+        else st.vout[c][idx] = vn;
       }
       break;
     case SM_AB2_EULER:  // v = (v + dt/2 w) sqrt(expk2) ; history = w

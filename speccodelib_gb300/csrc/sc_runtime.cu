@@ -578,7 +578,11 @@ template <typename T> struct Impl {
         z0.ustore = 1;
         return launch(h, "zinv_kx0", [&] { return L::zinv5_tma(h->logz, smap, lmap5, z0, wl, *g, tw(h, g->nz), h->derr, h->stream); });
       }
-      SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, st, *g, tw(h, g->nz), h->derr, h->stream); }));
+      CUtensorMap vmap_out = lmap;
+      const bool vstore = st.mode == sc::SM_RK4 && st.vout[1] == st.vout[0] + g->field &&
+                          st.vout[2] == st.vout[0] + 2 * g->field;
+      if (vstore) SC_TRY(encode_fields(h, st.vout[0], 3, 2, P, g->nz, &vmap_out));
+      SC_TRY(launch(h, "zfwd", [&] { return L::zfwd_tma(h->logz, lmap, vmap_out, vstore ? 1 : 0, st, *g, tw(h, g->nz), h->derr, h->stream); }));
     } else {
       if (les && h->tma && h->zinv5 && sin_spaced && L::zinv5_supported(h->logz)) {
         // LES operands u, w, S_ij: TMA-fed, eight transforms (not 12), u by bulk stores

@@ -276,11 +276,15 @@ zfwd_fields_tma_kernel(const __grid_constant__ CUtensorMap fmap, StageArgs<T> st
   zfwd_finish<E, T>(w, st, g, kx0, iy, nvalid, base, zstride, s_coef);
 }
 
-// z-forward pass of the Lamb vector + the spectral update (DNS).
-template <typename T, int LOGN>
+// z-forward pass of the Lamb vector + the spectral update (DNS).  MODE: the
+// update mode as a compile-time constant (-1: st.mode at run time).  With
+// MODE == SM_RK4 and vstore, the new state goes back into the tiles and
+// leaves by bulk tensor stores through vmap (st.vout, tiles as lmap); the
+// kx = 0 points that the fix-up kernel finishes keep their old state there.
+template <typename T, int LOGN, int MODE>
 __global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
-zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom g,
-                const C2<T>* __restrict__ tw, int* err) {
+zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap vmap, int vstore,
+                StageArgs<T> st, Geom g, const C2<T>* __restrict__ tw, int* err) {
   using Cfg = TmaCfg<T, LOGN>;
   using E = typename Cfg::Engine;
   using C = C2<T>;
@@ -325,6 +329,7 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom 
   // Epilogue in batches of EB points per thread: all state loads of a batch
   // are issued before any of them is used.
   constexpr int EB = NT >= 512 ? 2 : 4;
+  const bool tstore = MODE == SM_RK4 && vstore;
   for (int e0 = threadIdx.x; e0 < P * N; e0 += NT * EB) {
     C wv[EB][3], vv[EB][3], av[EB][3];
     bool act[EB];
@@ -335,7 +340,7 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom 
       act[i] = e < P * N && p < nvalid;
       if (!act[i]) continue;
       const long long idx = base + iz * zstride + p;
-      load_state<T>(st, idx, vv[i], av[i]);
+      load_state<T, MODE>(st, idx, vv[i], av[i]);
 #pragma unroll
       for (int c = 0; c < 3; ++c) wv[i][c] = w[c][e];
     }
@@ -360,12 +365,36 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, StageArgs<T> st, Geom 
           const long long s = ((long long)iz * g.ny + iy) * 3;
 #pragma unroll
           for (int c = 0; c < 3; ++c) st.side[s + c] = wp[c];
-          if (iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2)) continue;
+          if (iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2)) {
+            if (tstore)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) w[c][e] = vv[i][c];
+            continue;
+          }
         }
         if (iy == g.ny / 2 || iz == g.nz / 2 || ix == g.nxh - 1 || (ix == 0 && iy == 0 && iz == 0))
           wp[0] = wp[1] = wp[2] = czero<C>();
       }
-      finish_point_pre<T>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i]);
+      if (tstore) {
+        C vn[3];
+        finish_point_pre<T, MODE>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i], vn);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) w[c][e] = vn[c];
+      } else {
+        finish_point_pre<T, MODE>(st, g, idx, ix, iy, iz, kc_b, wp, vv[i], av[i]);
+      }
+    }
+  }
+  if (tstore) {
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int c = 0; c < 3; ++c)
+        for (int h = 0; h < Cfg::NBOX; ++h)
+          tma_store_4d(&vmap, reinterpret_cast<char*>(w[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), kx0 * Cfg::U,
+                       iy, h * Cfg::BOX, c);
+      tma_store_commit();
+      tma_store_wait_read<0>();
     }
   }
 }
