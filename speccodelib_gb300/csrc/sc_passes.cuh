@@ -374,7 +374,7 @@ template <typename T> struct StageArgs {
 
 // What the update of a mode reads at each point besides w.
 __host__ __device__ constexpr bool mode_reads_v(int m) {
-  return m == SM_RK1 || m == SM_RK2 || m == SM_RK3 || m == SM_RK4 || m == SM_AB2_EULER || m == SM_AB2 ||
+  return m == SM_RK1 || m == SM_RK2 || m == SM_RK3 || m == SM_AB2_EULER || m == SM_AB2 ||
          m == SM_AB2_MID;
 }
 __host__ __device__ constexpr bool mode_reads_acc(int m) {
@@ -435,20 +435,19 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
         else st.sout[c][idx] = sn;
       }
       break;
-    case SM_RK3:  // acc += 2 E dt w3 ; s4 = E^2 v + E dt w3
+    case SM_RK3:  // acc <- E^2 v + (acc + 2 E dt w3)/6 (stage 4 then needs no v) ; s4 = E^2 v + E dt w3
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        st.acc[c][idx] = cadd(av[c], cscale(w[c], T(2) * E * dt));
+        st.acc[c][idx] = cadd(cscale(vv[c], E2), cscale(cadd(av[c], cscale(w[c], T(2) * E * dt)), T(1) / T(6)));
         const C sn = cadd(cscale(vv[c], E2), cscale(w[c], E * dt));
         if (snext) snext[c] = sn;
         else st.sout[c][idx] = sn;
       }
       break;
-    case SM_RK4:  // v = E^2 v + (acc + dt w4)/6, then the 2/3 mask
+    case SM_RK4:  // v = E^2 v + (acc + dt w4)/6 = acc' + dt w4/6 (acc' from stage 3), then the 2/3 mask
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const C a = cadd(av[c], cscale(w[c], dt));
-        C vn = cadd(cscale(vv[c], E2), cscale(a, T(1) / T(6)));
+        C vn = cadd(av[c], cscale(cscale(w[c], dt), T(1) / T(6)));
         if (cut) vn = czero<C>();
         if (snext) snext[c] = vn;
         else st.vout[c][idx] = vn;

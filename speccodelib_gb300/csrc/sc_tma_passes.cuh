@@ -280,7 +280,8 @@ zfwd_fields_tma_kernel(const __grid_constant__ CUtensorMap fmap, StageArgs<T> st
 // update mode as a compile-time constant (-1: st.mode at run time).  With
 // MODE == SM_RK4 and vstore, the new state goes back into the tiles and
 // leaves by bulk tensor stores through vmap (st.vout, tiles as lmap); the
-// kx = 0 points that the fix-up kernel finishes keep their old state there.
+// kx = 0 points that the fix-up kernel finishes hold zeros until it writes
+// them (stage 4 reads no v: the fix-up needs only acc and the side plane).
 template <typename T, int LOGN, int MODE>
 __global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
 zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap vmap, int vstore,
@@ -368,7 +369,7 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant_
           if (iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2)) {
             if (tstore)
 #pragma unroll
-              for (int c = 0; c < 3; ++c) w[c][e] = vv[i][c];
+              for (int c = 0; c < 3; ++c) w[c][e] = czero<C>();
             continue;
           }
         }
