@@ -285,7 +285,8 @@ __device__ __forceinline__ void ens_yfwd(const EnsMember<T>& mb, int tile, int s
       const T Ef = exp(-arg);
       const T E2 = Ef * Ef, dt = mb.dt, hdt = T(0.5) * mb.dt;
       const long long idx = (long long)n * mb.nxp + ix;
-      const C v = mb.w[idx];
+      // stage 3 leaves E^2 v + (acc + 2 E dt w3)/6 in acc, so stage 4 reads no v
+      const C v = stage < 4 ? mb.w[idx] : czero<C>();
       switch (stage) {
         case 1:
           mb.acc[idx] = cscale(w, E2 * dt);
@@ -296,14 +297,12 @@ __device__ __forceinline__ void ens_yfwd(const EnsMember<T>& mb, int tile, int s
           mb.s[idx] = cadd(cscale(v, Ef), cscale(w, hdt));
           break;
         case 3:
-          mb.acc[idx] = cadd(mb.acc[idx], cscale(w, T(2) * Ef * dt));
+          mb.acc[idx] = cadd(cscale(v, E2), cscale(cadd(mb.acc[idx], cscale(w, T(2) * Ef * dt)), T(1) / T(6)));
           mb.s[idx] = cadd(cscale(v, E2), cscale(w, Ef * dt));
           break;
-        default: {
-          const C ac = cadd(mb.acc[idx], cscale(w, dt));
-          mb.w[idx] = cadd(cscale(v, E2), cscale(ac, T(1) / T(6)));
+        default:   // v = E^2 v + (acc + dt w4)/6 = acc' + dt w4/6
+          mb.w[idx] = cadd(mb.acc[idx], cscale(cscale(w, dt), T(1) / T(6)));
           break;
-        }
       }
     }
 }
