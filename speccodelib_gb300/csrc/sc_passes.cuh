@@ -365,8 +365,8 @@ template <typename T> struct StageArgs {
   int mask_rhs;         // also truncate the RHS (mask = rhs_and_step)
   int symmetrize;       // apply symmetrize.f90:32-64 to w
   int project;          // apply projection.f90 to w
-  // TMA z-forward kernels: slots (field indices of the slab map) of the
-  // fields the update reads, prefetched into L2 when a tile starts
+  // fused z kernel: slots (field indices of the slab map) of the fields the
+  // update reads, prefetched into L2 once a tile's Lamb vector is in
   int pf_n;
   int pf_slot[6];
 };
