@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -1112,7 +1113,10 @@ static int host_route(sc_handle* h, const void* p, void** dp) {
     cudaGetLastError();
     return 0;
   }
-  if (a.type == cudaMemoryTypeHost && h->copy_mode == 1 && a.devicePointer) {
+  // the repack kernel moves whole elements (8 or 16 bytes): a buffer not
+  // aligned to that goes through the staged copy
+  const bool aligned = reinterpret_cast<uintptr_t>(p) % h->csize == 0;
+  if (a.type == cudaMemoryTypeHost && h->copy_mode == 1 && a.devicePointer && aligned) {
     *dp = a.devicePointer;
     return 2;
   }

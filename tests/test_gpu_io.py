@@ -77,3 +77,29 @@ def test_state_round_trip_pinned_and_pageable(specns_lib, prec, mode, monkeypatc
         w_pageable = h.get_state()
     for a, b in zip(w_pinned, w_pageable):
         assert np.array_equal(a, b)
+
+
+def test_state_round_trip_misaligned_pinned(specns_lib):
+    """FP64 state from and to pinned host buffers that start 8 bytes past a
+    16-byte boundary (complex128 elements the repack kernel cannot move whole):
+    the copy takes the staged path and the state comes back bit for bit."""
+    torch = pytest.importorskip("torch")
+    from speccodelib_gb300 import specns as SP
+    from _util import hermitian_fields
+    import ctypes as C
+    nx, ny, nz = 32, 16, 8
+    v = [np.ascontiguousarray(a, np.complex128) for a in hermitian_fields((nx, ny, nz), 93)]
+    nbytes = v[0].nbytes
+    bufs = [torch.empty(nbytes + 16, dtype=torch.uint8, pin_memory=True) for _ in range(6)]
+    ptrs = [b.data_ptr() + (8 if b.data_ptr() % 16 == 0 else 0) for b in bufs]
+    assert all(p % 16 == 8 for p in ptrs)
+    for p_, a in zip(ptrs[:3], v):
+        C.memmove(p_, a.ctypes.data, nbytes)
+    p = S.default_params(nx, S.SC_FP64, ny=ny, nz=nz)
+    with S.SpectralNS(p) as h:
+        SP._check(SP.lib().sc_set_state(h.h, *[C.c_void_p(x) for x in ptrs[:3]]))
+        SP._check(SP.lib().sc_get_state(h.h, *[C.c_void_p(x) for x in ptrs[3:]]))
+    for p_, a in zip(ptrs[3:], v):
+        out = np.empty_like(a)
+        C.memmove(out.ctypes.data, p_, nbytes)
+        assert np.array_equal(out, a)
