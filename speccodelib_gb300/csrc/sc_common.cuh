@@ -87,7 +87,7 @@ __host__ __device__ inline int k2_lt(double t) { return k2_clamp(ceil(t)); }
 
 // floor(sqrt(k2) + 1/2) for an integer k2 >= 0, exactly: the n with
 // n^2 - n < k2 <= n^2 + n (a float root is within one of it).
-__device__ __forceinline__ int shell_index(int k2) {
+__host__ __device__ __forceinline__ int shell_index(int k2) {
   int n = (int)(sqrtf((float)k2) + 0.5f);
   const long long nn = (long long)n * n;
   if (nn + n < k2) ++n;
@@ -103,7 +103,7 @@ struct Walk3 {
   long long t, total, stride;
   int ix, iy, iz;
   int n, ny, dix, diy, diz;
-  __device__ __forceinline__ Walk3(long long t0, long long stride_, long long total_, int n_, int ny_)
+  __host__ __device__ __forceinline__ Walk3(long long t0, long long stride_, long long total_, int n_, int ny_)
       : t(t0), total(total_), stride(stride_), n(n_), ny(ny_) {
     const long long r = t0 / n_, sr = stride_ / n_;
     ix = (int)(t0 - r * n_);
@@ -113,8 +113,8 @@ struct Walk3 {
     diy = (int)(sr % ny_);
     diz = (int)(sr / ny_);
   }
-  __device__ __forceinline__ bool ok() const { return t < total; }
-  __device__ __forceinline__ void next() {
+  __host__ __device__ __forceinline__ bool ok() const { return t < total; }
+  __host__ __device__ __forceinline__ void next() {
     t += stride;
     ix += dix;
     int c = ix >= n;
@@ -124,7 +124,7 @@ struct Walk3 {
     if (c) iy -= ny;
     iz += diz + c;
   }
-  __device__ __forceinline__ long long row() const { return (long long)iz * ny + iy; }
+  __host__ __device__ __forceinline__ long long row() const { return (long long)iz * ny + iy; }
 };
 __host__ __device__ inline int k2_le(double t) { return k2_clamp(floor(t) + 1.0); }
 
