@@ -64,10 +64,14 @@ except ImportError:  # pragma: no cover
 
 WORKERS = int(os.environ.get("SC_ORACLE_WORKERS", "1"))
 
-# constant_sp.f90 / constant.f90 (the "-dp" build is followed: sp = double)
-PI_REF = 3.1415926536                      # constant.f90:40 (truncated pi)
-MYTINY_DP = float(np.finfo(np.float64).tiny)   # constant.f90:34 tiny(1.0_dp)
-MYTINY_SP = float(np.finfo(np.float32).tiny)   # constant.f90:36 tiny(1.0_sp)
+# mconstant: constant_sp.f90 makes kind sp single precision, constant.f90 and
+# constant_dp.f90 make it double (the "-dp" builds).  The arithmetic here is
+# FP64 throughout; MYTINY_SP is the single-precision build's tiny(1.0_sp),
+# used for k2(1,1,1) in both precisions (in the double build it is
+# tiny(1.0_d0): a difference confined to the mean mode).
+PI_REF = 3.1415926536                          # constant_sp.f90:20, constant.f90:17 (truncated pi)
+MYTINY_DP = float(np.finfo(np.float64).tiny)   # constant_sp.f90:16, constant.f90:12 tiny(1.0_dp)
+MYTINY_SP = float(np.finfo(np.float32).tiny)   # constant_sp.f90:15 tiny(1.0_sp)
 
 
 # --------------------------------------------------------------------------
