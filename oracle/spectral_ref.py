@@ -228,7 +228,7 @@ def skewness(ux, nx):
 
 
 def enstrophy_field(ux, uy, uz, nx):
-    """enstrophy.f90:1-36: 1/2 |curl u|^2 at every physical point, returned
+    """enstrophy.f90:1-34: 1/2 |curl u|^2 at every physical point, returned
     (nz, ny, nx) (the memory of the reference's real(dp) enstr(nx,ny,nz))."""
     ny, nz = ux.shape[1], ux.shape[0]
     kx, ky, kz, _ = wavenumber(nx, ny, nz)

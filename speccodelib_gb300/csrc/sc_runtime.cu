@@ -1816,7 +1816,7 @@ template <typename T> static int skewness_impl(sc_handle* h, const void* ux, dou
   return SC_OK;
 }
 
-// enstrophy(ux,uy,uz,kx,ky,kz,enstr,lx1,ly,lz,lx,nx,ny,nz), enstrophy.f90:1-36:
+// enstrophy(ux,uy,uz,kx,ky,kz,enstr,lx1,ly,lz,lx,nx,ny,nz), enstrophy.f90:1-34:
 // 1/2 |i k x u|^2 at every physical point, (nx, ny, nz) real(dp).
 template <typename T> static int enstrophy_impl(sc_handle* h, const void* const u[3], double* enstr) {
   using I = Impl<T>;
