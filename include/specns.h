@@ -124,6 +124,20 @@ int sc_rk4_steps(sc_handle* h, int nsteps);
  * the AB2 solver's own: no symmetrize (specdns-forced-omp-ft.f90:180-221). */
 int sc_ab2_steps(sc_handle* h, int npasses);
 
+/* npasses passes of the rotating solver's loop, spectral_rot_dns_ft.f90:
+ * 146-272 (replaces that program's time loop).  The state is the pair of
+ * helical amplitudes a+ = v . conj(h), a- = v . h (heliwave.f90:57-96), each
+ * advanced with exp(-nu k^2 dt +- 2 i dt kz om / |k|) (:101-111): pass 0 is
+ * an Euler half step, pass 1 a midpoint restart from the initial field, then
+ * AB2; after every pass the handle's state is v = a+ h + a- conj(h),
+ * truncated at k >= kcut.  Right-hand side (:189-211): Lamb vector,
+ * force_rot on the band fk1^2 <= k^2 < fk2^2 when the handle is forced
+ * (eps from sc_params), symmetrize, projection.  om is the rotation rate.
+ * The amplitudes (five extra fields with the previous right-hand side) are
+ * allocated on the first call; sc_set_state and sc_init_field restart the
+ * sequence at pass 0.  Handles with sgs != SC_SGS_NONE are rejected. */
+int sc_rot_steps(sc_handle* h, int npasses, double om, double fk1, double fk2);
+
 /* Discrete adjoint of nsteps IF-RK4 steps (DNS right-hand side) for
  * J = sum over shells kmin..kmax (floor(|k| + 1/2)) of k^2 q(k) at the final
  * time (q = 1/2-weighted |v|^2, the shell enstrophy).  Writes J and

@@ -538,6 +538,113 @@ def ab2_run(v, grid: Grid, nhalf_steps):
 
 
 # --------------------------------------------------------------------------
+# rotating solver: helical-wave IF-AB2 (spectral_rot_dns_ft.f90)
+# --------------------------------------------------------------------------
+def heliwave(kx, ky, kz, k2):
+    """Positive-helicity unit vectors h+ at every mode, heliwave.f90:57-96
+    (the low-memory form the rotating solver calls with 1D kx, ky, kz;
+    spectral_rot_dns_ft.f90:24,114).  h- = conj(h+), i k x h+ = |k| h+.
+
+    Rows with ky = kz = 0 (:73-81) use k2d = max(sqrt(kx^2 + ky^2),
+    smallest); the others (:82-91) k2d = sqrt(kz^2 + ky^2).  The floor only
+    acts at the mean mode, whose numerators are all zero, so h = 0 there."""
+    s = np.sqrt(2.0) / 2.0
+    KX = np.broadcast_to(kx[None, None, :], k2.shape)
+    KY = np.broadcast_to(ky[None, :, None], k2.shape)
+    KZ = np.broadcast_to(kz[:, None, None], k2.shape)
+    k = np.sqrt(k2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        k2d = np.sqrt(KZ * KZ + KY * KY)
+        hx = s * (1j * (KY * KY + KZ * KZ) / k / k2d)
+        hy = s * (-KZ / k2d - 1j * KX * KY / k / k2d)
+        hz = s * (KY / k2d - 1j * KZ * KX / k / k2d)
+    smallest = 2.0 * float(np.finfo(np.float32).eps)      # constant_sp.f90:7
+    kxa, k0 = kx, k[0, 0, :]
+    k2d0 = np.maximum(np.abs(kxa), smallest)               # ky = 0 on this row
+    hx[0, 0, :] = s * (-0.0 / k2d0 - 1j * kxa * 0.0 / k0 / k2d0)
+    hy[0, 0, :] = s * (kxa / k2d0 - 1j * 0.0 * 0.0 / k0 / k2d0)
+    hz[0, 0, :] = s * (1j * (kxa * kxa) / k0 / k2d0)
+    return hx, hy, hz
+
+
+def rot_factors(grid: Grid, om):
+    """efp = exp(-k2 nu dt + 2 i dt kz om / (sqrt(k2) + tiny)) and efm with
+    the opposite phase (spectral_rot_dns_ft.f90:101-111); sqrt is the
+    principal complex square root, as Fortran's."""
+    p = grid.p
+    KZ = grid.kz[:, None, None]
+    ph = 2.0 * p.dt * KZ * om / (np.sqrt(grid.k2) + MYTINY_SP)
+    efp = np.exp(-grid.k2 * p.nu * p.dt + 1j * ph)
+    efm = np.exp(-grid.k2 * p.nu * p.dt - 1j * ph)
+    return efp, efm, np.sqrt(efp), np.sqrt(efm)
+
+
+def rot_rhs(v, grid: Grid, fk1, fk2):
+    """Right-hand side of the rotating solver, spectral_rot_dns_ft.f90:189-211:
+    vorticity (:190-198), Lamb vector (:201), force_rot on the band
+    fk1^2 <= k2 < fk2^2 when forced (:204), symmetrize of each component
+    (:206-208), projection with +tiny (:211)."""
+    p = grid.p
+    kx, ky, kz, k2 = grid.kx, grid.ky, grid.kz, grid.k2
+    vx, vy, vz = v
+    wx, wy, wz = vorticity(vx, vy, vz, kx, ky, kz)
+    wx, wy, wz = convec_dns(vx, vy, vz, wx, wy, wz, p.nx)
+    if p.forced:
+        wx, wy, wz = force_rot(wx, wy, wz, vx, vy, vz, k2, fk1 * fk1, fk2 * fk2, p.eps, MYTINY_SP)
+    wx, wy, wz = symmetrize3d(wx), symmetrize3d(wy), symmetrize3d(wz)
+    return projection(wx, wy, wz, kx, ky, kz)
+
+
+def rot_run(v, grid: Grid, npasses, om, fk1=0.0, fk2=2.5, trace=None):
+    """`npasses` passes of the rotating solver's loop,
+    spectral_rot_dns_ft.f90:146-272: the state is the pair of helical
+    amplitudes a+ = v . conj(h), a- = v . h (:132-133); pass 0 is an Euler
+    half step (:215-223), pass 1 a midpoint restart from the initial field
+    (:225-237), then AB2 with the previous right-hand side (:239-256); after
+    each pass v = a+ h + a- conj(h) with the 2/3 truncation (:261-270), the
+    amplitudes themselves are not truncated.  Returns (v, (a+, a-), time).
+    With a list `trace`, each pass appends (its right-hand side, v after it)."""
+    p = grid.p
+    dt = p.dt
+    dt_h = 0.5 * dt                                                  # :135
+    hx, hy, hz = heliwave(grid.kx, grid.ky, grid.kz, grid.k2)
+    efp, efm, sqp, sqm = rot_factors(grid, om)
+    kcut2 = (2.0 * (p.nx // 2) / 3.0) ** 2                           # :85-86
+    v = [np.array(a, dtype=np.complex128) for a in v]
+    ox, oy, oz = v                                                   # :129-131
+    ap = v[0] * np.conj(hx) + v[1] * np.conj(hy) + v[2] * np.conj(hz)
+    am = v[0] * hx + v[1] * hy + v[2] * hz
+    o0 = None
+    t = 0.0
+    for istep in range(npasses):
+        wx, wy, wz = rot_rhs(v, grid, fk1, fk2)
+        if istep == 0:
+            ap = (ap + dt_h * (wx * np.conj(hx) + wy * np.conj(hy) + wz * np.conj(hz))) * sqp
+            am = (am + dt_h * (wx * hx + wy * hy + wz * hz)) * sqm
+            t += dt_h
+            o0 = (wx, wy, wz)                                        # :223 (written out)
+        elif istep == 1:
+            ap = ((ox * np.conj(hx) + oy * np.conj(hy) + oz * np.conj(hz)) * efp
+                  + dt * (wx * np.conj(hx) + wy * np.conj(hy) + wz * np.conj(hz)) * sqp)
+            am = (ox * hx + oy * hy + oz * hz) * efm + dt * (wx * hx + wy * hy + wz * hz) * sqm
+            t += dt_h
+            ox, oy, oz = o0                                          # :235 (read back)
+        else:
+            tx, ty, tz = 3.0 * wx - efp * ox, 3.0 * wy - efp * oy, 3.0 * wz - efp * oz
+            ap = (ap + dt_h * (tx * np.conj(hx) + ty * np.conj(hy) + tz * np.conj(hz))) * efp
+            tx, ty, tz = 3.0 * wx - efm * ox, 3.0 * wy - efm * oy, 3.0 * wz - efm * oz
+            am = (am + dt_h * (tx * hx + ty * hy + tz * hz)) * efm
+            ox, oy, oz = wx, wy, wz
+            t += dt
+        v = [ap * hx + am * np.conj(hx), ap * hy + am * np.conj(hy), ap * hz + am * np.conj(hz)]
+        m = grid.k2 >= kcut2
+        v = [np.where(m, 0.0, a) for a in v]
+        if trace is not None:
+            trace.append(((wx, wy, wz), tuple(v)))
+    return tuple(v), (ap, am), t
+
+
+# --------------------------------------------------------------------------
 # diagnostics (FP64)
 # --------------------------------------------------------------------------
 def _q(v):

@@ -39,6 +39,7 @@ SIGNATURES = {
     "sc_rhs": ([_P, _P, _P, _P], _I),
     "sc_rk4_steps": ([_P, _I], _I),
     "sc_ab2_steps": ([_P, _I], _I),
+    "sc_rot_steps": ([_P, _I, _D, _D, _D], _I),
     "sc_diagnostics": ([_P, _P, _P], _I),
     "sc_get_params": ([_P, _P], _I),
     "sc_output3d": ([_P, _CS, _I, _I], _I),

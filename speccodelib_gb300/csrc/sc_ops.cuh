@@ -8,6 +8,7 @@
 // (specdns-forced-omp-ft.f90:142-176).  All sums are accumulated in double.
 #pragma once
 #include "sc_passes.cuh"
+#include "sc_rot.cuh"
 
 namespace sc {
 
@@ -257,6 +258,63 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// helical-wave AB2 update of the rotating solver (rot_point, sc_rot.cuh)
+// ---------------------------------------------------------------------------
+template <typename T> struct RotArgs {
+  int pass;              // 0: Euler half step, 1: midpoint restart, >= 2: AB2
+  C2<T>* v[3];           // velocity: read at pass 0, rewritten every pass
+  const C2<T>* w[3];     // right-hand side of this pass
+  C2<T>* o[3];           // previous right-hand side (written at pass 0 and >= 2)
+  C2<T>* a[2];           // helical amplitudes a+, a-
+  double nu, dt, om;     // viscosity, time step, rotation rate
+  double kcut2;          // v = 0 where k2 >= kcut2
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) rot_update_kernel(RotArgs<T> ra, Geom g) {
+  using C = C2<T>;
+  const long long rows = (long long)g.ny * g.nz;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tstride = (long long)gridDim.x * blockDim.x;
+  const int kc_b = k2_lt(ra.kcut2);
+  const T nu = (T)ra.nu, dt = (T)ra.dt, om = (T)ra.om;
+  const int pass = ra.pass;
+  for (Walk3 it(t0, tstride, rows * g.nxh, g.nxh, g.ny); it.ok(); it.next()) {
+    const long long idx = it.row() * g.nxp + it.ix;
+    const int ky = wavenum(it.iy, g.ny), kz = wavenum(it.iz, g.nz);
+    const int k2 = it.ix * it.ix + ky * ky + kz * kz;
+    Cx<T> v[3], w[3], o[3], ap = cx(T(0), T(0)), am = cx(T(0), T(0));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const C wc = ra.w[c][idx];
+      w[c] = cx(wc.x, wc.y);
+      v[c] = o[c] = cx(T(0), T(0));
+      if (pass == 0) {
+        const C vc = ra.v[c][idx];
+        v[c] = cx(vc.x, vc.y);
+      }
+      if (pass >= 2) {
+        const C oc = ra.o[c][idx];
+        o[c] = cx(oc.x, oc.y);
+      }
+    }
+    if (pass > 0) {
+      const C a0 = ra.a[0][idx], a1 = ra.a[1][idx];
+      ap = cx(a0.x, a0.y);
+      am = cx(a1.x, a1.y);
+    }
+    rot_point<T>(pass, it.ix, ky, kz, k2 >= kc_b, nu, dt, om, v, w, o, ap, am);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ra.v[c][idx] = mk<C>(v[c].re, v[c].im);
+      if (pass != 1) ra.o[c][idx] = mk<C>(o[c].re, o[c].im);
+    }
+    ra.a[0][idx] = mk<C>(ap.re, ap.im);
+    ra.a[1][idx] = mk<C>(am.re, am.im);
+  }
+}
 
 // ---------------------------------------------------------------------------
 // post-processing on physical fields held as packed rows (x = 2m in .x,

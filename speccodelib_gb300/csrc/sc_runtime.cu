@@ -113,6 +113,8 @@ struct sc_handle {
   double* cpart = nullptr;        // forcing-adjoint band sums
   long long step = 0;             // RK4 steps taken (dynamic-coefficient cadence)
   int ab2_pass = 0;
+  void* rot = nullptr;            // rotating solver: a+, a-, previous RHS (3); allocated on first use
+  int rot_pass = 0;
   // profiling
   bool prof = false;
   struct Pend { std::string name; cudaEvent_t a, b; };
@@ -696,6 +698,80 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
+  // force_rot.f90:3-29 on w from the velocity v: band fk12 <= k2 < fk22
+  // (squared bounds), a = eps / (2 kinet + tiny), kinet the 1/2-weighted band
+  // energy as the difference of two FP64 sums; tiny is mytiny of the build's
+  // real kind (constant.f90:11, constant_sp.f90:14).
+  static int force_band(sc_handle* h, C* const w[3], const C* const v[3], double fk12, double fk22) {
+    double hi[sc::DQ_N], lo[sc::DQ_N];
+    SC_TRY(diag_run(h, v, 0, fk22, 0, hi));
+    if (fk12 > 0.0) SC_TRY(diag_run(h, v, 0, fk12, 0, lo));
+    const double tiny = sizeof(T) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+    const double kinet = fk12 > 0.0 ? hi[sc::DQ_ENERGY] - lo[sc::DQ_ENERGY] : hi[sc::DQ_ENERGY];
+    sc::SpecOpArgs<T> oa{};
+    for (int c = 0; c < 3; ++c) {
+      oa.f[c] = w[c];
+      oa.gsrc[c] = v[c];
+    }
+    oa.nfields = 3;
+    oa.op = sc::OP_FORCE_BAND;
+    oa.a = h->p.eps / (2.0 * kinet + tiny);
+    oa.kcut2 = fk22;
+    oa.b = fk12;
+    return specop(h, oa);
+  }
+
+  // One pass of the rotating solver's loop, spectral_rot_dns_ft.f90:189-270:
+  // the Lamb vector of v (TMA-fed passes, stored raw into the S_A slots),
+  // force_rot on the band fk1^2 <= k2 < fk2^2 when forced, symmetrize,
+  // projection, then the helical-wave AB2 update (rot_update_kernel).  The
+  // amplitudes a+, a- and the previous right-hand side live in h->rot.
+  static int rot_pass(sc_handle* h, double om, double fk1, double fk2) {
+    auto* g = &h->g;
+    if (!h->rot) {
+      const size_t bytes = 5 * h->csize * g->field;
+      if (cudaMalloc(&h->rot, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        h->rot = nullptr;
+        return fail(SC_ERR_NOMEM, "cannot allocate %zu bytes for the rotating solver", bytes);
+      }
+      SC_CUDA(cudaMemsetAsync(h->rot, 0, bytes, h->stream));
+    }
+    C* rb = reinterpret_cast<C*>(h->rot);
+    sc::StageArgs<T> st = stage_args(h);
+    st.mode = sc::SM_LAMB;
+    st.forced = 0;
+    st.symmetrize = 0;
+    st.project = 0;
+    st.mask_rhs = 0;
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    C* w[3] = {F(h, S_A), F(h, S_A + 1), F(h, S_A + 2)};
+    SC_TRY(rhs_pipeline(h, vin, st));
+    if (h->p.forced) SC_TRY(force_band(h, w, vin, fk1 * fk1, fk2 * fk2));
+    SC_TRY(symmetrize_fields(h, {S_A, S_A + 1, S_A + 2}));
+    sc::SpecOpArgs<T> oa{};
+    for (int c = 0; c < 3; ++c) oa.f[c] = w[c];
+    oa.nfields = 3;
+    oa.op = sc::OP_PROJECT;
+    SC_TRY(specop(h, oa));
+    sc::RotArgs<T> ra{};
+    ra.pass = h->rot_pass < 2 ? h->rot_pass : 2;
+    for (int c = 0; c < 3; ++c) {
+      ra.v[c] = F(h, S_V + c);
+      ra.w[c] = w[c];
+      ra.o[c] = rb + (size_t)(2 + c) * g->field;
+    }
+    ra.a[0] = rb;
+    ra.a[1] = rb + g->field;
+    ra.nu = h->p.nu;
+    ra.dt = h->p.dt;
+    ra.om = om;
+    ra.kcut2 = kcut2(h);
+    SC_TRY(launch(h, "rot_update", [&] { return L::rot(ra, *g, h->stream); }));
+    h->rot_pass += 1;
+    return SC_OK;
+  }
+
   static C* AF(sc_handle* h, size_t i) { return reinterpret_cast<C*>(h->adj) + i * h->g.field; }
 
   // adjoint of one right-hand side at stage input s; aa.lw holds its adjoint
@@ -1246,6 +1322,7 @@ int init_field(sc_handle* h, int seed, int kind, double akp, double u0, double k
   SC_CUDA(cudaStreamSynchronize(h->stream));
   h->step = 0;
   h->ab2_pass = 0;
+  h->rot_pass = 0;
   return SC_OK;
 }
 
@@ -1397,6 +1474,7 @@ int sc_destroy(sc_handle* h) {
   cudaFree(h->dout);
   cudaFree(h->adj);
   cudaFree(h->cpart);
+  cudaFree(h->rot);
   if (h->own) cudaStreamDestroy(h->own);
   delete h;
   return SC_OK;
@@ -1431,6 +1509,7 @@ int sc_set_state(sc_handle* h, const void* vx, const void* vy, const void* vz) {
   SC_CUDA(cudaStreamSynchronize(h->stream));
   h->step = 0;
   h->ab2_pass = 0;
+  h->rot_pass = 0;
   return SC_OK;
 }
 
@@ -1493,6 +1572,17 @@ int sc_ab2_steps(sc_handle* h, int npasses) {
   if (!h || npasses < 0) return fail(SC_ERR_INVALID, "need a handle and npasses >= 0");
   for (int i = 0; i < npasses; ++i)
     SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2_pass(h) : Impl<double>::ab2_pass(h));
+  return check_derr(h);
+}
+
+int sc_rot_steps(sc_handle* h, int npasses, double om, double fk1, double fk2) {
+  if (!h || npasses < 0) return fail(SC_ERR_INVALID, "need a handle and npasses >= 0");
+  if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the rotating solver has no SGS model");
+  if (!std::isfinite(om) || !std::isfinite(fk1) || !std::isfinite(fk2) || fk1 < 0.0 || fk2 < fk1)
+    return fail(SC_ERR_INVALID, "need finite om and 0 <= fk1 <= fk2");
+  for (int i = 0; i < npasses; ++i)
+    SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rot_pass(h, om, fk1, fk2) : Impl<double>::rot_pass(h, om, fk1, fk2));
+  SC_CUDA(cudaGetLastError());
   return check_derr(h);
 }
 

@@ -259,6 +259,12 @@ class SpectralNS:
     def ab2_steps(self, n=1):
         _check(lib().sc_ab2_steps(self.h, n))
 
+    def rot_steps(self, n=1, om=0.0, fk1=0.0, fk2=2.5):
+        """n passes of the rotating solver's helical-wave IF-AB2
+        (spectral_rot_dns_ft.f90:146-272) at rotation rate om, forcing band
+        fk1 <= |k| < fk2 when the solver is forced."""
+        _check(lib().sc_rot_steps(self.h, n, C.c_double(om), C.c_double(fk1), C.c_double(fk2)))
+
     def set_dt(self, dt):
         _check(lib().sc_set_dt(self.h, C.c_double(dt)))
 

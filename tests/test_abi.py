@@ -39,3 +39,9 @@ def test_f77_shims_export_every_declared_symbol(specns_lib):
         lib = _lib.load_f77(prec)
         missing = [n for n in declared if not hasattr(lib, n)]
         assert missing == [], (prec, missing)
+
+
+def test_rot_steps_rejects_bad_arguments_without_gpu(specns_lib):
+    """sc_rot_steps checks its handle and arguments before any CUDA call."""
+    assert specns_lib.sc_rot_steps(None, 1, 1.0, 0.0, 2.5) == 1    # SC_ERR_INVALID
+    assert specns_lib.sc_rot_steps(None, -1, 1.0, 0.0, 2.5) == 1

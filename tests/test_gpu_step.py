@@ -336,3 +336,47 @@ def test_fused_stage_passes_long_z(specns_lib, prec, monkeypatch):
         assert rel_l2(o, ref) < TOL[prec]
     for o in outs[1:]:
         assert rel_l2(outs[0], o) < (1e-13 if prec == S.SC_FP64 else 2e-6)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_rotating_solver_matches_oracle(specns_lib, prec):
+    """Five passes of the rotating solver's helical-wave IF-AB2
+    (spectral_rot_dns_ft.f90:146-272) with band forcing 1 <= |k| < 2.5, and a
+    restart through set_state, against the oracle."""
+    n, om = 32, 5.0
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3, forced=True, eps=0.1)
+    ref, _, _ = R.rot_run(v, g, 5, om, 1.0, 2.5)
+    ref2, _, _ = R.rot_run(v, g, 2, om, 1.0, 2.5)
+    with handle(n, prec, nu=0.01, dt=2e-3, forced=1, eps=0.1) as h:
+        h.set_state(*v)
+        h.rot_steps(5, om=om, fk1=1.0, fk2=2.5)
+        out = h.get_state()
+        h.set_state(*v)
+        h.rot_steps(2, om=om, fk1=1.0, fk2=2.5)
+        out2 = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
+    assert rel_l2(out2, ref2) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_rotating_solver_beltrami_inertial_waves(specns_lib, prec):
+    """An ABC (Beltrami, curl u = u) flow has a zero Lamb vector, so the
+    rotating solver advances its helical amplitudes by the integrating factor
+    alone: after p >= 2 passes a+ = a+(0) exp(-nu (p-1) dt + 2 i kz om
+    (p-1) dt / |k|), and v = a+ h."""
+    n, om, nu, dt, npass = 16, 3.0, 0.05, 1e-2, 7
+    z, y, x = np.meshgrid(*[np.arange(n) * 2 * np.pi / n for _ in range(3)], indexing="ij")
+    A, B, Cc = 1.0, 0.7, 0.4
+    u = [A * np.sin(z) + Cc * np.cos(y), B * np.sin(x) + A * np.cos(z), Cc * np.sin(y) + B * np.cos(x)]
+    v = [R.r2c(a) / n ** 3 for a in u]
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    h = R.heliwave(kx, ky, kz, k2)
+    ap0 = sum(a * np.conj(b) for a, b in zip(v, h))
+    ph = np.exp(-nu * (npass - 1) * dt + 2j * kz[:, None, None] * om * (npass - 1) * dt / np.sqrt(k2))
+    exact = [ap0 * ph * b for b in h]
+    with handle(n, prec, nu=nu, dt=dt, forced=0) as hd:
+        hd.set_state(*v)
+        hd.rot_steps(npass, om=om)
+        out = hd.get_state()
+    assert rel_l2(out, exact) < (1e-13 if prec == S.SC_FP64 else TOL[prec])

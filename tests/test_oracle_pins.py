@@ -14,6 +14,10 @@ oracle is pinned to the known answers its own source implies:
 * symmetrize.f90 / projection.f90 / force.f90 invariants, and the energy
   budget of the right-hand side: d E/dt = eps exactly (the Lamb vector is
   orthogonal to u pointwise).
+* heliwave.f90 gives the positive-helicity basis (unit, normal to k,
+  i k x h = |k| h), and the rotating solver of spectral_rot_dns_ft.f90 turns
+  an ABC (Beltrami) flow into exact inertial waves and reduces to the
+  velocity-form IF-AB2 without rotation.
 * the committed golden fixtures reproduce.
 """
 import os
@@ -166,3 +170,56 @@ def test_golden_fixtures_reproduce():
     kcut = 2 * (n // 2) / 3
     td, mm, lm, cs2 = R.dynsmag(*v0, kx, ky, kz, R.test_filter(k2, kcut / 2), n, delta, 2 * delta, True, 0.0)
     assert rel_l2(td, list(les["tau_dyn"])) < 1e-14 and abs(cs2 - float(les["cs2"])) < 1e-14 * abs(cs2)
+
+
+def abc_flow(n, A=1.0, B=0.7, C=0.4):
+    """Arnold-Beltrami-Childress flow, curl u = u (every mode at |k| = 1)."""
+    z, y, x = np.meshgrid(*[np.arange(n) * 2 * np.pi / n for _ in range(3)], indexing="ij")
+    u = [A * np.sin(z) + C * np.cos(y), B * np.sin(x) + A * np.cos(z), C * np.sin(y) + B * np.cos(x)]
+    return [R.r2c(a) / n ** 3 for a in u]
+
+
+def test_heliwave_is_the_positive_helical_basis():
+    """heliwave.f90:57-96 gives unit vectors normal to k with h . h = 0 and
+    i k x h = |k| h at every mode but the mean mode, where h = 0; so
+    v -> (v . conj h, v . h) -> a+ h + a- conj(h) is the identity on
+    solenoidal fields."""
+    n = 16
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    h = R.heliwave(kx, ky, kz, k2)
+    m = np.ones(k2.shape, bool)
+    m[0, 0, 0] = False
+    kdoth = kx[None, None, :] * h[0] + ky[None, :, None] * h[1] + kz[:, None, None] * h[2]
+    assert np.abs(kdoth).max() < 1e-14
+    assert np.abs(sum((a * np.conj(a)).real for a in h)[m] - 1.0).max() < 1e-14
+    assert np.abs(sum(a * a for a in h)).max() < 1e-14
+    curl = R.vorticity(*h, kx, ky, kz)
+    assert max(np.abs(c - np.sqrt(k2) * a)[m].max() for c, a in zip(curl, h)) < 1e-13
+    assert all(a[0, 0, 0] == 0 for a in h)
+    v = solenoidal_init(n)
+    ap = sum(a * np.conj(b) for a, b in zip(v, h))
+    am = sum(a * b for a, b in zip(v, h))
+    assert rel_l2([ap * b + am * np.conj(b) for b in h], v) < 1e-14
+
+
+def test_rotating_solver_known_answers():
+    """spectral_rot_dns_ft.f90's helical-wave IF-AB2: (a) an ABC flow (zero
+    Lamb vector) turns into exact inertial waves, a+(t) = a+(0)
+    exp(-nu t + 2 i kz om t / |k|); (b) without rotation and forcing it is
+    the velocity-form IF-AB2 of specdns-forced-omp-ft.f90:224-287;
+    (c) the passes advance time by dt/2, dt/2, then dt."""
+    n, om, nu, dt = 16, 3.0, 0.05, 1e-2
+    v = abc_flow(n)
+    kx, ky, kz, k2 = R.wavenumber(n, n, n)
+    assert max(np.abs(a - b).max() for a, b in zip(R.vorticity(*v, kx, ky, kz), v)) < 1e-15
+    h = R.heliwave(kx, ky, kz, k2)
+    ap0 = sum(a * np.conj(b) for a, b in zip(v, h))
+    g = R.Grid(R.Params(nx=n, nu=nu, dt=dt, forced=False))
+    for npass in (2, 3, 7):
+        out, _, t = R.rot_run(v, g, npass, om)
+        assert abs(t - (npass - 1) * dt) < 1e-15
+        ph = np.exp(-nu * t + 2j * kz[:, None, None] * om * t / np.sqrt(k2))
+        assert rel_l2(out, [ap0 * ph * b for b in h]) < 1e-14
+    v = solenoidal_init(n)
+    g = R.Grid(R.Params(nx=n, nu=0.01, dt=2e-3, forced=False))
+    assert rel_l2(R.rot_run(v, g, 6, 0.0)[0], R.ab2_run(v, g, 6)[0]) < 1e-14
