@@ -124,6 +124,28 @@ int sc_rk4_steps(sc_handle* h, int nsteps);
  * the AB2 solver's own: no symmetrize (specdns-forced-omp-ft.f90:180-221). */
 int sc_ab2_steps(sc_handle* h, int npasses);
 
+/* One pass of the variable-step IF-AB2 of spectral_dns.f90:173-290 (and of
+ * spectral_les.f90:199-316 with an SGS handle) with step dt.  Pass 0: an
+ * integrating-factor Euler step; pass 1: a restart from the initial field
+ * over dto + dt with the weights of dt/dto; later passes: AB2 weighted by
+ * dt/dto with the previous right-hand side.  Its RHS has no symmetrize
+ * (spectral_dns.f90:173-208).  After each pass v = 0 at k >= kcut and at the
+ * mean mode; spectral_dns.f90 cuts at k >= nx/2 (set kcut = nx/2),
+ * spectral_les.f90 at its kcut.  A dynsmag handle refreshes its coefficient
+ * on passes 0, 1, 11, 21, ... (spectral_les.f90:140,205-208).  The handle
+ * keeps the pass count and dto (two extra groups of three fields);
+ * sc_set_state and sc_init_field restart at pass 0. */
+int sc_ab2v_pass(sc_handle* h, double dt);
+/* The variable-step AB2's pass count and previous step dto (0 before the
+ * first pass). */
+int sc_ab2v_state(sc_handle* h, int* pass, double* dto);
+/* The solvers' step rule, spectral_dns.f90:212-217: dt = min(betadx/umax,
+ * 3 dto), cut to land on the output time twrite (halved when the remainder
+ * would be under 0.2 dt).  Before the first pass the reference's dto is the
+ * run's end time timemax (:111).  umax is theirs too: 3.5 sqrt(2E) every
+ * ieout steps (:141; E from sc_diagnostics).  No GPU needed. */
+int sc_ab2v_dt(double betadx, double umax, double dto, double time, double twrite, double* dt);
+
 /* npasses passes of the rotating solver's loop, spectral_rot_dns_ft.f90:
  * 146-272 (replaces that program's time loop).  The state is the pair of
  * helical amplitudes a+ = v . conj(h), a- = v . h (heliwave.f90:57-96), each

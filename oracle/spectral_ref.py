@@ -396,12 +396,13 @@ class Grid:
         self.g = test_filter(self.k2, p.k_test)
 
 
-def ratesdudt(v, grid: Grid, sgs_state=None):
+def ratesdudt(v, grid: Grid, sgs_state=None, symmetrize=True):
     """Right-hand side of dns-deform.f90:259-288 (plus the optional SGS term
     of spectral_les.f90:204-234, applied before symmetrize/projection).
 
     v: tuple of three spectral fields.  sgs_state: dict with keys 'cs2',
-    'update' for dynsmag; receives 'mm', 'lm', 'cs2' back.
+    'update' for dynsmag; receives 'mm', 'lm', 'cs2' back.  symmetrize=False
+    leaves out :281-283, as the variable-step solvers do.
     """
     p = grid.p
     kx, ky, kz, k2 = grid.kx, grid.ky, grid.kz, grid.k2
@@ -422,7 +423,8 @@ def ratesdudt(v, grid: Grid, sgs_state=None):
                 st["mm"], st["lm"] = mm, lm
         dx, dy, dz = sgs_divergence(tau, kx, ky, kz)
         wx, wy, wz = wx + dx, wy + dy, wz + dz
-    wx, wy, wz = symmetrize3d(wx), symmetrize3d(wy), symmetrize3d(wz)  # :281-283
+    if symmetrize:
+        wx, wy, wz = symmetrize3d(wx), symmetrize3d(wy), symmetrize3d(wz)  # :281-283
     wx, wy, wz = projection(wx, wy, wz, kx, ky, kz)                    # :286
     if p.mask == "rhs_and_step":
         m = k2 >= p.kcut * p.kcut
@@ -535,6 +537,90 @@ def ab2_run(v, grid: Grid, nhalf_steps):
         m = grid.k2 >= (2.0 * (p.nx // 2) / 3.0) ** 2
         v = [np.where(m, 0.0, a) for a in v]                         # :283-287
     return tuple(v), t
+
+
+# --------------------------------------------------------------------------
+# variable-step IF-AB2 (spectral_dns.f90, spectral_les.f90)
+# --------------------------------------------------------------------------
+def ab2v_rhs(v, grid: Grid, sgs_state=None):
+    """Right-hand side of the variable-step solvers: spectral_dns.f90:173-208
+    (vorticity, Lamb vector, forcing :189-205, projection :208) and, with an
+    SGS model, spectral_les.f90:199-238 (dynsmag :205-207, forcing :214-230,
+    SGS divergence :232-234, projection :237-238): ratesdudt without
+    symmetrize."""
+    return ratesdudt(v, grid, sgs_state, symmetrize=False)
+
+
+def ab2v_dt(betadx, umax, dto, time, twrite):
+    """Step of spectral_dns.f90:212-217 (spectral_les.f90:242-247): the CFL
+    step betadx / umax, at most 3 dto, shortened to land on the next output
+    time twrite (halved when it would leave a sliver under 0.2 dt)."""
+    dt = min(betadx / umax, 3.0 * dto)
+    if dt >= twrite - time:
+        dt = twrite - time
+    elif twrite - time - dt < 0.2 * dt:
+        dt = 0.5 * (twrite - time)
+    return dt
+
+
+def ab2v_weights(ipass, dt, dto):
+    """(S, ek, delta) of spectral_dns.f90:231-235 (pass 1) and :253-257
+    (passes >= 2); pass 0 has none."""
+    dtt = dt / dto
+    if ipass == 1:
+        return 0.5 * (1.0 + dtt * dtt), 0.5 * (1.0 - dtt * dtt), 0.5 * dto * (1.0 + dtt) ** 2
+    return (1.0 + 0.5 * dtt) * dt, -0.5 * dtt * dt, 0.0
+
+
+def ab2v_run(v, grid: Grid, dts, sgs_state=None, trace=None):
+    """Passes of the variable-step IF-AB2 of spectral_dns.f90:210-290
+    (spectral_les.f90:240-316) with steps dts[p]: pass 0 an integrating-factor
+    Euler step (:220-228), pass 1 a restart from the initial field over
+    dt0 + dt1 weighted by dt1/dt0 (:230-250), later passes AB2 weighted by
+    dt/dto with the previous right-hand side (:252-275); after each pass
+    v = 0 at k2 >= kcut^2 and at the mean mode (:281-290; spectral_dns.f90
+    cuts at lx^2, spectral_les.f90 at kcut^2: the grid's kcut).  With a
+    dynsmag grid the coefficient is refreshed on passes 0, 1, 11, 21, ...
+    (update is .true. at first and then mod(istep, 10) == 0 of the previous
+    pass, spectral_les.f90:140,205-208).  Returns (v, time, dto); with a list
+    `trace`, each pass appends (its right-hand side, v after it)."""
+    p = grid.p
+    k2 = grid.k2
+    v0 = [np.array(a, dtype=np.complex128) for a in v]             # :103-105
+    v = list(v0)
+    o = o0 = None
+    t, dto = 0.0, None
+    if p.sgs == "dynsmag" and sgs_state is None:
+        sgs_state = {"cs2": 0.0, "update": True}
+    for ip, dt in enumerate(dts):
+        if p.sgs == "dynsmag":
+            sgs_state["update"] = ip == 0 or (ip - 1) % p.dyn_every == 0
+        w = ab2v_rhs(v, grid, sgs_state)
+        e1 = np.exp(-p.nu * k2 * dt)
+        if ip == 0:
+            v = [(a + dt * b) * e1 for a, b in zip(v, w)]
+            dto = dt
+            o0 = w                                                     # :228 (written out)
+        elif ip == 1:
+            S, ek, dl = ab2v_weights(1, dt, dto)
+            e0 = np.exp(-p.nu * k2 * dto)
+            v = [(S * a0 * e0 + ek * a + dl * b) * e1 for a0, a, b in zip(v0, v, w)]
+            dto = dt + dto
+            o = o0                                                     # :250 (read back)
+        else:
+            S, ek, _ = ab2v_weights(ip, dt, dto)
+            e0 = np.exp(-p.nu * k2 * dto)
+            v = [(a + S * b + ek * c * e0) * e1 for a, b, c in zip(v, w, o)]
+            o = w
+            dto = dt
+        t += dt
+        m = k2 >= p.kcut * p.kcut
+        v = [np.where(m, 0.0, a) for a in v]
+        for a in v:
+            a[0, 0, 0] = 0.0
+        if trace is not None:
+            trace.append((w, tuple(v)))
+    return tuple(v), t, dto
 
 
 # --------------------------------------------------------------------------

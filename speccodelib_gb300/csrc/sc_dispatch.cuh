@@ -438,6 +438,14 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     return cudaGetLastError();                                                                   \
   }                                                                                              \
   template <>                                                                                    \
+  cudaError_t sc::Launch<T>::ab2v(const Ab2vArgs<T>& aa, const Geom& g, cudaStream_t s) {        \
+    long long n = (long long)g.ny * g.nz * g.nxh;                                                \
+    int nb = (int)((n + 255) / 256);                                                             \
+    if (nb > 152 * 16) nb = 152 * 16;                                                            \
+    sc::ab2v_update_kernel<T><<<nb, 256, 0, s>>>(aa, g);                                         \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
   cudaError_t sc::Launch<T>::moments(const C2<T>* d, const Geom& g, double* partial, int nblocks, \
                                      double* out, cudaStream_t s) {                              \
     const long long rows = (long long)g.ny * g.nz;                                               \

@@ -16,6 +16,7 @@ template <typename T> struct XArgs;
 template <typename T> struct DiagArgs;
 template <typename T> struct SpecOpArgs;
 template <typename T> struct RotArgs;
+template <typename T> struct Ab2vArgs;
 template <typename T> struct StrainArgs;
 template <typename T> struct PhysArgs;
 template <typename T> struct TmaPass;
@@ -41,6 +42,8 @@ template <typename T> struct Launch {
   static cudaError_t specop(const SpecOpArgs<T>& oa, const Geom& g, cudaStream_t s);
   // helical-wave AB2 update of the rotating solver at every mode
   static cudaError_t rot(const RotArgs<T>& ra, const Geom& g, cudaStream_t s);
+  // variable-step IF-AB2 update at every mode
+  static cudaError_t ab2v(const Ab2vArgs<T>& aa, const Geom& g, cudaStream_t s);
   static cudaError_t strain(const StrainArgs<T>& sa, const Geom& g, cudaStream_t s);
   // post-processing of physical packed rows: sums of d^2, d^3 into out[0..1]
   // (partial holds 2 doubles per block, nblocks at most); enstrophy density

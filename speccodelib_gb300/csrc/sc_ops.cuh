@@ -9,6 +9,7 @@
 #pragma once
 #include "sc_passes.cuh"
 #include "sc_rot.cuh"
+#include "sc_ab2v.cuh"
 
 namespace sc {
 
@@ -313,6 +314,59 @@ __global__ void __launch_bounds__(256) rot_update_kernel(RotArgs<T> ra, Geom g) 
     }
     ra.a[0][idx] = mk<C>(ap.re, ap.im);
     ra.a[1][idx] = mk<C>(am.re, am.im);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// variable-step IF-AB2 update (ab2v_point, sc_ab2v.cuh)
+// ---------------------------------------------------------------------------
+template <typename T> struct Ab2vArgs {
+  int pass;              // 0: Euler step, 1: restart from v0, >= 2: AB2
+  C2<T>* v[3];           // velocity, rewritten every pass
+  const C2<T>* w[3];     // right-hand side of this pass
+  C2<T>* o[3];           // previous right-hand side (written at pass 0 and >= 2)
+  C2<T>* v0[3];          // initial field (written at pass 0, read at pass 1)
+  double nu, dt, dto;    // viscosity, this step, the previous step
+  double s, ek, dl;      // the pass's weights
+  double kcut2;          // v = 0 where k2 >= kcut2 and at the mean mode
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) ab2v_update_kernel(Ab2vArgs<T> aa, Geom g) {
+  using C = C2<T>;
+  const long long rows = (long long)g.ny * g.nz;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tstride = (long long)gridDim.x * blockDim.x;
+  const int kc_b = k2_lt(aa.kcut2);
+  const T nu = (T)aa.nu, dt = (T)aa.dt, dto = (T)aa.dto, s = (T)aa.s, ek = (T)aa.ek, dl = (T)aa.dl;
+  const int pass = aa.pass;
+  for (Walk3 it(t0, tstride, rows * g.nxh, g.nxh, g.ny); it.ok(); it.next()) {
+    const long long idx = it.row() * g.nxp + it.ix;
+    const int ky = wavenum(it.iy, g.ny), kz = wavenum(it.iz, g.nz);
+    const int k2 = it.ix * it.ix + ky * ky + kz * kz;
+    Cx<T> v[3], w[3], o[3], v0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const C vc = aa.v[c][idx], wc = aa.w[c][idx];
+      v[c] = cx(vc.x, vc.y);
+      w[c] = cx(wc.x, wc.y);
+      o[c] = v0[c] = cx(T(0), T(0));
+      if (pass >= 2) {
+        const C oc = aa.o[c][idx];
+        o[c] = cx(oc.x, oc.y);
+      }
+      if (pass == 1) {
+        const C zc = aa.v0[c][idx];
+        v0[c] = cx(zc.x, zc.y);
+      }
+    }
+    ab2v_point<T>(pass, k2, k2 >= kc_b || k2 == 0, nu, dt, dto, s, ek, dl, v, w, o, v0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      aa.v[c][idx] = mk<C>(v[c].re, v[c].im);
+      if (pass != 1) aa.o[c][idx] = mk<C>(o[c].re, o[c].im);
+      if (pass == 0) aa.v0[c][idx] = mk<C>(v0[c].re, v0[c].im);
+    }
   }
 }
 

@@ -11,27 +11,13 @@
 // (:239-256); the velocity is rebuilt as a+ h + a- conj(h) and truncated at
 // k^2 >= kcut^2 (:261-270).  The amplitudes themselves are never truncated.
 //
-// Everything here is plain scalar arithmetic marked __host__ __device__, so
-// the same code runs in rot_update_kernel and in host-side checks.
+// Everything here is plain scalar arithmetic marked __host__ __device__
+// (sc_cx.cuh), so the same code runs in rot_update_kernel and in host-side
+// checks.
 #pragma once
-#include <math.h>
+#include "sc_cx.cuh"
 
 namespace sc {
-
-template <typename T> struct Cx { T re, im; };
-
-template <typename T> __host__ __device__ inline Cx<T> cx(T re, T im) { Cx<T> r; r.re = re; r.im = im; return r; }
-template <typename T> __host__ __device__ inline Cx<T> cx_add(Cx<T> a, Cx<T> b) { return cx(a.re + b.re, a.im + b.im); }
-template <typename T> __host__ __device__ inline Cx<T> cx_sub(Cx<T> a, Cx<T> b) { return cx(a.re - b.re, a.im - b.im); }
-template <typename T> __host__ __device__ inline Cx<T> cx_mul(Cx<T> a, Cx<T> b) {
-  return cx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
-}
-// a * conj(b)
-template <typename T> __host__ __device__ inline Cx<T> cx_mulc(Cx<T> a, Cx<T> b) {
-  return cx(a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im);
-}
-template <typename T> __host__ __device__ inline Cx<T> cx_scale(Cx<T> a, T s) { return cx(a.re * s, a.im * s); }
-template <typename T> __host__ __device__ inline Cx<T> cx_conj(Cx<T> a) { return cx(a.re, -a.im); }
 
 // h+ at integer wavenumber (kx, ky, kz), heliwave.f90:73-91.  Rows with
 // ky = kz = 0 (:73-81) have k2d = max(|kx|, smallest) and reduce to

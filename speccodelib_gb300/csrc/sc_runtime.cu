@@ -113,8 +113,11 @@ struct sc_handle {
   double* cpart = nullptr;        // forcing-adjoint band sums
   long long step = 0;             // RK4 steps taken (dynamic-coefficient cadence)
   int ab2_pass = 0;
-  void* rot = nullptr;            // rotating solver: a+, a-, previous RHS (3); allocated on first use
+  void* aux = nullptr;            // fields of the rotating and variable-step AB2 steppers (allocated on first use)
+  int aux_fields = 0;
   int rot_pass = 0;
+  int ab2v_pass = 0;
+  double ab2v_dto = 0.0;          // previous step of the variable-step AB2 (dto)
   // profiling
   bool prof = false;
   struct Pend { std::string name; cudaEvent_t a, b; };
@@ -698,6 +701,64 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
+  // One pass of the variable-step IF-AB2 of spectral_dns.f90:173-290
+  // (spectral_les.f90:199-316 with an SGS model) with step dt: the
+  // right-hand side without symmetrize (the same passes as sc_rhs, into the
+  // S_A slots), then ab2v_update_kernel.  The previous right-hand side and
+  // the initial field live in h->aux; h->ab2v_dto is the reference's dto.
+  static int ab2v_pass(sc_handle* h, double dt) {
+    auto* g = &h->g;
+    SC_TRY(ensure_aux(h, 6));
+    C* ab = reinterpret_cast<C*>(h->aux);
+    const int pass = h->ab2v_pass;
+    sc::StageArgs<T> st = stage_args(h);
+    st.mode = sc::SM_RHS;
+    st.symmetrize = 0;
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    // dynsmag's update flag is .true. at first, then mod(istep, 10) == 0 of
+    // the previous pass: refreshes on passes 0, 1, 11, 21, ...
+    // (spectral_les.f90:140,205-208)
+    if (h->p.sgs == SC_SGS_DYNSMAG && (pass == 0 || (pass - 1) % h->p.dyn_every == 0)) SC_TRY(dyn_update(h, vin));
+    SC_TRY(rhs_pipeline(h, vin, st));
+    sc::Ab2vArgs<T> aa{};
+    aa.pass = pass < 2 ? pass : 2;
+    for (int c = 0; c < 3; ++c) {
+      aa.v[c] = F(h, S_V + c);
+      aa.w[c] = F(h, S_A + c);
+      aa.o[c] = ab + (size_t)c * g->field;
+      aa.v0[c] = ab + (size_t)(3 + c) * g->field;
+    }
+    aa.nu = h->p.nu;
+    aa.dt = dt;
+    aa.dto = h->ab2v_dto;
+    aa.kcut2 = kcut2(h);
+    sc::ab2v_weights(pass, dt, h->ab2v_dto, aa.s, aa.ek, aa.dl);
+    SC_TRY(launch(h, "ab2v_update", [&] { return L::ab2v(aa, *g, h->stream); }));
+    h->ab2v_dto = pass == 1 ? dt + h->ab2v_dto : dt;   // :227, :249, :275
+    h->ab2v_pass += 1;
+    return SC_OK;
+  }
+
+  // At least n fields in h->aux (zero-filled when (re)allocated).
+  static int ensure_aux(sc_handle* h, int n) {
+    if (h->aux && h->aux_fields >= n) return SC_OK;
+    if (h->aux) {
+      SC_CUDA(cudaStreamSynchronize(h->stream));
+      cudaFree(h->aux);
+      h->aux = nullptr;
+      h->aux_fields = 0;
+    }
+    const size_t bytes = (size_t)n * h->csize * h->g.field;
+    if (cudaMalloc(&h->aux, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      h->aux = nullptr;
+      return fail(SC_ERR_NOMEM, "cannot allocate %zu bytes of stepper fields", bytes);
+    }
+    h->aux_fields = n;
+    SC_CUDA(cudaMemsetAsync(h->aux, 0, bytes, h->stream));
+    return SC_OK;
+  }
+
   // force_rot.f90:3-29 on w from the velocity v: band fk12 <= k2 < fk22
   // (squared bounds), a = eps / (2 kinet + tiny), kinet the 1/2-weighted band
   // energy as the difference of two FP64 sums; tiny is mytiny of the build's
@@ -725,19 +786,11 @@ template <typename T> struct Impl {
   // the Lamb vector of v (TMA-fed passes, stored raw into the S_A slots),
   // force_rot on the band fk1^2 <= k2 < fk2^2 when forced, symmetrize,
   // projection, then the helical-wave AB2 update (rot_update_kernel).  The
-  // amplitudes a+, a- and the previous right-hand side live in h->rot.
+  // amplitudes a+, a- and the previous right-hand side live in h->aux.
   static int rot_pass(sc_handle* h, double om, double fk1, double fk2) {
     auto* g = &h->g;
-    if (!h->rot) {
-      const size_t bytes = 5 * h->csize * g->field;
-      if (cudaMalloc(&h->rot, bytes) != cudaSuccess) {
-        cudaGetLastError();
-        h->rot = nullptr;
-        return fail(SC_ERR_NOMEM, "cannot allocate %zu bytes for the rotating solver", bytes);
-      }
-      SC_CUDA(cudaMemsetAsync(h->rot, 0, bytes, h->stream));
-    }
-    C* rb = reinterpret_cast<C*>(h->rot);
+    SC_TRY(ensure_aux(h, 5));
+    C* rb = reinterpret_cast<C*>(h->aux);
     sc::StageArgs<T> st = stage_args(h);
     st.mode = sc::SM_LAMB;
     st.forced = 0;
@@ -1323,6 +1376,7 @@ int init_field(sc_handle* h, int seed, int kind, double akp, double u0, double k
   h->step = 0;
   h->ab2_pass = 0;
   h->rot_pass = 0;
+  h->ab2v_pass = 0;
   return SC_OK;
 }
 
@@ -1474,7 +1528,7 @@ int sc_destroy(sc_handle* h) {
   cudaFree(h->dout);
   cudaFree(h->adj);
   cudaFree(h->cpart);
-  cudaFree(h->rot);
+  cudaFree(h->aux);
   if (h->own) cudaStreamDestroy(h->own);
   delete h;
   return SC_OK;
@@ -1510,6 +1564,7 @@ int sc_set_state(sc_handle* h, const void* vx, const void* vy, const void* vz) {
   h->step = 0;
   h->ab2_pass = 0;
   h->rot_pass = 0;
+  h->ab2v_pass = 0;
   return SC_OK;
 }
 
@@ -1573,6 +1628,32 @@ int sc_ab2_steps(sc_handle* h, int npasses) {
   for (int i = 0; i < npasses; ++i)
     SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2_pass(h) : Impl<double>::ab2_pass(h));
   return check_derr(h);
+}
+
+int sc_ab2v_pass(sc_handle* h, double dt) {
+  if (!h || !std::isfinite(dt) || !(dt > 0.0)) return fail(SC_ERR_INVALID, "need a handle and a finite dt > 0");
+  SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2v_pass(h, dt) : Impl<double>::ab2v_pass(h, dt));
+  SC_CUDA(cudaGetLastError());
+  return check_derr(h);
+}
+
+int sc_ab2v_state(sc_handle* h, int* pass, double* dto) {
+  if (!h || !pass || !dto) return fail(SC_ERR_INVALID, "null argument");
+  *pass = h->ab2v_pass;
+  *dto = h->ab2v_dto;
+  return SC_OK;
+}
+
+int sc_ab2v_dt(double betadx, double umax, double dto, double time, double twrite, double* dt) {
+  if (!dt) return fail(SC_ERR_INVALID, "null dt");
+  if (!(umax > 0.0) || !(dto > 0.0) || !std::isfinite(betadx) || !std::isfinite(time) || !std::isfinite(twrite))
+    return fail(SC_ERR_INVALID, "need umax > 0, dto > 0 and finite betadx, time, twrite");
+  // spectral_dns.f90:212-217
+  double d = std::min(betadx / umax, 3.0 * dto);
+  if (d >= twrite - time) d = twrite - time;
+  else if (twrite - time - d < 0.2 * d) d = 0.5 * (twrite - time);
+  *dt = d;
+  return SC_OK;
 }
 
 int sc_rot_steps(sc_handle* h, int npasses, double om, double fk1, double fk2) {

@@ -180,6 +180,14 @@ def dynsmag(ux, uy, uz, k_test, delta, delta_test, update, cs2=0.0):
 # ---------------------------------------------------------------------------
 # handle API
 # ---------------------------------------------------------------------------
+def ab2v_dt(betadx, umax, dto, time, twrite):
+    """The variable-step solvers' step rule (spectral_dns.f90:212-217)."""
+    d = C.c_double()
+    _check(lib().sc_ab2v_dt(C.c_double(betadx), C.c_double(umax), C.c_double(dto), C.c_double(time),
+                            C.c_double(twrite), C.byref(d)))
+    return d.value
+
+
 def default_params(n, precision=SC_FP32, **kw):
     p = Params()
     _check(lib().sc_default_params(C.byref(p), n, precision))
@@ -258,6 +266,16 @@ class SpectralNS:
 
     def ab2_steps(self, n=1):
         _check(lib().sc_ab2_steps(self.h, n))
+
+    def ab2v_pass(self, dt):
+        """One pass of the variable-step IF-AB2 (spectral_dns.f90:210-290)."""
+        _check(lib().sc_ab2v_pass(self.h, C.c_double(dt)))
+
+    def ab2v_state(self):
+        """(pass count, previous step dto) of the variable-step IF-AB2."""
+        p, d = C.c_int(), C.c_double()
+        _check(lib().sc_ab2v_state(self.h, C.byref(p), C.byref(d)))
+        return p.value, d.value
 
     def rot_steps(self, n=1, om=0.0, fk1=0.0, fk2=2.5):
         """n passes of the rotating solver's helical-wave IF-AB2

@@ -45,3 +45,23 @@ def test_rot_steps_rejects_bad_arguments_without_gpu(specns_lib):
     """sc_rot_steps checks its handle and arguments before any CUDA call."""
     assert specns_lib.sc_rot_steps(None, 1, 1.0, 0.0, 2.5) == 1    # SC_ERR_INVALID
     assert specns_lib.sc_rot_steps(None, -1, 1.0, 0.0, 2.5) == 1
+
+
+def test_ab2v_step_rule_matches_oracle(specns_lib):
+    """sc_ab2v_dt (host code, no GPU) is the oracle's step rule of
+    spectral_dns.f90:212-217 on a sweep that crosses all three branches, and
+    the variable-step entry points reject bad arguments before any CUDA call."""
+    import numpy as np
+    import speccodelib_gb300 as s
+    from oracle import spectral_ref as R
+    rng = np.random.default_rng(3)
+    for _ in range(2000):
+        betadx, umax = rng.uniform(0.01, 0.5), rng.uniform(0.5, 5.0)
+        dto, time = rng.uniform(1e-3, 0.2), rng.uniform(0.0, 1.0)
+        twrite = time + rng.uniform(1e-4, 0.3)
+        assert s.ab2v_dt(betadx, umax, dto, time, twrite) == R.ab2v_dt(betadx, umax, dto, time, twrite)
+    d = ctypes.c_double()
+    assert specns_lib.sc_ab2v_dt(0.1, 0.0, 1.0, 0.0, 1.0, ctypes.byref(d)) == 1
+    assert specns_lib.sc_ab2v_pass(None, 1e-3) == 1
+    p = ctypes.c_int()
+    assert specns_lib.sc_ab2v_state(None, ctypes.byref(p), ctypes.byref(d)) == 1

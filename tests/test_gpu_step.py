@@ -380,3 +380,52 @@ def test_rotating_solver_beltrami_inertial_waves(specns_lib, prec):
         hd.rot_steps(npass, om=om)
         out = hd.get_state()
     assert rel_l2(out, exact) < (1e-13 if prec == S.SC_FP64 else TOL[prec])
+
+
+STEPS_V = [2e-3, 2.6e-3, 1.4e-3, 2.2e-3, 1.8e-3, 2.4e-3]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_variable_step_ab2_matches_oracle(specns_lib, prec):
+    """Passes of spectral_dns.f90's variable-step IF-AB2 on an uneven step
+    sequence (its cut k >= nx/2), a restart through set_state, and the
+    pass count / dto bookkeeping, against the oracle."""
+    n = 32
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, forced=True, eps=0.1, kcut=n // 2)
+    ref, t, dto = R.ab2v_run(v, g, STEPS_V)
+    ref2, _, _ = R.ab2v_run(v, g, STEPS_V[:2])
+    with handle(n, prec, nu=0.01, forced=1, eps=0.1, kcut=n // 2) as h:
+        h.set_state(*v)
+        for dt in STEPS_V:
+            h.ab2v_pass(dt)
+        out = h.get_state()
+        npass, hdto = h.ab2v_state()
+        h.set_state(*v)
+        assert h.ab2v_state()[0] == 0
+        for dt in STEPS_V[:2]:
+            h.ab2v_pass(dt)
+        out2 = h.get_state()
+    assert npass == len(STEPS_V) and abs(hdto - dto) < 1e-15
+    assert rel_l2(out, ref) < TOL[prec]
+    assert rel_l2(out2, ref2) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("model", ["smag", "dynsmag"])
+def test_variable_step_ab2_les_matches_oracle(specns_lib, prec, model):
+    """spectral_les.f90:199-316: the variable-step IF-AB2 with the SGS
+    divergence in its right-hand side; with dynsmag the coefficient is
+    refreshed on passes 0, 1 and 11 of 12 (spectral_les.f90:140,205-208)."""
+    n = 32
+    v = solenoidal_init(n)
+    sgs = {"smag": S.SC_SGS_SMAG, "dynsmag": S.SC_SGS_DYNSMAG}[model]
+    steps = (STEPS_V * 2)[:12] if model == "dynsmag" else STEPS_V
+    g = oracle_grid(n, nu=1e-3, forced=True, eps=0.1, sgs=model, c1=0.0289)
+    ref, _, _ = R.ab2v_run(v, g, steps)
+    with handle(n, prec, nu=1e-3, forced=1, eps=0.1, sgs=sgs, c1=0.0289) as h:
+        h.set_state(*v)
+        for dt in steps:
+            h.ab2v_pass(dt)
+        out = h.get_state()
+    assert rel_l2(out, ref) < (1e-11 if prec == S.SC_FP64 else 2e-5)

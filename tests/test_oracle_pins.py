@@ -223,3 +223,34 @@ def test_rotating_solver_known_answers():
     v = solenoidal_init(n)
     g = R.Grid(R.Params(nx=n, nu=0.01, dt=2e-3, forced=False))
     assert rel_l2(R.rot_run(v, g, 6, 0.0)[0], R.ab2_run(v, g, 6)[0]) < 1e-14
+
+
+def test_variable_step_ab2_known_answers():
+    """spectral_dns.f90's variable-step IF-AB2: (a) the Roberts flow (zero
+    Lamb vector) decays as exp(-2 nu t) exactly over an uneven step
+    sequence; (b) on a forced turbulent field the error against a fine-step
+    IF-AB2 falls by ~4 per halving of an uneven step sequence (second order,
+    which pins the restart and AB2 weights); (c) the step rule of
+    spectral_dns.f90:212-217 lands on the output time."""
+    n = 16
+    v = roberts(n)
+    g = R.Grid(R.Params(nx=n, nu=0.05, forced=False))
+    out, t, dto = R.ab2v_run(v, g, [0.01, 0.013, 0.007, 0.011, 0.009, 0.012])
+    assert abs(t - 0.062) < 1e-15 and dto == 0.012
+    assert rel_l2(out, [a * np.exp(-2 * 0.05 * t) for a in v]) < 1e-14
+    v = solenoidal_init(n)
+    T = 0.2
+    g = R.Grid(R.Params(nx=n, nu=0.02, dt=T / 800, forced=True))
+    ref, _ = R.ab2_run(v, g, 801)
+    base = np.array([1.0, 1.3, 0.7, 1.1, 0.9, 1.2, 0.8, 1.0])
+    errs = []
+    for m in (2, 4, 8):
+        d = np.tile(base, m)
+        out, t, _ = R.ab2v_run(v, g, list(d * T / d.sum()))
+        assert abs(t - T) < 1e-12
+        errs.append(rel_l2(out, ref))
+    assert 3.5 < errs[0] / errs[1] < 4.6 and 3.5 < errs[1] / errs[2] < 4.6
+    assert R.ab2v_dt(0.1, 2.0, 1.0, 0.0, 1.0) == 0.05
+    assert R.ab2v_dt(0.1, 2.0, 1.0, 0.96, 1.0) == pytest.approx(0.04)
+    assert R.ab2v_dt(0.1, 2.0, 1.0, 0.945, 1.0) == pytest.approx(0.0275)
+    assert R.ab2v_dt(0.1, 2.0, 0.01, 0.0, 1.0) == 0.03
