@@ -160,6 +160,24 @@ int sc_ab2v_dt(double betadx, double umax, double dto, double time, double twrit
  * sequence at pass 0.  Handles with sgs != SC_SGS_NONE are rejected. */
 int sc_rot_steps(sc_handle* h, int npasses, double om, double fk1, double fk2);
 
+/* The passive scalar phi of the rotating scalar solver (reference layout,
+ * host or device pointer).  Setting it restarts the rotating passes at 0;
+ * before the first set it is zero. */
+int sc_set_scalar(sc_handle* h, const void* phi);
+int sc_get_scalar(sc_handle* h, void* phi);
+/* npasses passes of the rotating solver with a passive scalar,
+ * spectral_rot_dns_scalar_ft.f90:203-291 (that program does not compile as
+ * written: its kx, ky, kz are declared rank 3 at :20 and allocated rank 1 at
+ * :84; this is its evident intent with 1D wavenumbers).  Per pass: Lamb
+ * vector and wphi = convecphi_dns; force_rot called with fk1, fk2 as its
+ * squared bounds (band fk1 <= k^2 < fk2), as :213 does; when scalarforced,
+ * forcephi_rot on fk1^2 <= k^2 < fk2^2 with epsphi; dealiasing of w and wphi;
+ * projection; the helical AB2 of sc_rot_steps for v (not truncated after)
+ * and the same schedule for phi with exp(-nu k^2 dt / pr).  Handles with
+ * sgs != SC_SGS_NONE are rejected. */
+int sc_rot_scalar_steps(sc_handle* h, int npasses, double om, double fk1, double fk2, double pr, int scalarforced,
+                        double epsphi);
+
 /* Discrete adjoint of nsteps IF-RK4 steps (DNS right-hand side) for
  * J = sum over shells kmin..kmax (floor(|k| + 1/2)) of k^2 q(k) at the final
  * time (q = 1/2-weighted |v|^2, the shell enstrophy).  Writes J and

@@ -730,6 +730,86 @@ def rot_run(v, grid: Grid, npasses, om, fk1=0.0, fk2=2.5, trace=None):
     return tuple(v), (ap, am), t
 
 
+def forcephi_rot(phi, wphi, k2, fk1, fk2, epsphi):
+    """forcephi_rot.f90:1-27: wphi += a phi on fk1^2 <= k2 < fk2^2,
+    a = epsphi / (2 kinet), kinet the 1/2-weighted band variance of phi."""
+    m = (k2 < fk2 * fk2) & (k2 >= fk1 * fk1)
+    tmp = np.where(m, (phi * np.conj(phi)).real, 0.0)
+    tmp[:, :, 0] *= 0.5
+    a = epsphi / (2.0 * float(np.sum(tmp)))
+    return np.where(m, wphi + a * phi, wphi)
+
+
+def rot_scalar_run(v, phi, grid: Grid, npasses, om, fk1, fk2, pr, scalarforced=False, epsphi=0.0,
+                   trace=None):
+    """`npasses` passes of the rotating solver with a passive scalar,
+    spectral_rot_dns_scalar_ft.f90:203-291 (the program as written does not
+    compile: :20 declares kx, ky, kz rank 3 and :84 allocates them rank 1;
+    this follows its evident intent with the 1D wavenumbers of
+    spectral_rot_dns_ft.f90).  Per pass: Lamb vector and wphi =
+    convecphi_dns (:209-210); force_rot with fk1, fk2 passed as its squared
+    bounds, so the band is fk1 <= k2 < fk2 (:213); forcephi_rot on
+    fk1^2 <= k2 < fk2^2 (:214); dealiasing (symmetrize, then zero
+    k2 >= ly^2/9) of w and wphi (:216-219); projection (:222); the helical
+    AB2 of rot_run for the velocity and the same schedule for phi with
+    efphi = exp(-nu k2 dt / pr) (:104, :230, :249, :278-279); the rebuilt
+    velocity is not truncated (:289-291).  Returns (v, phi, (a+, a-), time);
+    with a list `trace`, each pass appends (w, wphi, v after it, phi after it)."""
+    p = grid.p
+    dt = p.dt
+    dt_h = 0.5 * dt
+    kx, ky, kz, k2 = grid.kx, grid.ky, grid.kz, grid.k2
+    hx, hy, hz = heliwave(kx, ky, kz, k2)
+    efp, efm, sqp, sqm = rot_factors(grid, om)
+    efphi = np.exp(-k2 * p.nu * dt / pr)
+    sqphi = np.sqrt(efphi)
+    v = [np.array(a, dtype=np.complex128) for a in v]
+    phi = np.array(phi, dtype=np.complex128)
+    ox, oy, oz = v                                                   # :133-135
+    ophi = phi                                                       # :136
+    ap = v[0] * np.conj(hx) + v[1] * np.conj(hy) + v[2] * np.conj(hz)
+    am = v[0] * hx + v[1] * hy + v[2] * hz
+    o0 = ophi0 = None
+    t = 0.0
+    for istep in range(npasses):
+        vx, vy, vz = v
+        wx, wy, wz = vorticity(vx, vy, vz, kx, ky, kz)
+        wx, wy, wz = convec_dns(vx, vy, vz, wx, wy, wz, p.nx)
+        wphi = convecphi_dns(vx, vy, vz, phi, p.nx)
+        if p.forced:
+            wx, wy, wz = force_rot(wx, wy, wz, vx, vy, vz, k2, fk1, fk2, p.eps, MYTINY_SP)
+        if scalarforced:
+            wphi = forcephi_rot(phi, wphi, k2, fk1, fk2, epsphi)
+        wx, wy, wz, wphi = (dealiasing(a, k2) for a in (wx, wy, wz, wphi))
+        wx, wy, wz = projection(wx, wy, wz, kx, ky, kz)
+        if istep == 0:
+            ap = (ap + dt_h * (wx * np.conj(hx) + wy * np.conj(hy) + wz * np.conj(hz))) * sqp
+            am = (am + dt_h * (wx * hx + wy * hy + wz * hz)) * sqm
+            phi = (phi + dt_h * wphi) * sqphi
+            t += dt_h
+            o0, ophi0 = (wx, wy, wz), wphi                           # :236-237 (written out)
+        elif istep == 1:
+            ap = ((ox * np.conj(hx) + oy * np.conj(hy) + oz * np.conj(hz)) * efp
+                  + dt * (wx * np.conj(hx) + wy * np.conj(hy) + wz * np.conj(hz)) * sqp)
+            am = (ox * hx + oy * hy + oz * hz) * efm + dt * (wx * hx + wy * hy + wz * hz) * sqm
+            phi = ophi * efphi + dt * wphi * sqphi
+            t += dt_h
+            (ox, oy, oz), ophi = o0, ophi0                           # :255-256 (read back)
+        else:
+            tx, ty, tz = 3.0 * wx - efp * ox, 3.0 * wy - efp * oy, 3.0 * wz - efp * oz
+            ap = (ap + dt_h * (tx * np.conj(hx) + ty * np.conj(hy) + tz * np.conj(hz))) * efp
+            tx, ty, tz = 3.0 * wx - efm * ox, 3.0 * wy - efm * oy, 3.0 * wz - efm * oz
+            am = (am + dt_h * (tx * hx + ty * hy + tz * hz)) * efm
+            ox, oy, oz = wx, wy, wz
+            phi = (phi + dt_h * (3.0 * wphi - ophi * efphi)) * efphi
+            ophi = wphi
+            t += dt
+        v = [ap * hx + am * np.conj(hx), ap * hy + am * np.conj(hy), ap * hz + am * np.conj(hz)]
+        if trace is not None:
+            trace.append(((wx, wy, wz), wphi, tuple(v), phi))
+    return tuple(v), phi, (ap, am), t
+
+
 # --------------------------------------------------------------------------
 # diagnostics (FP64)
 # --------------------------------------------------------------------------

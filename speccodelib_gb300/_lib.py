@@ -40,6 +40,9 @@ SIGNATURES = {
     "sc_rk4_steps": ([_P, _I], _I),
     "sc_ab2_steps": ([_P, _I], _I),
     "sc_rot_steps": ([_P, _I, _D, _D, _D], _I),
+    "sc_set_scalar": ([_P, _P], _I),
+    "sc_get_scalar": ([_P, _P], _I),
+    "sc_rot_scalar_steps": ([_P, _I, _D, _D, _D, _D, _I, _D], _I),
     "sc_ab2v_pass": ([_P, _D], _I),
     "sc_ab2v_state": ([_P, C.POINTER(_I), C.POINTER(_D)], _I),
     "sc_ab2v_dt": ([_D, _D, _D, _D, _D, C.POINTER(_D)], _I),

@@ -131,7 +131,7 @@ enum SpecOp {
   OP_AXPBY = 8,         // f[c] = alpha f[c] + beta g[c]
   OP_PMUL = 9,          // packed physical rows: f[c] = (f[c].x g0.x, f[c].y g0.y) (convecphi_dns.f90:23)
   OP_IDIV = 10,         // f[0] = a i (kx f0 + ky f1 + kz f2) (convecphi_dns.f90:25-45)
-  OP_FORCE_BAND = 11,   // force_rot.f90:24-28: f += a g on b <= k2 < kcut2
+  OP_FORCE_BAND = 11,   // force_rot.f90:24-28: f[0..n-1] += a g[0..n-1] on b <= k2 < kcut2
   OP_DX = 12,           // f[0] = i kx f[0] (skewness.f90:17-21)
   OP_CURL = 13          // f[0..2] = i k x f[0..2] (enstrophy.f90:16-18)
 };
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
       case OP_FORCE_BAND:
         if (k2i < kc_b && !(k2i < b_b)) {
           const T a = (T)oa.a;
-          for (int c = 0; c < 3; ++c) oa.f[c][idx] = cadd(oa.f[c][idx], cscale(oa.gsrc[c][idx], a));
+          for (int c = 0; c < oa.nfields; ++c) oa.f[c][idx] = cadd(oa.f[c][idx], cscale(oa.gsrc[c][idx], a));
         }
         break;
       default:
@@ -270,7 +270,16 @@ template <typename T> struct RotArgs {
   C2<T>* o[3];           // previous right-hand side (written at pass 0 and >= 2)
   C2<T>* a[2];           // helical amplitudes a+, a-
   double nu, dt, om;     // viscosity, time step, rotation rate
-  double kcut2;          // v = 0 where k2 >= kcut2
+  double kcut2;          // v = 0 where k2 >= kcut2 (when mask_v)
+  int mask_v;            // truncate the rebuilt velocity
+  // passive scalar (when phi is set): phi, its right-hand side, the previous
+  // right-hand side (written at pass 0 and >= 2), the initial phi (written at
+  // pass 0, read at pass 1); Prandtl number pr
+  C2<T>* phi;
+  const C2<T>* wphi;
+  C2<T>* ophi;
+  C2<T>* phi0;
+  double pr;
 };
 
 template <typename T>
@@ -306,7 +315,23 @@ __global__ void __launch_bounds__(256) rot_update_kernel(RotArgs<T> ra, Geom g) 
       ap = cx(a0.x, a0.y);
       am = cx(a1.x, a1.y);
     }
-    rot_point<T>(pass, it.ix, ky, kz, k2 >= kc_b, nu, dt, om, v, w, o, ap, am);
+    rot_point<T>(pass, it.ix, ky, kz, ra.mask_v && k2 >= kc_b, nu, dt, om, v, w, o, ap, am);
+    if (ra.phi) {
+      const C p = ra.phi[idx], wp = ra.wphi[idx];
+      Cx<T> ph = cx(p.x, p.y), op = cx(T(0), T(0)), p0 = cx(T(0), T(0));
+      if (pass >= 2) {
+        const C q = ra.ophi[idx];
+        op = cx(q.x, q.y);
+      }
+      if (pass == 1) {
+        const C q = ra.phi0[idx];
+        p0 = cx(q.x, q.y);
+      }
+      rot_scalar_point<T>(pass, k2, nu, dt, (T)ra.pr, ph, cx(wp.x, wp.y), op, p0);
+      ra.phi[idx] = mk<C>(ph.re, ph.im);
+      if (pass != 1) ra.ophi[idx] = mk<C>(op.re, op.im);
+      if (pass == 0) ra.phi0[idx] = mk<C>(p0.re, p0.im);
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       ra.v[c][idx] = mk<C>(v[c].re, v[c].im);

@@ -104,4 +104,27 @@ __host__ __device__ inline void rot_point(int pass, int kx, int ky, int kz, bool
     v[c] = cut ? cx(T(0), T(0)) : cx_add(cx_mul(np_, h[c]), cx_mul(nm_, cx_conj(h[c])));
 }
 
+// The passive scalar of spectral_rot_dns_scalar_ft.f90 on the same pass
+// schedule, with efphi = exp(-nu k2 dt / pr) (:104):
+//   pass 0: phi0 = phi, ophi = wphi, phi = (phi + dt/2 wphi) sqrt(efphi)  (:230)
+//   pass 1: phi = phi0 efphi + dt wphi sqrt(efphi)                       (:249)
+//   pass >= 2: phi = (phi + dt/2 (3 wphi - ophi efphi)) efphi, ophi = wphi (:278-279)
+template <typename T>
+__host__ __device__ inline void rot_scalar_point(int pass, int k2, T nu, T dt, T pr, Cx<T>& phi, Cx<T> wphi,
+                                                 Cx<T>& ophi, Cx<T>& phi0) {
+  const T decay = -(T)k2 * nu * dt / pr;
+  const T ef = exp(decay), sq = exp(T(0.5) * decay);
+  const T dth = T(0.5) * dt;
+  if (pass == 0) {
+    phi0 = phi;
+    ophi = wphi;
+    phi = cx_scale(cx_add(phi, cx_scale(wphi, dth)), sq);
+  } else if (pass == 1) {
+    phi = cx_add(cx_scale(phi0, ef), cx_scale(cx_scale(wphi, dt), sq));
+  } else {
+    phi = cx_scale(cx_add(phi, cx_scale(cx_sub(cx_scale(wphi, T(3)), cx_scale(ophi, ef)), dth)), ef);
+    ophi = wphi;
+  }
+}
+
 }  // namespace sc

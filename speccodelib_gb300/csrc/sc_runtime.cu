@@ -224,6 +224,7 @@ int check_derr(sc_handle* h) {
 // precision-templated implementation
 // ---------------------------------------------------------------------------
 int copy_in(sc_handle* h, void* dst, const void* src);  // host -> padded device field
+int copy_out(sc_handle* h, void* dst, const void* src);  // padded device field -> host
 
 void drop_graphs(sc_handle* h) {
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
@@ -701,6 +702,25 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
+  // convecphi_dns.f90:17-47 on the work slots: v in S_W + 0..2, phi in
+  // S_W + 3, zeros in S_W + 4..5; leaves wphi = i k . (u phi)^ / N^3 in S_W.
+  static int convecphi_core(sc_handle* h) {
+    auto* g = &h->g;
+    auto w6 = range(h, S_W, 6);
+    SC_TRY(inverse(h, w6, 6));   // u (0-2) and phi (3) in physical space
+    sc::SpecOpArgs<T> oa{};
+    for (int c = 0; c < 3; ++c) oa.f[c] = F(h, S_W + c);
+    oa.gsrc[0] = F(h, S_W + 3);
+    oa.nfields = 3;
+    oa.op = sc::OP_PMUL;
+    SC_TRY(specop(h, oa));
+    auto w3 = range(h, S_W, 3);
+    SC_TRY(forward(h, w3, 3));
+    oa.op = sc::OP_IDIV;
+    oa.a = 1.0 / ((double)g->nx * g->ny * g->nz);
+    return specop(h, oa);
+  }
+
   // One pass of the variable-step IF-AB2 of spectral_dns.f90:173-290
   // (spectral_les.f90:199-316 with an SGS model) with step dt: the
   // right-hand side without symmetrize (the same passes as sc_rhs, into the
@@ -782,27 +802,81 @@ template <typename T> struct Impl {
     return specop(h, oa);
   }
 
+  // The passive scalar of spectral_rot_dns_scalar_ft.f90 (sc_rot_scalar_steps).
+  struct RotScalar {
+    double pr;          // Prandtl number: efphi = exp(-nu k2 dt / pr)
+    int forced;         // forcephi_rot on the band fk1^2 <= k2 < fk2^2
+    double epsphi;
+  };
+  // h->aux layout of the rotating solvers
+  enum { RA_AP = 0, RA_AM = 1, RA_O = 2, RA_PHI = 5, RA_OPHI = 6, RA_PHI0 = 7, RA_WPHI = 8, RA_ZERO = 9,
+         RA_FIELDS = 10 };
+  static C* AX(sc_handle* h, int i) { return reinterpret_cast<C*>(h->aux) + (size_t)i * h->g.field; }
+
   // One pass of the rotating solver's loop, spectral_rot_dns_ft.f90:189-270:
   // the Lamb vector of v (TMA-fed passes, stored raw into the S_A slots),
   // force_rot on the band fk1^2 <= k2 < fk2^2 when forced, symmetrize,
   // projection, then the helical-wave AB2 update (rot_update_kernel).  The
   // amplitudes a+, a- and the previous right-hand side live in h->aux.
-  static int rot_pass(sc_handle* h, double om, double fk1, double fk2) {
+  // With `sc`, one pass of spectral_rot_dns_scalar_ft.f90:203-291 instead:
+  // wphi = convecphi_dns (:210), force_rot called with fk1, fk2 as its
+  // squared bounds (:213), forcephi_rot (:214), dealiasing of w and wphi in
+  // place of symmetrize (:216-219), the scalar advanced with the velocity and
+  // the rebuilt velocity left untruncated (:289-291).
+  static int rot_pass(sc_handle* h, double om, double fk1, double fk2, const RotScalar* sc = nullptr) {
     auto* g = &h->g;
-    SC_TRY(ensure_aux(h, 5));
-    C* rb = reinterpret_cast<C*>(h->aux);
+    SC_TRY(ensure_aux(h, sc ? (int)RA_FIELDS : 5));
+    const size_t fb = h->csize * g->field;
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    C* w[3] = {F(h, S_A), F(h, S_A + 1), F(h, S_A + 2)};
+    if (sc) {
+      for (int c = 0; c < 3; ++c)
+        SC_CUDA(cudaMemcpyAsync(F(h, S_W + c), vin[c], fb, cudaMemcpyDeviceToDevice, h->stream));
+      SC_CUDA(cudaMemcpyAsync(F(h, S_W + 3), AX(h, RA_PHI), fb, cudaMemcpyDeviceToDevice, h->stream));
+      SC_CUDA(cudaMemsetAsync(F(h, S_W + 4), 0, 2 * fb, h->stream));
+      SC_TRY(convecphi_core(h));
+      SC_CUDA(cudaMemcpyAsync(AX(h, RA_WPHI), F(h, S_W), fb, cudaMemcpyDeviceToDevice, h->stream));
+    }
     sc::StageArgs<T> st = stage_args(h);
     st.mode = sc::SM_LAMB;
     st.forced = 0;
     st.symmetrize = 0;
     st.project = 0;
     st.mask_rhs = 0;
-    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
-    C* w[3] = {F(h, S_A), F(h, S_A + 1), F(h, S_A + 2)};
     SC_TRY(rhs_pipeline(h, vin, st));
-    if (h->p.forced) SC_TRY(force_band(h, w, vin, fk1 * fk1, fk2 * fk2));
-    SC_TRY(symmetrize_fields(h, {S_A, S_A + 1, S_A + 2}));
+    if (h->p.forced) SC_TRY(sc ? force_band(h, w, vin, fk1, fk2) : force_band(h, w, vin, fk1 * fk1, fk2 * fk2));
     sc::SpecOpArgs<T> oa{};
+    if (sc && sc->forced) {
+      // forcephi_rot.f90:14-26: a = epsphi / (2 kinet), kinet the band variance of phi
+      const C* pz[3] = {AX(h, RA_PHI), AX(h, RA_ZERO), AX(h, RA_ZERO)};
+      double hi[sc::DQ_N], lo[sc::DQ_N];
+      SC_TRY(diag_run(h, pz, 0, fk2 * fk2, 0, hi));
+      if (fk1 > 0.0) SC_TRY(diag_run(h, pz, 0, fk1 * fk1, 0, lo));
+      const double kinet = fk1 > 0.0 ? hi[sc::DQ_ENERGY] - lo[sc::DQ_ENERGY] : hi[sc::DQ_ENERGY];
+      oa.f[0] = AX(h, RA_WPHI);
+      oa.gsrc[0] = AX(h, RA_PHI);
+      oa.nfields = 1;
+      oa.op = sc::OP_FORCE_BAND;
+      oa.a = sc->epsphi / (2.0 * kinet);
+      oa.kcut2 = fk2 * fk2;
+      oa.b = fk1 * fk1;
+      SC_TRY(specop(h, oa));
+    }
+    if (sc) {
+      // dealiasing.f90:2-37 on w and wphi: symmetrize, then zero k2 >= ly^2/9
+      oa = sc::SpecOpArgs<T>{};
+      for (int c = 0; c < 3; ++c) oa.f[c] = w[c];
+      oa.f[3] = AX(h, RA_WPHI);
+      oa.nfields = 4;
+      oa.kcut2 = (double)g->ny * g->ny / 9.0;
+      for (int op : {sc::OP_ZERO_PLANES, sc::OP_KX0_COPY, sc::OP_MASK}) {
+        oa.op = op;
+        SC_TRY(specop(h, oa));
+      }
+    } else {
+      SC_TRY(symmetrize_fields(h, {S_A, S_A + 1, S_A + 2}));
+    }
+    oa = sc::SpecOpArgs<T>{};
     for (int c = 0; c < 3; ++c) oa.f[c] = w[c];
     oa.nfields = 3;
     oa.op = sc::OP_PROJECT;
@@ -812,16 +886,39 @@ template <typename T> struct Impl {
     for (int c = 0; c < 3; ++c) {
       ra.v[c] = F(h, S_V + c);
       ra.w[c] = w[c];
-      ra.o[c] = rb + (size_t)(2 + c) * g->field;
+      ra.o[c] = AX(h, RA_O + c);
     }
-    ra.a[0] = rb;
-    ra.a[1] = rb + g->field;
+    ra.a[0] = AX(h, RA_AP);
+    ra.a[1] = AX(h, RA_AM);
     ra.nu = h->p.nu;
     ra.dt = h->p.dt;
     ra.om = om;
     ra.kcut2 = kcut2(h);
+    ra.mask_v = sc ? 0 : 1;
+    if (sc) {
+      ra.phi = AX(h, RA_PHI);
+      ra.wphi = AX(h, RA_WPHI);
+      ra.ophi = AX(h, RA_OPHI);
+      ra.phi0 = AX(h, RA_PHI0);
+      ra.pr = sc->pr;
+    }
     SC_TRY(launch(h, "rot_update", [&] { return L::rot(ra, *g, h->stream); }));
     h->rot_pass += 1;
+    return SC_OK;
+  }
+
+  // the passive scalar phi in and out (reference layout, host or device)
+  static int set_scalar(sc_handle* h, const void* phi) {
+    SC_TRY(ensure_aux(h, RA_FIELDS));
+    SC_TRY(copy_in(h, AX(h, RA_PHI), phi));
+    SC_CUDA(cudaStreamSynchronize(h->stream));
+    h->rot_pass = 0;
+    return SC_OK;
+  }
+  static int get_scalar(sc_handle* h, void* phi) {
+    SC_TRY(ensure_aux(h, RA_FIELDS));
+    SC_TRY(copy_out(h, phi, AX(h, RA_PHI)));
+    SC_CUDA(cudaStreamSynchronize(h->stream));
     return SC_OK;
   }
 
@@ -1656,6 +1753,36 @@ int sc_ab2v_dt(double betadx, double umax, double dto, double time, double twrit
   return SC_OK;
 }
 
+int sc_set_scalar(sc_handle* h, const void* phi) {
+  if (!h || !phi) return fail(SC_ERR_INVALID, "null argument");
+  return h->p.precision == SC_FP32 ? Impl<float>::set_scalar(h, phi) : Impl<double>::set_scalar(h, phi);
+}
+
+int sc_get_scalar(sc_handle* h, void* phi) {
+  if (!h || !phi) return fail(SC_ERR_INVALID, "null argument");
+  return h->p.precision == SC_FP32 ? Impl<float>::get_scalar(h, phi) : Impl<double>::get_scalar(h, phi);
+}
+
+int sc_rot_scalar_steps(sc_handle* h, int npasses, double om, double fk1, double fk2, double pr, int scalarforced,
+                        double epsphi) {
+  if (!h || npasses < 0) return fail(SC_ERR_INVALID, "need a handle and npasses >= 0");
+  if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the rotating solver has no SGS model");
+  if (!std::isfinite(om) || !std::isfinite(fk1) || !std::isfinite(fk2) || fk1 < 0.0 || fk2 < fk1 ||
+      !std::isfinite(pr) || !(pr > 0.0) || !std::isfinite(epsphi))
+    return fail(SC_ERR_INVALID, "need finite om, epsphi, 0 <= fk1 <= fk2 and pr > 0");
+  for (int i = 0; i < npasses; ++i) {
+    if (h->p.precision == SC_FP32) {
+      const Impl<float>::RotScalar sc{pr, scalarforced, epsphi};
+      SC_TRY(Impl<float>::rot_pass(h, om, fk1, fk2, &sc));
+    } else {
+      const Impl<double>::RotScalar sc{pr, scalarforced, epsphi};
+      SC_TRY(Impl<double>::rot_pass(h, om, fk1, fk2, &sc));
+    }
+  }
+  SC_CUDA(cudaGetLastError());
+  return check_derr(h);
+}
+
 int sc_rot_steps(sc_handle* h, int npasses, double om, double fk1, double fk2) {
   if (!h || npasses < 0) return fail(SC_ERR_INVALID, "need a handle and npasses >= 0");
   if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the rotating solver has no SGS model");
@@ -1947,19 +2074,7 @@ template <typename T> static int convecphi_impl(sc_handle* h, const void* const 
   for (int c = 0; c < 3; ++c) SC_TRY(copy_in(h, slot(h, S_W + c), v[c]));
   SC_TRY(copy_in(h, slot(h, S_W + 3), phi));
   SC_CUDA(cudaMemsetAsync(slot(h, S_W + 4), 0, 2 * h->csize * g->field, h->stream));
-  auto w6 = I::range(h, S_W, 6);
-  SC_TRY(I::inverse(h, w6, 6));   // u (0-2) and phi (3) in physical space
-  sc::SpecOpArgs<T> oa{};
-  for (int c = 0; c < 3; ++c) oa.f[c] = I::F(h, S_W + c);
-  oa.gsrc[0] = I::F(h, S_W + 3);
-  oa.nfields = 3;
-  oa.op = sc::OP_PMUL;
-  SC_TRY(I::specop(h, oa));
-  auto w3 = I::range(h, S_W, 3);
-  SC_TRY(I::forward(h, w3, 3));
-  oa.op = sc::OP_IDIV;
-  oa.a = 1.0 / ((double)g->nx * g->ny * g->nz);
-  SC_TRY(I::specop(h, oa));
+  SC_TRY(I::convecphi_core(h));
   SC_TRY(copy_out(h, wphi, slot(h, S_W)));
   SC_CUDA(cudaStreamSynchronize(h->stream));
   return SC_OK;

@@ -277,6 +277,21 @@ class SpectralNS:
         _check(lib().sc_ab2v_state(self.h, C.byref(p), C.byref(d)))
         return p.value, d.value
 
+    def set_scalar(self, phi):
+        (phi,) = self._arrs([phi])
+        _check(lib().sc_set_scalar(self.h, _ptr(phi)))
+
+    def get_scalar(self):
+        phi = self.empty()
+        _check(lib().sc_get_scalar(self.h, _ptr(phi, True)))
+        return phi
+
+    def rot_scalar_steps(self, n=1, om=0.0, fk1=0.0, fk2=2.5, pr=1.0, scalarforced=False, epsphi=0.0):
+        """n passes of the rotating solver with its passive scalar
+        (spectral_rot_dns_scalar_ft.f90:203-291)."""
+        _check(lib().sc_rot_scalar_steps(self.h, n, C.c_double(om), C.c_double(fk1), C.c_double(fk2),
+                                         C.c_double(pr), 1 if scalarforced else 0, C.c_double(epsphi)))
+
     def rot_steps(self, n=1, om=0.0, fk1=0.0, fk2=2.5):
         """n passes of the rotating solver's helical-wave IF-AB2
         (spectral_rot_dns_ft.f90:146-272) at rotation rate om, forcing band

@@ -65,3 +65,9 @@ def test_ab2v_step_rule_matches_oracle(specns_lib):
     assert specns_lib.sc_ab2v_pass(None, 1e-3) == 1
     p = ctypes.c_int()
     assert specns_lib.sc_ab2v_state(None, ctypes.byref(p), ctypes.byref(d)) == 1
+
+
+def test_scalar_entry_points_reject_bad_arguments_without_gpu(specns_lib):
+    assert specns_lib.sc_set_scalar(None, None) == 1
+    assert specns_lib.sc_get_scalar(None, None) == 1
+    assert specns_lib.sc_rot_scalar_steps(None, 1, 1.0, 0.0, 2.5, 1.0, 0, 0.0) == 1

@@ -429,3 +429,23 @@ def test_variable_step_ab2_les_matches_oracle(specns_lib, prec, model):
             h.ab2v_pass(dt)
         out = h.get_state()
     assert rel_l2(out, ref) < (1e-11 if prec == S.SC_FP64 else 2e-5)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_rotating_scalar_solver_matches_oracle(specns_lib, prec):
+    """Five passes of the rotating solver with its passive scalar
+    (spectral_rot_dns_scalar_ft.f90:203-291), velocity and scalar forcing on,
+    against the oracle; the scalar round-trips through set/get."""
+    n, om, pr = 32, 5.0, 0.7
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, dt=2e-3, forced=True, eps=0.1)
+    phi = R.dealiasing(hermitian_fields((n, n, n), 7, ncomp=1)[0], g.k2)
+    ref_v, ref_phi, _, _ = R.rot_scalar_run(v, phi, g, 5, om, 1.0, 2.5, pr, True, 0.05)
+    with handle(n, prec, nu=0.01, dt=2e-3, forced=1, eps=0.1) as h:
+        h.set_state(*v)
+        h.set_scalar(phi)
+        assert rel_l2(h.get_scalar(), phi) < (1e-15 if prec == S.SC_FP64 else 1e-7)
+        h.rot_scalar_steps(5, om=om, fk1=1.0, fk2=2.5, pr=pr, scalarforced=True, epsphi=0.05)
+        out_v, out_phi = h.get_state(), h.get_scalar()
+    assert rel_l2(out_v, ref_v) < TOL[prec]
+    assert rel_l2(out_phi, ref_phi) < TOL[prec]

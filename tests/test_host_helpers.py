@@ -101,35 +101,45 @@ ROT_PROGRAM = r'''
 #include <vector>
 #include "sc_common.cuh"
 #include "sc_rot.cuh"
-// Reads: int nx, ny, nz, npasses; double nu, dt, om, kcut2; v0 (3 fields),
-// then npasses right-hand sides (3 fields each), complex128 (nz, ny, nx/2+1).
-// Writes, for T = double then float, v after every pass (complex128).
+// Reads: int nx, ny, nz, npasses, scalar; double nu, dt, om, kcut2, pr; v0
+// (3 fields) [phi0 (1 field) when scalar], then per pass the right-hand side
+// (3 fields) [and wphi (1 field)], complex128 (nz, ny, nx/2+1).  Writes, for
+// T = double then float, v [and phi] after every pass (complex128).  With a
+// scalar the rebuilt velocity is not truncated, as in rot_update_kernel.
 template <typename T>
-static void run(int nx, int ny, int nz, int np, const double* sc4, const std::vector<double>& v0,
-                const std::vector<double>& ws, FILE* out) {
+static void run(const int* hd, const double* sc, const std::vector<double>& in0, const std::vector<double>& ws,
+                FILE* out) {
+  const int nx = hd[0], ny = hd[1], nz = hd[2], np = hd[3], scalar = hd[4];
+  const int nf = scalar ? 4 : 3;
   const long long nxh = nx / 2 + 1, field = (long long)nz * ny * nxh;
-  std::vector<sc::Cx<T>> v(3 * field), o(3 * field), a(2 * field);
-  for (long long i = 0; i < 3 * field; ++i) v[i] = sc::cx((T)v0[2 * i], (T)v0[2 * i + 1]);
-  const int kc = sc::k2_lt(sc4[3]);
+  std::vector<sc::Cx<T>> f(nf * field), o(3 * field), a(2 * field), op(field), p0(field);
+  for (long long i = 0; i < nf * field; ++i) f[i] = sc::cx((T)in0[2 * i], (T)in0[2 * i + 1]);
+  const int kc = sc::k2_lt(sc[3]);
   for (int p = 0; p < np; ++p) {
-    const double* w = ws.data() + (size_t)p * 6 * field;
+    const double* w = ws.data() + (size_t)p * 2 * nf * field;
     for (int iz = 0; iz < nz; ++iz)
       for (int iy = 0; iy < ny; ++iy)
         for (int ix = 0; ix < nxh; ++ix) {
           const long long idx = ((long long)iz * ny + iy) * nxh + ix;
           const int ky = iy < ny / 2 ? iy : iy - ny, kz = iz < nz / 2 ? iz : iz - nz;
+          const int k2 = ix * ix + ky * ky + kz * kz;
           sc::Cx<T> vv[3], ww[3], oo[3];
           for (int c = 0; c < 3; ++c) {
-            vv[c] = v[c * field + idx];
+            vv[c] = f[c * field + idx];
             oo[c] = o[c * field + idx];
             ww[c] = sc::cx((T)w[2 * (c * field + idx)], (T)w[2 * (c * field + idx) + 1]);
           }
-          sc::rot_point<T>(p < 2 ? p : 2, ix, ky, kz, ix * ix + ky * ky + kz * kz >= kc, (T)sc4[0], (T)sc4[1],
-                           (T)sc4[2], vv, ww, oo, a[idx], a[field + idx]);
-          for (int c = 0; c < 3; ++c) { v[c * field + idx] = vv[c]; o[c * field + idx] = oo[c]; }
+          sc::rot_point<T>(p < 2 ? p : 2, ix, ky, kz, !scalar && k2 >= kc, (T)sc[0], (T)sc[1], (T)sc[2], vv, ww, oo,
+                           a[idx], a[field + idx]);
+          for (int c = 0; c < 3; ++c) { f[c * field + idx] = vv[c]; o[c * field + idx] = oo[c]; }
+          if (scalar) {
+            const sc::Cx<T> wp = sc::cx((T)w[2 * (3 * field + idx)], (T)w[2 * (3 * field + idx) + 1]);
+            sc::rot_scalar_point<T>(p < 2 ? p : 2, k2, (T)sc[0], (T)sc[1], (T)sc[4], f[3 * field + idx], wp,
+                                    op[idx], p0[idx]);
+          }
         }
-    for (long long i = 0; i < 3 * field; ++i) {
-      const double z[2] = {(double)v[i].re, (double)v[i].im};
+    for (long long i = 0; i < nf * field; ++i) {
+      const double z[2] = {(double)f[i].re, (double)f[i].im};
       fwrite(z, sizeof(double), 2, out);
     }
   }
@@ -138,19 +148,44 @@ int main(int argc, char** argv) {
   FILE* in = fopen(argv[1], "rb");
   FILE* out = fopen(argv[2], "wb");
   if (!in || !out) return 2;
-  int hd[4];
-  double sc4[4];
-  if (fread(hd, sizeof(int), 4, in) != 4 || fread(sc4, sizeof(double), 4, in) != 4) return 3;
+  int hd[5];
+  double sc[5];
+  if (fread(hd, sizeof(int), 5, in) != 5 || fread(sc, sizeof(double), 5, in) != 5) return 3;
+  const int nf = hd[4] ? 4 : 3;
   const long long field = (long long)hd[2] * hd[1] * (hd[0] / 2 + 1);
-  std::vector<double> v0(6 * field), ws((size_t)hd[3] * 6 * field);
-  if (fread(v0.data(), sizeof(double), v0.size(), in) != v0.size()) return 4;
+  std::vector<double> in0(2 * nf * field), ws((size_t)hd[3] * 2 * nf * field);
+  if (fread(in0.data(), sizeof(double), in0.size(), in) != in0.size()) return 4;
   if (fread(ws.data(), sizeof(double), ws.size(), in) != ws.size()) return 5;
-  run<double>(hd[0], hd[1], hd[2], hd[3], sc4, v0, ws, out);
-  run<float>(hd[0], hd[1], hd[2], hd[3], sc4, v0, ws, out);
+  run<double>(hd, sc, in0, ws, out);
+  run<float>(hd, sc, in0, ws, out);
   fclose(out);
   return 0;
 }
 '''
+
+
+def _run_rot_program(tmp_path, n, npass, header_d, start, per_pass):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    src = tmp_path / "rot.cu"
+    src.write_text(ROT_PROGRAM)
+    exe = tmp_path / "rot"
+    cmd = [nvcc, "-std=c++17", "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I", CSRC, str(src), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    nf = len(start)
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        f.write(np.array([n, n, n, npass, 1 if nf == 4 else 0], np.int32).tobytes())
+        f.write(np.array(header_d, np.float64).tobytes())
+        f.write(np.ascontiguousarray(np.stack(start), np.complex128).tobytes())
+        for fields in per_pass:
+            f.write(np.ascontiguousarray(np.stack(fields), np.complex128).tobytes())
+    r = subprocess.run([str(exe), str(fin), str(fout)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout[-500:]
+    return np.fromfile(fout, np.complex128).reshape(2, npass, nf, n, n, n // 2 + 1)
 
 
 @pytest.mark.parametrize("om", [0.0, 40.0, 900.0])
@@ -163,35 +198,38 @@ def test_rotating_update_matches_oracle(tmp_path, om):
     square root of the integrating factor matters."""
     from oracle import spectral_ref as R
     from _util import rel_l2, solenoidal_init
-    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    if not os.path.exists(nvcc):
-        pytest.skip("nvcc not available")
     n, npass = 16, 4
     g = R.Grid(R.Params(nx=n, nu=0.01, dt=2e-3, forced=True, eps=0.1))
     v0 = solenoidal_init(n)
     trace = []
     R.rot_run(v0, g, npass, om, 1.0, 2.5, trace=trace)
     kcut2 = (2.0 * (n // 2) / 3.0) ** 2
-    src = tmp_path / "rot.cu"
-    src.write_text(ROT_PROGRAM)
-    exe = tmp_path / "rot"
-    cmd = [nvcc, "-std=c++17", "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a",
-           "-I", CSRC, str(src), "-o", str(exe)]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
-    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
-    with open(fin, "wb") as f:
-        f.write(np.array([n, n, n, npass], np.int32).tobytes())
-        f.write(np.array([g.p.nu, g.p.dt, om, kcut2], np.float64).tobytes())
-        f.write(np.ascontiguousarray(np.stack(v0), np.complex128).tobytes())
-        for w, _ in trace:
-            f.write(np.ascontiguousarray(np.stack(w), np.complex128).tobytes())
-    r = subprocess.run([str(exe), str(fin), str(fout)], capture_output=True, text=True, timeout=120)
-    assert r.returncode == 0, r.stdout[-500:]
-    out = np.fromfile(fout, np.complex128).reshape(2, npass, 3, n, n, n // 2 + 1)
+    out = _run_rot_program(tmp_path, n, npass, [g.p.nu, g.p.dt, om, kcut2, 1.0], list(v0),
+                           [list(w) for w, _ in trace])
     for p, (_, vref) in enumerate(trace):
         assert rel_l2(list(out[0, p]), list(vref)) < 1e-13, p
         assert rel_l2(list(out[1, p]), list(vref)) < 1e-5, p
+
+
+def test_rotating_scalar_update_matches_oracle(tmp_path):
+    """The same with the passive scalar of spectral_rot_dns_scalar_ft.f90
+    (rot_scalar_point; velocity not truncated after the update), scalar
+    forcing on: velocity and scalar pass by pass."""
+    from oracle import spectral_ref as R
+    from _util import hermitian_fields, rel_l2, solenoidal_init
+    n, npass, om, pr = 16, 4, 40.0, 0.7
+    g = R.Grid(R.Params(nx=n, nu=0.01, dt=2e-3, forced=True, eps=0.1))
+    v0 = solenoidal_init(n)
+    phi0 = R.dealiasing(hermitian_fields((n, n, n), 7, ncomp=1)[0], g.k2)
+    trace = []
+    R.rot_scalar_run(v0, phi0, g, npass, om, 1.0, 2.5, pr, True, 0.05, trace=trace)
+    out = _run_rot_program(tmp_path, n, npass, [g.p.nu, g.p.dt, om, 0.0, pr], list(v0) + [phi0],
+                           [list(w) + [wphi] for w, wphi, _, _ in trace])
+    for p, (_, _, vref, pref) in enumerate(trace):
+        assert rel_l2(list(out[0, p, :3]), list(vref)) < 1e-13, p
+        assert rel_l2(out[0, p, 3], pref) < 1e-13, p
+        assert rel_l2(list(out[1, p, :3]), list(vref)) < 1e-5, p
+        assert rel_l2(out[1, p, 3], pref) < 1e-5, p
 
 
 AB2V_PROGRAM = r'''

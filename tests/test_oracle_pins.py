@@ -254,3 +254,24 @@ def test_variable_step_ab2_known_answers():
     assert R.ab2v_dt(0.1, 2.0, 1.0, 0.96, 1.0) == pytest.approx(0.04)
     assert R.ab2v_dt(0.1, 2.0, 1.0, 0.945, 1.0) == pytest.approx(0.0275)
     assert R.ab2v_dt(0.1, 2.0, 0.01, 0.0, 1.0) == 0.03
+
+
+def test_rotating_scalar_solver_known_answers():
+    """spectral_rot_dns_scalar_ft.f90's scalar: with no velocity it only
+    diffuses, exactly as exp(-nu k^2 t / pr) through the Euler half step,
+    the midpoint restart and AB2; the velocity of an ABC flow still turns
+    into exact inertial waves (dealiasing in place of symmetrize)."""
+    n, pr = 16, 0.7
+    g = R.Grid(R.Params(nx=n, nu=0.01, dt=2e-3, forced=False))
+    phi = R.dealiasing(hermitian_fields((n, n, n), 7, ncomp=1)[0], g.k2)
+    zero = [np.zeros_like(phi) for _ in range(3)]
+    _, out, _, t = R.rot_scalar_run(zero, phi, g, 7, 2.0, 1.0, 2.5, pr)
+    assert abs(t - 6 * 2e-3) < 1e-15
+    assert rel_l2(out, phi * np.exp(-0.01 * g.k2 * t / pr)) < 1e-14
+    v = abc_flow(n)
+    kx, ky, kz, k2 = g.kx, g.ky, g.kz, g.k2
+    h = R.heliwave(kx, ky, kz, k2)
+    ap0 = sum(a * np.conj(b) for a, b in zip(v, h))
+    outv, _, _, t = R.rot_scalar_run(v, phi, g, 5, 3.0, 1.0, 2.5, pr)
+    ph = np.exp(-0.01 * t + 2j * kz[:, None, None] * 3.0 * t / np.sqrt(k2))
+    assert rel_l2(outv, [ap0 * ph * b for b in h]) < 1e-14
