@@ -113,8 +113,10 @@ struct sc_handle {
   double* cpart = nullptr;        // forcing-adjoint band sums
   long long step = 0;             // RK4 steps taken (dynamic-coefficient cadence)
   int ab2_pass = 0;
-  void* aux = nullptr;            // fields of the rotating and variable-step AB2 steppers (allocated on first use)
+  void* aux = nullptr;            // fields of the rotating steppers (allocated on first use)
   int aux_fields = 0;
+  void* aux2 = nullptr;           // fields of the variable-step AB2 (allocated on first use)
+  int aux2_fields = 0;
   int rot_pass = 0;
   int ab2v_pass = 0;
   double ab2v_dto = 0.0;          // previous step of the variable-step AB2 (dto)
@@ -725,11 +727,11 @@ template <typename T> struct Impl {
   // (spectral_les.f90:199-316 with an SGS model) with step dt: the
   // right-hand side without symmetrize (the same passes as sc_rhs, into the
   // S_A slots), then ab2v_update_kernel.  The previous right-hand side and
-  // the initial field live in h->aux; h->ab2v_dto is the reference's dto.
+  // the initial field live in h->aux2; h->ab2v_dto is the reference's dto.
   static int ab2v_pass(sc_handle* h, double dt) {
     auto* g = &h->g;
-    SC_TRY(ensure_aux(h, 6));
-    C* ab = reinterpret_cast<C*>(h->aux);
+    SC_TRY(ensure_fields(h, &h->aux2, &h->aux2_fields, 6));
+    C* ab = reinterpret_cast<C*>(h->aux2);
     const int pass = h->ab2v_pass;
     sc::StageArgs<T> st = stage_args(h);
     st.mode = sc::SM_RHS;
@@ -740,6 +742,7 @@ template <typename T> struct Impl {
     // (spectral_les.f90:140,205-208)
     if (h->p.sgs == SC_SGS_DYNSMAG && (pass == 0 || (pass - 1) % h->p.dyn_every == 0)) SC_TRY(dyn_update(h, vin));
     SC_TRY(rhs_pipeline(h, vin, st));
+    h->ab2_pass = 0;   // the S_A slots held the fixed-step AB2's history
     sc::Ab2vArgs<T> aa{};
     aa.pass = pass < 2 ? pass : 2;
     for (int c = 0; c < 3; ++c) {
@@ -759,25 +762,26 @@ template <typename T> struct Impl {
     return SC_OK;
   }
 
-  // At least n fields in h->aux (zero-filled when (re)allocated).
-  static int ensure_aux(sc_handle* h, int n) {
-    if (h->aux && h->aux_fields >= n) return SC_OK;
-    if (h->aux) {
+  // At least n fields in a stepper buffer (zero-filled when (re)allocated).
+  static int ensure_fields(sc_handle* h, void** buf, int* have, int n) {
+    if (*buf && *have >= n) return SC_OK;
+    if (*buf) {
       SC_CUDA(cudaStreamSynchronize(h->stream));
-      cudaFree(h->aux);
-      h->aux = nullptr;
-      h->aux_fields = 0;
+      cudaFree(*buf);
+      *buf = nullptr;
+      *have = 0;
     }
     const size_t bytes = (size_t)n * h->csize * h->g.field;
-    if (cudaMalloc(&h->aux, bytes) != cudaSuccess) {
+    if (cudaMalloc(buf, bytes) != cudaSuccess) {
       cudaGetLastError();
-      h->aux = nullptr;
+      *buf = nullptr;
       return fail(SC_ERR_NOMEM, "cannot allocate %zu bytes of stepper fields", bytes);
     }
-    h->aux_fields = n;
-    SC_CUDA(cudaMemsetAsync(h->aux, 0, bytes, h->stream));
+    *have = n;
+    SC_CUDA(cudaMemsetAsync(*buf, 0, bytes, h->stream));
     return SC_OK;
   }
+  static int ensure_aux(sc_handle* h, int n) { return ensure_fields(h, &h->aux, &h->aux_fields, n); }
 
   // force_rot.f90:3-29 on w from the velocity v: band fk12 <= k2 < fk22
   // (squared bounds), a = eps / (2 kinet + tiny), kinet the 1/2-weighted band
@@ -844,6 +848,7 @@ template <typename T> struct Impl {
     st.project = 0;
     st.mask_rhs = 0;
     SC_TRY(rhs_pipeline(h, vin, st));
+    h->ab2_pass = 0;   // the S_A slots held the fixed-step AB2's history
     if (h->p.forced) SC_TRY(sc ? force_band(h, w, vin, fk1, fk2) : force_band(h, w, vin, fk1 * fk1, fk2 * fk2));
     sc::SpecOpArgs<T> oa{};
     if (sc && sc->forced) {
@@ -1626,6 +1631,7 @@ int sc_destroy(sc_handle* h) {
   cudaFree(h->adj);
   cudaFree(h->cpart);
   cudaFree(h->aux);
+  cudaFree(h->aux2);
   if (h->own) cudaStreamDestroy(h->own);
   delete h;
   return SC_OK;
