@@ -333,6 +333,14 @@ int sc_force(int precision, void* wx, void* wy, void* wz, const void* vx, const 
  * bounds, as the reference passes them), K the band energy (FP64). */
 int sc_force_rot(int precision, void* wx, void* wy, void* wz, const void* vx, const void* vy,
                  const void* vz, int lx1, int ly, int lz, double fk12, double fk22, double eps);
+/* forcephi(phi,wphi,k2,lx1,ly,lz,fkmax,epsphi), forcephi.f90:1: the passive
+ * scalar's forcing wphi += epsphi/(2 K) phi on k^2 < fkmax^2, K the
+ * 1/2-weighted variance of phi there (FP64 sum); wphi in place. */
+int sc_forcephi(int precision, const void* phi, void* wphi, int lx1, int ly, int lz, double fkmax, double epsphi);
+/* forcephi_rot(phi,wphi,k2,lx1,ly,lz,fk1,fk2,epsphi), forcephi_rot.f90:1: the
+ * same on the band fk1^2 <= k^2 < fk2^2. */
+int sc_forcephi_rot(int precision, const void* phi, void* wphi, int lx1, int ly, int lz, double fk1, double fk2,
+                    double epsphi);
 
 /* convecphi_dns(vx,vy,vz,phi,wphi,kx,ky,kz,lx1,ly,lz,nx,ny,nz),
  * convecphi_dns.f90:1: wphi <- i k . (u phi)^ / N^3, the spectral flux

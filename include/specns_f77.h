@@ -39,6 +39,14 @@ void force_rot_(void* wx, void* wy, void* wz, const void* vx, const void* vy, co
                 const sc_f77_real* k2, const int* lx1, const int* ly, const int* lz,
                 const sc_f77_real* fk12, const sc_f77_real* fk22, const sc_f77_real* eps);
 
+/* forcephi.f90:1 (k2 accepted and ignored) */
+void forcephi_(const void* phi, void* wphi, const sc_f77_real* k2, const int* lx1, const int* ly, const int* lz,
+               const sc_f77_real* fkmax, const sc_f77_real* epsphi);
+
+/* forcephi_rot.f90:1 (k2 accepted and ignored) */
+void forcephi_rot_(const void* phi, void* wphi, const sc_f77_real* k2, const int* lx1, const int* ly, const int* lz,
+                   const sc_f77_real* fk1, const sc_f77_real* fk2, const sc_f77_real* epsphi);
+
 /* convecphi_dns.f90:1 (kx, ky, kz accepted and ignored) */
 void convecphi_dns_(const void* vx, const void* vy, const void* vz, const void* phi, void* wphi,
                     const sc_f77_real* kx, const sc_f77_real* ky, const sc_f77_real* kz,

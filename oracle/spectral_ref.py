@@ -730,6 +730,16 @@ def rot_run(v, grid: Grid, npasses, om, fk1=0.0, fk2=2.5, trace=None):
     return tuple(v), (ap, am), t
 
 
+def forcephi(phi, wphi, k2, fkmax, epsphi):
+    """forcephi.f90:1-27: wphi += a phi on k2 < fkmax^2, a = epsphi / (2
+    kinet), kinet the 1/2-weighted variance of phi there."""
+    m = k2 < fkmax * fkmax
+    tmp = np.where(m, (phi * np.conj(phi)).real, 0.0)
+    tmp[:, :, 0] *= 0.5
+    a = epsphi / (2.0 * float(np.sum(tmp)))
+    return np.where(m, wphi + a * phi, wphi)
+
+
 def forcephi_rot(phi, wphi, k2, fk1, fk2, epsphi):
     """forcephi_rot.f90:1-27: wphi += a phi on fk1^2 <= k2 < fk2^2,
     a = epsphi / (2 kinet), kinet the 1/2-weighted band variance of phi."""

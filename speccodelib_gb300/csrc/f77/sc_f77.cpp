@@ -48,6 +48,17 @@ void force_rot_(void* wx, void* wy, void* wz, const void* vx, const void* vy, co
         "force_rot");
 }
 
+void forcephi_(const void* phi, void* wphi, const sc_f77_real*, const int* lx1, const int* ly, const int* lz,
+               const sc_f77_real* fkmax, const sc_f77_real* epsphi) {
+  check(sc_forcephi(kPrec, phi, wphi, *lx1, *ly, *lz, (double)*fkmax, (double)*epsphi), "forcephi");
+}
+
+void forcephi_rot_(const void* phi, void* wphi, const sc_f77_real*, const int* lx1, const int* ly, const int* lz,
+                   const sc_f77_real* fk1, const sc_f77_real* fk2, const sc_f77_real* epsphi) {
+  check(sc_forcephi_rot(kPrec, phi, wphi, *lx1, *ly, *lz, (double)*fk1, (double)*fk2, (double)*epsphi),
+        "forcephi_rot");
+}
+
 void convecphi_dns_(const void* vx, const void* vy, const void* vz, const void* phi, void* wphi,
                     const sc_f77_real*, const sc_f77_real*, const sc_f77_real*, const int* lx1, const int* ly,
                     const int* lz, const int* nx, const int* ny, const int* nz) {

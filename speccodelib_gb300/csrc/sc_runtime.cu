@@ -806,6 +806,28 @@ template <typename T> struct Impl {
     return specop(h, oa);
   }
 
+  // forcephi.f90:13-25 / forcephi_rot.f90:13-25 on wphi from phi: the band
+  // lo2 <= k2 < hi2 (lo2 = 0: every mode below hi2, the mean mode included),
+  // a = epsphi / (2 kinet), kinet the 1/2-weighted band variance of phi as
+  // FP64 sums (the difference of two when lo2 > 0); `zero` is a zero field.
+  static int scalar_band_force(sc_handle* h, C* wphi, const C* phi, const C* zero, double lo2, double hi2,
+                               double epsphi) {
+    const C* pz[3] = {phi, zero, zero};
+    double hi[sc::DQ_N], lo[sc::DQ_N];
+    SC_TRY(diag_run(h, pz, 0, hi2, 0, hi));
+    if (lo2 > 0.0) SC_TRY(diag_run(h, pz, 0, lo2, 0, lo));
+    const double kinet = lo2 > 0.0 ? hi[sc::DQ_ENERGY] - lo[sc::DQ_ENERGY] : hi[sc::DQ_ENERGY];
+    sc::SpecOpArgs<T> oa{};
+    oa.f[0] = wphi;
+    oa.gsrc[0] = phi;
+    oa.nfields = 1;
+    oa.op = sc::OP_FORCE_BAND;
+    oa.a = epsphi / (2.0 * kinet);
+    oa.kcut2 = hi2;
+    oa.b = lo2;
+    return specop(h, oa);
+  }
+
   // The passive scalar of spectral_rot_dns_scalar_ft.f90 (sc_rot_scalar_steps).
   struct RotScalar {
     double pr;          // Prandtl number: efphi = exp(-nu k2 dt / pr)
@@ -851,22 +873,8 @@ template <typename T> struct Impl {
     h->ab2_pass = 0;   // the S_A slots held the fixed-step AB2's history
     if (h->p.forced) SC_TRY(sc ? force_band(h, w, vin, fk1, fk2) : force_band(h, w, vin, fk1 * fk1, fk2 * fk2));
     sc::SpecOpArgs<T> oa{};
-    if (sc && sc->forced) {
-      // forcephi_rot.f90:14-26: a = epsphi / (2 kinet), kinet the band variance of phi
-      const C* pz[3] = {AX(h, RA_PHI), AX(h, RA_ZERO), AX(h, RA_ZERO)};
-      double hi[sc::DQ_N], lo[sc::DQ_N];
-      SC_TRY(diag_run(h, pz, 0, fk2 * fk2, 0, hi));
-      if (fk1 > 0.0) SC_TRY(diag_run(h, pz, 0, fk1 * fk1, 0, lo));
-      const double kinet = fk1 > 0.0 ? hi[sc::DQ_ENERGY] - lo[sc::DQ_ENERGY] : hi[sc::DQ_ENERGY];
-      oa.f[0] = AX(h, RA_WPHI);
-      oa.gsrc[0] = AX(h, RA_PHI);
-      oa.nfields = 1;
-      oa.op = sc::OP_FORCE_BAND;
-      oa.a = sc->epsphi / (2.0 * kinet);
-      oa.kcut2 = fk2 * fk2;
-      oa.b = fk1 * fk1;
-      SC_TRY(specop(h, oa));
-    }
+    if (sc && sc->forced)
+      SC_TRY(scalar_band_force(h, AX(h, RA_WPHI), AX(h, RA_PHI), AX(h, RA_ZERO), fk1 * fk1, fk2 * fk2, sc->epsphi));
     if (sc) {
       // dealiasing.f90:2-37 on w and wphi: symmetrize, then zero k2 >= ly^2/9
       oa = sc::SpecOpArgs<T>{};
@@ -2085,6 +2093,44 @@ template <typename T> static int convecphi_impl(sc_handle* h, const void* const 
   SC_CUDA(cudaStreamSynchronize(h->stream));
   return SC_OK;
 }
+
+// forcephi / forcephi_rot on host arrays (phi in S_W, wphi in S_W + 1, a
+// zero field in S_W + 2).
+template <typename T> static int forcephi_impl(sc_handle* h, const void* phi, void* wphi, double lo2, double hi2,
+                                               double epsphi) {
+  using I = Impl<T>;
+  SC_TRY(copy_in(h, slot(h, S_W), phi));
+  SC_TRY(copy_in(h, slot(h, S_W + 1), wphi));
+  SC_CUDA(cudaMemsetAsync(slot(h, S_W + 2), 0, h->csize * h->g.field, h->stream));
+  SC_TRY(I::scalar_band_force(h, I::F(h, S_W + 1), I::F(h, S_W), I::F(h, S_W + 2), lo2, hi2, epsphi));
+  SC_TRY(copy_out(h, wphi, slot(h, S_W + 1)));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+extern "C" {
+
+// forcephi(phi,wphi,k2,lx1,ly,lz,fkmax,epsphi), forcephi.f90:1-27
+int sc_forcephi(int precision, const void* phi, void* wphi, int lx1, int ly, int lz, double fkmax, double epsphi) {
+  if (!phi || !wphi) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  const double hi2 = fkmax * fkmax;
+  return precision == SC_FP32 ? forcephi_impl<float>(h, phi, wphi, 0.0, hi2, epsphi)
+                              : forcephi_impl<double>(h, phi, wphi, 0.0, hi2, epsphi);
+}
+
+// forcephi_rot(phi,wphi,k2,lx1,ly,lz,fk1,fk2,epsphi), forcephi_rot.f90:1-27
+int sc_forcephi_rot(int precision, const void* phi, void* wphi, int lx1, int ly, int lz, double fk1, double fk2,
+                    double epsphi) {
+  if (!phi || !wphi) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  return precision == SC_FP32 ? forcephi_impl<float>(h, phi, wphi, fk1 * fk1, fk2 * fk2, epsphi)
+                              : forcephi_impl<double>(h, phi, wphi, fk1 * fk1, fk2 * fk2, epsphi);
+}
+
+}  // extern "C"
 
 // skewness(ux,kx,s,nx,ny,nz), skewness.f90:1-48: S = <d^3> / <d^2>^(3/2),
 // d = du_x/dx in physical space, moments summed in FP64.

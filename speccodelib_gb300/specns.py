@@ -120,6 +120,20 @@ def force_rot(wx, wy, wz, vx, vy, vz, fk12, fk22, eps):
                               _ptr(vz), lx1, ly, lz, C.c_double(fk12), C.c_double(fk22), C.c_double(eps)))
 
 
+def forcephi(phi, wphi, fkmax, epsphi):
+    """forcephi.f90:1 -- wphi += epsphi/(2 K) phi on k2 < fkmax^2; in place on wphi."""
+    prec, lx1, ly, lz = _same(phi, wphi)
+    _check(lib().sc_forcephi(prec, _ptr(phi), _ptr(wphi, True), lx1, ly, lz, C.c_double(fkmax),
+                             C.c_double(epsphi)))
+
+
+def forcephi_rot(phi, wphi, fk1, fk2, epsphi):
+    """forcephi_rot.f90:1 -- the same on fk1^2 <= k2 < fk2^2; in place on wphi."""
+    prec, lx1, ly, lz = _same(phi, wphi)
+    _check(lib().sc_forcephi_rot(prec, _ptr(phi), _ptr(wphi, True), lx1, ly, lz, C.c_double(fk1),
+                                 C.c_double(fk2), C.c_double(epsphi)))
+
+
 def skewness(ux, nx):
     """skewness.f90:1 -- velocity-derivative skewness <d^3>/<d^2>^(3/2), d = du_x/dx."""
     prec, lx1, ly, lz = _same(ux)

@@ -275,3 +275,18 @@ def test_rotating_scalar_solver_known_answers():
     outv, _, _, t = R.rot_scalar_run(v, phi, g, 5, 3.0, 1.0, 2.5, pr)
     ph = np.exp(-0.01 * t + 2j * kz[:, None, None] * 3.0 * t / np.sqrt(k2))
     assert rel_l2(outv, [ap0 * ph * b for b in h]) < 1e-14
+
+
+def test_scalar_forcing_injects_exactly_epsphi():
+    """forcephi.f90 / forcephi_rot.f90: the forcing raises the 1/2-weighted
+    scalar variance at the rate epsphi exactly: sum over the band of
+    2 Re(conj(phi) a phi) (1/2 at kx = 0) = 2 a kinet = epsphi."""
+    n = 16
+    phi = hermitian_fields((n, n, n), 8, ncomp=1)[0]
+    _, _, _, k2 = R.wavenumber(n, n, n)
+    zero = np.zeros_like(phi)
+    for f in (lambda: R.forcephi(phi, zero, k2, 2.5, 0.05), lambda: R.forcephi_rot(phi, zero, k2, 1.0, 2.5, 0.05)):
+        dw = f()
+        rate = 2.0 * (np.conj(phi) * dw).real
+        rate[:, :, 0] *= 0.5
+        assert abs(float(np.sum(rate)) - 0.05) < 1e-15
