@@ -113,25 +113,3 @@ def test_f77_skewness_and_enstrophy(specns_lib, prec, dtype, real, tol):
     f.enstrophy_(*[a.ctypes.data_as(C.c_void_p) for a in uu + kd + [e]], *ref_int(n // 2 + 1, n, n, n // 2, n, n, n))
     e_ref = R.enstrophy_field(*v, n)
     assert np.sqrt(np.sum((e - e_ref) ** 2) / np.sum(e_ref ** 2)) < 1e-12
-
-
-@pytest.mark.parametrize("prec,dtype,real,tol", [("dp", np.complex128, C.c_double, 1e-12),
-                                                  ("sp", np.complex64, C.c_float, 1e-5)])
-def test_f77_forcephi(specns_lib, prec, dtype, real, tol):
-    """forcephi_(phi,wphi,k2,lx1,ly,lz,fkmax,epsphi) and
-    forcephi_rot_(phi,wphi,k2,lx1,ly,lz,fk1,fk2,epsphi)."""
-    f = _lib.load_f77(prec)
-    n = 16
-    phi = hermitian_fields((n, n, n), 44, ncomp=1)[0]
-    w = hermitian_fields((n, n, n), 45, ncomp=1)[0]
-    _, _, _, k2 = R.wavenumber(n, n, n)
-    k2r = np.ascontiguousarray(k2, np.float64 if prec == "dp" else np.float32)
-    pp = np.ascontiguousarray(phi, dtype)
-    ww = np.ascontiguousarray(w, dtype)
-    f.forcephi_(pp.ctypes.data_as(C.c_void_p), ww.ctypes.data_as(C.c_void_p), k2r.ctypes.data_as(C.c_void_p),
-                *ref_int(n // 2 + 1, n, n), C.byref(real(2.5)), C.byref(real(0.05)))
-    assert rel_l2(ww, R.forcephi(phi, w, k2, 2.5, 0.05)) < tol
-    ww = np.ascontiguousarray(w, dtype)
-    f.forcephi_rot_(pp.ctypes.data_as(C.c_void_p), ww.ctypes.data_as(C.c_void_p), k2r.ctypes.data_as(C.c_void_p),
-                    *ref_int(n // 2 + 1, n, n), C.byref(real(1.0)), C.byref(real(2.5)), C.byref(real(0.05)))
-    assert rel_l2(ww, R.forcephi_rot(phi, w, k2, 1.0, 2.5, 0.05)) < tol

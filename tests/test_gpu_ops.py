@@ -173,20 +173,3 @@ def test_skewness_and_enstrophy(specns_lib, prec, tol, shape):
     e_ref = R.enstrophy_field(*v, nx)
     assert e.shape == e_ref.shape
     assert np.sqrt(np.sum((e - e_ref) ** 2) / np.sum(e_ref ** 2)) < tol * 10
-
-
-@pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("fk1,fk2", [(0.0, 2.5), (1.0, 2.5), (2.0, 5.0)])
-def test_forcephi_and_forcephi_rot(specns_lib, prec, fk1, fk2):
-    """The passive scalar's forcing (forcephi.f90 on k2 < fk2^2,
-    forcephi_rot.f90 on fk1^2 <= k2 < fk2^2) against the oracle."""
-    shape = (16, 16, 16)
-    phi = hermitian_fields(shape, 8, ncomp=1)[0]
-    w = complex_noise(shape, 9, ncomp=1)[0]
-    _, _, _, k2 = R.wavenumber(*shape)
-    pp, ww = cast([phi], prec)[0], cast([w], prec)[0]
-    S.forcephi(pp, ww, fk2, 0.05)
-    assert rel_l2(ww, R.forcephi(phi, w, k2, fk2, 0.05)) < TOL[prec]
-    ww = cast([w], prec)[0]
-    S.forcephi_rot(pp, ww, fk1, fk2, 0.05)
-    assert rel_l2(ww, R.forcephi_rot(phi, w, k2, fk1, fk2, 0.05)) < TOL[prec]

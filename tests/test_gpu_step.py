@@ -336,116 +336,3 @@ def test_fused_stage_passes_long_z(specns_lib, prec, monkeypatch):
         assert rel_l2(o, ref) < TOL[prec]
     for o in outs[1:]:
         assert rel_l2(outs[0], o) < (1e-13 if prec == S.SC_FP64 else 2e-6)
-
-
-@pytest.mark.parametrize("prec", PRECS)
-def test_rotating_solver_matches_oracle(specns_lib, prec):
-    """Five passes of the rotating solver's helical-wave IF-AB2
-    (spectral_rot_dns_ft.f90:146-272) with band forcing 1 <= |k| < 2.5, and a
-    restart through set_state, against the oracle."""
-    n, om = 32, 5.0
-    v = solenoidal_init(n)
-    g = oracle_grid(n, nu=0.01, dt=2e-3, forced=True, eps=0.1)
-    ref, _, _ = R.rot_run(v, g, 5, om, 1.0, 2.5)
-    ref2, _, _ = R.rot_run(v, g, 2, om, 1.0, 2.5)
-    with handle(n, prec, nu=0.01, dt=2e-3, forced=1, eps=0.1) as h:
-        h.set_state(*v)
-        h.rot_steps(5, om=om, fk1=1.0, fk2=2.5)
-        out = h.get_state()
-        h.set_state(*v)
-        h.rot_steps(2, om=om, fk1=1.0, fk2=2.5)
-        out2 = h.get_state()
-    assert rel_l2(out, ref) < TOL[prec]
-    assert rel_l2(out2, ref2) < TOL[prec]
-
-
-@pytest.mark.parametrize("prec", PRECS)
-def test_rotating_solver_beltrami_inertial_waves(specns_lib, prec):
-    """An ABC (Beltrami, curl u = u) flow has a zero Lamb vector, so the
-    rotating solver advances its helical amplitudes by the integrating factor
-    alone: after p >= 2 passes a+ = a+(0) exp(-nu (p-1) dt + 2 i kz om
-    (p-1) dt / |k|), and v = a+ h."""
-    n, om, nu, dt, npass = 16, 3.0, 0.05, 1e-2, 7
-    z, y, x = np.meshgrid(*[np.arange(n) * 2 * np.pi / n for _ in range(3)], indexing="ij")
-    A, B, Cc = 1.0, 0.7, 0.4
-    u = [A * np.sin(z) + Cc * np.cos(y), B * np.sin(x) + A * np.cos(z), Cc * np.sin(y) + B * np.cos(x)]
-    v = [R.r2c(a) / n ** 3 for a in u]
-    kx, ky, kz, k2 = R.wavenumber(n, n, n)
-    h = R.heliwave(kx, ky, kz, k2)
-    ap0 = sum(a * np.conj(b) for a, b in zip(v, h))
-    ph = np.exp(-nu * (npass - 1) * dt + 2j * kz[:, None, None] * om * (npass - 1) * dt / np.sqrt(k2))
-    exact = [ap0 * ph * b for b in h]
-    with handle(n, prec, nu=nu, dt=dt, forced=0) as hd:
-        hd.set_state(*v)
-        hd.rot_steps(npass, om=om)
-        out = hd.get_state()
-    assert rel_l2(out, exact) < (1e-13 if prec == S.SC_FP64 else TOL[prec])
-
-
-STEPS_V = [2e-3, 2.6e-3, 1.4e-3, 2.2e-3, 1.8e-3, 2.4e-3]
-
-
-@pytest.mark.parametrize("prec", PRECS)
-def test_variable_step_ab2_matches_oracle(specns_lib, prec):
-    """Passes of spectral_dns.f90's variable-step IF-AB2 on an uneven step
-    sequence (its cut k >= nx/2), a restart through set_state, and the
-    pass count / dto bookkeeping, against the oracle."""
-    n = 32
-    v = solenoidal_init(n)
-    g = oracle_grid(n, nu=0.01, forced=True, eps=0.1, kcut=n // 2)
-    ref, t, dto = R.ab2v_run(v, g, STEPS_V)
-    ref2, _, _ = R.ab2v_run(v, g, STEPS_V[:2])
-    with handle(n, prec, nu=0.01, forced=1, eps=0.1, kcut=n // 2) as h:
-        h.set_state(*v)
-        for dt in STEPS_V:
-            h.ab2v_pass(dt)
-        out = h.get_state()
-        npass, hdto = h.ab2v_state()
-        h.set_state(*v)
-        assert h.ab2v_state()[0] == 0
-        for dt in STEPS_V[:2]:
-            h.ab2v_pass(dt)
-        out2 = h.get_state()
-    assert npass == len(STEPS_V) and abs(hdto - dto) < 1e-15
-    assert rel_l2(out, ref) < TOL[prec]
-    assert rel_l2(out2, ref2) < TOL[prec]
-
-
-@pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("model", ["smag", "dynsmag"])
-def test_variable_step_ab2_les_matches_oracle(specns_lib, prec, model):
-    """spectral_les.f90:199-316: the variable-step IF-AB2 with the SGS
-    divergence in its right-hand side; with dynsmag the coefficient is
-    refreshed on passes 0, 1 and 11 of 12 (spectral_les.f90:140,205-208)."""
-    n = 32
-    v = solenoidal_init(n)
-    sgs = {"smag": S.SC_SGS_SMAG, "dynsmag": S.SC_SGS_DYNSMAG}[model]
-    steps = (STEPS_V * 2)[:12] if model == "dynsmag" else STEPS_V
-    g = oracle_grid(n, nu=1e-3, forced=True, eps=0.1, sgs=model, c1=0.0289)
-    ref, _, _ = R.ab2v_run(v, g, steps)
-    with handle(n, prec, nu=1e-3, forced=1, eps=0.1, sgs=sgs, c1=0.0289) as h:
-        h.set_state(*v)
-        for dt in steps:
-            h.ab2v_pass(dt)
-        out = h.get_state()
-    assert rel_l2(out, ref) < (1e-11 if prec == S.SC_FP64 else 2e-5)
-
-
-@pytest.mark.parametrize("prec", PRECS)
-def test_rotating_scalar_solver_matches_oracle(specns_lib, prec):
-    """Five passes of the rotating solver with its passive scalar
-    (spectral_rot_dns_scalar_ft.f90:203-291), velocity and scalar forcing on,
-    against the oracle; the scalar round-trips through set/get."""
-    n, om, pr = 32, 5.0, 0.7
-    v = solenoidal_init(n)
-    g = oracle_grid(n, nu=0.01, dt=2e-3, forced=True, eps=0.1)
-    phi = R.dealiasing(hermitian_fields((n, n, n), 7, ncomp=1)[0], g.k2)
-    ref_v, ref_phi, _, _ = R.rot_scalar_run(v, phi, g, 5, om, 1.0, 2.5, pr, True, 0.05)
-    with handle(n, prec, nu=0.01, dt=2e-3, forced=1, eps=0.1) as h:
-        h.set_state(*v)
-        h.set_scalar(phi)
-        assert rel_l2(h.get_scalar(), phi) < (1e-15 if prec == S.SC_FP64 else 1e-7)
-        h.rot_scalar_steps(5, om=om, fk1=1.0, fk2=2.5, pr=pr, scalarforced=True, epsphi=0.05)
-        out_v, out_phi = h.get_state(), h.get_scalar()
-    assert rel_l2(out_v, ref_v) < TOL[prec]
-    assert rel_l2(out_phi, ref_phi) < TOL[prec]
