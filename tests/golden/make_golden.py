@@ -9,7 +9,12 @@ E = 0.5), its right-hand side, the state after 1 and 10 IF-RK4 steps, after
 the forced-DNS configuration at 128^3 in FP64 (nu = 0.01, dt = 2e-3, the same
 seeded field) after 1, 10 and 100 steps, stored compactly as the block of
 wavenumbers |kx|, |ky|, |kz| <= 6 plus, after 100 steps, the shell spectrum,
-energy and dissipation (python tests/golden/make_golden.py c1; a few minutes).  The
+energy and dissipation (python tests/golden/make_golden.py c1; a few minutes).
+schemes16: from the same 16^3 field, the rotating solver after 5 passes
+(om = 5, band forcing 1 <= |k| < 2.5), the same with a passive scalar (a
+seeded dealiased white-noise phi, pr = 0.7, scalar forcing on) and the
+variable-step IF-AB2 after 6 uneven steps (cut at k >= nx/2)
+(python tests/golden/make_golden.py schemes).  The
 reference itself cannot be run here; these fixtures freeze the oracle's
 outputs so that both the oracle and the CUDA library are checked against the
 same committed numbers.
@@ -74,8 +79,28 @@ def c1():
     np.savez_compressed(os.path.join(HERE, "c1_128.npz"), n=n, kmax=C1_K, nu=NU, dt=DT, **out)
 
 
+STEPS_V = [2e-3, 2.6e-3, 1.4e-3, 2.2e-3, 1.8e-3, 2.4e-3]
+
+
+def schemes():
+    kcut = 2.0 * (N // 2) / 3.0
+    v0 = R.initialize_dealiased(N, N, N, 1, 4.0, 1.0 / np.sqrt(3.0), kcut)
+    g = R.Grid(R.Params(nx=N, nu=NU, dt=DT, forced=True, eps=0.1))
+    v_rot, _, _ = R.rot_run(v0, g, 5, 5.0, 1.0, 2.5)
+    rng = np.random.default_rng(7)
+    phi0 = R.dealiasing(R.r2c(rng.standard_normal((N, N, N))) / N ** 3, g.k2)
+    v_rs, phi_rs, _, _ = R.rot_scalar_run(v0, phi0, g, 5, 5.0, 1.0, 2.5, 0.7, True, 0.05)
+    gv = R.Grid(R.Params(nx=N, nu=NU, forced=True, eps=0.1, kcut=N // 2))
+    v_ab2v, t, dto = R.ab2v_run(v0, gv, STEPS_V)
+    np.savez_compressed(os.path.join(HERE, "schemes16.npz"), v0=np.stack(v0), v_rot5=np.stack(v_rot),
+                        phi0=phi0, v_rs5=np.stack(v_rs), phi_rs5=phi_rs, v_ab2v=np.stack(v_ab2v),
+                        steps_v=np.array(STEPS_V), t_ab2v=t, dto_ab2v=dto, n=N, nu=NU, dt=DT)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["c1"]:
         c1()
+    elif sys.argv[1:] == ["schemes"]:
+        schemes()
     else:
         main()

@@ -290,3 +290,20 @@ def test_scalar_forcing_injects_exactly_epsphi():
         rate = 2.0 * (np.conj(phi) * dw).real
         rate[:, :, 0] *= 0.5
         assert abs(float(np.sum(rate)) - 0.05) < 1e-15
+
+
+def test_golden_scheme_fixtures_reproduce():
+    """tests/golden/schemes16.npz (rotating solver, its passive scalar and the
+    variable-step IF-AB2 from the seeded 16^3 field) reproduces."""
+    d = np.load(os.path.join(GOLD, "schemes16.npz"))
+    n = int(d["n"])
+    v0 = solenoidal_init(n)
+    assert rel_l2(v0, list(d["v0"])) < 1e-15
+    g = R.Grid(R.Params(nx=n, nu=float(d["nu"]), dt=float(d["dt"]), forced=True, eps=0.1))
+    assert rel_l2(R.rot_run(v0, g, 5, 5.0, 1.0, 2.5)[0], list(d["v_rot5"])) < 1e-14
+    v, phi, _, _ = R.rot_scalar_run(v0, d["phi0"], g, 5, 5.0, 1.0, 2.5, 0.7, True, 0.05)
+    assert rel_l2(v, list(d["v_rs5"])) < 1e-14 and rel_l2(phi, d["phi_rs5"]) < 1e-14
+    gv = R.Grid(R.Params(nx=n, nu=float(d["nu"]), forced=True, eps=0.1, kcut=n // 2))
+    v, t, dto = R.ab2v_run(v0, gv, list(d["steps_v"]))
+    assert rel_l2(v, list(d["v_ab2v"])) < 1e-14
+    assert abs(t - float(d["t_ab2v"])) < 1e-15 and dto == float(d["dto_ab2v"])

@@ -191,3 +191,27 @@ def test_f77_forcephi(specns_lib, prec, dtype, real, tol):
     f.forcephi_rot_(pp.ctypes.data_as(C.c_void_p), ww.ctypes.data_as(C.c_void_p), k2r.ctypes.data_as(C.c_void_p),
                     *ref_int(n // 2 + 1, n, n), C.byref(real(1.0)), C.byref(real(2.5)), C.byref(real(0.05)))
     assert rel_l2(ww, R.forcephi_rot(phi, w, k2, 1.0, 2.5, 0.05)) < tol
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_schemes_against_committed_golden_fixtures(specns_lib, prec):
+    """tests/golden/schemes16.npz: the rotating solver, its passive scalar and
+    the variable-step IF-AB2 from the seeded 16^3 field."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "schemes16.npz"))
+    n, nu, dt = int(d["n"]), float(d["nu"]), float(d["dt"])
+    v0 = list(d["v0"])
+    with handle(n, prec, nu=nu, dt=dt, forced=1, eps=0.1) as h:
+        h.set_state(*v0)
+        h.rot_steps(5, om=5.0, fk1=1.0, fk2=2.5)
+        assert rel_l2(h.get_state(), list(d["v_rot5"])) < TOL[prec]
+        h.set_state(*v0)
+        h.set_scalar(d["phi0"])
+        h.rot_scalar_steps(5, om=5.0, fk1=1.0, fk2=2.5, pr=0.7, scalarforced=True, epsphi=0.05)
+        assert rel_l2(h.get_state(), list(d["v_rs5"])) < TOL[prec]
+        assert rel_l2(h.get_scalar(), d["phi_rs5"]) < TOL[prec]
+    with handle(n, prec, nu=nu, forced=1, eps=0.1, kcut=n // 2) as h:
+        h.set_state(*v0)
+        for s in d["steps_v"]:
+            h.ab2v_pass(float(s))
+        assert rel_l2(h.get_state(), list(d["v_ab2v"])) < TOL[prec]
