@@ -362,6 +362,10 @@ int sc_enstrophy(int precision, const void* ux, const void* uy, const void* uz, 
 int sc_symmetrize(int precision, void* c, int lx1, int ly, int lz);
 
 /* dealiasing(c,k2,lx1,ly,lz), dealiasing.f90:2. */
+/* hermitianize(c,lx1,ly,lz), hermitianize.f90:1: the kx = 0 plane's conjugate
+ * symmetry c(1,iy,iz) = conj(c(1,-iy,-iz)) for iz > lz/2 and on the line
+ * kz = 0, iy > ly/2, without symmetrize's zeroing; c in place. */
+int sc_hermitianize(int precision, void* c, int lx1, int ly, int lz);
 int sc_dealiasing(int precision, void* c, int lx1, int ly, int lz);
 
 /* smag(vx,vy,vz,t11,t12,t13,t22,t23,t33,kx,ky,kz,lx1,ly,lz,nx,ny,nz,delta),

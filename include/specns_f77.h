@@ -72,6 +72,9 @@ void projection_(void* vx, void* vy, void* vz, const sc_f77_real* kx, const sc_f
 void __msymmetrize_MOD_symmetrize3d(void* c, const int* lx1, const int* ly, const int* lz);
 void symmetrize3d_(void* c, const int* lx1, const int* ly, const int* lz);
 
+/* hermitianize.f90:1 */
+void hermitianize_(void* c, const int* lx1, const int* ly, const int* lz);
+
 /* dealiasing.f90:2 (k2 accepted and ignored) */
 void dealiasing_(void* c, const sc_f77_real* k2, const int* lx1, const int* ly, const int* lz);
 

@@ -145,6 +145,19 @@ def symmetrize3d(c):
     return c
 
 
+def hermitianize(c):
+    """hermitianize.f90:1-24 (returns a new array): the kx = 0 copies of
+    symmetrize.f90:52-62 alone, without its zeroing."""
+    c = np.array(c, dtype=np.complex128, copy=True)
+    nz, ny, nxh = c.shape
+    jz = np.arange(nz // 2 + 1, nz)                                  # :10-16
+    jy = np.arange(ny)
+    c[jz[:, None], jy[None, :], 0] = np.conj(c[(nz - jz)[:, None], np.mod(ny - jy, ny)[None, :], 0])
+    jy2 = np.arange(ny // 2 + 1, ny)                                 # :19-21
+    c[0, jy2, 0] = np.conj(c[0, ny - jy2, 0])
+    return c
+
+
 def symmetrize2d(c):
     """symmetrize.f90:8-30 (returns a new array); c shape (ny, nxh)."""
     c = np.array(c, dtype=np.complex128, copy=True)

@@ -40,6 +40,7 @@ SIGNATURES = {
     "sc_rk4_steps": ([_P, _I], _I),
     "sc_ab2_steps": ([_P, _I], _I),
     "sc_rot_steps": ([_P, _I, _D, _D, _D], _I),
+    "sc_hermitianize": ([_I, _P, _I, _I, _I], _I),
     "sc_forcephi": ([_I, _P, _P, _I, _I, _I, _D, _D], _I),
     "sc_forcephi_rot": ([_I, _P, _P, _I, _I, _I, _D, _D, _D], _I),
     "sc_set_scalar": ([_P, _P], _I),

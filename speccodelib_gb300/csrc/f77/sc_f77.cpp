@@ -90,6 +90,10 @@ void symmetrize3d_(void* c, const int* lx1, const int* ly, const int* lz) {
   check(sc_symmetrize(kPrec, c, *lx1, *ly, *lz), "symmetrize");
 }
 
+void hermitianize_(void* c, const int* lx1, const int* ly, const int* lz) {
+  check(sc_hermitianize(kPrec, c, *lx1, *ly, *lz), "hermitianize");
+}
+
 void dealiasing_(void* c, const sc_f77_real*, const int* lx1, const int* ly, const int* lz) {
   check(sc_dealiasing(kPrec, c, *lx1, *ly, *lz), "dealiasing");
 }

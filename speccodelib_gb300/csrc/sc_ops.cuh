@@ -133,7 +133,8 @@ enum SpecOp {
   OP_IDIV = 10,         // f[0] = a i (kx f0 + ky f1 + kz f2) (convecphi_dns.f90:25-45)
   OP_FORCE_BAND = 11,   // force_rot.f90:24-28: f[0..n-1] += a g[0..n-1] on b <= k2 < kcut2
   OP_DX = 12,           // f[0] = i kx f[0] (skewness.f90:17-21)
-  OP_CURL = 13          // f[0..2] = i k x f[0..2] (enstrophy.f90:16-18)
+  OP_CURL = 13,         // f[0..2] = i k x f[0..2] (enstrophy.f90:16-18)
+  OP_HERMITIANIZE = 14  // hermitianize.f90:10-22: the kx = 0 copy of OP_KX0_COPY, ky = -ny/2 row included
 };
 
 template <typename T> struct SpecOpArgs {
@@ -156,13 +157,16 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
   const long long tstride = (long long)gridDim.x * blockDim.x;
   T sfac = T(1);
   if (oa.op == OP_SCALE) sfac = oa.dscal ? (T)sqrt(oa.a / *oa.dscal) : (T)oa.a;
-  if (oa.op == OP_KX0_COPY) {
+  if (oa.op == OP_KX0_COPY || oa.op == OP_HERMITIANIZE) {
+    // destinations (iz > nz/2, or the line iz = 0, iy > ny/2) never serve as sources
+    const bool zero_nyq = oa.op == OP_KX0_COPY;   // after OP_ZERO_PLANES that row's sources are zero
     for (long long t = t0; t < rows; t += tstride) {
       const int iy = (int)(t % g.ny), iz = (int)(t / g.ny);
       if (!(iz > g.nz / 2 || (iz == 0 && iy > g.ny / 2))) continue;
       const int sy = (g.ny - iy) % g.ny, sz = (g.nz - iz) % g.nz;
       const long long d = ((long long)iz * g.ny + iy) * g.nxp, s = ((long long)sz * g.ny + sy) * g.nxp;
-      for (int c = 0; c < oa.nfields; ++c) oa.f[c][d] = (iy == g.ny / 2) ? czero<C>() : cconj(oa.f[c][s]);
+      for (int c = 0; c < oa.nfields; ++c)
+        oa.f[c][d] = (zero_nyq && iy == g.ny / 2) ? czero<C>() : cconj(oa.f[c][s]);
     }
     return;
   }

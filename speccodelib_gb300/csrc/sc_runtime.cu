@@ -2012,6 +2012,17 @@ int sc_symmetrize(int precision, void* c, int lx1, int ly, int lz) {
                               : specop_host<double>(h, sc::OP_ZERO_PLANES, 1, io, 0, 0, nullptr);
 }
 
+// hermitianize(c,lx1,ly,lz), hermitianize.f90:1-24: the kx = 0 conjugate
+// copy alone (no zeroing).
+int sc_hermitianize(int precision, void* c, int lx1, int ly, int lz) {
+  if (!c) return fail(SC_ERR_INVALID, "null array");
+  sc_handle* h = nullptr;
+  SC_TRY(scratch(precision, 2 * (lx1 - 1), ly, lz, SC_SGS_NONE, &h));
+  void* io[1] = {c};
+  return precision == SC_FP32 ? specop_host<float>(h, sc::OP_HERMITIANIZE, 1, io, 0, 0, nullptr)
+                              : specop_host<double>(h, sc::OP_HERMITIANIZE, 1, io, 0, 0, nullptr);
+}
+
 int sc_dealiasing(int precision, void* c, int lx1, int ly, int lz) {
   if (!c) return fail(SC_ERR_INVALID, "null array");
   sc_handle* h = nullptr;

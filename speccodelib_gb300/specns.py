@@ -162,6 +162,12 @@ def symmetrize(c):
     _check(lib().sc_symmetrize(prec, _ptr(c, True), lx1, ly, lz))
 
 
+def hermitianize(c):
+    """hermitianize.f90:1 -- the kx = 0 conjugate symmetry alone; in place."""
+    prec, lx1, ly, lz = _same(c)
+    _check(lib().sc_hermitianize(prec, _ptr(c, True), lx1, ly, lz))
+
+
 def dealiasing(c):
     """dealiasing.f90:2 -- symmetrize + zero k2 >= ly^2/9; in place."""
     prec, lx1, ly, lz = _same(c)

@@ -34,7 +34,7 @@ def test_default_params_and_errors_without_gpu(specns_lib):
 
 def test_f77_shims_export_every_declared_symbol(specns_lib):
     declared = _lib.declared_f77_symbols()
-    assert "convec_dns_" in declared and "forcephi_rot_" in declared and len(declared) == 14
+    assert "convec_dns_" in declared and "hermitianize_" in declared and len(declared) == 15
     for prec in ("sp", "dp"):
         lib = _lib.load_f77(prec)
         missing = [n for n in declared if not hasattr(lib, n)]

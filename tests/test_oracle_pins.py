@@ -307,3 +307,23 @@ def test_golden_scheme_fixtures_reproduce():
     v, t, dto = R.ab2v_run(v0, gv, list(d["steps_v"]))
     assert rel_l2(v, list(d["v_ab2v"])) < 1e-14
     assert abs(t - float(d["t_ab2v"])) < 1e-15 and dto == float(d["dto_ab2v"])
+
+
+def test_hermitianize_is_symmetrize_without_zeroing():
+    """hermitianize.f90 is the kx = 0 copy of symmetrize.f90:52-62 alone:
+    symmetrize = hermitianize after symmetrize's zeroing (:43-49), and a
+    field of a real signal is left unchanged."""
+    n = 16
+    rng = np.random.default_rng(4)
+    c = rng.standard_normal((n, n, n // 2 + 1)) + 1j * rng.standard_normal((n, n, n // 2 + 1))
+    z = c.copy()
+    z[:, n // 2, :] = 0
+    z[n // 2] = 0
+    z[..., -1] = 0
+    z[0, 0, 0] = 0
+    assert np.array_equal(R.hermitianize(z), R.symmetrize3d(c))
+    h = R.hermitianize(c)
+    assert not np.array_equal(h[n // 2 + 1:, n // 2, 0], 0)     # the ky = -n/2 row is copied, not zeroed
+    real = R.r2c(rng.standard_normal((n, n, n)))
+    assert np.array_equal(R.hermitianize(R.hermitianize(c)), h)
+    assert rel_l2(R.hermitianize(real), real) < 1e-15

@@ -215,3 +215,18 @@ def test_schemes_against_committed_golden_fixtures(specns_lib, prec):
         for s in d["steps_v"]:
             h.ab2v_pass(float(s))
         assert rel_l2(h.get_state(), list(d["v_ab2v"])) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_hermitianize(specns_lib, prec):
+    """hermitianize.f90 (sc_hermitianize and the hermitianize_ shim) against
+    the oracle on a field with no symmetry."""
+    n = 16
+    c = complex_noise((n, n, n), 12, ncomp=1)[0]
+    (cc,) = cast([c], prec)
+    S.hermitianize(cc)
+    assert rel_l2(cc, R.hermitianize(c)) < TOL[prec]
+    f = _lib.load_f77("dp" if prec == S.SC_FP64 else "sp")
+    (cc,) = cast([c], prec)
+    f.hermitianize_(cc.ctypes.data_as(C.c_void_p), *ref_int(n // 2 + 1, n, n))
+    assert rel_l2(cc, R.hermitianize(c)) < TOL[prec]
