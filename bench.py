@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-les", action="store_true")
+    ap.add_argument("--schemes", action="store_true",
+                    help="also time the rotating solver, its passive scalar and the variable-step IF-AB2 "
+                         "(passes per second on the same grid and initial field)")
     return ap.parse_args()
 
 
@@ -462,6 +465,49 @@ def run_ours(a):
         ens.close()
         del ens
 
+    # ---- opt-in: the other steppers on the headline grid ----
+    schemes = None
+    if a.schemes:
+        schemes = {"grid": n, "dtype": "f32", "om": 5.0, "band": [1.0, 2.5], "pr": 0.7,
+                   "note": "passes through the public API; forced passes read two FP64 band sums on the "
+                           "host (one synchronisation each), ab2v_pass checks its status every call"}
+
+        def time_calls(fn, k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            barrier()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            fn(k)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            return e0.elapsed_time(e1)
+
+        hs = make(S.SC_FP32)
+        start = hs.get_state()
+        ks = max(a.steps, 4)
+        hs.rot_steps(2, om=5.0, fk1=1.0, fk2=2.5)   # Euler half step and restart
+        ms_r = time_calls(lambda k: hs.rot_steps(k, om=5.0, fk1=1.0, fk2=2.5), ks)
+        hs.set_state(*start)
+        hs.set_scalar(start[0])
+        hs.rot_scalar_steps(2, om=5.0, fk1=1.0, fk2=2.5, pr=0.7, scalarforced=True, epsphi=0.05)
+        ms_s = time_calls(lambda k: hs.rot_scalar_steps(k, om=5.0, fk1=1.0, fk2=2.5, pr=0.7,
+                                                        scalarforced=True, epsphi=0.05), ks)
+        hs.set_state(*start)
+        hs.ab2v_pass(DT)
+        hs.ab2v_pass(DT)
+
+        def ab2v(k):
+            for _ in range(k):
+                hs.ab2v_pass(DT)
+
+        ms_v = time_calls(ab2v, ks)
+        hs.close()
+        del hs
+        torch.cuda.empty_cache()
+        for name, ms_x in (("rotating", ms_r), ("rotating_scalar", ms_s), ("ab2_variable_step", ms_v)):
+            schemes[name] = {"passes": ks, "passes_per_s": ks / (ms_x / 1e3), "ms_per_pass": ms_x / ks}
+
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
         workers = len(os.sched_getaffinity(0))
@@ -488,6 +534,8 @@ def run_ours(a):
                "les256": les,
                "ensemble2d": ensemble,
                "cpu_baseline": cpu}
+        if schemes is not None:
+            out["schemes"] = schemes
         print(json.dumps(out), flush=True)
     if dist:
         td.destroy_process_group()
