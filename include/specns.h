@@ -218,6 +218,11 @@ int sc_adjoint_rk4_vjp(sc_handle* h, int nsteps, int checkpoint_every, const voi
  * loads the state as sc_set_state does. */
 int sc_output3d(sc_handle* h, const char* dir, int idump, int file_precision);
 int sc_input3d(sc_handle* h, const char* dir, int idump, int file_precision);
+/* The passive scalar as outputphi / inputphi write and read it
+ * (outputphi.f90:1-20, inputphi.f90:1-22): <dir>/phi<idump>.dat, one record of
+ * complex(sp) (nx/2+1, ny, nz); sc_inputphi loads it as sc_set_scalar does. */
+int sc_outputphi(sc_handle* h, const char* dir, int idump, int file_precision);
+int sc_inputphi(sc_handle* h, const char* dir, int idump, int file_precision);
 
 /* One record of a gfortran sequential unformatted file, host memory only: a
  * 4-byte little-endian length marker, the bytes, the marker again; records

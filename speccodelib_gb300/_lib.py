@@ -40,6 +40,8 @@ SIGNATURES = {
     "sc_rk4_steps": ([_P, _I], _I),
     "sc_ab2_steps": ([_P, _I], _I),
     "sc_rot_steps": ([_P, _I, _D, _D, _D], _I),
+    "sc_outputphi": ([_P, _CS, _I, _I], _I),
+    "sc_inputphi": ([_P, _CS, _I, _I], _I),
     "sc_hermitianize": ([_I, _P, _I, _I, _I], _I),
     "sc_forcephi": ([_I, _P, _P, _I, _I, _I, _D, _D], _I),
     "sc_forcephi_rot": ([_I, _P, _P, _I, _I, _I, _D, _D, _D], _I),

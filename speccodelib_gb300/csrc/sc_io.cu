@@ -99,6 +99,23 @@ std::string field_path(const char* dir, const char* comp, int idump) {
   return d + comp + std::to_string(idump) + ".dat";
 }
 
+// n complex values stored in precision `from` as precision `to` (SC_FP32:
+// two floats each, SC_FP64: two doubles each).
+std::vector<char> convert_values(const std::vector<char>& in, size_t n, int from, int to) {
+  if (from == to) return in;
+  std::vector<char> out(n * (to == SC_FP32 ? 8 : 16));
+  if (to == SC_FP32) {
+    const double* s = reinterpret_cast<const double*>(in.data());
+    float* d = reinterpret_cast<float*>(out.data());
+    for (size_t i = 0; i < 2 * n; ++i) d[i] = (float)s[i];
+  } else {
+    const float* s = reinterpret_cast<const float*>(in.data());
+    double* d = reinterpret_cast<double*>(out.data());
+    for (size_t i = 0; i < 2 * n; ++i) d[i] = (double)s[i];
+  }
+  return out;
+}
+
 }  // namespace
 
 extern "C" {
@@ -173,6 +190,34 @@ int sc_input3d(sc_handle* h, const char* dir, int idump, int file_precision) {
     }
   }
   return sc_set_state(h, v[0].data(), v[1].data(), v[2].data());
+}
+
+// outputphi(phi,idump,lx1,ly,lz), outputphi.f90:1-20: <dir>/phi<idump>.dat,
+// one record of complex(sp) (nx/2+1, ny, nz).
+int sc_outputphi(sc_handle* h, const char* dir, int idump, int file_precision) {
+  sc_params p{};
+  if (!h || sc_get_params(h, &p) != SC_OK) return sc::set_last_error(SC_ERR_INVALID, "null handle");
+  if (file_precision != SC_FP32 && file_precision != SC_FP64)
+    return sc::set_last_error(SC_ERR_INVALID, "file precision must be SC_FP32 or SC_FP64");
+  const size_t n = (size_t)(p.nx / 2 + 1) * p.ny * p.nz;
+  std::vector<char> v(n * (p.precision == SC_FP32 ? 8 : 16));
+  if (int r = sc_get_scalar(h, v.data())) return r;
+  const std::vector<char> out = convert_values(v, n, p.precision, file_precision);
+  return write_record(field_path(dir, "phi", idump).c_str(), out.data(), (long long)out.size(), 0);
+}
+
+// inputphi(phi,idump,lx1,ly,lz), inputphi.f90:1-22: loads the scalar as
+// sc_set_scalar does.
+int sc_inputphi(sc_handle* h, const char* dir, int idump, int file_precision) {
+  sc_params p{};
+  if (!h || sc_get_params(h, &p) != SC_OK) return sc::set_last_error(SC_ERR_INVALID, "null handle");
+  if (file_precision != SC_FP32 && file_precision != SC_FP64)
+    return sc::set_last_error(SC_ERR_INVALID, "file precision must be SC_FP32 or SC_FP64");
+  const size_t n = (size_t)(p.nx / 2 + 1) * p.ny * p.nz;
+  std::vector<char> in(n * (file_precision == SC_FP32 ? 8 : 16));
+  if (int r = read_record(field_path(dir, "phi", idump).c_str(), in.data(), (long long)in.size())) return r;
+  const std::vector<char> v = convert_values(in, n, file_precision, p.precision);
+  return sc_set_scalar(h, v.data());
 }
 
 }  // extern "C"

@@ -350,6 +350,17 @@ class SpectralNS:
         fp = self.p.precision if file_precision is None else file_precision
         _check(lib().sc_input3d(self.h, str(directory).encode(), int(idump), fp))
 
+    def outputphi(self, directory, idump, file_precision=None):
+        """Write the passive scalar as the reference's outputphi does:
+        <directory>/phi<idump>.dat."""
+        fp = self.p.precision if file_precision is None else file_precision
+        _check(lib().sc_outputphi(self.h, str(directory).encode(), int(idump), fp))
+
+    def inputphi(self, directory, idump, file_precision=None):
+        """Load the passive scalar from the reference's outputphi file."""
+        fp = self.p.precision if file_precision is None else file_precision
+        _check(lib().sc_inputphi(self.h, str(directory).encode(), int(idump), fp))
+
     def set_adjoint_budget(self, nbytes):
         """Bytes for the adjoint's stage-input store (< 0: 90% of free memory,
         0: pure checkpointing with recomputation)."""

@@ -71,3 +71,8 @@ def test_scalar_entry_points_reject_bad_arguments_without_gpu(specns_lib):
     assert specns_lib.sc_set_scalar(None, None) == 1
     assert specns_lib.sc_get_scalar(None, None) == 1
     assert specns_lib.sc_rot_scalar_steps(None, 1, 1.0, 0.0, 2.5, 1.0, 0, 0.0) == 1
+
+
+def test_scalar_file_entry_points_reject_bad_arguments_without_gpu(specns_lib):
+    assert specns_lib.sc_outputphi(None, b".", 0, 0) == 1
+    assert specns_lib.sc_inputphi(None, b".", 0, 0) == 1

@@ -230,3 +230,31 @@ def test_hermitianize(specns_lib, prec):
     (cc,) = cast([c], prec)
     f.hermitianize_(cc.ctypes.data_as(C.c_void_p), *ref_int(n // 2 + 1, n, n))
     assert rel_l2(cc, R.hermitianize(c)) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_outputphi_inputphi_files_and_round_trip(specns_lib, prec, tmp_path):
+    """sc_outputphi / sc_inputphi: the scalar as outputphi.f90 writes it
+    (phi<n>.dat, one Fortran unformatted record of complex(sp)
+    (nx/2+1, ny, nz)), bit for bit, and back, also through a file of the
+    other precision."""
+    import os
+    from oracle import fortran_record as FR
+    n = 16
+    phi = hermitian_fields((n, n, n), 13, ncomp=1)[0]
+    dt = np.complex128 if prec == S.SC_FP64 else np.complex64
+    with handle(n, prec) as h:
+        h.set_scalar(phi)
+        ref = h.get_scalar()
+        h.outputphi(tmp_path, 4)
+        raw = open(os.path.join(tmp_path, "phi4.dat"), "rb").read()
+        assert np.array_equal(np.frombuffer(FR.read_record(raw), dtype=dt).reshape(ref.shape), ref)
+        h.set_scalar(np.zeros_like(ref))
+        h.inputphi(tmp_path, 4)
+        assert np.array_equal(h.get_scalar(), ref)
+        other = S.SC_FP32 if prec == S.SC_FP64 else S.SC_FP64
+        h.outputphi(tmp_path, 5, file_precision=other)
+        h.inputphi(tmp_path, 5, file_precision=other)
+        assert rel_l2(h.get_scalar(), ref) < (1e-7 if prec == S.SC_FP64 else 1e-15)
+        with pytest.raises(S.SpecNSError):
+            h.inputphi(tmp_path, 99)
