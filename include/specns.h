@@ -136,6 +136,16 @@ int sc_ab2_steps(sc_handle* h, int npasses);
  * keeps the pass count and dto (two extra groups of three fields);
  * sc_set_state and sc_init_field restart at pass 0. */
 int sc_ab2v_pass(sc_handle* h, double dt);
+/* One pass of spectral_dns_scalar.f90:222-342: the variable-step IF-AB2 of
+ * sc_ab2v_pass carrying the passive scalar of sc_set_scalar.  Velocity RHS:
+ * Lamb vector, force, symmetrize (its five-argument symmetrize(w, k2, ...)
+ * read as symmetrize3d), projection; scalar RHS: convecphi_dns, minus
+ * meangrad * v_z when scalarforced (:244-246), symmetrized; the scalar
+ * advances with exp(-nu k^2 dt / pr); v is not truncated after the update.
+ * history_rhs = 0 keeps the program as written: pass 0 saves phi after its
+ * update as the scalar's history (outputphi(phi, 0), :278); 1 saves wphi.
+ * Shares the pass count and dto of sc_ab2v_pass; sc_set_scalar restarts. */
+int sc_ab2v_scalar_pass(sc_handle* h, double dt, double pr, int scalarforced, double meangrad, int history_rhs);
 /* The variable-step AB2's pass count and previous step dto (0 before the
  * first pass). */
 int sc_ab2v_state(sc_handle* h, int* pass, double* dto);

@@ -585,6 +585,66 @@ def ab2v_weights(ipass, dt, dto):
     return (1.0 + 0.5 * dtt) * dt, -0.5 * dtt * dt, 0.0
 
 
+def ab2v_scalar_run(v, phi, grid: Grid, dts, pr, scalarforced=False, meangrad=0.0, history="as_written",
+                    trace=None):
+    """Passes of spectral_dns_scalar.f90:222-342, the variable-step IF-AB2
+    with a passive scalar.  Its `symmetrize(w, k2, lx1, ly, lz)` calls
+    (:248-251) have five arguments, matching none of symmetrize.f90's forms;
+    dealiasing.f90:1 states that dealiasing differs from symmetrize only in
+    its last statement (the 2/3 mask), so they are read as symmetrize3d with
+    an unused k2.  Per pass: the velocity RHS of ratesdudt (vorticity, Lamb
+    vector, force, symmetrize, projection, :222-254); wphi = convecphi_dns
+    (:236), minus meangrad v_z when scalarforced (:244-246; the reference
+    derives meangrad from epsphi, u0, phirms and a placeholder constant,
+    :8, :87), symmetrized (:251); then the variable-step updates of
+    spectral_dns.f90 for v and, with exp(-nu k2 dt / pr), for phi
+    (:265-339), with no truncation of v afterwards.  As written, pass 0
+    saves phi after its update as the scalar's history (outputphi(phi, 0),
+    :278, read back at :308), not wphi: pass 2 uses that value; the
+    velocity's history is w (:277).  history="rhs" saves wphi instead (the
+    evident intent, as spectral_rot_dns_scalar_ft.f90:237 does).  Returns
+    (v, phi, time, dto); with a list
+    `trace`, each pass appends (w, wphi, v after it, phi after it)."""
+    p = grid.p
+    k2 = grid.k2
+    v0 = [np.array(a, dtype=np.complex128) for a in v]
+    v = list(v0)
+    phi0 = np.array(phi, dtype=np.complex128)
+    phi = phi0
+    o = o0 = ophi = None
+    t, dto = 0.0, None
+    for ip, dt in enumerate(dts):
+        w = ratesdudt(v, grid)
+        wphi = convecphi_dns(v[0], v[1], v[2], phi, p.nx)
+        if scalarforced:
+            wphi = wphi - meangrad * v[2]
+        wphi = symmetrize3d(wphi)
+        e1, e1p = np.exp(-p.nu * k2 * dt), np.exp(-p.nu * k2 * dt / pr)
+        if ip == 0:
+            v = [(a + dt * b) * e1 for a, b in zip(v, w)]
+            phi = (phi + dt * wphi) * e1p
+            dto = dt
+            o0, ophi = w, (phi if history == "as_written" else wphi)   # :277-278
+        elif ip == 1:
+            S, ek, dl = ab2v_weights(1, dt, dto)
+            e0, e0p = np.exp(-p.nu * k2 * dto), np.exp(-p.nu * k2 * dto / pr)
+            v = [(S * a0 * e0 + ek * a + dl * b) * e1 for a0, a, b in zip(v0, v, w)]
+            phi = (S * phi0 * e0p + ek * phi + dl * wphi) * e1p
+            dto = dt + dto
+            o = o0                                                     # :307-308
+        else:
+            S, ek, _ = ab2v_weights(ip, dt, dto)
+            e0, e0p = np.exp(-p.nu * k2 * dto), np.exp(-p.nu * k2 * dto / pr)
+            v = [(a + S * b + ek * c * e0) * e1 for a, b, c in zip(v, w, o)]
+            phi = (phi + S * wphi + ek * ophi * e0p) * e1p
+            o, ophi = w, wphi
+            dto = dt
+        t += dt
+        if trace is not None:
+            trace.append((w, wphi, tuple(v), phi))
+    return tuple(v), phi, t, dto
+
+
 def ab2v_run(v, grid: Grid, dts, sgs_state=None, trace=None):
     """Passes of the variable-step IF-AB2 of spectral_dns.f90:210-290
     (spectral_les.f90:240-316) with steps dts[p]: pass 0 an integrating-factor

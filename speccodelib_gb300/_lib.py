@@ -49,6 +49,7 @@ SIGNATURES = {
     "sc_get_scalar": ([_P, _P], _I),
     "sc_rot_scalar_steps": ([_P, _I, _D, _D, _D, _D, _I, _D], _I),
     "sc_ab2v_pass": ([_P, _D], _I),
+    "sc_ab2v_scalar_pass": ([_P, _D, _D, _I, _D, _I], _I),
     "sc_ab2v_state": ([_P, C.POINTER(_I), C.POINTER(_D)], _I),
     "sc_ab2v_dt": ([_D, _D, _D, _D, _D, C.POINTER(_D)], _I),
     "sc_diagnostics": ([_P, _P, _P], _I),

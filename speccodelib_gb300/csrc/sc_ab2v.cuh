@@ -65,4 +65,31 @@ __host__ __device__ inline void ab2v_point(int pass, int k2, bool zero, T nu, T 
     for (int c = 0; c < 3; ++c) v[c] = cx(T(0), T(0));
 }
 
+// The passive scalar of spectral_dns_scalar.f90 on the same passes, with
+// exp(-nu k2 dt / pr) (:267-329).  The history saved at pass 0 is phi after
+// its update when hist_rhs is false, as written (outputphi(phi, 0), :278,
+// read back at :308), else wphi (the evident intent).
+//   pass 0: phi0 = phi, phi = (phi + dt wphi) e(dt), ophi = phi or wphi
+//   pass 1: phi = (S phi0 e(dto) + ek phi + delta wphi) e(dt)
+//   pass >= 2: phi = (phi + S wphi + ek ophi e(dto)) e(dt), ophi = wphi
+template <typename T>
+__host__ __device__ inline void ab2v_scalar_point(int pass, int k2, bool hist_rhs, T nu, T dt, T dto, T pr, T s, T ek,
+                                                  T dl, Cx<T>& phi, Cx<T> wphi, Cx<T>& ophi, Cx<T>& phi0) {
+  const T e1 = exp(-(T)k2 * nu * dt / pr);
+  if (pass == 0) {
+    phi0 = phi;
+    phi = cx_scale(cx_add(phi, cx_scale(wphi, dt)), e1);                                   // :273
+    ophi = hist_rhs ? wphi : phi;
+    return;
+  }
+  const T e0 = exp(-(T)k2 * nu * dto / pr);
+  Cx<T> pn;
+  if (pass == 1)                                                                            // :295
+    pn = cx_add(cx_add(cx_scale(cx_scale(phi0, s), e0), cx_scale(phi, ek)), cx_scale(wphi, dl));
+  else                                                                                      // :321
+    pn = cx_add(cx_add(phi, cx_scale(wphi, s)), cx_scale(cx_scale(ophi, ek), e0));
+  phi = cx_scale(pn, e1);                                                                   // :303, :329
+  if (pass >= 2) ophi = wphi;                                                               // :335
+}
+
 }  // namespace sc

@@ -357,7 +357,16 @@ template <typename T> struct Ab2vArgs {
   C2<T>* v0[3];          // initial field (written at pass 0, read at pass 1)
   double nu, dt, dto;    // viscosity, this step, the previous step
   double s, ek, dl;      // the pass's weights
-  double kcut2;          // v = 0 where k2 >= kcut2 and at the mean mode
+  double kcut2;          // v = 0 where k2 >= kcut2 and at the mean mode (when mask_v)
+  int mask_v;
+  // passive scalar (when phi is set): phi, its right-hand side, its history,
+  // the initial phi; Prandtl number; hist_rhs: history at pass 0 is wphi
+  C2<T>* phi;
+  const C2<T>* wphi;
+  C2<T>* ophi;
+  C2<T>* phi0;
+  double pr;
+  int hist_rhs;
 };
 
 template <typename T>
@@ -389,7 +398,23 @@ __global__ void __launch_bounds__(256) ab2v_update_kernel(Ab2vArgs<T> aa, Geom g
         v0[c] = cx(zc.x, zc.y);
       }
     }
-    ab2v_point<T>(pass, k2, k2 >= kc_b || k2 == 0, nu, dt, dto, s, ek, dl, v, w, o, v0);
+    ab2v_point<T>(pass, k2, aa.mask_v && (k2 >= kc_b || k2 == 0), nu, dt, dto, s, ek, dl, v, w, o, v0);
+    if (aa.phi) {
+      const C p = aa.phi[idx], wp = aa.wphi[idx];
+      Cx<T> ph = cx(p.x, p.y), op = cx(T(0), T(0)), p0 = cx(T(0), T(0));
+      if (pass >= 2) {
+        const C q = aa.ophi[idx];
+        op = cx(q.x, q.y);
+      }
+      if (pass == 1) {
+        const C q = aa.phi0[idx];
+        p0 = cx(q.x, q.y);
+      }
+      ab2v_scalar_point<T>(pass, k2, aa.hist_rhs != 0, nu, dt, dto, (T)aa.pr, s, ek, dl, ph, cx(wp.x, wp.y), op, p0);
+      aa.phi[idx] = mk<C>(ph.re, ph.im);
+      if (pass != 1) aa.ophi[idx] = mk<C>(op.re, op.im);
+      if (pass == 0) aa.phi0[idx] = mk<C>(p0.re, p0.im);
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       aa.v[c][idx] = mk<C>(v[c].re, v[c].im);

@@ -728,21 +728,59 @@ template <typename T> struct Impl {
   // right-hand side without symmetrize (the same passes as sc_rhs, into the
   // S_A slots), then ab2v_update_kernel.  The previous right-hand side and
   // the initial field live in h->aux2; h->ab2v_dto is the reference's dto.
-  static int ab2v_pass(sc_handle* h, double dt) {
+  // The passive scalar of spectral_dns_scalar.f90 (sc_ab2v_scalar_pass).
+  struct Ab2vScalar {
+    double pr;          // Prandtl number
+    int forced;         // wphi -= meangrad v_z (:244-246)
+    double meangrad;
+    int hist_rhs;       // history at pass 0: wphi (1) or, as written, phi after the update (0)
+  };
+
+  // With `sc`, one pass of spectral_dns_scalar.f90:222-342 instead: the
+  // velocity RHS with symmetrize (its five-argument symmetrize read as
+  // symmetrize3d), wphi = convecphi_dns (- meangrad v_z), symmetrized, both
+  // advanced, and v not truncated after the update.
+  static int ab2v_pass(sc_handle* h, double dt, const Ab2vScalar* sc = nullptr) {
     auto* g = &h->g;
     SC_TRY(ensure_fields(h, &h->aux2, &h->aux2_fields, 6));
+    if (sc) SC_TRY(ensure_aux(h, RA_FIELDS));
     C* ab = reinterpret_cast<C*>(h->aux2);
     const int pass = h->ab2v_pass;
+    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    if (sc) {
+      const size_t fb = h->csize * g->field;
+      for (int c = 0; c < 3; ++c)
+        SC_CUDA(cudaMemcpyAsync(F(h, S_W + c), vin[c], fb, cudaMemcpyDeviceToDevice, h->stream));
+      SC_CUDA(cudaMemcpyAsync(F(h, S_W + 3), AX(h, RA_PHI), fb, cudaMemcpyDeviceToDevice, h->stream));
+      SC_CUDA(cudaMemsetAsync(F(h, S_W + 4), 0, 2 * fb, h->stream));
+      SC_TRY(convecphi_core(h));
+      SC_CUDA(cudaMemcpyAsync(AX(h, RA_WPHI), F(h, S_W), fb, cudaMemcpyDeviceToDevice, h->stream));
+    }
     sc::StageArgs<T> st = stage_args(h);
     st.mode = sc::SM_RHS;
-    st.symmetrize = 0;
-    const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+    st.symmetrize = sc ? 1 : 0;
     // dynsmag's update flag is .true. at first, then mod(istep, 10) == 0 of
     // the previous pass: refreshes on passes 0, 1, 11, 21, ...
     // (spectral_les.f90:140,205-208)
     if (h->p.sgs == SC_SGS_DYNSMAG && (pass == 0 || (pass - 1) % h->p.dyn_every == 0)) SC_TRY(dyn_update(h, vin));
     SC_TRY(rhs_pipeline(h, vin, st));
     h->ab2_pass = 0;   // the S_A slots held the fixed-step AB2's history
+    if (sc) {
+      sc::SpecOpArgs<T> oa{};
+      oa.f[0] = AX(h, RA_WPHI);
+      oa.nfields = 1;
+      if (sc->forced) {   // wphi = wphi - meangrad v_z
+        oa.gsrc[0] = vin[2];
+        oa.op = sc::OP_AXPBY;
+        oa.a = 1.0;
+        oa.b = -sc->meangrad;
+        SC_TRY(specop(h, oa));
+      }
+      for (int op : {sc::OP_ZERO_PLANES, sc::OP_KX0_COPY}) {
+        oa.op = op;
+        SC_TRY(specop(h, oa));
+      }
+    }
     sc::Ab2vArgs<T> aa{};
     aa.pass = pass < 2 ? pass : 2;
     for (int c = 0; c < 3; ++c) {
@@ -756,6 +794,15 @@ template <typename T> struct Impl {
     aa.dto = h->ab2v_dto;
     aa.kcut2 = kcut2(h);
     sc::ab2v_weights(pass, dt, h->ab2v_dto, aa.s, aa.ek, aa.dl);
+    aa.mask_v = sc ? 0 : 1;
+    if (sc) {
+      aa.phi = AX(h, RA_PHI);
+      aa.wphi = AX(h, RA_WPHI);
+      aa.ophi = AX(h, RA_OPHI);
+      aa.phi0 = AX(h, RA_PHI0);
+      aa.pr = sc->pr;
+      aa.hist_rhs = sc->hist_rhs;
+    }
     SC_TRY(launch(h, "ab2v_update", [&] { return L::ab2v(aa, *g, h->stream); }));
     h->ab2v_dto = pass == 1 ? dt + h->ab2v_dto : dt;   // :227, :249, :275
     h->ab2v_pass += 1;
@@ -926,6 +973,7 @@ template <typename T> struct Impl {
     SC_TRY(copy_in(h, AX(h, RA_PHI), phi));
     SC_CUDA(cudaStreamSynchronize(h->stream));
     h->rot_pass = 0;
+    h->ab2v_pass = 0;
     return SC_OK;
   }
   static int get_scalar(sc_handle* h, void* phi) {
@@ -1744,6 +1792,21 @@ int sc_ab2_steps(sc_handle* h, int npasses) {
 int sc_ab2v_pass(sc_handle* h, double dt) {
   if (!h || !std::isfinite(dt) || !(dt > 0.0)) return fail(SC_ERR_INVALID, "need a handle and a finite dt > 0");
   SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::ab2v_pass(h, dt) : Impl<double>::ab2v_pass(h, dt));
+  SC_CUDA(cudaGetLastError());
+  return check_derr(h);
+}
+
+int sc_ab2v_scalar_pass(sc_handle* h, double dt, double pr, int scalarforced, double meangrad, int history_rhs) {
+  if (!h || !std::isfinite(dt) || !(dt > 0.0)) return fail(SC_ERR_INVALID, "need a handle and a finite dt > 0");
+  if (!std::isfinite(pr) || !(pr > 0.0) || !std::isfinite(meangrad)) return fail(SC_ERR_INVALID, "need pr > 0, finite meangrad");
+  if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the scalar solver has no SGS model");
+  if (h->p.precision == SC_FP32) {
+    const Impl<float>::Ab2vScalar sc{pr, scalarforced, meangrad, history_rhs};
+    SC_TRY(Impl<float>::ab2v_pass(h, dt, &sc));
+  } else {
+    const Impl<double>::Ab2vScalar sc{pr, scalarforced, meangrad, history_rhs};
+    SC_TRY(Impl<double>::ab2v_pass(h, dt, &sc));
+  }
   SC_CUDA(cudaGetLastError());
   return check_derr(h);
 }

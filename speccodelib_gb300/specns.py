@@ -291,6 +291,12 @@ class SpectralNS:
         """One pass of the variable-step IF-AB2 (spectral_dns.f90:210-290)."""
         _check(lib().sc_ab2v_pass(self.h, C.c_double(dt)))
 
+    def ab2v_scalar_pass(self, dt, pr=1.0, scalarforced=False, meangrad=0.0, history_rhs=False):
+        """One pass of spectral_dns_scalar.f90's variable-step IF-AB2 with the
+        passive scalar (history_rhs: save wphi, not phi, at pass 0)."""
+        _check(lib().sc_ab2v_scalar_pass(self.h, C.c_double(dt), C.c_double(pr), 1 if scalarforced else 0,
+                                         C.c_double(meangrad), 1 if history_rhs else 0))
+
     def ab2v_state(self):
         """(pass count, previous step dto) of the variable-step IF-AB2."""
         p, d = C.c_int(), C.c_double()

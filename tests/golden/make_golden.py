@@ -13,8 +13,9 @@ energy and dissipation (python tests/golden/make_golden.py c1; a few minutes).
 schemes16: from the same 16^3 field, the rotating solver after 5 passes
 (om = 5, band forcing 1 <= |k| < 2.5), the same with a passive scalar (a
 seeded dealiased white-noise phi, pr = 0.7, scalar forcing on) and the
-variable-step IF-AB2 after 6 uneven steps (cut at k >= nx/2)
-(python tests/golden/make_golden.py schemes).  The
+variable-step IF-AB2 after 6 uneven steps (cut at k >= nx/2), and the
+variable-step scalar solver after the same steps (mean-gradient forcing, the
+history as written) (python tests/golden/make_golden.py schemes).  The
 reference itself cannot be run here; these fixtures freeze the oracle's
 outputs so that both the oracle and the CUDA library are checked against the
 same committed numbers.
@@ -92,9 +93,12 @@ def schemes():
     v_rs, phi_rs, _, _ = R.rot_scalar_run(v0, phi0, g, 5, 5.0, 1.0, 2.5, 0.7, True, 0.05)
     gv = R.Grid(R.Params(nx=N, nu=NU, forced=True, eps=0.1, kcut=N // 2))
     v_ab2v, t, dto = R.ab2v_run(v0, gv, STEPS_V)
+    phis = R.symmetrize3d(phi0)
+    v_vs, phi_vs, _, _ = R.ab2v_scalar_run(v0, phis, g, STEPS_V, 0.7, True, 0.3)
     np.savez_compressed(os.path.join(HERE, "schemes16.npz"), v0=np.stack(v0), v_rot5=np.stack(v_rot),
                         phi0=phi0, v_rs5=np.stack(v_rs), phi_rs5=phi_rs, v_ab2v=np.stack(v_ab2v),
-                        steps_v=np.array(STEPS_V), t_ab2v=t, dto_ab2v=dto, n=N, nu=NU, dt=DT)
+                        steps_v=np.array(STEPS_V), t_ab2v=t, dto_ab2v=dto, v_vs=np.stack(v_vs),
+                        phi_vs=phi_vs, n=N, nu=NU, dt=DT)
 
 
 if __name__ == "__main__":

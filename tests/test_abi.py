@@ -76,3 +76,7 @@ def test_scalar_entry_points_reject_bad_arguments_without_gpu(specns_lib):
 def test_scalar_file_entry_points_reject_bad_arguments_without_gpu(specns_lib):
     assert specns_lib.sc_outputphi(None, b".", 0, 0) == 1
     assert specns_lib.sc_inputphi(None, b".", 0, 0) == 1
+
+
+def test_ab2v_scalar_pass_rejects_bad_arguments_without_gpu(specns_lib):
+    assert specns_lib.sc_ab2v_scalar_pass(None, 1e-3, 1.0, 0, 0.0, 0) == 1

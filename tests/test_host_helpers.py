@@ -232,28 +232,32 @@ def test_rotating_scalar_update_matches_oracle(tmp_path):
         assert rel_l2(out[1, p, 3], pref) < 1e-5, p
 
 
-AB2V_PROGRAM = r'''
+AB2V_PROGRAM = r"""
 #include <cstdio>
 #include <vector>
 #include "sc_common.cuh"
 #include "sc_ab2v.cuh"
-// Reads: int nx, ny, nz, npasses; double nu, kcut2; npasses steps dt; v0
-// (3 fields), then npasses right-hand sides (3 fields each), complex128
-// (nz, ny, nx/2+1).  Writes, for T = double then float, v after every pass,
-// with the weights and the dto bookkeeping of the library's ab2v_pass.
+// Reads: int nx, ny, nz, npasses, scalar, hist_rhs; double nu, kcut2, pr;
+// npasses steps dt; v0 (3 fields) [phi0 when scalar], then per pass the
+// right-hand side (3 fields) [and wphi], complex128 (nz, ny, nx/2+1).
+// Writes, for T = double then float, v [and phi] after every pass, with the
+// weights and the dto bookkeeping of the library's ab2v_pass; with a scalar
+// the velocity is not truncated, as in ab2v_update_kernel.
 template <typename T>
-static void run(int nx, int ny, int nz, int np, double nu, double kcut2, const std::vector<double>& dts,
-                const std::vector<double>& vin, const std::vector<double>& ws, FILE* out) {
+static void run(const int* hd, const double* sc, const std::vector<double>& dts, const std::vector<double>& in0,
+                const std::vector<double>& ws, FILE* out) {
+  const int nx = hd[0], ny = hd[1], nz = hd[2], np = hd[3], scalar = hd[4], hist = hd[5];
+  const int nf = scalar ? 4 : 3;
   const long long nxh = nx / 2 + 1, field = (long long)nz * ny * nxh;
-  std::vector<sc::Cx<T>> v(3 * field), o(3 * field), v0(3 * field);
-  for (long long i = 0; i < 3 * field; ++i) v[i] = sc::cx((T)vin[2 * i], (T)vin[2 * i + 1]);
-  const int kc = sc::k2_lt(kcut2);
+  std::vector<sc::Cx<T>> f(nf * field), o(3 * field), v0(3 * field), op(field), p0(field);
+  for (long long i = 0; i < nf * field; ++i) f[i] = sc::cx((T)in0[2 * i], (T)in0[2 * i + 1]);
+  const int kc = sc::k2_lt(sc[1]);
   double dto = 0.0;
   for (int p = 0; p < np; ++p) {
     const double dt = dts[p];
     double s, ek, dl;
     sc::ab2v_weights(p, dt, dto, s, ek, dl);
-    const double* w = ws.data() + (size_t)p * 6 * field;
+    const double* w = ws.data() + (size_t)p * 2 * nf * field;
     for (int iz = 0; iz < nz; ++iz)
       for (int iy = 0; iy < ny; ++iy)
         for (int ix = 0; ix < nxh; ++ix) {
@@ -262,22 +266,27 @@ static void run(int nx, int ny, int nz, int np, double nu, double kcut2, const s
           const int k2 = ix * ix + ky * ky + kz * kz;
           sc::Cx<T> vv[3], ww[3], oo[3], zz[3];
           for (int c = 0; c < 3; ++c) {
-            vv[c] = v[c * field + idx];
+            vv[c] = f[c * field + idx];
             oo[c] = o[c * field + idx];
             zz[c] = v0[c * field + idx];
             ww[c] = sc::cx((T)w[2 * (c * field + idx)], (T)w[2 * (c * field + idx) + 1]);
           }
-          sc::ab2v_point<T>(p < 2 ? p : 2, k2, k2 >= kc || k2 == 0, (T)nu, (T)dt, (T)dto, (T)s, (T)ek, (T)dl,
-                            vv, ww, oo, zz);
+          sc::ab2v_point<T>(p < 2 ? p : 2, k2, !scalar && (k2 >= kc || k2 == 0), (T)sc[0], (T)dt, (T)dto, (T)s,
+                            (T)ek, (T)dl, vv, ww, oo, zz);
           for (int c = 0; c < 3; ++c) {
-            v[c * field + idx] = vv[c];
+            f[c * field + idx] = vv[c];
             o[c * field + idx] = oo[c];
             v0[c * field + idx] = zz[c];
           }
+          if (scalar) {
+            const sc::Cx<T> wp = sc::cx((T)w[2 * (3 * field + idx)], (T)w[2 * (3 * field + idx) + 1]);
+            sc::ab2v_scalar_point<T>(p < 2 ? p : 2, k2, hist != 0, (T)sc[0], (T)dt, (T)dto, (T)sc[2], (T)s, (T)ek,
+                                     (T)dl, f[3 * field + idx], wp, op[idx], p0[idx]);
+          }
         }
     dto = p == 1 ? dt + dto : dt;
-    for (long long i = 0; i < 3 * field; ++i) {
-      const double z[2] = {(double)v[i].re, (double)v[i].im};
+    for (long long i = 0; i < nf * field; ++i) {
+      const double z[2] = {(double)f[i].re, (double)f[i].im};
       fwrite(z, sizeof(double), 2, out);
     }
   }
@@ -286,40 +295,28 @@ int main(int argc, char** argv) {
   FILE* in = fopen(argv[1], "rb");
   FILE* out = fopen(argv[2], "wb");
   if (!in || !out) return 2;
-  int hd[4];
-  double sc2[2];
-  if (fread(hd, sizeof(int), 4, in) != 4 || fread(sc2, sizeof(double), 2, in) != 2) return 3;
+  int hd[6];
+  double sc[3];
+  if (fread(hd, sizeof(int), 6, in) != 6 || fread(sc, sizeof(double), 3, in) != 3) return 3;
   std::vector<double> dts(hd[3]);
   if (fread(dts.data(), sizeof(double), dts.size(), in) != dts.size()) return 4;
+  const int nf = hd[4] ? 4 : 3;
   const long long field = (long long)hd[2] * hd[1] * (hd[0] / 2 + 1);
-  std::vector<double> v0(6 * field), ws((size_t)hd[3] * 6 * field);
-  if (fread(v0.data(), sizeof(double), v0.size(), in) != v0.size()) return 5;
+  std::vector<double> in0(2 * nf * field), ws((size_t)hd[3] * 2 * nf * field);
+  if (fread(in0.data(), sizeof(double), in0.size(), in) != in0.size()) return 5;
   if (fread(ws.data(), sizeof(double), ws.size(), in) != ws.size()) return 6;
-  run<double>(hd[0], hd[1], hd[2], hd[3], sc2[0], sc2[1], dts, v0, ws, out);
-  run<float>(hd[0], hd[1], hd[2], hd[3], sc2[0], sc2[1], dts, v0, ws, out);
+  run<double>(hd, sc, dts, in0, ws, out);
+  run<float>(hd, sc, dts, in0, ws, out);
   fclose(out);
   return 0;
 }
-'''
+"""
 
 
-def test_variable_step_ab2_update_matches_oracle(tmp_path):
-    """The per-mode variable-step IF-AB2 update that ab2v_update_kernel runs
-    (ab2v_point and ab2v_weights, sc_ab2v.cuh),
-    compiled for the host, reproduces the oracle's passes of
-    spectral_dns.f90:210-290 on an uneven step sequence when fed the
-    oracle's right-hand sides: FP64 to 1e-13, FP32 to 1e-5."""
-    from oracle import spectral_ref as R
-    from _util import rel_l2, solenoidal_init
+def _run_ab2v_program(tmp_path, n, dts, header_d, hist, start, per_pass):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    n = 16
-    dts = [2e-3, 2.6e-3, 1.4e-3, 2.2e-3, 1.8e-3]
-    g = R.Grid(R.Params(nx=n, nu=0.01, forced=True, eps=0.1, kcut=n // 2))
-    v0 = solenoidal_init(n)
-    trace = []
-    R.ab2v_run(v0, g, dts, trace=trace)
     src = tmp_path / "ab2v.cu"
     src.write_text(AB2V_PROGRAM)
     exe = tmp_path / "ab2v"
@@ -327,17 +324,58 @@ def test_variable_step_ab2_update_matches_oracle(tmp_path):
            "-I", CSRC, str(src), "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+    nf = len(start)
     fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
     with open(fin, "wb") as f:
-        f.write(np.array([n, n, n, len(dts)], np.int32).tobytes())
-        f.write(np.array([g.p.nu, g.p.kcut ** 2], np.float64).tobytes())
+        f.write(np.array([n, n, n, len(dts), 1 if nf == 4 else 0, hist], np.int32).tobytes())
+        f.write(np.array(header_d, np.float64).tobytes())
         f.write(np.array(dts, np.float64).tobytes())
-        f.write(np.ascontiguousarray(np.stack(v0), np.complex128).tobytes())
-        for w, _ in trace:
-            f.write(np.ascontiguousarray(np.stack(w), np.complex128).tobytes())
+        f.write(np.ascontiguousarray(np.stack(start), np.complex128).tobytes())
+        for fields in per_pass:
+            f.write(np.ascontiguousarray(np.stack(fields), np.complex128).tobytes())
     r = subprocess.run([str(exe), str(fin), str(fout)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout[-500:]
-    out = np.fromfile(fout, np.complex128).reshape(2, len(dts), 3, n, n, n // 2 + 1)
+    return np.fromfile(fout, np.complex128).reshape(2, len(dts), nf, n, n, n // 2 + 1)
+
+
+def test_variable_step_ab2_update_matches_oracle(tmp_path):
+    """The per-mode variable-step IF-AB2 update that ab2v_update_kernel runs
+    (ab2v_point and ab2v_weights, sc_ab2v.cuh), compiled for the host,
+    reproduces the oracle's passes of spectral_dns.f90:210-290 on an uneven
+    step sequence when fed the oracle's right-hand sides: FP64 to 1e-13,
+    FP32 to 1e-5."""
+    from oracle import spectral_ref as R
+    from _util import rel_l2, solenoidal_init
+    n = 16
+    dts = [2e-3, 2.6e-3, 1.4e-3, 2.2e-3, 1.8e-3]
+    g = R.Grid(R.Params(nx=n, nu=0.01, forced=True, eps=0.1, kcut=n // 2))
+    v0 = solenoidal_init(n)
+    trace = []
+    R.ab2v_run(v0, g, dts, trace=trace)
+    out = _run_ab2v_program(tmp_path, n, dts, [g.p.nu, g.p.kcut ** 2, 1.0], 0, list(v0),
+                            [list(w) for w, _ in trace])
     for p, (_, vref) in enumerate(trace):
         assert rel_l2(list(out[0, p]), list(vref)) < 1e-13, p
         assert rel_l2(list(out[1, p]), list(vref)) < 1e-5, p
+
+
+@pytest.mark.parametrize("history", ["as_written", "rhs"])
+def test_variable_step_scalar_update_matches_oracle(tmp_path, history):
+    """The same with the passive scalar of spectral_dns_scalar.f90
+    (ab2v_scalar_point, both scalar histories; velocity not truncated)."""
+    from oracle import spectral_ref as R
+    from _util import hermitian_fields, rel_l2, solenoidal_init
+    n = 16
+    dts = [2e-3, 2.6e-3, 1.4e-3, 2.2e-3, 1.8e-3]
+    g = R.Grid(R.Params(nx=n, nu=0.01, forced=True, eps=0.1))
+    v0 = solenoidal_init(n)
+    phi0 = R.symmetrize3d(hermitian_fields((n, n, n), 7, ncomp=1)[0])
+    trace = []
+    R.ab2v_scalar_run(v0, phi0, g, dts, 0.7, True, 0.3, history=history, trace=trace)
+    out = _run_ab2v_program(tmp_path, n, dts, [g.p.nu, 0.0, 0.7], 1 if history == "rhs" else 0,
+                            list(v0) + [phi0], [list(w) + [wphi] for w, wphi, _, _ in trace])
+    for p, (_, _, vref, pref) in enumerate(trace):
+        assert rel_l2(list(out[0, p, :3]), list(vref)) < 1e-13, p
+        assert rel_l2(out[0, p, 3], pref) < 1e-13, p
+        assert rel_l2(list(out[1, p, :3]), list(vref)) < 1e-5, p
+        assert rel_l2(out[1, p, 3], pref) < 1e-5, p

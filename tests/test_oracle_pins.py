@@ -307,6 +307,8 @@ def test_golden_scheme_fixtures_reproduce():
     v, t, dto = R.ab2v_run(v0, gv, list(d["steps_v"]))
     assert rel_l2(v, list(d["v_ab2v"])) < 1e-14
     assert abs(t - float(d["t_ab2v"])) < 1e-15 and dto == float(d["dto_ab2v"])
+    v, phi, _, _ = R.ab2v_scalar_run(v0, R.symmetrize3d(d["phi0"]), g, list(d["steps_v"]), 0.7, True, 0.3)
+    assert rel_l2(v, list(d["v_vs"])) < 1e-14 and rel_l2(phi, d["phi_vs"]) < 1e-14
 
 
 def test_hermitianize_is_symmetrize_without_zeroing():
@@ -327,3 +329,25 @@ def test_hermitianize_is_symmetrize_without_zeroing():
     real = R.r2c(rng.standard_normal((n, n, n)))
     assert np.array_equal(R.hermitianize(R.hermitianize(c)), h)
     assert rel_l2(R.hermitianize(real), real) < 1e-15
+
+
+def test_variable_step_scalar_known_answers():
+    """spectral_dns_scalar.f90's variable-step scalar: with no velocity (and
+    the mean-gradient forcing acting on v_z = 0) it only diffuses, exactly as
+    exp(-nu k^2 t / pr) over uneven steps when the pass-0 history is wphi;
+    as written (phi after pass 0 saved as the history, :278) the second AB2
+    pass picks up a spurious ek phi_1 term, 1e-3 here; the Roberts velocity
+    still decays exactly."""
+    n = 16
+    g = R.Grid(R.Params(nx=n, nu=0.05, forced=False))
+    phi = R.symmetrize3d(hermitian_fields((n, n, n), 7, ncomp=1)[0])
+    zero = [np.zeros_like(phi) for _ in range(3)]
+    dts = [0.01, 0.013, 0.007, 0.011, 0.009, 0.012]
+    _, out, t, _ = R.ab2v_scalar_run(zero, phi, g, dts, 0.7, True, 0.3, history="rhs")
+    exact = phi * np.exp(-0.05 * g.k2 * t / 0.7)
+    assert rel_l2(out, exact) < 1e-14
+    _, out, _, _ = R.ab2v_scalar_run(zero, phi, g, dts, 0.7, True, 0.3)
+    assert 1e-4 < rel_l2(out, exact) < 1e-2
+    v = roberts(n)
+    out_v, _, t, _ = R.ab2v_scalar_run(v, phi, g, dts, 0.7)
+    assert rel_l2(out_v, [a * np.exp(-2 * 0.05 * t) for a in v]) < 1e-14

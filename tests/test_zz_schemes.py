@@ -215,6 +215,13 @@ def test_schemes_against_committed_golden_fixtures(specns_lib, prec):
         for s in d["steps_v"]:
             h.ab2v_pass(float(s))
         assert rel_l2(h.get_state(), list(d["v_ab2v"])) < TOL[prec]
+    with handle(n, prec, nu=nu, forced=1, eps=0.1) as h:
+        h.set_state(*v0)
+        h.set_scalar(R.symmetrize3d(d["phi0"]))
+        for s in d["steps_v"]:
+            h.ab2v_scalar_pass(float(s), pr=0.7, scalarforced=True, meangrad=0.3)
+        assert rel_l2(h.get_state(), list(d["v_vs"])) < TOL[prec]
+        assert rel_l2(h.get_scalar(), d["phi_vs"]) < TOL[prec]
 
 
 @pytest.mark.parametrize("prec", PRECS)
@@ -258,3 +265,24 @@ def test_outputphi_inputphi_files_and_round_trip(specns_lib, prec, tmp_path):
         assert rel_l2(h.get_scalar(), ref) < (1e-7 if prec == S.SC_FP64 else 1e-15)
         with pytest.raises(S.SpecNSError):
             h.inputphi(tmp_path, 99)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("history", ["as_written", "rhs"])
+def test_variable_step_scalar_matches_oracle(specns_lib, prec, history):
+    """Passes of spectral_dns_scalar.f90's variable-step IF-AB2 with the
+    passive scalar, mean-gradient forcing on, both scalar histories, against
+    the oracle."""
+    n = 32
+    v = solenoidal_init(n)
+    g = oracle_grid(n, nu=0.01, forced=True, eps=0.1)
+    phi = R.symmetrize3d(hermitian_fields((n, n, n), 7, ncomp=1)[0])
+    ref_v, ref_phi, _, _ = R.ab2v_scalar_run(v, phi, g, STEPS_V, 0.7, True, 0.3, history=history)
+    with handle(n, prec, nu=0.01, forced=1, eps=0.1) as h:
+        h.set_state(*v)
+        h.set_scalar(phi)
+        for dt in STEPS_V:
+            h.ab2v_scalar_pass(dt, pr=0.7, scalarforced=True, meangrad=0.3, history_rhs=history == "rhs")
+        out_v, out_phi = h.get_state(), h.get_scalar()
+    assert rel_l2(out_v, ref_v) < TOL[prec]
+    assert rel_l2(out_phi, ref_phi) < TOL[prec]
