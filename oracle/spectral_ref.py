@@ -31,8 +31,13 @@ robertsflow.f90:23-25 (zero Lamb vector, exact e^{-2 nu t} decay under the
 integrating factor), single-mode transform identities in FFTW's sign and
 normalisation convention, the energy normalisation 3/2 u0^2 of
 initialize.f90:362-368, the Hermitian/Nyquist rules of symmetrize.f90:32-64 and
-the divergence-free output of projection.f90.  Golden fixtures under
-tests/golden/ are generated from this oracle by tests/golden/make_golden.py.
+the divergence-free output of projection.f90; for the other steppers, the
+helical-basis identities of heliwave.f90 (i k x h = |k| h), exact inertial
+waves of an ABC flow under the rotating solver, exact Roberts decay and
+second-order convergence of the variable-step IF-AB2 on uneven steps, exact
+scalar diffusion, and the forcing's injection rates (eps, epsphi).  Golden
+fixtures under tests/golden/ are generated from this oracle by
+tests/golden/make_golden.py.
 """
 from __future__ import annotations
 
