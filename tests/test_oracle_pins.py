@@ -16,8 +16,16 @@ oracle is pinned to the known answers its own source implies:
   orthogonal to u pointwise).
 * heliwave.f90 gives the positive-helicity basis (unit, normal to k,
   i k x h = |k| h), and the rotating solver of spectral_rot_dns_ft.f90 turns
-  an ABC (Beltrami) flow into exact inertial waves and reduces to the
-  velocity-form IF-AB2 without rotation.
+  an ABC (Beltrami) flow into exact inertial waves, reduces to the
+  velocity-form IF-AB2 without rotation and injects exactly eps.
+* the variable-step IF-AB2 of spectral_dns.f90 decays the Roberts flow
+  exactly over uneven steps and converges at second order; its step rule
+  lands on the output time.
+* the passive scalars (spectral_rot_dns_scalar_ft.f90,
+  spectral_dns_scalar.f90) diffuse exactly without a velocity (the latter's
+  as-written pass-0 history shows as a 1e-3 deviation); forcephi /
+  forcephi_rot inject exactly epsphi; hermitianize is symmetrize without its
+  zeroing.
 * the committed golden fixtures reproduce.
 """
 import os
@@ -351,3 +359,20 @@ def test_variable_step_scalar_known_answers():
     v = roberts(n)
     out_v, _, t, _ = R.ab2v_scalar_run(v, phi, g, dts, 0.7)
     assert rel_l2(out_v, [a * np.exp(-2 * 0.05 * t) for a in v]) < 1e-14
+
+
+def test_rotating_rhs_energy_budget_equals_injection():
+    """The rotating solver's right-hand side (spectral_rot_dns_ft.f90:189-211)
+    injects energy at exactly eps through force_rot: the Lamb vector does no
+    work, and with tiny in force_rot's normalisation the band term gives
+    2 a kinet = eps (to the relative size of tiny)."""
+    n = 32
+    v = solenoidal_init(n)
+    g = R.Grid(R.Params(nx=n, eps=0.1))
+    w = R.rot_rhs(v, g, 1.0, 2.5)
+    rate = 0.0
+    for a, b in zip(v, w):
+        q = 2 * (np.conj(a) * b).real
+        q[:, :, 0] *= 0.5
+        rate += q.sum()
+    assert abs(rate - 0.1) < 1e-12
