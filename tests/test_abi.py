@@ -80,3 +80,49 @@ def test_scalar_file_entry_points_reject_bad_arguments_without_gpu(specns_lib):
 
 def test_ab2v_scalar_pass_rejects_bad_arguments_without_gpu(specns_lib):
     assert specns_lib.sc_ab2v_scalar_pass(None, 1e-3, 1.0, 0, 0.0, 0) == 1
+
+
+def _fortran_interfaces(path):
+    """(function name, bind name, dummy names) of each interface in a free-form
+    Fortran module, continuation lines joined."""
+    import re
+    text = open(path).read()
+    text = re.sub(r"&\s*\n\s*", "", text)
+    out = []
+    for m in re.finditer(r"function\s+(\w+)\(([^)]*)\)\s*bind\(C,\s*name=\"(\w+)\"\)", text):
+        args = [a.strip() for a in m.group(2).split(",") if a.strip()]
+        out.append((m.group(1), m.group(3), args))
+    return text, out
+
+
+def test_fortran_module_matches_the_c_header():
+    """include/specns.f90 (the ISO_C_BINDING module for the reference's
+    Fortran programs) binds every function of include/specns.h under its C
+    name with the C argument count, declares every dummy, and repeats the
+    header's constants and the sc_params / sc_diag layouts.  No Fortran
+    compiler is needed: this reads both files."""
+    import re
+    header = open(os.path.join(ROOT, "include", "specns.h")).read()
+    decls = {m.group(1): [a for a in " ".join(m.group(2).split()).split(",") if a.strip() not in ("", "void")]
+             for m in re.finditer(r"^(?:int|const char\*)\s+(sc_\w+)\(([^;]*)\);", header, re.M)}
+    text, ifaces = _fortran_interfaces(os.path.join(ROOT, "include", "specns.f90"))
+    assert sorted(b for _, b, _ in ifaces) == sorted(decls)
+    for fname, bname, args in ifaces:
+        assert fname == bname and len(args) == len(decls[bname]), bname
+        body = text[text.index("function %s(" % fname):text.index("end function %s" % fname)]
+        for a in args:
+            assert re.search(r"::\s*%s\s*$" % a, body, re.M), (fname, a)
+    for name, val in re.findall(r"^#define (SC_\w+) (\d+)", header, re.M):
+        assert re.search(r"parameter :: %s = %s$" % (name, val), text, re.M), name
+
+    def c_fields(struct):
+        body = header[header.index("typedef struct %s {" % struct):]
+        body = body[:body.index("}")]
+        return [n for line in body.split("\n")[1:] for n in re.findall(r"(\w+)[,;]", line.split("/*")[0])]
+
+    def f_fields(typ):
+        body = text[text.index("type, bind(C) :: %s" % typ):text.index("end type %s" % typ)]
+        return [n.strip() for line in body.split("\n")[1:] if "::" in line for n in line.split("::")[1].split(",")]
+
+    for t in ("sc_params", "sc_diag"):
+        assert c_fields(t) == f_fields(t), t
