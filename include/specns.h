@@ -319,8 +319,11 @@ int sc_ens_variant(sc_ensemble* e, int* variant, int* count, double* tune_ms, in
  * Block partial sums live in one static device array of 4.04 MiB per GPU
  * (held until exit), sized for nx, ny, nz <= 1024; larger grids are
  * rejected.  All calls share that array: calls that overlap on the GPU race.
- * The first call on a device looks up the array's address; make it before
- * any stream capture. */
+ * The first call on a device looks up the array's address and keeps it for
+ * the life of the process; make it before any stream capture.  The kept
+ * address belongs to the device's primary context: after cudaDeviceReset
+ * (or any other teardown of that context) it is stale, and this entry point
+ * must not be called on that device again. */
 int sc_diagnostics_noalloc(int precision, const void* vx, const void* vy, const void* vz, int nx,
                            int ny, int nz, double* out, void* stream);
 

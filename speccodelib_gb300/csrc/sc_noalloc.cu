@@ -25,7 +25,11 @@
 //    race on the array and give wrong results; serialise them.
 //  * The first call on a device, with that device current, looks up the
 //    array's device address (cudaGetSymbolAddress) and caches it; make that
-//    first call before any stream capture begins.
+//    first call before any stream capture begins.  The cached address is the
+//    array's place in the device's primary context: a cudaDeviceReset (or
+//    other teardown of that context) unloads the module and leaves the
+//    address stale, so this entry point is not for use on a device after a
+//    reset.
 #include <cuda_runtime.h>
 
 #include <cstdio>

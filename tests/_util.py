@@ -14,6 +14,15 @@ def rel_l2(a, b):
     return float(np.sqrt(num / den)) if den > 0 else float(np.sqrt(num))
 
 
+def fresh(a, dtype):
+    """A new C-contiguous array of `dtype` holding a's values.  Every buffer
+    handed to an in-place GPU call is made this way: np.ascontiguousarray
+    returns its argument itself when the dtype already matches, and an
+    in-place call would then also change the array the reference result is
+    computed from."""
+    return np.array(a, dtype=dtype, order="C", copy=True)
+
+
 def hermitian_fields(shape, seed, ncomp=3, kcut=None):
     """Spectral fields of seeded real white-noise physical fields (so every
     kx = 0 / Nyquist symmetry is exact), shape = (nx, ny, nz)."""

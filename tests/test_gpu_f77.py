@@ -7,7 +7,7 @@ import pytest
 
 from oracle import spectral_ref as R
 from speccodelib_gb300 import _lib
-from _util import hermitian_fields, rel_l2
+from _util import fresh, hermitian_fields, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -25,18 +25,18 @@ def test_f77_convec_projection_symmetrize(specns_lib, prec, dtype, real, tol):
     kx, ky, kz, k2 = R.wavenumber(n, n, n)
     w = list(R.vorticity(*v, kx, ky, kz))
     ref = R.convec_dns(*v, *w, n)
-    vv = [np.ascontiguousarray(a, dtype) for a in v]
-    ww = [np.ascontiguousarray(a, dtype) for a in w]
+    vv = [fresh(a, dtype) for a in v]
+    ww = [fresh(a, dtype) for a in w]
     f.convec_dns_(*[a.ctypes.data_as(C.c_void_p) for a in vv + ww], *ref_int(n // 2 + 1, n, n, n, n, n))
     assert rel_l2(ww, ref) < tol
     # projection_(vx,vy,vz,kx,ky,kz,lx1,ly,lz)
     ref_p = R.projection(*w, kx, ky, kz)
-    ww = [np.ascontiguousarray(a, dtype) for a in w]
-    kr = [np.ascontiguousarray(a, np.float64 if prec == "dp" else np.float32) for a in (kx, ky, kz)]
+    ww = [fresh(a, dtype) for a in w]
+    kr = [fresh(a, np.float64 if prec == "dp" else np.float32) for a in (kx, ky, kz)]
     f.projection_(*[a.ctypes.data_as(C.c_void_p) for a in ww], *[a.ctypes.data_as(C.c_void_p) for a in kr],
                   *ref_int(n // 2 + 1, n, n))
     assert rel_l2(ww, ref_p) < tol
-    c = np.ascontiguousarray(w[0], dtype)
+    c = fresh(w[0], dtype)
     f.__msymmetrize_MOD_symmetrize3d(c.ctypes.data_as(C.c_void_p), *ref_int(n // 2 + 1, n, n))
     assert rel_l2(c, R.symmetrize3d(w[0])) < tol
 
@@ -53,11 +53,11 @@ def test_f77_dynsmag_recovers_test_filter(specns_lib, prec, dtype, real, tol):
     g = R.test_filter(k2, kcut / 2)
     ref, mm, lm, cs2 = R.dynsmag(*v, kx, ky, kz, g, n, delta, 2 * delta, True, 0.0)
     rdt = np.float64 if prec == "dp" else np.float32
-    vv = [np.ascontiguousarray(a, dtype) for a in v]
+    vv = [fresh(a, dtype) for a in v]
     t = [np.zeros_like(vv[0]) for _ in range(6)]
-    k3 = [np.ascontiguousarray(np.broadcast_to(a, k2.shape), rdt) for a in
+    k3 = [fresh(np.broadcast_to(a, k2.shape), rdt) for a in
           (kx[None, None, :], ky[None, :, None], kz[:, None, None])]
-    gg = np.ascontiguousarray(g, rdt)
+    gg = fresh(g, rdt)
     out = [real(0), real(0), real(0)]
     f.dynsmag_(*[a.ctypes.data_as(C.c_void_p) for a in vv + t + k3 + [gg]],
                *ref_int(n // 2 + 1, n, n, n, n, n, n // 2),
@@ -78,16 +78,16 @@ def test_f77_convecphi_and_force_rot(specns_lib, prec, dtype, real, tol):
     phi = hermitian_fields((n, n, n), 42, ncomp=1)[0]
     kx, ky, kz, k2 = R.wavenumber(n, n, n)
     rdt = np.float64 if prec == "dp" else np.float32
-    vv = [np.ascontiguousarray(a, dtype) for a in v]
-    pp = np.ascontiguousarray(phi, dtype)
+    vv = [fresh(a, dtype) for a in v]
+    pp = fresh(phi, dtype)
     out = np.zeros_like(pp)
-    kr = [np.ascontiguousarray(a, rdt) for a in (kx, ky, kz)]
+    kr = [fresh(a, rdt) for a in (kx, ky, kz)]
     f.convecphi_dns_(*[a.ctypes.data_as(C.c_void_p) for a in vv + [pp, out] + kr], *ref_int(n // 2 + 1, n, n, n, n, n))
     assert rel_l2(out, R.convecphi_dns(*v, phi, n)) < tol
-    w = [np.ascontiguousarray(a, dtype) for a in hermitian_fields((n, n, n), 43)]
+    w = [fresh(a, dtype) for a in hermitian_fields((n, n, n), 43)]
     tiny = R.MYTINY_DP if prec == "dp" else R.MYTINY_SP
     ref = R.force_rot(*[a.astype(np.complex128) for a in w], *v, k2, 4.0, 16.0, 0.1, tiny)
-    k2r = np.ascontiguousarray(k2, rdt)
+    k2r = fresh(k2, rdt)
     f.force_rot_(*[a.ctypes.data_as(C.c_void_p) for a in w + vv], k2r.ctypes.data_as(C.c_void_p),
                  *ref_int(n // 2 + 1, n, n), C.byref(real(4.0)), C.byref(real(16.0)), C.byref(real(0.1)))
     assert rel_l2(w, ref) < tol
@@ -102,12 +102,12 @@ def test_f77_skewness_and_enstrophy(specns_lib, prec, dtype, real, tol):
     n = 16
     v = hermitian_fields((n, n, n), 61, kcut=2 * (n // 2) / 3)
     kx, ky, kz, k2 = R.wavenumber(n, n, n)
-    u = np.ascontiguousarray(v[0], dtype)
-    kr = np.ascontiguousarray(kx, np.float64 if prec == "dp" else np.float32)
+    u = fresh(v[0], dtype)
+    kr = fresh(kx, np.float64 if prec == "dp" else np.float32)
     s = real(0)
     f.skewness_(u.ctypes.data_as(C.c_void_p), kr.ctypes.data_as(C.c_void_p), C.byref(s), *ref_int(n, n, n))
     assert abs(s.value - R.skewness(v[0], n)) < tol * 10
-    uu = [np.ascontiguousarray(a, np.complex128) for a in v]
+    uu = [fresh(a, np.complex128) for a in v]
     kd = [np.zeros((n, n, n // 2 + 1)) for _ in range(3)]
     e = np.zeros((n, n, n))
     f.enstrophy_(*[a.ctypes.data_as(C.c_void_p) for a in uu + kd + [e]], *ref_int(n // 2 + 1, n, n, n // 2, n, n, n))

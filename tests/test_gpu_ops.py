@@ -8,7 +8,7 @@ import pytest
 
 import speccodelib_gb300 as S
 from oracle import spectral_ref as R
-from _util import complex_noise, hermitian_fields, rel_l2
+from _util import complex_noise, fresh, hermitian_fields, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -19,7 +19,7 @@ SHAPES = [(8, 8, 8), (16, 16, 16), (32, 32, 32), (64, 64, 64), (32, 16, 8), (16,
 
 
 def cast(fields, prec):
-    return [np.ascontiguousarray(a, dtype=DT[prec]) for a in fields]
+    return [fresh(a, DT[prec]) for a in fields]
 
 
 @pytest.mark.parametrize("prec", PRECS)

@@ -18,7 +18,8 @@ import numpy as np
 import pytest
 
 import speccodelib_gb300 as S
-from _util import solenoidal_init
+from oracle import spectral_ref as R
+from _util import fresh, hermitian_fields, solenoidal_init
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +32,7 @@ def test_noalloc_diagnostics_match_handle_diagnostics(specns_lib, prec):
     n, nu = 32, 0.01
     v = solenoidal_init(n)
     dtype = np.complex128 if prec == S.SC_FP64 else np.complex64
-    v = [np.ascontiguousarray(a, dtype) for a in v]
+    v = [fresh(a, dtype) for a in v]
     with S.SpectralNS(S.default_params(n, prec, nu=nu)) as h:
         h.set_state(*v)
         d, eks = h.diagnostics()
@@ -50,6 +51,36 @@ def test_noalloc_diagnostics_match_handle_diagnostics(specns_lib, prec):
         assert abs(o[2] - d["max_div"]) <= TOL * max(d["max_div"], 1e-300) + 1e-300
         assert o[3] == 0 and d["nonfinite"] == 0
         assert np.max(np.abs(o[5:] - eks)) <= TOL * np.max(eks)
+
+
+# Non-cubic grids, grids whose ny*nz rows do not fill one block each, and the
+# grids at the scratch array's two bounds: the most shells (nx = 1024, 512
+# shells) and the most blocks (ny*nz = 2^20 rows, 1024 blocks of 1024 rows).
+@pytest.mark.parametrize("prec", [S.SC_FP64, S.SC_FP32])
+@pytest.mark.parametrize("shape", [(64, 16, 8), (16, 16, 8), (32, 64, 64), (1024, 8, 8), (8, 1024, 1024)])
+def test_noalloc_diagnostics_on_other_grids_match_oracle(specns_lib, prec, shape):
+    torch = pytest.importorskip("torch")
+    nx, ny, nz = shape
+    v = hermitian_fields(shape, 77)
+    kx, ky, kz, k2 = R.wavenumber(nx, ny, nz)
+    ref = [R.energy(v), R.enstrophy(v, k2), R.max_divergence(v, kx, ky, kz)]
+    ref_eks = R.spectrum(v, k2, nx)
+    dtype = np.complex128 if prec == S.SC_FP64 else np.complex64
+    tol = TOL if prec == S.SC_FP64 else 1e-5
+    dev = [torch.from_numpy(fresh(a, dtype)).cuda() for a in v]
+    out = torch.empty(5 + nx // 2, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        out.fill_(float("nan"))
+        rc = specns_lib.sc_diagnostics_noalloc(prec, *[C.c_void_p(t.data_ptr()) for t in dev], nx, ny, nz,
+                                               C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
+        assert rc == 0, specns_lib.sc_last_error()
+        stream.synchronize()
+        o = out.cpu().numpy()
+        for got, want in zip(o[:3], ref):
+            assert abs(got - want) <= tol * abs(want) + 1e-300
+        assert o[3] == 0
+        assert np.max(np.abs(o[5:] - ref_eks)) <= tol * np.max(ref_eks)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(specns_lib):

@@ -16,7 +16,7 @@ import pytest
 import speccodelib_gb300 as S
 from oracle import spectral_ref as R
 from speccodelib_gb300 import _lib
-from _util import complex_noise, hermitian_fields, rel_l2, solenoidal_init
+from _util import complex_noise, fresh, hermitian_fields, rel_l2, solenoidal_init
 
 pytestmark = pytest.mark.gpu
 
@@ -34,7 +34,7 @@ def oracle_grid(n, **kw):
 
 def cast(fields, prec):
     dt = np.complex128 if prec == S.SC_FP64 else np.complex64
-    return [np.ascontiguousarray(a, dt) for a in fields]
+    return [fresh(a, dt) for a in fields]
 
 
 def ref_int(*xs):
@@ -163,12 +163,18 @@ def test_forcephi_and_forcephi_rot(specns_lib, prec, fk1, fk2):
     phi = hermitian_fields(shape, 8, ncomp=1)[0]
     w = complex_noise(shape, 9, ncomp=1)[0]
     _, _, _, k2 = R.wavenumber(*shape)
-    pp, ww = cast([phi], prec)[0], cast([w], prec)[0]
+    ref = R.forcephi(phi, w, k2, fk2, 0.05)
+    ref_rot = R.forcephi_rot(phi, w, k2, fk1, fk2, 0.05)
+    (pp,) = cast([phi], prec)
+    (ww,) = cast([w], prec)
     S.forcephi(pp, ww, fk2, 0.05)
-    assert rel_l2(ww, R.forcephi(phi, w, k2, fk2, 0.05)) < TOL[prec]
-    ww = cast([w], prec)[0]
+    assert rel_l2(ww, ref) < TOL[prec]
+    assert np.array_equal(pp, cast([phi], prec)[0])      # phi is read only
+    (ww,) = cast([w], prec)
     S.forcephi_rot(pp, ww, fk1, fk2, 0.05)
-    assert rel_l2(ww, R.forcephi_rot(phi, w, k2, fk1, fk2, 0.05)) < TOL[prec]
+    assert rel_l2(ww, ref_rot) < TOL[prec]
+    # the forcing changes w by far more than the tolerance (an identity would fail)
+    assert rel_l2(ref, w) > 10 * TOL[prec]
 
 
 @pytest.mark.parametrize("prec,dtype,real,tol", [("dp", np.complex128, C.c_double, 1e-12),
@@ -181,16 +187,19 @@ def test_f77_forcephi(specns_lib, prec, dtype, real, tol):
     phi = hermitian_fields((n, n, n), 44, ncomp=1)[0]
     w = hermitian_fields((n, n, n), 45, ncomp=1)[0]
     _, _, _, k2 = R.wavenumber(n, n, n)
-    k2r = np.ascontiguousarray(k2, np.float64 if prec == "dp" else np.float32)
-    pp = np.ascontiguousarray(phi, dtype)
-    ww = np.ascontiguousarray(w, dtype)
+    ref = R.forcephi(phi, w, k2, 2.5, 0.05)
+    ref_rot = R.forcephi_rot(phi, w, k2, 1.0, 2.5, 0.05)
+    k2r = fresh(k2, np.float64 if prec == "dp" else np.float32)
+    pp = fresh(phi, dtype)
+    ww = fresh(w, dtype)
     f.forcephi_(pp.ctypes.data_as(C.c_void_p), ww.ctypes.data_as(C.c_void_p), k2r.ctypes.data_as(C.c_void_p),
                 *ref_int(n // 2 + 1, n, n), C.byref(real(2.5)), C.byref(real(0.05)))
-    assert rel_l2(ww, R.forcephi(phi, w, k2, 2.5, 0.05)) < tol
-    ww = np.ascontiguousarray(w, dtype)
+    assert rel_l2(ww, ref) < tol
+    ww = fresh(w, dtype)
     f.forcephi_rot_(pp.ctypes.data_as(C.c_void_p), ww.ctypes.data_as(C.c_void_p), k2r.ctypes.data_as(C.c_void_p),
                     *ref_int(n // 2 + 1, n, n), C.byref(real(1.0)), C.byref(real(2.5)), C.byref(real(0.05)))
-    assert rel_l2(ww, R.forcephi_rot(phi, w, k2, 1.0, 2.5, 0.05)) < tol
+    assert rel_l2(ww, ref_rot) < tol
+    assert rel_l2(ref, w) > 10 * tol
 
 
 @pytest.mark.parametrize("prec", PRECS)
@@ -230,13 +239,16 @@ def test_hermitianize(specns_lib, prec):
     the oracle on a field with no symmetry."""
     n = 16
     c = complex_noise((n, n, n), 12, ncomp=1)[0]
+    ref = R.hermitianize(c)
+    # the copy changes the field: a test of the identity would pass otherwise
+    assert rel_l2(ref, c) > 0.1
     (cc,) = cast([c], prec)
     S.hermitianize(cc)
-    assert rel_l2(cc, R.hermitianize(c)) < TOL[prec]
+    assert rel_l2(cc, ref) < TOL[prec]
     f = _lib.load_f77("dp" if prec == S.SC_FP64 else "sp")
     (cc,) = cast([c], prec)
     f.hermitianize_(cc.ctypes.data_as(C.c_void_p), *ref_int(n // 2 + 1, n, n))
-    assert rel_l2(cc, R.hermitianize(c)) < TOL[prec]
+    assert rel_l2(cc, ref) < TOL[prec]
 
 
 @pytest.mark.parametrize("prec", PRECS)
