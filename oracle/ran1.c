@@ -61,6 +61,26 @@ static double oracle_ran1(oracle_ran1_state *s) {
   return r < rnmx ? r : rnmx;
 }
 
+/* The generator's integer state idum after `ncalls` calls of ran1 from a
+ * fresh generator seeded with `seed` (the warm-up's 8 + 32 Park-Miller steps
+ * run in the first call).  Each call advances idum by exactly one
+ * Park-Miller step, so from seed 1 the state after 9960 calls is z_10000 of
+ * the minimal standard sequence started at z_0 = 1. */
+int32_t oracle_ran1_state_after(int32_t seed, int64_t ncalls) {
+  oracle_ran1_state s = {0};
+  s.idum = seed;
+  for (int64_t i = 0; i < ncalls; ++i) (void)oracle_ran1(&s);
+  return s.idum;
+}
+
+/* z_n of the bare Park-Miller minimal standard generator from z_0 = z0
+ * (Schrage's factorisation, the same step ran1 uses). */
+int32_t oracle_park_miller_after(int32_t z0, int64_t n) {
+  int32_t z = z0;
+  for (int64_t i = 0; i < n; ++i) z = park_miller(z);
+  return z;
+}
+
 /* First `count` ran1 values for a fresh generator seeded with `seed`. */
 void oracle_ran1_sequence(int32_t seed, int64_t count, double *out) {
   oracle_ran1_state s = {0};

@@ -971,6 +971,10 @@ def _ran1_lib():
                                         ctypes.c_void_p]
     lib.oracle_ran1_sequence.argtypes = [ctypes.c_int32, ctypes.c_int64,
                                          ctypes.c_void_p]
+    lib.oracle_ran1_state_after.argtypes = [ctypes.c_int32, ctypes.c_int64]
+    lib.oracle_ran1_state_after.restype = ctypes.c_int32
+    lib.oracle_park_miller_after.argtypes = [ctypes.c_int32, ctypes.c_int64]
+    lib.oracle_park_miller_after.restype = ctypes.c_int32
     _LIB = lib
     return lib
 
@@ -985,6 +989,17 @@ def build_c(here=None):
                            os.path.join(here, "ran1.c"), "-lm"])
     os.replace(tmp, so)
     return so
+
+
+def ran1_state_after(seed, ncalls):
+    """ran1's integer state idum after `ncalls` calls (initialize.f90:516-548)."""
+    return int(_ran1_lib().oracle_ran1_state_after(seed, ncalls))
+
+
+def park_miller_after(z0, n):
+    """z_n of the Park-Miller minimal standard generator (the multiplier 16807,
+    modulus 2^31 - 1 and Schrage constants of initialize.f90:521-523)."""
+    return int(_ran1_lib().oracle_park_miller_after(z0, n))
 
 
 def ran1_sequence(seed, count):

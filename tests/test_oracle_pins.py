@@ -49,6 +49,21 @@ def test_ran1_c_matches_python_and_seed_quirk():
     assert s.min() > 0 and s.max() < 1 and abs(s.mean() - 0.5) < 0.01
 
 
+def test_ran1_park_miller_published_check_value():
+    """The minimal standard generator's published known answer (Park and
+    Miller, "Random number generators: good ones are hard to find", CACM 31
+    (1988)): started at z_0 = 1, z_10000 = 1043618065.  ran1 seeded with 1
+    (idum = max(-1, 1) = 1, initialize.f90:530) runs 40 Park-Miller steps of
+    warm-up in its first call and one per call after that, so its state after
+    9960 calls is that same z_10000: the stream of the reference's seeded
+    fields is pinned to a value from outside this repository."""
+    assert R.park_miller_after(1, 10000) == 1043618065
+    assert R.ran1_state_after(1, 10000 - 40) == 1043618065
+    assert R.ran1_state_after(-1, 10000 - 40) == 1043618065
+    # the Python restatement draws the same values from that stream
+    assert np.array_equal(R.ran1_sequence(1, 10000), R.ran1_sequence_py(1, 10000))
+
+
 def test_ran1_golden():
     g = np.load(os.path.join(GOLD, "ran1_seed1.npz"))
     assert np.array_equal(R.ran1_sequence(1, 4096), g["seq"])
