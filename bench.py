@@ -14,9 +14,10 @@ Every field (539 MB in FP32) is larger than L2 (129 MB), so no flush is
 needed between steps.
 
 `--impl reference` times the reference algorithm on the host cores instead:
-the FP64 NumPy/SciPy restatement of the reference (the reference's Fortran +
-FFTW sources cannot be compiled here), one right-hand side of the 512^3 step
-per sample (a quarter of an RK4 step), reported as steps/s.
+whole IF-RK4 steps of the same 512^3 workload from the same seeded field, in
+the reference's single-precision build (constant_sp.f90), computed by the
+threaded restatement oracle/cpu_step.py on every host core (the reference's
+Fortran + FFTW sources cannot be compiled here or on the GPU host).
 """
 from __future__ import annotations
 
@@ -63,8 +64,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-les", action="store_true")
-    ap.add_argument("--schemes", action="store_true",
-                    help="also time the rotating solver, its passive scalar and the variable-step IF-AB2 "
+    ap.add_argument("--no-schemes", action="store_true",
+                    help="skip timing the rotating solver, its passive scalar and the variable-step IF-AB2 "
                          "(passes per second on the same grid and initial field)")
     return ap.parse_args()
 
@@ -135,16 +136,18 @@ class Clocks:
 
 # algorithmic bytes per launch, in fields F = (nx/2+1) ny nz complex elements
 # (exact reads + writes of each pass; RK stage averages).  Unfused, zfwd runs
-# all four stages (12, 15, 15, 12 F).  With stages 1-3 fused into zfwd_zinv
-# (15, 18, 18 F: the RHS, v, acc read; acc and the next u, w written) zfwd
-# runs stage 4 only (12 F); zinv runs once per step and zinv_kx0 covers one
-# kx tile (not counted).
+# all four stages (12, 15, 15, 9 F: stage 4 reads the Lamb vector and the
+# accumulator, which stage 3 left holding E^2 v + its partial sum, and
+# writes the state).  With stages 1-3 fused into zfwd_zinv (15, 18, 18 F:
+# the RHS, v, acc read; acc and the next u, w written) zfwd runs stage 4
+# only (9 F); zinv runs once per step and zinv_kx0 covers one kx tile (not
+# counted).
 KERNELS = ["zinv", "ypass_inv", "xpass", "ypass_fwd", "zfwd", "zfwd_zinv", "zinv_kx0", "fixup"]
 
 
 def kernel_fields(fused):
     return {"zinv": 9.0, "ypass_inv": 12.0, "xpass": 9.0, "ypass_fwd": 6.0,
-            "zfwd": 12.0 if fused else 13.5, "zfwd_zinv": 17.0, "zinv_kx0": 0.0, "fixup": 0.0}
+            "zfwd": 9.0 if fused else 12.75, "zfwd_zinv": 17.0, "zinv_kx0": 0.0, "fixup": 0.0}
 
 
 def traffic_from_profiles(kernel):
@@ -160,46 +163,97 @@ def traffic_from_profiles(kernel):
     return None
 
 
-def cpu_reference_rhs(n, workers):
-    """Time one right-hand side of the oracle at n^3 (FP64) on the host."""
-    os.environ["SC_ORACLE_WORKERS"] = str(workers)
-    from oracle import spectral_ref as R
-    R.WORKERS = workers
+def seeded_field(n):
+    """The workload's initial field as the reference generates it
+    (initialize.f90:284-371, ran1 seed 1), from the oracle."""
     import numpy as np
-    rng = np.random.default_rng(1)
-    v = []
-    for _ in range(3):
-        a = (rng.standard_normal((n, n, n // 2 + 1)) + 1j * rng.standard_normal((n, n, n // 2 + 1))) * 1e-3
-        v.append(a)
-    g = R.Grid(R.Params(nx=n, nu=NU, dt=DT))
+    from oracle import spectral_ref as R
+    return R.initialize_dealiased(n, n, n, SEED, AKP, U0, 2.0 * (n // 2) / 3.0)
+
+
+def cpu_stepper(n, workers, precision):
+    """The threaded CPU restatement of the 512^3 IF-RK4 step
+    (oracle/cpu_step.py); precision "f32" is the reference's single build
+    (constant_sp.f90), "f64" its double build (constant.f90)."""
+    import numpy as np
+    from oracle import spectral_ref as R
+    from oracle.cpu_step import CpuRK4
+    R.WORKERS = workers
+    g = R.Grid(R.Params(nx=n, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX))
+    return CpuRK4(g, workers, np.complex64 if precision == "f32" else np.complex128)
+
+
+def cpu_time_steps(st, v, k):
     t0 = time.perf_counter()
-    R.ratesdudt(tuple(v), g)
-    return time.perf_counter() - t0
+    for _ in range(k):
+        st.step(v)
+    return (time.perf_counter() - t0) / k
 
 
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    import numpy as np
     workers = len(os.sched_getaffinity(0))
     n = a.n
+    v0 = seeded_field(n)
+    st = cpu_stepper(n, workers, "f32")
+    v = [np.array(x, np.complex64) for x in v0]
+    del v0
     for _ in range(max(a.warmup, 0)):
-        cpu_reference_rhs(n, workers)
-    ts = [cpu_reference_rhs(n, workers) for _ in range(a.steps)]
-    t_rhs = sum(ts) / len(ts)
-    v = 1.0 / (4.0 * t_rhs)
-    sample = ("one right-hand side (1/4 of an RK4 step) of the %d^3 step per sample, FP64 "
-              "NumPy/scipy.fft restatement, workers=%d" % (n, workers))
-    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": 4000.0 * t_rhs, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        st.step(v)
+    t_step = cpu_time_steps(st, v, a.steps)
+    st.close()
+    val = 1.0 / t_step
+    sample = ("%d whole IF-RK4 steps (4 right-hand sides each) of the %d^3 forced DNS from the ran1 "
+              "seed-1 field after %d warm-up steps, single-precision build (constant_sp.f90) restated by "
+              "oracle/cpu_step.py: scipy.fft with %d workers and the pointwise passes threaded over "
+              "z-slabs" % (a.steps, n, a.warmup, workers))
+    out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
            "impl": "reference",
            "config": workload_config(n, world),
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": workers, "kind": "port",
                             "sample": sample},
-           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     return 0
+
+
+def cpu_baseline_leg(n):
+    """The bounded CPU samples beside the GPU number (rank 0, N = 1): one
+    whole RK4 step on every core in each build of the reference, and one
+    right-hand side on one core (the reference's single-threaded FFTW plans,
+    fftwplan.f90:11-14), reported per step as 4 right-hand sides."""
+    import numpy as np
+    workers = len(os.sched_getaffinity(0))
+    v0 = seeded_field(n)
+    out = {}
+    for prec, dt in (("f32", np.complex64), ("f64", np.complex128)):
+        st = cpu_stepper(n, workers, prec)
+        v = [np.array(x, dt) for x in v0]
+        st.step(v)                       # warm-up: allocation, transform plans
+        t = cpu_time_steps(st, v, 1)
+        st.close()
+        out[prec] = {"steps_per_s": 1.0 / t, "s_per_step": t, "workers": workers,
+                     "sample": "1 whole RK4 step after 1 warm-up step"}
+        del st, v
+    st = cpu_stepper(n, 1, "f32")
+    v = [np.array(x, np.complex64) for x in v0]
+    st.rhs(v)
+    t0 = time.perf_counter()
+    st.rhs(v)
+    t_rhs = time.perf_counter() - t0
+    st.close()
+    out["f32_one_core"] = {"steps_per_s": 1.0 / (4.0 * t_rhs), "s_per_step": 4.0 * t_rhs, "workers": 1,
+                           "sample": "1 right-hand side after 1 warm-up right-hand side, x4 per step"}
+    return {"value": out["f32"]["steps_per_s"], "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": "one whole IF-RK4 step of the %d^3 forced DNS from the ran1 seed-1 field, "
+                      "single-precision build (constant_sp.f90) restated by oracle/cpu_step.py on %d "
+                      "cores; the double build and one core beside it" % (n, workers),
+            "by_build": out}
 
 
 def run_ours(a):
@@ -337,6 +391,20 @@ def run_ours(a):
         del h64
         fp64 = {"steps_per_s": k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64,
                 "speedup_fp32_over_fp64": (value / world) / (k64 / (ms64 / 1e3))}
+        # compute ceiling: the FFT flop model (9 real 3D transforms per right-hand side,
+        # 2.5 N log2 N flops each, 4 right-hand sides per step) against the measured FP64 FMA rate
+        npts = float(n) * (a.ny or n) * (a.nz or n)
+        flops = 4 * 9 * 2.5 * npts * np.log2(npts)
+        peak64 = S.fp64_peak_probe()
+        ach64 = flops / (ms64 / k64 / 1e3) / 1e12
+        fp64["roofline"] = {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
+                            "frac": ach64 / peak64,
+                            "peak_source": "measured: sc_fp64_peak_probe (FP64 FMA loop, 8 chains per thread)",
+                            "flop_model": "4 RHS x 9 real 3D FFTs x 2.5 N^3 log2 N^3 per step (%.3g flop)" % flops}
+        b64 = 4 * 51 * 2.0 * F
+        fp64["hbm_roofline"] = {"bound": "hbm", "achieved": b64 / (ms64 / k64 / 1e3) / 1e9, "peak": hbm,
+                                "unit": "GB/s", "frac": b64 / (ms64 / k64 / 1e3) / 1e9 / hbm,
+                                "bytes_model": "4 x 51 F per step, F = %.3g B (FP64)" % (2.0 * F)}
         # shells holding energy above the FP32 round-off floor of the total
         m = e64 > 1e-10 * float(np.sum(e64))
         fp64["fp32_vs_fp64_after_2_steps"] = {
@@ -423,6 +491,16 @@ def run_ours(a):
             del hl
             les[name] = {"steps_per_s": kl / (ms_l / 1e3), "ms_per_step": ms_l / kl,
                          "energy_after": d_l["energy"], "cs2": d_l["cs2"]}
+            # field-pass model: P = 3 + 4 n_i + 4 n_f + 12 with 12 inverse and 9 forward
+            # transforms (P = 99); the dynamic procedure adds 42 transforms (168 F) on one
+            # step in ten
+            Fl = 129 * 256 * 256 * 8.0
+            bl = 4 * 99 * Fl + (168 * Fl / 10 if sgs == S.SC_SGS_DYNSMAG else 0.0)
+            gbs = bl / (ms_l / kl / 1e3) / 1e9
+            les[name]["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                                     "frac": gbs / hbm, "bytes_per_step": bl,
+                                     "bytes_model": "4 x 99 F per step%s, F = %.3g B" %
+                                     (" + 168 F / 10" if sgs == S.SC_SGS_DYNSMAG else "", Fl)}
         torch.cuda.empty_cache()
 
     # ---- batched 2D ensemble: 24 x 256^2, 24 x 512^2, 16 x 1024^2 ----
@@ -462,12 +540,21 @@ def run_ours(a):
                     "ensemble_steps_per_s": ke / t_b,
                     "one_at_a_time_steps_per_s": k1 / t_1,
                     "speedup_vs_one_at_a_time": (ke / t_b) / (k1 / t_1)}
+        # field-pass model of the 2D step: per RHS P = 1 + 2 n_i + 2 n_f + 4 with the
+        # inverse transforms of u, v, w (n_i = 3) and the forward ones of (u w, v w) (n_f = 2)
+        F2 = sum((m // 2 + 1) * m * 8.0 for m in sizes)
+        b2 = 4 * 15 * F2
+        gb2 = b2 * ke / t_b / 1e9
+        ensemble["roofline"] = {"bound": "hbm", "achieved": gb2, "peak": hbm, "unit": "GB/s",
+                                "frac": gb2 / hbm, "bytes_per_step": b2,
+                                "bytes_model": "4 x 15 F per step summed over the members, sum F = %.3g B "
+                                               "(the whole ensemble's fields fit in the 129 MB L2)" % F2}
         ens.close()
         del ens
 
     # ---- opt-in: the other steppers on the headline grid ----
     schemes = None
-    if a.schemes:
+    if not a.no_schemes:
         schemes = {"grid": n, "dtype": "f32", "om": 5.0, "band": [1.0, 2.5], "pr": 0.7,
                    "note": "passes through the public API; forced passes read two FP64 band sums on the "
                            "host (one synchronisation each), ab2v_pass checks its status every call"}
@@ -510,11 +597,7 @@ def run_ours(a):
 
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
-        workers = len(os.sched_getaffinity(0))
-        t_rhs = cpu_reference_rhs(n, workers)
-        cpu = {"value": 1.0 / (4.0 * t_rhs), "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": "one right-hand side (1/4 RK4 step) of the %d^3 step, FP64 NumPy/scipy.fft "
-                         "restatement of the reference, workers=%d" % (n, workers)}
+        cpu = cpu_baseline_leg(n)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,

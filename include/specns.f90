@@ -290,6 +290,10 @@ module specns
       type(c_ptr), value :: h
       real(c_double), intent(out) :: bytes_per_step
     end function sc_step_bytes
+    integer(c_int) function sc_fp64_peak_probe(tflops) bind(C, name="sc_fp64_peak_probe")
+      import
+      real(c_double), intent(out) :: tflops
+    end function sc_fp64_peak_probe
     type(c_ptr) function sc_last_error() bind(C, name="sc_last_error")
       import
     end function sc_last_error

@@ -257,6 +257,13 @@ int sc_profile_read(sc_handle* h, const char* name, long long* launches, double*
 /* Algorithmic bytes (field-pass model) of one RK4 step for this handle. */
 int sc_step_bytes(sc_handle* h, double* bytes_per_step);
 
+/* No reference counterpart: a measurement helper.  Runs a bounded FP64 FMA
+ * throughput kernel (eight independent fma chains per thread, four blocks of
+ * 256 threads per SM) on the current device and returns the best rate of
+ * three timed launches in TFLOP/s: the compute ceiling of the plain-FP64
+ * step's roofline. */
+int sc_fp64_peak_probe(double* tflops);
+
 const char* sc_last_error(void);
 
 /* ---------------------------------------------------------------------

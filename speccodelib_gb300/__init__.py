@@ -8,4 +8,5 @@ from .specns import (SC_FP32, SC_FP64, SC_SGS_DYNSMAG, SC_SGS_NONE, SC_SGS_SMAG,
                      SC_MASK_AFTER_STEP, SC_MASK_RHS_AND_STEP, SpecNSError, SpectralNS,
                      convec_dns, dealiasing, default_params, dynsmag, force, projection,
                      smag, symmetrize, Ensemble2D, force_rot, convecphi_dns,
-                     skewness, enstrophy, ab2v_dt, forcephi, forcephi_rot, hermitianize)
+                     skewness, enstrophy, ab2v_dt, forcephi, forcephi_rot, hermitianize,
+                     fp64_peak_probe)

@@ -64,6 +64,7 @@ SIGNATURES = {
     "sc_adjoint_kept_segments": ([_P, _P], _I),
     "sc_profile_enable": ([_P, _I], _I),
     "sc_profile_read": ([_P, C.c_char_p, _P, _P], _I),
+    "sc_fp64_peak_probe": ([_P], _I),
     "sc_step_bytes": ([_P, _P], _I),
     "sc_diagnostics_noalloc": ([_I, _P, _P, _P, _I, _I, _I, _P, _P], _I),
     "sc_ens_create": ([_I, _I, _P, _P, _P, _D, _P], _I),

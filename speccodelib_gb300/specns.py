@@ -208,6 +208,14 @@ def ab2v_dt(betadx, umax, dto, time, twrite):
     return d.value
 
 
+def fp64_peak_probe():
+    """FP64 FMA rate of the current GPU in TFLOP/s (sc_fp64_peak_probe: a
+    bounded throughput kernel, the compute ceiling of the FP64 roofline)."""
+    t = C.c_double(0)
+    _check(lib().sc_fp64_peak_probe(C.byref(t)))
+    return t.value
+
+
 def default_params(n, precision=SC_FP32, **kw):
     p = Params()
     _check(lib().sc_default_params(C.byref(p), n, precision))

@@ -391,3 +391,25 @@ def test_rotating_rhs_energy_budget_equals_injection():
         q[:, :, 0] *= 0.5
         rate += q.sum()
     assert abs(rate - 0.1) < 1e-12
+
+
+@pytest.mark.parametrize("shape,fkmax", [((32, 32, 32), 2.5), ((32, 16, 8), 2.5), ((16, 32, 64), 6.0)])
+def test_threaded_cpu_step_matches_rk4_step(shape, fkmax):
+    """oracle/cpu_step.py (the timed CPU baseline: slab-threaded pointwise
+    passes, multi-threaded transforms) gives rk4_step's state: FP64 to
+    rounding of the summation order, the single-precision build to FP32
+    round-off."""
+    from oracle.cpu_step import CpuRK4
+    nx, ny, nz = shape
+    v = hermitian_fields(shape, 5, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = tuple(R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz))
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.01, dt=2e-3, fkmax=fkmax))
+    ref = R.rk4_run(v, g, 3)
+    for dtype, workers, tol in ((np.complex128, 1, 1e-15), (np.complex128, 4, 1e-15), (np.complex64, 4, 1e-6)):
+        st = CpuRK4(g, workers, dtype)
+        vv = [np.array(a, dtype) for a in v]
+        for _ in range(3):
+            st.step(vv)
+        st.close()
+        assert rel_l2(vv, ref) <= tol, (dtype, workers)
