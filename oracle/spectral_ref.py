@@ -23,10 +23,13 @@ unnormalised both ways exactly like FFTW's ``rfftwnd_f77_one_*``:
 
 Parity status
 -------------
-The reference cannot be built here (no Fortran compiler, no FFTW; the FFTW
-version it links is not pinned anywhere), so this oracle is NOT pinned to
-reference binaries.  It is pinned instead to the known answers the reference's
-own files imply (tests/test_oracle_pins.py): the Roberts/Beltrami flow of
+The reference cannot be built here or on the GPU host (no Fortran compiler,
+no FFTW; the FFTW version it links is not pinned anywhere), so this oracle is
+NOT pinned to reference binaries.  It is pinned instead to a published known
+answer -- the Park-Miller minimal standard generator inside ran1 reaches
+z_10000 = 1043618065 from z_0 = 1 (Park and Miller, CACM 31, 1988) -- and to
+the known answers the reference's own files imply
+(tests/test_oracle_pins.py): the Roberts/Beltrami flow of
 robertsflow.f90:23-25 (zero Lamb vector, exact e^{-2 nu t} decay under the
 integrating factor), single-mode transform identities in FFTW's sign and
 normalisation convention, the energy normalisation 3/2 u0^2 of

@@ -128,6 +128,8 @@ template <typename T, int LOGN>
 cudaError_t launch_zfwd_tma(const CUtensorMap& lmap, const CUtensorMap& vmap, int vstore, const StageArgs<T>& st,
                             const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
   if (st.mode == SM_RK4) return launch_zfwd_tma_mode<T, LOGN, SM_RK4>(lmap, vmap, vstore, st, g, tw, err, s);
+  // the variable-step AB2 with its update in the epilogue has an instance of its own
+  if (st.mode == SM_AB2V) return launch_zfwd_tma_mode<T, LOGN, SM_AB2V>(lmap, vmap, 0, st, g, tw, err, s);
   return launch_zfwd_tma_mode<T, LOGN, -1>(lmap, vmap, 0, st, g, tw, err, s);
 }
 
@@ -395,7 +397,8 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     long long n = (long long)g.ny * g.nz;                                                        \
     int nb = (int)((n + 255) / 256);                                                             \
     if (nb > 4096) nb = 4096;                                                                    \
-    sc::fixup_kx0_kernel<T><<<nb, 256, 0, s>>>(st, g);                                           \
+    if (st.mode == sc::SM_AB2V) sc::fixup_kx0_kernel<T, sc::SM_AB2V><<<nb, 256, 0, s>>>(st, g);   \
+    else sc::fixup_kx0_kernel<T><<<nb, 256, 0, s>>>(st, g);                                      \
     return cudaGetLastError();                                                                   \
   }
 
@@ -435,6 +438,11 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     int nb = (int)((n + 255) / 256);                                                             \
     if (nb > 152 * 16) nb = 152 * 16;                                                            \
     sc::rot_update_kernel<T><<<nb, 256, 0, s>>>(ra, g);                                          \
+    return cudaGetLastError();                                                                   \
+  }                                                                                              \
+  template <>                                                                                    \
+  cudaError_t sc::Launch<T>::band_coef(const BandArgs<T>& ba, const Geom& g, cudaStream_t s) {   \
+    sc::band_coef_kernel<T><<<1, 256, 0, s>>>(ba, g);                                            \
     return cudaGetLastError();                                                                   \
   }                                                                                              \
   template <>                                                                                    \

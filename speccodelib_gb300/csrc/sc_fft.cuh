@@ -87,6 +87,56 @@ template <bool INV, typename C> __device__ __forceinline__ void dft8(C* v) {
   }
 }
 
+template <typename R> struct W16;
+template <> struct W16<float> {
+  static constexpr float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+  static constexpr float h = 0.70710678118654752440f;
+};
+template <> struct W16<double> {
+  static constexpr double c1 = 0.92387953251128675613, s1 = 0.38268343236508977173;
+  static constexpr double h = 0.70710678118654752440;
+};
+
+// 16-point DFT in registers as 4 x 4 (n = n1 + 4 n2, k = k2 + 4 k1), in
+// place: radix-4 over n2 for each n1, twiddles W16^{n1 k2}, radix-4 over n1
+// for each k2, then a 4 x 4 register transpose into natural order.
+template <bool INV, typename C> __device__ __forceinline__ void dft16(C* v) {
+  using R = decltype(C::x);
+#pragma unroll
+  for (int n1 = 0; n1 < 4; ++n1) {
+    C t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+    dft4<INV>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[n1 + 4 * k2] = t[k2];
+  }
+#pragma unroll
+  for (int n1 = 1; n1 < 4; ++n1)
+#pragma unroll
+    for (int k2 = 1; k2 < 4; ++k2) {
+      const int e = n1 * k2;
+      R c, sn;   // W16^e = cos(2 pi e/16) - i sin(2 pi e/16) (forward)
+      switch (e) {
+        case 1: c = W16<R>::c1; sn = W16<R>::s1; break;
+        case 2: c = W16<R>::h; sn = W16<R>::h; break;
+        case 3: c = W16<R>::s1; sn = W16<R>::c1; break;
+        case 4: c = 0; sn = 1; break;
+        case 6: c = -W16<R>::h; sn = W16<R>::h; break;
+        default: c = -W16<R>::c1; sn = -W16<R>::s1; break;   // e = 9
+      }
+      v[n1 + 4 * k2] = cmul(v[n1 + 4 * k2], mk<C>(c, INV ? sn : -sn));
+    }
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) dft4<INV>(v + 4 * k2);   // X[k2 + 4 k1] now at v[k1 + 4 k2]
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j) {
+      const C t = v[j + 4 * i];
+      v[j + 4 * i] = v[i + 4 * j];
+      v[i + 4 * j] = t;
+    }
+}
+
 template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C* v) {
   if constexpr (R == 2) dft2<INV>(v);
   else if constexpr (R == 4) dft4<INV>(v);
@@ -305,10 +355,75 @@ struct FFTEngine {
     last_stage<INV>(out, sm, tw);
   }
 
+  // N = 512 with 32 threads per pencil (NT = 32 P, 16 points each): two
+  // passes, 512 = 16 x 32, instead of three radix-8 stages.  Thread (p, j),
+  // p = t % P, j = t / P:
+  //  1. a 16-point DFT over x[j + 32 m] (m = 0..15) and the twiddles
+  //     W512^(j k1): Y[k1][j];
+  //  2. Y[k1][j] to slot k1 * 32 + j (the exchange);
+  //  3. thread (p, j) with k1 = j/2, e = j%2 takes the 16 points
+  //     Y[k1][2 m + e]: a 16-point DFT gives A_e[k'], and X[k1 + 16 k2] =
+  //     A_0[k'] +- W32^k' A_1[k'] (k2 = k' or k' + 16) is finished across
+  //     the lane pair (lane ^ P), each lane keeping eight k'.
+  // Every shared access of a warp covers whole 128-byte rows of the tile
+  // (conflict-free), and the transform takes three barriers instead of six.
+  static constexpr bool TWO_PASS = LOGN == 9 && PFAST && PS == P && PADSHIFT == 0 && NT == 32 * P &&
+                                   RMAX == 8 && 32 % P == 0;
+  template <bool INV>
+  __device__ static void inplace_512(C* sm, const C* __restrict__ tw) {
+    const int t = threadIdx.x;
+    const int p = t % P, j = t / P;
+    C v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = sm[(j + 32 * m) * PS + p];
+    dft16<INV>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) {
+      const C w = __ldg(&tw[j * k1]);
+      v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + j) * PS + p] = v[k1];
+    __syncthreads();
+    const int k1 = j >> 1, e = j & 1;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = sm[(k1 * 32 + 2 * m + e) * PS + p];
+    dft16<INV>(v);
+    // odd lanes of a pair: W32^k' A_1[k'] (tw[0] = 1 exactly for the even ones)
+#pragma unroll
+    for (int k = 1; k < 16; ++k) {
+      const C w = __ldg(&tw[16 * k * e]);
+      v[k] = INV ? cmulc(v[k], w) : cmul(v[k], w);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      // even lane: keeps A_0[i], sends A_0[8 + i], gets W A_1[i];
+      // odd lane: keeps W A_1[8 + i], sends W A_1[i], gets A_0[8 + i]
+      const C snd = e ? v[i] : v[8 + i];
+      C rcv;
+      rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, P);
+      rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, P);
+      const C a0 = e ? rcv : v[i];
+      const C b = e ? v[8 + i] : rcv;
+      const int kp = 8 * e + i;
+      sm[(k1 + 16 * kp) * PS + p] = cadd(a0, b);
+      sm[(k1 + 16 * (kp + 16)) * PS + p] = csub(a0, b);
+    }
+    __syncthreads();
+  }
+
   // Input and output in shared memory, natural order, in place.  Ends with a
   // barrier.
   template <bool INV>
   __device__ static void run_inplace(C* sm, const C* __restrict__ tw) {
+#ifndef SC_NO_TWO_PASS
+    if constexpr (TWO_PASS) {
+      inplace_512<INV>(sm, tw);
+      return;
+    }
+#endif
     all_stages<0, INV>(sm, tw);
   }
 

@@ -23,6 +23,7 @@ template <typename T> struct TmaPass;
 template <typename T> struct AdjArgs;
 template <typename T> struct AdjOpArgs;
 template <typename T> struct FusedArgs;
+template <typename T> struct BandArgs;
 
 template <typename T> struct Launch {
   static int tile();                                   // pencil tile width P
@@ -42,6 +43,8 @@ template <typename T> struct Launch {
   static cudaError_t specop(const SpecOpArgs<T>& oa, const Geom& g, cudaStream_t s);
   // helical-wave AB2 update of the rotating solver at every mode
   static cudaError_t rot(const RotArgs<T>& ra, const Geom& g, cudaStream_t s);
+  // force_rot's coefficient into *ba.out on the device (one block)
+  static cudaError_t band_coef(const BandArgs<T>& ba, const Geom& g, cudaStream_t s);
   // variable-step IF-AB2 update at every mode
   static cudaError_t ab2v(const Ab2vArgs<T>& aa, const Geom& g, cudaStream_t s);
   static cudaError_t strain(const StrainArgs<T>& sa, const Geom& g, cudaStream_t s);

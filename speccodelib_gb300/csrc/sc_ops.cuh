@@ -265,6 +265,52 @@ __global__ void __launch_bounds__(256) specop_kernel(SpecOpArgs<T> oa, Geom g) {
 
 
 // ---------------------------------------------------------------------------
+// force_rot.f90's coefficient on the device: a = eps / (2 kinet + tiny), kinet
+// the 1/2-weighted (kx = 0) energy of v on lo2 <= k2 < hi2 (force_rot.f90:
+// 16-27).  One block walks the band's bounding box |k_i| <= floor(sqrt(hi2))
+// in a fixed order and sums in FP64, so the result is deterministic and no
+// host synchronisation is needed (the rotating pass reads *out in its
+// z-forward epilogue).
+// ---------------------------------------------------------------------------
+template <typename T> struct BandArgs {
+  const C2<T>* v[3];
+  double lo2, hi2, eps, tiny;
+  double* out;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) band_coef_kernel(BandArgs<T> ba, Geom g) {
+  __shared__ double red[256 / 32 + 1];
+  const int lo_b = k2_lt(ba.lo2), hi_b = k2_lt(ba.hi2);
+  int kb = 0;
+  while ((kb + 1) * (kb + 1) < hi_b) ++kb;   // largest |k_i| with k_i^2 < hi2
+  const int nkx = min(kb, g.nxh - 1) + 1;
+  const int ky0 = max(-kb, -g.ny / 2), ky1 = min(kb, g.ny / 2 - 1);
+  const int kz0 = max(-kb, -g.nz / 2), kz1 = min(kb, g.nz / 2 - 1);
+  const int nky = ky1 - ky0 + 1, nkz = kz1 - kz0 + 1;
+  const long long total = (long long)nkx * nky * nkz;
+  double q = 0.0;
+  for (long long t = threadIdx.x; t < total; t += blockDim.x) {
+    const int ix = (int)(t % nkx);
+    const int ky = ky0 + (int)((t / nkx) % nky);
+    const int kz = kz0 + (int)(t / ((long long)nkx * nky));
+    const int k2 = ix * ix + ky * ky + kz * kz;
+    if (k2 < lo_b || k2 >= hi_b) continue;
+    const int iy = ky < 0 ? ky + g.ny : ky, iz = kz < 0 ? kz + g.nz : kz;
+    const long long idx = ((long long)iz * g.ny + iy) * g.nxp + ix;
+    double e = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const C2<T> a = ba.v[c][idx];
+      e += (double)a.x * a.x + (double)a.y * a.y;
+    }
+    q += ix == 0 ? 0.5 * e : e;
+  }
+  const double kinet = block_sum<256>(q, red);
+  if (threadIdx.x == 0) *ba.out = ba.eps / (2.0 * kinet + ba.tiny);
+}
+
+// ---------------------------------------------------------------------------
 // helical-wave AB2 update of the rotating solver (rot_point, sc_rot.cuh)
 // ---------------------------------------------------------------------------
 template <typename T> struct RotArgs {

@@ -16,6 +16,7 @@
 //   fixup (kx = 0 plane) finishes the Hermitian copy of symmetrize.f90:52-62.
 #pragma once
 #include "sc_fft.cuh"
+#include "sc_ab2v.cuh"
 
 namespace sc {
 
@@ -339,7 +340,10 @@ enum StageMode {
   SM_RHS = 0,                       // store the right-hand side
   SM_RK1 = 1, SM_RK2 = 2, SM_RK3 = 3, SM_RK4 = 4,   // IF-RK4 stages
   SM_AB2_EULER = 10, SM_AB2_MID = 11, SM_AB2 = 12,  // IF-AB2 passes
-  SM_LAMB = 20                      // store the raw transform (no update)
+  SM_LAMB = 20,                     // store the raw transform (no update)
+  // a stepper whose per-mode update runs in the z-forward epilogue; only
+  // kernel instances with the mode as a compile-time constant carry it
+  SM_AB2V = 30                      // variable-step IF-AB2 (sc_ab2v.cuh)
 };
 
 template <typename T> struct StageArgs {
@@ -369,13 +373,24 @@ template <typename T> struct StageArgs {
   // update reads, prefetched into L2 once a tile's Lamb vector is in
   int pf_n;
   int pf_slot[6];
+  // SM_AB2V
+  int pass;             // 0, 1 or >= 2 (ab2v_point)
+  C2<T>* hist[3];       // the previous right-hand side o
+  C2<T>* vinit[3];      // the initial field (pass 0 writes it, pass 1 reads it)
+  double nu;            // viscosity
+  double dto;           // the previous step
+  double wgt[3];        // the pass's weights s, ek, dl (ab2v_weights)
+  // forcing with a coefficient computed on the device (force_rot.f90): when
+  // fcoef is set, w += (*fcoef) sin on the band fband_lo2 <= k2 < fkmax2
+  const double* fcoef;
+  double fband_lo2;
 };
 
 
 // What the update of a mode reads at each point besides w.
 __host__ __device__ constexpr bool mode_reads_v(int m) {
   return m == SM_RK1 || m == SM_RK2 || m == SM_RK3 || m == SM_AB2_EULER || m == SM_AB2 ||
-         m == SM_AB2_MID;
+         m == SM_AB2_MID || m == SM_AB2V;
 }
 __host__ __device__ constexpr bool mode_reads_acc(int m) {
   return m == SM_RK2 || m == SM_RK3 || m == SM_RK4 || m == SM_AB2;
@@ -406,6 +421,34 @@ __device__ __forceinline__ void finish_point_pre(const StageArgs<T>& st, const G
   }
   const bool cut = k2i >= kcut_b && !(ix == 0 && iy == 0 && iz == 0);
   if (st.mask_rhs && cut) w[0] = w[1] = w[2] = czero<C>();
+  if constexpr (MODE == SM_AB2V) {
+    // spectral_dns.f90:220-290 at this mode (ab2v_point); v = 0 where cut and
+    // at the mean mode
+    const int pass = st.pass;
+    Cx<T> v[3], wc[3], o[3], z[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v[c] = cx(vv[c].x, vv[c].y);
+      wc[c] = cx(w[c].x, w[c].y);
+      o[c] = z[c] = cx(T(0), T(0));
+      if (pass >= 2) {
+        const C q = st.hist[c][idx];
+        o[c] = cx(q.x, q.y);
+      } else if (pass == 1) {
+        const C q = st.vinit[c][idx];
+        z[c] = cx(q.x, q.y);
+      }
+    }
+    ab2v_point<T>(pass, k2i, cut || k2i == 0, (T)st.nu, st.dt, (T)st.dto, (T)st.wgt[0], (T)st.wgt[1],
+                  (T)st.wgt[2], v, wc, o, z);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      st.vout[c][idx] = mk<C>(v[c].re, v[c].im);
+      if (pass != 1) st.hist[c][idx] = mk<C>(o[c].re, o[c].im);
+      if (pass == 0) st.vinit[c][idx] = mk<C>(z[c].re, z[c].im);
+    }
+    return;
+  }
   const int mode = MODE >= 0 ? MODE : st.mode;
   if (mode == SM_RHS || mode == SM_LAMB) {
 #pragma unroll
@@ -493,12 +536,12 @@ __device__ __forceinline__ void load_state(const StageArgs<T>& st, long long idx
   }
 }
 
-template <typename T>
+template <typename T, int MODE = -1>
 __device__ __forceinline__ void finish_point(const StageArgs<T>& st, const Geom& g, long long idx,
                                              int ix, int iy, int iz, int kcut_b, C2<T>* w) {
   C2<T> vv[3], av[3];
-  load_state<T>(st, idx, vv, av);
-  finish_point_pre<T>(st, g, idx, ix, iy, iz, kcut_b, w, vv, av);
+  load_state<T, MODE>(st, idx, vv, av);
+  finish_point_pre<T, MODE>(st, g, idx, ix, iy, iz, kcut_b, w, vv, av);
 }
 
 // K_f of force.f90:16-22 from the zinv partial sums, fixed order.
@@ -660,7 +703,7 @@ zfwd_stage_kernel(FieldList<T> fin, StageArgs<T> st, Geom g, const C2<T>* __rest
 
 // Hermitian copy on the kx = 0 plane (symmetrize.f90:52-62):
 // w(0,iy,iz) = conj(w(0,-iy,-iz)) for iz > nz/2, and for iz = 0, iy > ny/2.
-template <typename T>
+template <typename T, int MODE = -1>
 __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
   using C = C2<T>;
   const long long total = (long long)g.ny * g.nz;
@@ -675,7 +718,7 @@ __global__ void fixup_kx0_kernel(StageArgs<T> st, Geom g) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) w[c] = (iy == g.ny / 2) ? czero<C>() : cconj(st.side[s + c]);
     const long long idx = ((long long)iz * g.ny + iy) * g.nxp;
-    finish_point<T>(st, g, idx, 0, iy, iz, kc_b, w);
+    finish_point<T, MODE>(st, g, idx, 0, iy, iz, kc_b, w);
   }
 }
 

@@ -97,11 +97,12 @@ struct sc_handle {
   bool fuse = true;               // RK stages 1-3: zfwd fused with the next zinv
   bool graph = true;              // replay captured CUDA graphs (steps, adjoint)
   bool prefetch = true;           // L2 prefetch of the update operands in the fused z kernel
+  bool fuse_steppers = true;      // rotating and variable-step AB2 updates in the z-forward epilogue
   cudaGraphExec_t step_exec = nullptr;   // one RK4 step
   cudaGraphExec_t adj_exec = nullptr;    // one adjoint call, for adj_key
   long long adj_key[7] = {0, 0, 0, 0, 0, 0, 0};
   double* jpin = nullptr;         // pinned host word for J
-  double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch
+  double* dscal = nullptr;        // [0] c1 or cs2, [1] lm, [2] mm, [3] energy scratch, [4] force_rot coefficient
   double* dpart = nullptr;        // reduction partials
   size_t dpart_len = 0;
   double* dout = nullptr;         // reduction outputs
@@ -539,7 +540,7 @@ template <typename T> struct Impl {
     for (int c = 0; c < 3; ++c) st.sin[c] = sin[c];
     sc::ZvArgs<T> za{};
     for (int c = 0; c < 3; ++c) za.v[c] = sin[c];
-    za.fs.enabled = h->p.forced && st.mode != sc::SM_LAMB;
+    za.fs.enabled = h->p.forced && st.mode != sc::SM_LAMB && !st.fcoef;
     za.fs.fkmax2 = h->p.fkmax * h->p.fkmax;
     za.fs.partial = const_cast<double*>(st.kf_partial);
     auto wl = range(h, S_W, nw);
@@ -723,6 +724,14 @@ template <typename T> struct Impl {
     return specop(h, oa);
   }
 
+  // Whether a stepper's pass runs its right-hand side through the DNS
+  // TMA-fed kernels with work in the z-forward epilogue: the variable-step
+  // AB2's update (SM_AB2V), the rotating solver's force_rot with a device
+  // coefficient, symmetrize and projection.
+  static bool stepper_in_epilogue(sc_handle* h) {
+    return h->fuse_steppers && h->tma && h->p.sgs == SC_SGS_NONE;
+  }
+
   // One pass of the variable-step IF-AB2 of spectral_dns.f90:173-290
   // (spectral_les.f90:199-316 with an SGS model) with step dt: the
   // right-hand side without symmetrize (the same passes as sc_rhs, into the
@@ -746,6 +755,27 @@ template <typename T> struct Impl {
     if (sc) SC_TRY(ensure_aux(h, RA_FIELDS));
     C* ab = reinterpret_cast<C*>(h->aux2);
     const int pass = h->ab2v_pass;
+    if (!sc && stepper_in_epilogue(h)) {
+      // the right-hand side (forcing and projection, no symmetrize) and the
+      // update in one z-forward epilogue: w never goes through HBM
+      const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
+      sc::StageArgs<T> st = stage_args(h);
+      st.mode = sc::SM_AB2V;
+      st.symmetrize = 0;
+      st.pass = pass < 2 ? pass : 2;
+      for (int c = 0; c < 3; ++c) {
+        st.hist[c] = ab + (size_t)c * g->field;
+        st.vinit[c] = ab + (size_t)(3 + c) * g->field;
+      }
+      st.nu = h->p.nu;
+      st.dt = (T)dt;
+      st.dto = h->ab2v_dto;
+      sc::ab2v_weights(pass, dt, h->ab2v_dto, st.wgt[0], st.wgt[1], st.wgt[2]);
+      SC_TRY(rhs_pipeline(h, vin, st));
+      h->ab2v_dto = pass == 1 ? dt + h->ab2v_dto : dt;   // :227, :249, :275
+      h->ab2v_pass += 1;
+      return SC_OK;
+    }
     const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
     if (sc) {
       const size_t fb = h->csize * g->field;
@@ -902,6 +932,30 @@ template <typename T> struct Impl {
     const size_t fb = h->csize * g->field;
     const C* vin[3] = {F(h, S_V), F(h, S_V + 1), F(h, S_V + 2)};
     C* w[3] = {F(h, S_A), F(h, S_A + 1), F(h, S_A + 2)};
+    if (!sc && stepper_in_epilogue(h)) {
+      // force_rot's coefficient from FP64 band sums on the device (no host
+      // synchronisation), the right-hand side with force_rot, symmetrize and
+      // projection applied in the z-forward epilogue (the kx = 0 copy targets
+      // in the fix-up) into the S_A slots, then the helical update
+      sc::StageArgs<T> st = stage_args(h);
+      st.mode = sc::SM_RHS;
+      if (h->p.forced) {
+        sc::BandArgs<T> ba{};
+        for (int c = 0; c < 3; ++c) ba.v[c] = vin[c];
+        ba.lo2 = fk1 * fk1;
+        ba.hi2 = fk2 * fk2;
+        ba.eps = h->p.eps;
+        ba.tiny = sizeof(T) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+        ba.out = h->dscal + 4;
+        SC_TRY(launch(h, "band_coef", [&] { return L::band_coef(ba, *g, h->stream); }));
+        st.fcoef = h->dscal + 4;
+        st.fband_lo2 = fk1 * fk1;
+        st.fkmax2 = fk2 * fk2;
+      }
+      SC_TRY(rhs_pipeline(h, vin, st));
+      h->ab2_pass = 0;   // the S_A slots held the fixed-step AB2's history
+      return rot_update(h, om, w, nullptr);
+    }
     if (sc) {
       for (int c = 0; c < 3; ++c)
         SC_CUDA(cudaMemcpyAsync(F(h, S_W + c), vin[c], fb, cudaMemcpyDeviceToDevice, h->stream));
@@ -941,6 +995,13 @@ template <typename T> struct Impl {
     oa.nfields = 3;
     oa.op = sc::OP_PROJECT;
     SC_TRY(specop(h, oa));
+    return rot_update(h, om, w, sc);
+  }
+
+  // rot_update_kernel over every mode: the helical AB2 of a pass from the
+  // projected right-hand side w (and, with `sc`, the scalar's update)
+  static int rot_update(sc_handle* h, double om, C* const w[3], const RotScalar* sc) {
+    auto* g = &h->g;
     sc::RotArgs<T> ra{};
     ra.pass = h->rot_pass < 2 ? h->rot_pass : 2;
     for (int c = 0; c < 3; ++c) {
@@ -1631,6 +1692,8 @@ int sc_create(const sc_params* pin, sc_handle** out) {
     h->copy_mode = !cp ? 1 : (std::strcmp(cp, "staged") == 0 ? 0 : (std::strcmp(cp, "strided") == 0 ? 2 : 1));
     const char* pf = std::getenv("SPECNS_NO_PREFETCH");
     h->prefetch = !(pf && pf[0] == '1');
+    const char* fs = std::getenv("SPECNS_NO_FUSE_STEPPERS");
+    h->fuse_steppers = !(fs && fs[0] == '1');
   }
   {
     int dev = 0;

@@ -318,9 +318,15 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant_
   }
   const bool fblock = st.forced && ((double)kx0 * kx0 + (double)ky * ky < st.fkmax2);
   const int kyi = wavenum(iy, g.ny), fk_b = k2_lt(st.fkmax2), kc_b = k2_lt(st.kcut2);
+  // lower edge of the forcing band (0 for force.f90's k2 < fkmax^2)
+  const int flo_b = k2_lt(st.fband_lo2);
   if (fblock && threadIdx.x == 0) {
-    const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
-    s_coef = st.eps / (2.0 * kf);
+    if (st.fcoef) {
+      s_coef = *st.fcoef;
+    } else {
+      const double kf = forcing_energy(st.kf_partial, st.kf_tiles, st.kf_ptile, g.ny, st.fkmax2);
+      s_coef = st.eps / (2.0 * kf);
+    }
   }
   __syncthreads();
   for (int c = 0; c < 3; ++c) {
@@ -355,7 +361,8 @@ zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant_
       C* wp = wv[i];
       if (fblock) {
         const int kz = wavenum(iz, g.nz);
-        if (ix * ix + kyi * kyi + kz * kz < fk_b) {
+        const int k2 = ix * ix + kyi * kyi + kz * kz;
+        if (k2 < fk_b && k2 >= flo_b) {
           const T ac = (T)s_coef;
 #pragma unroll
           for (int c = 0; c < 3; ++c) wp[c] = cadd(wp[c], cscale(st.sin[c][idx], ac));

@@ -26,56 +26,6 @@
 
 namespace sc {
 
-template <typename R> struct W16;
-template <> struct W16<float> {
-  static constexpr float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
-  static constexpr float h = 0.70710678118654752440f;
-};
-template <> struct W16<double> {
-  static constexpr double c1 = 0.92387953251128675613, s1 = 0.38268343236508977173;
-  static constexpr double h = 0.70710678118654752440;
-};
-
-// 16-point DFT in registers as 4 x 4 (n = n1 + 4 n2, k = k2 + 4 k1), in
-// place: radix-4 over n2 for each n1, twiddles W16^{n1 k2}, radix-4 over n1
-// for each k2, then a 4 x 4 register transpose into natural order.
-template <bool INV, typename C> __device__ __forceinline__ void dft16(C* v) {
-  using R = decltype(C::x);
-#pragma unroll
-  for (int n1 = 0; n1 < 4; ++n1) {
-    C t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
-    dft4<INV>(t);
-#pragma unroll
-    for (int k2 = 0; k2 < 4; ++k2) v[n1 + 4 * k2] = t[k2];
-  }
-#pragma unroll
-  for (int n1 = 1; n1 < 4; ++n1)
-#pragma unroll
-    for (int k2 = 1; k2 < 4; ++k2) {
-      const int e = n1 * k2;
-      R c, sn;   // W16^e = cos(2 pi e/16) - i sin(2 pi e/16) (forward)
-      switch (e) {
-        case 1: c = W16<R>::c1; sn = W16<R>::s1; break;
-        case 2: c = W16<R>::h; sn = W16<R>::h; break;
-        case 3: c = W16<R>::s1; sn = W16<R>::c1; break;
-        case 4: c = 0; sn = 1; break;
-        case 6: c = -W16<R>::h; sn = W16<R>::h; break;
-        default: c = -W16<R>::c1; sn = -W16<R>::s1; break;   // e = 9
-      }
-      v[n1 + 4 * k2] = cmul(v[n1 + 4 * k2], mk<C>(c, INV ? sn : -sn));
-    }
-#pragma unroll
-  for (int k2 = 0; k2 < 4; ++k2) dft4<INV>(v + 4 * k2);   // X[k2 + 4 k1] now at v[k1 + 4 k2]
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = i + 1; j < 4; ++j) {
-      const C t = v[j + 4 * i];
-      v[j + 4 * i] = v[i + 4 * j];
-      v[i + 4 * j] = t;
-    }
-}
-
 template <int E, bool INV, typename C> __device__ __forceinline__ void dftE(C* v) {
   if constexpr (E == 2) dft2<INV>(v);
   else if constexpr (E == 4) dft4<INV>(v);

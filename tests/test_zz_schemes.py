@@ -63,6 +63,58 @@ def test_rotating_solver_matches_oracle(specns_lib, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("shape,band", [((32, 32, 32), (0.0, 2.5)), ((64, 32, 16), (1.0, 4.0)),
+                                        ((128, 32, 32), (2.0, 5.0))])
+def test_rotating_update_in_epilogue_and_separate(specns_lib, prec, shape, band, monkeypatch):
+    """The rotating pass with force_rot's coefficient summed on the device
+    and force_rot, symmetrize and projection in the z-forward epilogue
+    (default), and with host-side band sums and a kernel for each of those
+    operators (SPECNS_NO_FUSE_STEPPERS=1): both give the oracle's passes, on
+    cubic and non-cubic grids, bands with and without the mean mode."""
+    nx, ny, nz = shape
+    fk1, fk2 = band
+    v = hermitian_fields(shape, 71, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.02, dt=2e-3, forced=True, eps=0.1))
+    ref, _, _ = R.rot_run(v, g, 4, 4.0, fk1, fk2)
+    outs = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_FUSE_STEPPERS", env)
+        with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.02, dt=2e-3, forced=1, eps=0.1)) as h:
+            h.set_state(*v)
+            h.rot_steps(4, om=4.0, fk1=fk1, fk2=fk2)
+            outs.append(h.get_state())
+    for o in outs:
+        assert rel_l2(o, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 16, 32)])
+def test_variable_step_update_in_epilogue_and_separate(specns_lib, prec, shape, monkeypatch):
+    """The variable-step IF-AB2 with its update in the z-forward epilogue
+    (default) and in its own kernel (SPECNS_NO_FUSE_STEPPERS=1): both give
+    the oracle's passes over an uneven step sequence."""
+    nx, ny, nz = shape
+    v = hermitian_fields(shape, 73, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.01, forced=True, eps=0.1, kcut=nx // 2))
+    ref, _, _ = R.ab2v_run(v, g, STEPS_V)
+    outs = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_FUSE_STEPPERS", env)
+        with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.01, forced=1, eps=0.1,
+                                           kcut=nx // 2)) as h:
+            h.set_state(*v)
+            for dt in STEPS_V:
+                h.ab2v_pass(dt)
+            outs.append(h.get_state())
+    for o in outs:
+        assert rel_l2(o, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_rotating_solver_beltrami_inertial_waves(specns_lib, prec):
     """An ABC (Beltrami, curl u = u) flow has a zero Lamb vector, so the
     rotating solver advances its helical amplitudes by the integrating factor
