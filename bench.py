@@ -556,8 +556,9 @@ def run_ours(a):
     schemes = None
     if not a.no_schemes:
         schemes = {"grid": n, "dtype": "f32", "om": 5.0, "band": [1.0, 2.5], "pr": 0.7,
-                   "note": "passes through the public API; forced passes read two FP64 band sums on the "
-                           "host (one synchronisation each), ab2v_pass checks its status every call"}
+                   "note": "passes through the public API; the rotating pass sums force_rot's band on the "
+                           "device and replays passes >= 2 as one captured graph; the rotating-scalar pass "
+                           "reads its band sums on the host; ab2v_pass checks its status every call"}
 
         def time_calls(fn, k):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -360,15 +360,18 @@ struct FFTEngine {
   // p = t % P, j = t / P:
   //  1. a 16-point DFT over x[j + 32 m] (m = 0..15) and the twiddles
   //     W512^(j k1): Y[k1][j];
-  //  2. Y[k1][j] to slot k1 * 32 + j (the exchange);
-  //  3. thread (p, j) with k1 = j/2, e = j%2 takes the 16 points
-  //     Y[k1][2 m + e]: a 16-point DFT gives A_e[k'], and X[k1 + 16 k2] =
-  //     A_0[k'] +- W32^k' A_1[k'] (k2 = k' or k' + 16) is finished across
-  //     the lane pair (lane ^ P), each lane keeping eight k'.
-  // Every shared access of a warp covers whole 128-byte rows of the tile
-  // (conflict-free), and the transform takes three barriers instead of six.
+  //  2. Y[k1][j] to row k1 * 32 + (j ^ (k1 & 1)) (the exchange);
+  //  3. thread (p, j) with k1 = (j & 1) | (j / 4) * 2, e = (j / 2) & 1
+  //     takes the 16 points Y[k1][2 m + e]: a 16-point DFT gives A_e[k'],
+  //     and X[k1 + 16 k2] = A_0[k'] +- W32^k' A_1[k'] (k2 = k' or k' + 16)
+  //     is finished across the lane pair (lane ^ 2P), each lane keeping
+  //     eight k'.
+  // The pairing and the row swizzle put the two 64-byte rows that each
+  // half-warp (8-byte elements) or quarter-warp (16-byte elements) touches in
+  // opposite halves of the banks, so every phase is free of bank conflicts;
+  // the transform takes three barriers instead of six.
   static constexpr bool TWO_PASS = LOGN == 9 && PFAST && PS == P && PADSHIFT == 0 && NT == 32 * P &&
-                                   RMAX == 8 && 32 % P == 0;
+                                   RMAX == 8 && P <= 8 && 32 % P == 0;
   template <bool INV>
   __device__ static void inplace_512(C* sm, const C* __restrict__ tw) {
     const int t = threadIdx.x;
@@ -384,13 +387,13 @@ struct FFTEngine {
     }
     __syncthreads();
 #pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + j) * PS + p] = v[k1];
+    for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + (j ^ (k1 & 1))) * PS + p] = v[k1];
     __syncthreads();
-    const int k1 = j >> 1, e = j & 1;
+    const int k1 = (j & 1) | ((j >> 2) << 1), e = (j >> 1) & 1;
 #pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = sm[(k1 * 32 + 2 * m + e) * PS + p];
+    for (int m = 0; m < 16; ++m) v[m] = sm[(k1 * 32 + ((2 * m + e) ^ (k1 & 1))) * PS + p];
     dft16<INV>(v);
-    // odd lanes of a pair: W32^k' A_1[k'] (tw[0] = 1 exactly for the even ones)
+    // the e = 1 lane of a pair: W32^k' A_1[k'] (tw[0] = 1 exactly for e = 0)
 #pragma unroll
     for (int k = 1; k < 16; ++k) {
       const C w = __ldg(&tw[16 * k * e]);
@@ -399,12 +402,12 @@ struct FFTEngine {
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      // even lane: keeps A_0[i], sends A_0[8 + i], gets W A_1[i];
-      // odd lane: keeps W A_1[8 + i], sends W A_1[i], gets A_0[8 + i]
+      // e = 0: keeps A_0[i], sends A_0[8 + i], gets W A_1[i];
+      // e = 1: keeps W A_1[8 + i], sends W A_1[i], gets A_0[8 + i]
       const C snd = e ? v[i] : v[8 + i];
       C rcv;
-      rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, P);
-      rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, P);
+      rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, 2 * P);
+      rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, 2 * P);
       const C a0 = e ? rcv : v[i];
       const C b = e ? v[8 + i] : rcv;
       const int kp = 8 * e + i;
@@ -412,6 +415,56 @@ struct FFTEngine {
       sm[(k1 + 16 * (kp + 16)) * PS + p] = csub(a0, b);
     }
     __syncthreads();
+  }
+
+  // The same transform with its 16 outputs left in registers: out[r] is
+  // point k = k1 + 16 (8 e + r) for r < 8 and k1 + 16 (8 e + r + 8) for
+  // r >= 8 of pencil p, with k1 and e of step 3 (out_pos_512).  The last
+  // shared-memory read is followed by a barrier, so the tile may be refilled
+  // once every thread has returned.
+  template <bool INV>
+  __device__ static void smem_512(C (&out)[16], C* sm, const C* __restrict__ tw) {
+    const int t = threadIdx.x;
+    const int p = t % P, j = t / P;
+    C v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = sm[(j + 32 * m) * PS + p];
+    dft16<INV>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) {
+      const C w = __ldg(&tw[j * k1]);
+      v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + (j ^ (k1 & 1))) * PS + p] = v[k1];
+    __syncthreads();
+    const int k1 = (j & 1) | ((j >> 2) << 1), e = (j >> 1) & 1;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = sm[(k1 * 32 + ((2 * m + e) ^ (k1 & 1))) * PS + p];
+    dft16<INV>(v);
+#pragma unroll
+    for (int k = 1; k < 16; ++k) {
+      const C w = __ldg(&tw[16 * k * e]);
+      v[k] = INV ? cmulc(v[k], w) : cmul(v[k], w);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const C snd = e ? v[i] : v[8 + i];
+      C rcv;
+      rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, 2 * P);
+      rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, 2 * P);
+      const C a0 = e ? rcv : v[i];
+      const C b = e ? v[8 + i] : rcv;
+      out[i] = cadd(a0, b);
+      out[8 + i] = csub(a0, b);
+    }
+  }
+  __device__ static __forceinline__ void out_pos_512(int r, int& p, int& n) {
+    const int t = threadIdx.x, j = t / P;
+    p = t % P;
+    n = ((j & 1) | ((j >> 2) << 1)) + 16 * (8 * ((j >> 1) & 1) + (r & 7) + (r >= 8 ? 16 : 0));
   }
 
   // Input and output in shared memory, natural order, in place.  Ends with a

@@ -99,6 +99,8 @@ struct sc_handle {
   bool prefetch = true;           // L2 prefetch of the update operands in the fused z kernel
   bool fuse_steppers = true;      // rotating and variable-step AB2 updates in the z-forward epilogue
   cudaGraphExec_t step_exec = nullptr;   // one RK4 step
+  cudaGraphExec_t rot_exec = nullptr;    // one pass >= 2 of the rotating solver, for rot_key
+  double rot_key[4] = {0, 0, 0, 0};      // om, fk1, fk2, the aux buffer it was captured with
   cudaGraphExec_t adj_exec = nullptr;    // one adjoint call, for adj_key
   long long adj_key[7] = {0, 0, 0, 0, 0, 0, 0};
   double* jpin = nullptr;         // pinned host word for J
@@ -232,8 +234,10 @@ int copy_out(sc_handle* h, void* dst, const void* src);  // padded device field 
 void drop_graphs(sc_handle* h) {
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->adj_exec) cudaGraphExecDestroy(h->adj_exec);
+  if (h->rot_exec) cudaGraphExecDestroy(h->rot_exec);
   h->step_exec = nullptr;
   h->adj_exec = nullptr;
+  h->rot_exec = nullptr;
   for (auto& k : h->adj_key) k = 0;
 }
 
@@ -844,6 +848,7 @@ template <typename T> struct Impl {
     if (*buf && *have >= n) return SC_OK;
     if (*buf) {
       SC_CUDA(cudaStreamSynchronize(h->stream));
+      drop_graphs(h);   // a captured pass holds the old buffer's addresses
       cudaFree(*buf);
       *buf = nullptr;
       *have = 0;
@@ -1928,8 +1933,33 @@ int sc_rot_steps(sc_handle* h, int npasses, double om, double fk1, double fk2) {
   if (h->p.sgs != SC_SGS_NONE) return fail(SC_ERR_INVALID, "the rotating solver has no SGS model");
   if (!std::isfinite(om) || !std::isfinite(fk1) || !std::isfinite(fk2) || fk1 < 0.0 || fk2 < fk1)
     return fail(SC_ERR_INVALID, "need finite om and 0 <= fk1 <= fk2");
-  for (int i = 0; i < npasses; ++i)
-    SC_TRY(h->p.precision == SC_FP32 ? Impl<float>::rot_pass(h, om, fk1, fk2) : Impl<double>::rot_pass(h, om, fk1, fk2));
+  auto pass = [&] {
+    return h->p.precision == SC_FP32 ? Impl<float>::rot_pass(h, om, fk1, fk2) : Impl<double>::rot_pass(h, om, fk1, fk2);
+  };
+  // Passes 0 and 1 differ; from pass 2 on a pass (its right-hand side with
+  // force_rot's coefficient on the device, and the helical update) is the
+  // same launch sequence without host synchronisation, so it is captured
+  // once per (om, fk1, fk2) and replayed.
+  const bool graphable = h->graph && !h->prof && h->fuse_steppers && h->tma;
+  int i = 0;
+  for (; i < npasses && (h->rot_pass < 2 || !graphable || npasses - i < 2); ++i) SC_TRY(pass());
+  if (i < npasses) {
+    const double key[4] = {om, fk1, fk2, (double)(uintptr_t)h->aux};
+    bool same = h->rot_exec != nullptr;
+    for (int k = 0; k < 4; ++k) same = same && key[k] == h->rot_key[k];
+    if (!same) {
+      if (h->rot_exec) cudaGraphExecDestroy(h->rot_exec);
+      h->rot_exec = nullptr;
+      const int p0 = h->rot_pass;
+      SC_TRY(capture(h, &h->rot_exec, pass));
+      h->rot_pass = p0;   // the capture ran nothing
+      for (int k = 0; k < 4; ++k) h->rot_key[k] = key[k];
+    }
+    for (; i < npasses; ++i) {
+      SC_CUDA(cudaGraphLaunch(h->rot_exec, h->stream));
+      h->rot_pass += 1;
+    }
+  }
   SC_CUDA(cudaGetLastError());
   return check_derr(h);
 }

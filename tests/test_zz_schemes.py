@@ -90,6 +90,29 @@ def test_rotating_update_in_epilogue_and_separate(specns_lib, prec, shape, band,
 
 
 @pytest.mark.parametrize("prec", PRECS)
+def test_rotating_passes_replayed_from_a_graph(specns_lib, prec, monkeypatch):
+    """From pass 2 on, sc_rot_steps replays one captured pass; the state is
+    bit-identical to launching every kernel (SPECNS_NO_GRAPH=1), across calls,
+    a change of om (a new capture) and a restart through set_state."""
+    n = 32
+    v = solenoidal_init(n)
+    outs = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_GRAPH", env)
+        with handle(n, prec, nu=0.01, dt=2e-3, forced=1, eps=0.1) as h:
+            h.set_state(*v)
+            h.rot_steps(5, om=5.0, fk1=1.0, fk2=2.5)
+            h.rot_steps(3, om=5.0, fk1=1.0, fk2=2.5)
+            h.rot_steps(2, om=2.0, fk1=1.0, fk2=2.5)
+            a = h.get_state()
+            h.set_state(*v)
+            h.rot_steps(4, om=5.0, fk1=0.0, fk2=3.0)
+            outs.append((a, h.get_state()))
+    assert rel_l2(outs[0][0], outs[1][0]) == 0.0
+    assert rel_l2(outs[0][1], outs[1][1]) == 0.0
+
+
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("shape", [(32, 32, 32), (64, 16, 32)])
 def test_variable_step_update_in_epilogue_and_separate(specns_lib, prec, shape, monkeypatch):
     """The variable-step IF-AB2 with its update in the z-forward epilogue
