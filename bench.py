@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-les", action="store_true")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="only time the CPU port on the other configurations (forced DNS 128^3 FP64, LES "
+                         "256^3 Smagorinsky and dynamic, the 2D ensemble members one at a time) and print "
+                         "one JSON line")
     ap.add_argument("--no-schemes", action="store_true",
                     help="skip timing the rotating solver, its passive scalar and the variable-step IF-AB2 "
                          "(passes per second on the same grid and initial field)")
@@ -626,8 +630,58 @@ def run_ours(a):
     return 0
 
 
+def run_cpu_configs(a):
+    """CPU seconds per step of the oracle port on the configurations beside
+    the headline, on every host core: forced DNS 128^3 (the threaded step,
+    double build), LES 256^3 (the oracle's rk4_run, transforms on every core,
+    pointwise work on one), the 2D ensemble (each member's Lawson RK4 step in
+    turn).  A bounded sample of each, stated in the output."""
+    import numpy as np
+    from oracle import spectral_ref as R
+    workers = len(os.sched_getaffinity(0))
+    R.WORKERS = workers
+    out = {"cores": workers, "kind": "port"}
+    # C1: forced DNS 128^3, nu 0.01, dt 2e-3, double build
+    v = R.initialize_dealiased(128, 128, 128, SEED, AKP, U0, 2.0 * 64 / 3.0)
+    from oracle.cpu_step import CpuRK4
+    st = CpuRK4(R.Grid(R.Params(nx=128, nu=0.01, dt=2e-3)), workers, np.complex128)
+    vv = [np.array(x) for x in v]
+    st.step(vv)
+    t = cpu_time_steps(st, vv, 5)
+    st.close()
+    out["dns128_fp64"] = {"s_per_step": t, "sample": "5 whole RK4 steps after 1 warm-up, threaded port"}
+    # C3: LES 256^3, nu 1e-4, dt 1e-3, c1 = 0.17^2
+    v = R.initialize_dealiased(256, 256, 256, SEED, AKP, U0, 2.0 * 128 / 3.0, spectrum_kind="kolmogorov",
+                               kmin=2.0, kmax=85.0)
+    for sgs in ("smag", "dynsmag"):
+        g = R.Grid(R.Params(nx=256, nu=1e-4, dt=1e-3, sgs=sgs, c1=0.17 ** 2))
+        state = {"cs2": 0.0, "update": True} if sgs == "dynsmag" else None
+        t0 = time.perf_counter()
+        R.rk4_step(v, g, state, dyn_update=True)
+        out["les256_" + sgs] = {"s_per_step": time.perf_counter() - t0,
+                                "sample": "1 RK4 step (dynamic: its coefficient refreshed, one step in ten "
+                                          "does this), oracle restatement"}
+    # C5: 24 x 256^2, 24 x 512^2, 16 x 1024^2, members one at a time
+    tot = 0.0
+    for n2, count in ((256, 24), (512, 24), (1024, 16)):
+        kmax = 2.0 * (n2 // 2) / 3.0
+        dt2 = 0.5 / n2
+        p2 = R.Params2D(n=n2, alpha=0.01, nu8=1.0 / (kmax ** 8 * dt2), dt=dt2)
+        w = R.initialize2d(n2, 1)
+        R.rk4_step2d(w, p2)
+        t0 = time.perf_counter()
+        R.rk4_step2d(w, p2)
+        tot += count * (time.perf_counter() - t0)
+    out["ensemble2d"] = {"s_per_step": tot, "sample": "one RK4 step of one member of each size, times the "
+                                                      "member count, oracle restatement"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     a = parse()
+    if a.cpu_configs:
+        return run_cpu_configs(a)
     if a.impl == "reference":
         return run_reference(a)
     return run_ours(a)

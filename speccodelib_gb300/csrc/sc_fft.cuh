@@ -417,56 +417,6 @@ struct FFTEngine {
     __syncthreads();
   }
 
-  // The same transform with its 16 outputs left in registers: out[r] is
-  // point k = k1 + 16 (8 e + r) for r < 8 and k1 + 16 (8 e + r + 8) for
-  // r >= 8 of pencil p, with k1 and e of step 3 (out_pos_512).  The last
-  // shared-memory read is followed by a barrier, so the tile may be refilled
-  // once every thread has returned.
-  template <bool INV>
-  __device__ static void smem_512(C (&out)[16], C* sm, const C* __restrict__ tw) {
-    const int t = threadIdx.x;
-    const int p = t % P, j = t / P;
-    C v[16];
-#pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = sm[(j + 32 * m) * PS + p];
-    dft16<INV>(v);
-#pragma unroll
-    for (int k1 = 1; k1 < 16; ++k1) {
-      const C w = __ldg(&tw[j * k1]);
-      v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + (j ^ (k1 & 1))) * PS + p] = v[k1];
-    __syncthreads();
-    const int k1 = (j & 1) | ((j >> 2) << 1), e = (j >> 1) & 1;
-#pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = sm[(k1 * 32 + ((2 * m + e) ^ (k1 & 1))) * PS + p];
-    dft16<INV>(v);
-#pragma unroll
-    for (int k = 1; k < 16; ++k) {
-      const C w = __ldg(&tw[16 * k * e]);
-      v[k] = INV ? cmulc(v[k], w) : cmul(v[k], w);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const C snd = e ? v[i] : v[8 + i];
-      C rcv;
-      rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, 2 * P);
-      rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, 2 * P);
-      const C a0 = e ? rcv : v[i];
-      const C b = e ? v[8 + i] : rcv;
-      out[i] = cadd(a0, b);
-      out[8 + i] = csub(a0, b);
-    }
-  }
-  __device__ static __forceinline__ void out_pos_512(int r, int& p, int& n) {
-    const int t = threadIdx.x, j = t / P;
-    p = t % P;
-    n = ((j & 1) | ((j >> 2) << 1)) + 16 * (8 * ((j >> 1) & 1) + (r & 7) + (r >= 8 ? 16 : 0));
-  }
-
   // Input and output in shared memory, natural order, in place.  Ends with a
   // barrier.
   template <bool INV>
