@@ -9,7 +9,10 @@
  * libspecns_f77_sp.so (REAL = float, the reference built with
  * constant_sp.f90).  Arrays are host memory; each call copies to the GPU,
  * runs the CUDA passes of libspecns.so and copies back.  On error the shim
- * prints sc_last_error() and aborts (the reference has no status returns).
+ * prints sc_last_error() and aborts by default (the reference has no status
+ * returns and its programs stop on fatal states); a caller that wants to
+ * recover turns that off with specns_f77_set_abort_ and reads
+ * specns_f77_status_ after its calls.
  */
 #ifndef SPECNS_F77_H
 #define SPECNS_F77_H
@@ -92,6 +95,16 @@ void dynsmag_(const void* ux, const void* uy, const void* uz, void* t11, void* t
               const int* lz, const int* nx, const int* ny, const int* nz, const int* lx,
               const sc_f77_real* delta, const sc_f77_real* delta_test, sc_f77_real* mm,
               sc_f77_real* lm, sc_f77_real* cs2, const int* update);
+
+/* No reference counterpart.  on = 0: a failing shim records its status
+ * (SC_ERR_*) and returns at once, its output arrays undefined; on = 1 (the
+ * default): it prints sc_last_error() and aborts.  Fortran:
+ * call specns_f77_set_abort(0). */
+void specns_f77_set_abort_(const int* on);
+
+/* No reference counterpart.  The status of the first failure since the
+ * previous query (SC_OK if none), then cleared. */
+void specns_f77_status_(int* status);
 
 #ifdef __cplusplus
 }

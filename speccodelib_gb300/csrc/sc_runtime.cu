@@ -969,6 +969,42 @@ template <typename T> struct Impl {
       SC_TRY(convecphi_core(h));
       SC_CUDA(cudaMemcpyAsync(AX(h, RA_WPHI), F(h, S_W), fb, cudaMemcpyDeviceToDevice, h->stream));
     }
+    if (sc && stepper_in_epilogue(h)) {
+      // the velocity's right-hand side as in the pass without a scalar, with
+      // force_rot's bounds unsquared (:213) and dealiasing's mask k2 >= ly^2/9
+      // as the RHS mask (it commutes with the per-mode projection); the
+      // scalar's forcing and dealiasing on wphi follow
+      sc::StageArgs<T> st = stage_args(h);
+      st.mode = sc::SM_RHS;
+      st.mask_rhs = 1;
+      st.kcut2 = (double)g->ny * g->ny / 9.0;
+      if (h->p.forced) {
+        sc::BandArgs<T> ba{};
+        for (int c = 0; c < 3; ++c) ba.v[c] = vin[c];
+        ba.lo2 = fk1;
+        ba.hi2 = fk2;
+        ba.eps = h->p.eps;
+        ba.tiny = sizeof(T) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+        ba.out = h->dscal + 4;
+        SC_TRY(launch(h, "band_coef", [&] { return L::band_coef(ba, *g, h->stream); }));
+        st.fcoef = h->dscal + 4;
+        st.fband_lo2 = fk1;
+        st.fkmax2 = fk2;
+      }
+      SC_TRY(rhs_pipeline(h, vin, st));
+      h->ab2_pass = 0;   // the S_A slots held the fixed-step AB2's history
+      if (sc->forced)
+        SC_TRY(scalar_band_force(h, AX(h, RA_WPHI), AX(h, RA_PHI), AX(h, RA_ZERO), fk1 * fk1, fk2 * fk2, sc->epsphi));
+      sc::SpecOpArgs<T> oa{};
+      oa.f[0] = AX(h, RA_WPHI);
+      oa.nfields = 1;
+      oa.kcut2 = (double)g->ny * g->ny / 9.0;
+      for (int op : {sc::OP_ZERO_PLANES, sc::OP_KX0_COPY, sc::OP_MASK}) {
+        oa.op = op;
+        SC_TRY(specop(h, oa));
+      }
+      return rot_update(h, om, w, sc);
+    }
     sc::StageArgs<T> st = stage_args(h);
     st.mode = sc::SM_LAMB;
     st.forced = 0;

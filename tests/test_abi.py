@@ -34,7 +34,7 @@ def test_default_params_and_errors_without_gpu(specns_lib):
 
 def test_f77_shims_export_every_declared_symbol(specns_lib):
     declared = _lib.declared_f77_symbols()
-    assert "convec_dns_" in declared and "hermitianize_" in declared and len(declared) == 15
+    assert "convec_dns_" in declared and "hermitianize_" in declared and len(declared) == 17
     for prec in ("sp", "dp"):
         lib = _lib.load_f77(prec)
         missing = [n for n in declared if not hasattr(lib, n)]
@@ -126,3 +126,24 @@ def test_fortran_module_matches_the_c_header():
 
     for t in ("sc_params", "sc_diag"):
         assert c_fields(t) == f_fields(t), t
+
+
+def test_f77_shims_report_errors_when_abort_is_off(specns_lib):
+    """specns_f77_set_abort_(0): a shim given an inconsistent shape records
+    SC_ERR_INVALID and returns (no abort, no CUDA call); the status is read
+    once and cleared."""
+    for prec in ("sp", "dp"):
+        lib = _lib.load_f77(prec)
+        i = ctypes.c_int
+        lib.specns_f77_set_abort_(ctypes.byref(i(0)))
+        st = i(-1)
+        lib.specns_f77_status_(ctypes.byref(st))
+        assert st.value == 0
+        buf = (ctypes.c_double * 64)()
+        # lx1 = 4 does not match nx = 16 (needs nx/2 + 1 = 9)
+        lib.convec_dns_(buf, buf, buf, buf, buf, buf, *[ctypes.byref(i(x)) for x in (4, 16, 16, 16, 16, 16)])
+        lib.specns_f77_status_(ctypes.byref(st))
+        assert st.value == 1
+        lib.specns_f77_status_(ctypes.byref(st))
+        assert st.value == 0
+        lib.specns_f77_set_abort_(ctypes.byref(i(1)))

@@ -90,6 +90,32 @@ def test_rotating_update_in_epilogue_and_separate(specns_lib, prec, shape, band,
 
 
 @pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 32, 16)])
+def test_rotating_scalar_epilogue_and_separate(specns_lib, prec, shape, monkeypatch):
+    """The rotating pass with a passive scalar: the velocity's right-hand
+    side with force_rot (unsquared bounds), symmetrize, projection and the
+    dealiasing mask in the z-forward epilogue (default), and with a kernel
+    for each operator (SPECNS_NO_FUSE_STEPPERS=1): both give the oracle's
+    velocity and scalar."""
+    nx, ny, nz = shape
+    pr = 0.7
+    v = hermitian_fields(shape, 75, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, k2 = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    phi = R.dealiasing(hermitian_fields(shape, 76, ncomp=1)[0], k2)
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.01, dt=2e-3, forced=True, eps=0.1))
+    ref_v, ref_phi, _, _ = R.rot_scalar_run(v, phi, g, 4, 5.0, 1.0, 2.5, pr, True, 0.05)
+    for env in ("0", "1"):
+        monkeypatch.setenv("SPECNS_NO_FUSE_STEPPERS", env)
+        with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.01, dt=2e-3, forced=1, eps=0.1)) as h:
+            h.set_state(*v)
+            h.set_scalar(phi)
+            h.rot_scalar_steps(4, om=5.0, fk1=1.0, fk2=2.5, pr=pr, scalarforced=True, epsphi=0.05)
+            assert rel_l2(h.get_state(), ref_v) < TOL[prec], env
+            assert rel_l2(h.get_scalar(), ref_phi) < TOL[prec], env
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_rotating_passes_replayed_from_a_graph(specns_lib, prec, monkeypatch):
     """From pass 2 on, sc_rot_steps replays one captured pass; the state is
     bit-identical to launching every kernel (SPECNS_NO_GRAPH=1), across calls,
