@@ -372,20 +372,27 @@ struct FFTEngine {
   // the transform takes three barriers instead of six.
   static constexpr bool TWO_PASS = LOGN == 9 && PFAST && PS == P && PADSHIFT == 0 && NT == 32 * P &&
                                    RMAX == 8 && P <= 8 && 32 % P == 0;
+  // Step 1 on values in registers: v[m] = x[j + 32 m] of this thread's
+  // pencil p and column j on entry, Y[k1][j] = W512^(j k1) DFT16(v)[k1] on
+  // return.
   template <bool INV>
-  __device__ static void inplace_512(C* sm, const C* __restrict__ tw) {
-    const int t = threadIdx.x;
-    const int p = t % P, j = t / P;
-    C v[16];
-#pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = sm[(j + 32 * m) * PS + p];
+  __device__ static __forceinline__ void phase1_512(C (&v)[16], const C* __restrict__ tw) {
+    const int j = threadIdx.x / P;
     dft16<INV>(v);
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) {
       const C w = __ldg(&tw[j * k1]);
       v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
     }
-    __syncthreads();
+  }
+
+  // Steps 2 and 3 from the step-1 values in registers, through the tile sm
+  // (whose previous contents every thread must be done with), leaving the
+  // transform in sm in natural order.  Ends with a barrier.
+  template <bool INV>
+  __device__ static __forceinline__ void finish_512(C (&v)[16], C* sm, const C* __restrict__ tw) {
+    const int t = threadIdx.x;
+    const int p = t % P, j = t / P;
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + (j ^ (k1 & 1))) * PS + p] = v[k1];
     __syncthreads();
@@ -415,6 +422,18 @@ struct FFTEngine {
       sm[(k1 + 16 * (kp + 16)) * PS + p] = csub(a0, b);
     }
     __syncthreads();
+  }
+
+  template <bool INV>
+  __device__ static void inplace_512(C* sm, const C* __restrict__ tw) {
+    const int t = threadIdx.x;
+    const int p = t % P, j = t / P;
+    C v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = sm[(j + 32 * m) * PS + p];
+    phase1_512<INV>(v, tw);
+    __syncthreads();
+    finish_512<INV>(v, sm, tw);
   }
 
   // Input and output in shared memory, natural order, in place.  Ends with a

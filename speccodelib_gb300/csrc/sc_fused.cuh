@@ -23,6 +23,7 @@
 // 112 KB for 32 KB tiles, so two CTAs share an SM.
 #pragma once
 #include "sc_tma_passes.cuh"
+#include "sc_tmem.cuh"
 
 #ifndef ZI_DIV
 #define ZI_DIV 16
@@ -107,6 +108,103 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
   constexpr int PH = P / 2;
   using ZF = ZiFields<MODE>;
   const T ky = (T)wavenum(iy, g.ny);
+#ifndef SC_NO_TMEM_W
+  // FP32 512-point pencils with bulk stores: w_x and w_y as whole-tile
+  // two-pass transforms.  Each thread forms its 16 step-1 points of both
+  // from the stage-input tiles and parks the step-1 values in TMEM; s
+  // becomes u in place; u_z leaves, w_z = i kx u_y - i ky u_x takes its
+  // tile, u_x and u_y leave; their tiles are then the exchange buffers that
+  // finish w_x and w_y, which leave by bulk stores as well.  No half tiles,
+  // no work buffer, no element stores (SC_NO_TMEM_W: the half-tile path).
+  if constexpr (MODE == ZV_DNS && EF::TWO_PASS && sizeof(T) == 4) {
+    if (umap) {
+      using Cfg = TmaCfg<T, LOGN>;
+      __shared__ uint32_t s_tmem;
+      const int t = threadIdx.x, warp = t >> 5;
+      const int p = t % P, j = t / P;
+      if (warp == 0) tmem_alloc(&s_tmem, 128);
+      tmem_fence_before_sync();
+      __syncthreads();
+      tmem_fence_after_sync();
+      // lanes 32 (warp % 4) .., columns 64 (warp / 4) .. + 63: w_x at +0, w_y at +32
+      const uint32_t tw_addr = s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64u * (uint32_t)(warp >> 2);
+      const T kx = (T)(kx0 + p);
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) {
+        C v[16];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          const int n = j + 32 * m, e = n * P + p;
+          v[m] = zv_gen<MODE>(3 + q, rt[0][e], rt[1][e], rt[2][e], kx, ky, (T)wavenum(n, g.nz), true);
+        }
+        EF::template phase1_512<true>(v, tw);
+        uint32_t r[32];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          r[2 * m] = __float_as_uint(v[m].x);
+          r[2 * m + 1] = __float_as_uint(v[m].y);
+        }
+        tmem_store32(tw_addr + 32u * q, r);
+      }
+      tmem_wait_store();
+      __syncthreads();
+      for (int c = 0; c < 3; ++c) EF::template run_inplace<true>(rt[c], tw);
+      auto store = [&](int c, int f) {
+        for (int h = 0; h < Cfg::NBOX; ++h)
+          tma_store_4d(umap, rt[c] + (size_t)h * Cfg::BOX * P, kx0 * Cfg::U, iy, h * Cfg::BOX, f);
+      };
+      fence_proxy_async();
+      __syncthreads();
+      if (t == 0) {
+        store(2, 2);
+        tma_store_commit();
+        store(0, 0);
+        store(1, 1);
+        tma_store_commit();
+        tma_store_wait_read<1>();
+      }
+      __syncthreads();
+      for (int e = t; e < P * N; e += NT) {
+        const int pe = e % P;
+        const C ux = rt[0][e], uy = rt[1][e];
+        rt[2][e] = cmuli(csub(cscale(uy, (T)(kx0 + pe)), cscale(ux, ky)));
+      }
+      fence_proxy_async();
+      __syncthreads();
+      if (t == 0) {
+        store(2, 5);
+        tma_store_commit();
+        tma_store_wait_read<1>();   // u_x and u_y have left their tiles
+      }
+      __syncthreads();
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) {
+        uint32_t r[32];
+        tmem_load32(tw_addr + 32u * q, r);
+        C v[16];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = mk<C>(__uint_as_float(r[2 * m]), __uint_as_float(r[2 * m + 1]));
+        EF::template finish_512<true>(v, rt[q], tw);
+      }
+      fence_proxy_async();
+      tmem_fence_before_sync();
+      __syncthreads();
+      tmem_fence_after_sync();
+      if (t == 0) {
+        store(0, 3);
+        store(1, 4);
+        tma_store_commit();
+        tma_store_wait_read<0>();
+      }
+      if (warp == 0) {
+        __syncwarp();   // the warp-collective release after thread 0's stores
+        tmem_dealloc(s_tmem, 128);
+      }
+      __syncthreads();
+      return;
+    }
+  }
+#endif
 #pragma unroll 1
   for (int q = 0; q < ZF::NKZ; ++q) {
     const int f = ZF::kz_field(q);

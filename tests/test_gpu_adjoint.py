@@ -10,7 +10,7 @@ import pytest
 
 import speccodelib_gb300 as S
 from oracle import spectral_ref as R
-from _util import rel_l2, solenoidal_init
+from _util import hermitian_fields, rel_l2, solenoidal_init
 
 pytestmark = pytest.mark.gpu
 
@@ -210,3 +210,24 @@ def test_adjoint_graph_replay_matches_eager(specns_lib, monkeypatch):
     for J, grad in res[1:]:
         assert J == res[0][0]
         assert rel_l2(grad, res[0][1]) == 0.0
+
+
+@pytest.mark.parametrize("prec,tol", [(S.SC_FP64, 1e-11), (S.SC_FP32, 1e-4)])
+def test_adjoint_long_z_matches_oracle(specns_lib, prec, tol):
+    """nz = 512 (the length of the two-pass tile transforms, whose FP32 form
+    keeps the vorticity's step-1 values in tensor memory): the adjoint's
+    z-inverse of the stage inputs runs through it; the gradient against the
+    FP64 oracle adjoint, both schedules."""
+    nx, ny, nz, T, K = 32, 16, 512, 3, 2
+    v = hermitian_fields((nx, ny, nz), 9, kcut=2 * (nx // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.02, fkmax=6.0))
+    ref, Jref = R.adjoint_gradient(v, g, T, kmin=2, kmax=5, checkpoint=K)
+    with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.02, fkmax=6.0)) as h:
+        for budget in (-1.0, 0.0):
+            h.set_adjoint_budget(budget)
+            h.set_state(*v)
+            J, grad = h.adjoint(T, K, kmin=2, kmax=5)
+            assert abs(J - Jref) < tol * abs(Jref)
+            assert rel_l2(grad, ref) < tol, (budget, rel_l2(grad, ref))
