@@ -370,11 +370,17 @@ struct FFTEngine {
   // half-warp (8-byte elements) or quarter-warp (16-byte elements) touches in
   // opposite halves of the banks, so every phase is free of bank conflicts;
   // the transform takes three barriers instead of six.
-  static constexpr bool TWO_PASS = LOGN == 9 && PFAST && PS == P && PADSHIFT == 0 && NT == 32 * P &&
-                                   RMAX == 8 && P <= 8 && 32 % P == 0;
-  // Step 1 on values in registers: v[m] = x[j + 32 m] of this thread's
-  // pencil p and column j on entry, Y[k1][j] = W512^(j k1) DFT16(v)[k1] on
-  // return.
+  static constexpr bool TWO_PASS = PFAST && PS == P && PADSHIFT == 0 && RMAX == 8 &&
+                                   ((LOGN == 9 && NT == 32 * P && P <= 8 && 32 % P == 0) ||
+                                    (LOGN == 8 && NT == 16 * P && (32 % P == 0 || P % 32 == 0)));
+  // N = 256 takes the same two passes as 16 x 16: step 1 as for 512 (points
+  // j + 16 m), the exchange at row k1 * 16 + j, and thread (p, k1) finishes
+  // the 16-point DFT over j alone (no lane pairs); rows of 8 or 16 elements
+  // are whole 128-byte lines, so every access is conflict-free.
+  static constexpr int S1 = N / 16;   // stride of the step-1 points
+  // Step 1 on values in registers: v[m] = x[j + S1 m] of this thread's
+  // pencil p and column j on entry, Y[k1][j] = W_N^(j k1) DFT16(v)[k1] on
+  // return (the names say 512; N = 256 uses them too).
   template <bool INV>
   __device__ static __forceinline__ void phase1_512(C (&v)[16], const C* __restrict__ tw) {
     const int j = threadIdx.x / P;
@@ -393,6 +399,20 @@ struct FFTEngine {
   __device__ static __forceinline__ void finish_512(C (&v)[16], C* sm, const C* __restrict__ tw) {
     const int t = threadIdx.x;
     const int p = t % P, j = t / P;
+    if constexpr (LOGN == 8) {
+#pragma unroll
+      for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 16 + j) * PS + p] = v[k1];
+      __syncthreads();
+      // thread (p, k1 = j): the 16-point DFT over the exchange row's j
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = sm[(j * 16 + m) * PS + p];
+      dft16<INV>(v);
+      __syncthreads();
+#pragma unroll
+      for (int k2 = 0; k2 < 16; ++k2) sm[(j + 16 * k2) * PS + p] = v[k2];
+      __syncthreads();
+      return;
+    }
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) sm[(k1 * 32 + (j ^ (k1 & 1))) * PS + p] = v[k1];
     __syncthreads();
@@ -430,7 +450,7 @@ struct FFTEngine {
     const int p = t % P, j = t / P;
     C v[16];
 #pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = sm[(j + 32 * m) * PS + p];
+    for (int m = 0; m < 16; ++m) v[m] = sm[(j + S1 * m) * PS + p];
     phase1_512<INV>(v, tw);
     __syncthreads();
     finish_512<INV>(v, sm, tw);

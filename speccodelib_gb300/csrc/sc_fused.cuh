@@ -109,7 +109,7 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
   using ZF = ZiFields<MODE>;
   const T ky = (T)wavenum(iy, g.ny);
 #ifndef SC_NO_TMEM_W
-  // FP32 512-point pencils with bulk stores: w_x and w_y as whole-tile
+  // FP32 512- and 256-point pencils with bulk stores: w_x and w_y as whole-tile
   // two-pass transforms.  Each thread forms its 16 step-1 points of both
   // from the stage-input tiles and parks the step-1 values in TMEM; s
   // becomes u in place; u_z leaves, w_z = i kx u_y - i ky u_x takes its
@@ -134,7 +134,7 @@ __device__ __forceinline__ void zinv_from_tiles(C2<T>* const rt[3], C2<T>* work,
         C v[16];
 #pragma unroll
         for (int m = 0; m < 16; ++m) {
-          const int n = j + 32 * m, e = n * P + p;
+          const int n = j + EF::S1 * m, e = n * P + p;
           v[m] = zv_gen<MODE>(3 + q, rt[0][e], rt[1][e], rt[2][e], kx, ky, (T)wavenum(n, g.nz), true);
         }
         EF::template phase1_512<true>(v, tw);

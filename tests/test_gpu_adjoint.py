@@ -213,12 +213,13 @@ def test_adjoint_graph_replay_matches_eager(specns_lib, monkeypatch):
 
 
 @pytest.mark.parametrize("prec,tol", [(S.SC_FP64, 1e-11), (S.SC_FP32, 1e-4)])
-def test_adjoint_long_z_matches_oracle(specns_lib, prec, tol):
-    """nz = 512 (the length of the two-pass tile transforms, whose FP32 form
-    keeps the vorticity's step-1 values in tensor memory): the adjoint's
-    z-inverse of the stage inputs runs through it; the gradient against the
-    FP64 oracle adjoint, both schedules."""
-    nx, ny, nz, T, K = 32, 16, 512, 3, 2
+@pytest.mark.parametrize("nz", [256, 512])
+def test_adjoint_long_z_matches_oracle(specns_lib, prec, tol, nz):
+    """nz = 256 and 512 (the lengths of the two-pass tile transforms, whose
+    FP32 form keeps the vorticity's step-1 values in tensor memory): the
+    adjoint's z-inverse of the stage inputs runs through them; the gradient
+    against the FP64 oracle adjoint, both schedules."""
+    nx, ny, T, K = 32, 16, 3, 2
     v = hermitian_fields((nx, ny, nz), 9, kcut=2 * (nx // 2) / 3)
     kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
     v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]

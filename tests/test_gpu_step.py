@@ -313,12 +313,14 @@ def test_c1_forced_dns_128_against_fixture(specns_lib, prec, tol):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-def test_fused_stage_passes_long_z(specns_lib, prec, monkeypatch):
-    """nz = 512 with a small (nx, ny): the 512-point z-passes of the fused
-    step (FP64 tiles of 4 pencils, FP32 of 8) against the oracle, in all three
-    z-pass arrangements, forcing band wide enough to reach kx tiles past the
+@pytest.mark.parametrize("nz", [256, 512])
+def test_fused_stage_passes_long_z(specns_lib, prec, nz, monkeypatch):
+    """nz = 256 and 512 with a small (nx, ny): the z-passes of the fused step
+    at the lengths of the two-pass tile transforms (FP32 with the vorticity's
+    step-1 values in tensor memory) against the oracle, in all three z-pass
+    arrangements, forcing band wide enough to reach kx tiles past the
     first."""
-    nx, ny, nz = 32, 16, 512
+    nx, ny = 32, 16
     v = hermitian_fields((nx, ny, nz), 5, kcut=2 * (nx // 2) / 3)
     kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
     v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
