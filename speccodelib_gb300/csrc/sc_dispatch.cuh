@@ -118,7 +118,7 @@ cudaError_t launch_zfwd_tma_mode(const CUtensorMap& lmap, const CUtensorMap& vma
   static cudaError_t attr = smem_attr(k, sm);
   if (attr != cudaSuccess) return attr;
   dim3 grid((g.nxh + Cfg::P - 1) / Cfg::P, g.ny);
-  k<<<grid, Cfg::NT, sm, s>>>(lmap, vmap, vstore, st, g, tw, err);
+  k<<<grid, ZfCfg<T, LOGN>::NT, sm, s>>>(lmap, vmap, vstore, st, g, tw, err);
   return cudaGetLastError();
 }
 

@@ -285,16 +285,29 @@ zfwd_fields_tma_kernel(const __grid_constant__ CUtensorMap fmap, StageArgs<T> st
 // leaves by bulk tensor stores through vmap (st.vout, tiles as lmap); the
 // kx = 0 points that the fix-up kernel finishes hold zeros until it writes
 // them (stage 4 reads no v: the fix-up needs only acc and the side plane).
+// Thread count of zfwd_tma_kernel: for 512- and 256-point pencils 16 points
+// per thread, which gives its in-place transforms the two-pass form
+// (SC_ZFWD_NT8: 8 points per thread, the radix-8 stages).
+template <typename T, int LOGN> struct ZfCfg {
+  using Cfg = TmaCfg<T, LOGN>;
+#ifdef SC_ZFWD_NT8
+  static constexpr int NT = Cfg::NT;
+#else
+  static constexpr int NT = (LOGN == 9 || LOGN == 8) ? Cfg::P * Cfg::N / 16 : Cfg::NT;
+#endif
+  using Engine = FFTEngine<T, LOGN, Cfg::P, Cfg::P, NT, true>;
+};
+
 template <typename T, int LOGN, int MODE>
-__global__ void __launch_bounds__(TmaCfg<T, LOGN>::NT, 2)
+__global__ void __launch_bounds__(ZfCfg<T, LOGN>::NT, 2)
 zfwd_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap vmap, int vstore,
                 StageArgs<T> st, Geom g, const C2<T>* __restrict__ tw, int* err) {
   using Cfg = TmaCfg<T, LOGN>;
-  using E = typename Cfg::Engine;
+  using E = typename ZfCfg<T, LOGN>::Engine;
   using C = C2<T>;
   constexpr int P = Cfg::P;
   constexpr int N = Cfg::N;
-  constexpr int NT = Cfg::NT;
+  constexpr int NT = ZfCfg<T, LOGN>::NT;
   extern __shared__ __align__(128) unsigned char smdyn[];
   unsigned char* smraw = align128(smdyn);
   C* w[3];
