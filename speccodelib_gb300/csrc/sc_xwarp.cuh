@@ -235,7 +235,15 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   // per warp: the transpose buffer + the rows kept in scrambled order (u;
   // XW_SMAG also S_ij)
   static constexpr int KEPT = MODE == XW_SMAG ? 9 : 3;
-  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M;
+  // two staging buffers for the warp's next input rows (points 0 .. M,
+  // rounded up to 16 bytes)
+  static constexpr int STG = (int)((((WarpFFT<T, LOGM>::M + 1) * sizeof(C2<T>) + 15) / 16 * 16) / sizeof(C2<T>));
+#ifdef SC_XW_NO_STAGE
+  static constexpr int STAGED = 0;
+#else
+  static constexpr int STAGED = 2 * STG;
+#endif
+  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M + STAGED;
   // 8 warps per CTA unless that passes 110 KB of shared memory
   static constexpr int WARPS = sizeof(C2<T>) * PER_WARP * 8 <= 110 * 1024 ? 8 : 4;
   static constexpr int NT = 32 * WARPS;
@@ -253,6 +261,44 @@ template <typename T, int LOGM> struct XwRow {
   const C* twN;
   long long off;
   int lane;
+  // Input rows staged through shared memory by cp.async: seq lists the
+  // fields in the order load_z consumes their rows; while a row is
+  // transformed the next one streams into the other buffer (stg == nullptr:
+  // load_z reads global memory directly)
+  C* stg = nullptr;
+  int stg_elems = 0;
+  const C* const* seq = nullptr;
+  int nseq = 0;
+  int used = 0;
+
+  __device__ __forceinline__ void stage_issue(int i) {
+    const char* src = reinterpret_cast<const char*>(seq[i] + off);
+    char* dst = reinterpret_cast<char*>(stg + (i & 1) * stg_elems);
+    const int chunks = stg_elems * (int)sizeof(C) / 16;
+    for (int c = lane; c < chunks; c += 32)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                       static_cast<uint32_t>(__cvta_generic_to_shared(dst + 16 * c))),
+                   "l"(src + 16 * c)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  __device__ __forceinline__ void stage_start() {
+    stage_issue(0);
+    if (nseq > 1) stage_issue(1);
+  }
+  // the row of seq[used], staged and visible to the whole warp
+  __device__ __forceinline__ const C* stage_acquire() {
+    if (used + 1 < nseq) asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncwarp();
+    return stg + (used & 1) * stg_elems;
+  }
+  // every lane is done with that row: its buffer takes the row after next
+  __device__ __forceinline__ void stage_release() {
+    __syncwarp();
+    if (used + 2 < nseq) stage_issue(used + 2);
+    ++used;
+  }
 
   // wn[r] = W_N^{lane + 32 r}, N = 2M: one table load times compile-time
   // roots (SC_XW_HALFLOAD: one table load each)
@@ -266,8 +312,8 @@ template <typename T, int LOGM> struct XwRow {
   }
 
   // half-length c2r pre-processing of a row into natural-order Z
-  __device__ __forceinline__ void load_z(const C* __restrict__ fp, C (&x)[E]) const {
-    const C* __restrict__ rp = fp + off;
+  __device__ __forceinline__ void load_z(const C* __restrict__ fp, C (&x)[E]) {
+    const C* __restrict__ rp = stg ? stage_acquire() : fp + off;
     C wn[E];
     half_twiddles(wn);
 #pragma unroll
@@ -279,10 +325,11 @@ template <typename T, int LOGM> struct XwRow {
       const C o = cmulc(csub(xk, cconj(xm)), wn[r]);
       x[r] = cadd(e, cmuli(o));
     }
+    if (stg) stage_release();
   }
 
   // a_c = c2r of rows f[0..2], kept in shared memory
-  __device__ __forceinline__ void load_a(const C* const f[3]) const {
+  __device__ __forceinline__ void load_a(const C* const f[3]) {
 #pragma unroll 1
     for (int c = 0; c < 3; ++c) {
       C x[E];
@@ -322,7 +369,7 @@ template <typename T, int LOGM> struct XwRow {
   // out = r2c(sc * (a x b)), b = c2r of rows bf[0..2]; the cross product is
   // accumulated as the b components arrive (convec_dns.f90:30-38: even
   // points in .x, odd points in .y)
-  __device__ __forceinline__ void cross_store(const C* const bf[3], C* const of[3], T sc) const {
+  __device__ __forceinline__ void cross_store(const C* const bf[3], C* const of[3], T sc) {
     auto A = [&](int c, int i) { return as[(c * E + i) * 32 + lane]; };
     C l[3][E];
     {
@@ -364,7 +411,7 @@ template <typename T, int LOGM> struct XwRow {
 
   // S_ij rows sf[0..5] (order 11 12 13 22 23 33) -> c2r, kept in shared
   // memory after the three a rows
-  __device__ __forceinline__ void load_s(const C* const sf[6]) const {
+  __device__ __forceinline__ void load_s(const C* const sf[6]) {
 #pragma unroll 1
     for (int q = 0; q < 6; ++q) {
       C x[E];
@@ -428,6 +475,26 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
   R.twN = twN;
   R.off = row * g.nxp;
   R.lane = lane;
+  // the input fields in the order their rows are consumed
+  const C* seq[Cfg::KEPT == 9 ? 12 : (MODE == XW_ADJ ? 9 : 6)];
+  if constexpr (MODE == XW_DNS) {
+    for (int f = 0; f < 6; ++f) seq[f] = fin.f[f];
+  } else if constexpr (MODE == XW_SMAG) {
+    for (int f = 0; f < 3; ++f) seq[f] = fin.f[f];          // u (load_a)
+    for (int f = 0; f < 6; ++f) seq[3 + f] = fin.f[6 + f];  // S_ij (load_s)
+    for (int f = 0; f < 3; ++f) seq[9 + f] = fin.f[3 + f];  // w (cross_store)
+  } else {
+    for (int f = 0; f < 3; ++f) seq[f] = fin.f[6 + f];      // phi (load_a)
+    for (int f = 0; f < 3; ++f) seq[3 + f] = fin.f[3 + f];  // w
+    for (int f = 0; f < 3; ++f) seq[6 + f] = fin.f[f];      // u
+  }
+  if constexpr (Cfg::STAGED > 0) {
+    R.stg = R.sm + WarpFFT<T, LOGM>::SMEM + Cfg::KEPT * WarpFFT<T, LOGM>::M;
+    R.stg_elems = Cfg::STG;
+    R.seq = seq;
+    R.nseq = (int)(sizeof(seq) / sizeof(seq[0]));
+    R.stage_start();
+  }
   if constexpr (MODE == XW_DNS) {
     const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
     const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
