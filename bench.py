@@ -419,64 +419,70 @@ def run_ours(a):
             "energy_rel_err": abs(d32["energy"] - d64["energy"]) / d64["energy"],
             "max_div_fp32": d32["max_div"], "max_div_fp64": d64["max_div"]}
 
-    # ---- discrete adjoint cost (256^3 FP32, T = 200, checkpoints every 20) ----
+    # ---- discrete adjoint cost (FP32, T = 200, checkpoints every 20; 256^3 and 128^3) ----
     adjoint = None
     if not a.no_adjoint:
-        na, Ta, Ka = 256, 200, 20
-        p = S.default_params(na, S.SC_FP32, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX)
-        ha = S.SpectralNS(p)
-        ha.set_stream(stream.cuda_stream)
-        ha.init_field(seed=SEED, akp=AKP, u0=U0)
-        init_a = ha.get_state()
-        ha.rk4_steps(3)
-        ha.set_state(*init_a)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ha.rk4_steps(Ta)
-        torch.cuda.synchronize()
-        t_fwd = time.perf_counter() - t0
-        schedules = {}
-        Ja = None
         import ctypes
 
-        def adj_device(nsteps, k):
-            """sc_adjoint_rk4 with the gradient left in HBM (null host outputs)."""
-            J = ctypes.c_double(0)
-            SP._check(SP.lib().sc_adjoint_rk4(ha.h, nsteps, k, 8, 16, None, None, None, ctypes.byref(J)))
-            return J.value
-
-        for mode, budget in (("stage_inputs_kept", -1.0), ("checkpoint_recompute", 0.0)):
-            ha.set_adjoint_budget(budget)
-            ha.set_state(*init_a)
-            adj_device(Ta, Ka)   # warm-up (allocates the store; the next call replays a graph)
+        def adjoint_cost(na, Ta=200, Ka=20, host_gradient=False):
+            p = S.default_params(na, S.SC_FP32, nu=NU, dt=DT, eps=EPS, fkmax=FKMAX)
+            ha = S.SpectralNS(p)
+            ha.set_stream(stream.cuda_stream)
+            ha.init_field(seed=SEED, akp=AKP, u0=U0)
+            init_a = ha.get_state()
+            ha.rk4_steps(3)
             ha.set_state(*init_a)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            Ja = adj_device(Ta, Ka)
+            ha.rk4_steps(Ta)
             torch.cuda.synchronize()
-            t_adj = time.perf_counter() - t0
-            schedules[mode] = {"kept_segments": ha.adjoint_kept_segments(),
-                               "adjoint_call_ms_per_step": 1e3 * t_adj / Ta,
-                               "cost_ratio": t_adj / t_fwd}
-        # the same call returning dJ/dv0 in host arrays (3 x 75 MB to pageable memory)
-        ha.set_adjoint_budget(-1.0)
-        ha.set_state(*init_a)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ha.adjoint(Ta, Ka, kmin=8, kmax=16)
-        t_host = time.perf_counter() - t0
-        schedules["stage_inputs_kept"]["with_host_gradient_ms_per_step"] = 1e3 * t_host / Ta
-        ha.close()
-        del ha, init_a
-        adjoint = {"grid": na, "steps": Ta, "checkpoint_every": Ka, "J": Ja,
-                   "forward_ms_per_step": 1e3 * t_fwd / Ta, "schedules": schedules,
-                   "note": "cost_ratio = adjoint call through the C ABI, J returned and the gradient "
+            t_fwd = time.perf_counter() - t0
+            schedules = {}
+            Ja = None
+
+            def adj_device(nsteps, k):
+                """sc_adjoint_rk4 with the gradient left in HBM (null host outputs)."""
+                J = ctypes.c_double(0)
+                SP._check(SP.lib().sc_adjoint_rk4(ha.h, nsteps, k, 8, 16, None, None, None, ctypes.byref(J)))
+                return J.value
+
+            for mode, budget in (("stage_inputs_kept", -1.0), ("checkpoint_recompute", 0.0)):
+                ha.set_adjoint_budget(budget)
+                ha.set_state(*init_a)
+                adj_device(Ta, Ka)   # warm-up (allocates the store; the next call replays a graph)
+                ha.set_state(*init_a)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                Ja = adj_device(Ta, Ka)
+                torch.cuda.synchronize()
+                t_adj = time.perf_counter() - t0
+                schedules[mode] = {"kept_segments": ha.adjoint_kept_segments(),
+                                   "adjoint_call_ms_per_step": 1e3 * t_adj / Ta,
+                                   "cost_ratio": t_adj / t_fwd}
+            if host_gradient:
+                # the same call returning dJ/dv0 in host arrays (pageable memory)
+                ha.set_adjoint_budget(-1.0)
+                ha.set_state(*init_a)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                ha.adjoint(Ta, Ka, kmin=8, kmax=16)
+                t_host = time.perf_counter() - t0
+                schedules["stage_inputs_kept"]["with_host_gradient_ms_per_step"] = 1e3 * t_host / Ta
+            ha.close()
+            del ha, init_a
+            torch.cuda.empty_cache()
+            return {"grid": na, "steps": Ta, "checkpoint_every": Ka, "J": Ja,
+                    "forward_ms_per_step": 1e3 * t_fwd / Ta, "schedules": schedules}
+
+        adjoint = adjoint_cost(256, host_gradient=True)
+        adjoint["grid_128"] = adjoint_cost(128)
+        adjoint["note"] = ("cost_ratio = adjoint call through the C ABI, J returned and the gradient "
                            "left in HBM (forward sweep + any segment recompute + backward "
                            "sweep) / plain forward of the same steps; stage_inputs_kept: the default "
                            "memory budget keeps every segment's stage inputs (12 fields per step) from "
                            "the forward sweep; checkpoint_recompute: budget 0, state checkpoints every "
-                           "K steps and each segment recomputed"}
-        torch.cuda.empty_cache()
+                           "K steps, the last segment's stage inputs recorded by the forward sweep and "
+                           "every other segment recomputed; grid_128: the same at 128^3")
 
     # ---- LES at 256^3 FP32: Smagorinsky (c1 = 0.17^2) and dynamic (update every 10) ----
     les = None

@@ -1318,10 +1318,19 @@ template <typename T> struct Impl {
       return rk4_core(h, st, vo, true);
     };
     const long long step0 = h->step;
+    // the last segment is the first the backward sweep needs: when it is
+    // not kept, the forward sweep records it straight into the recompute
+    // area (one segment long), and the backward sweep does not recompute it
+    const bool last_in_ra = first_kept == ncp;
     // forward sweep
     for (int sg = 0; sg < ncp; ++sg) {
       const int len = seg_len(sg);
-      if (sg < first_kept) {
+      if (sg == ncp - 1 && last_in_ra) {
+        for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(cpf(sg, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+        for (int c = 0; c < 3; ++c)
+          SC_CUDA(cudaMemcpyAsync(slot(ra0, 0, 0, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
+        for (int i = 0; i < len; ++i) SC_TRY(kept_step(ra0, i, len));
+      } else if (sg < first_kept) {
         for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(cpf(sg, c), F(h, S_V + c), fb, cudaMemcpyDeviceToDevice, h->stream));
         for (int i = 0; i < len; ++i) SC_TRY(rk4_step(h));
       } else {
@@ -1359,8 +1368,11 @@ template <typename T> struct Impl {
       size_t base = seg0[sg];
       if (sg < first_kept) {
         base = ra0;
-        for (int c = 0; c < 3; ++c) SC_CUDA(cudaMemcpyAsync(slot(ra0, 0, 0, c), cpf(sg, c), fb, cudaMemcpyDeviceToDevice, h->stream));
-        for (int i = 0; i < len; ++i) SC_TRY(kept_step(ra0, i, len));
+        if (!(sg == ncp - 1 && last_in_ra)) {
+          for (int c = 0; c < 3; ++c)
+            SC_CUDA(cudaMemcpyAsync(slot(ra0, 0, 0, c), cpf(sg, c), fb, cudaMemcpyDeviceToDevice, h->stream));
+          for (int i = 0; i < len; ++i) SC_TRY(kept_step(ra0, i, len));
+        }
       }
       for (int i = len - 1; i >= 0; --i) {
         C* st[4][3];
