@@ -9,6 +9,17 @@
 
 namespace sc {
 
+// Lane-major twiddle tables of the warp FFT, after the 4096-entry table of
+// power-of-two lengths: for M = 32 E (LOGM 5 .. 9) a block of 1024 entries
+// at 4096 + 1024 (LOGM - 5) holding W_M^{j lane} at (j - 1) 32 + lane and
+// W_M^{j q E} at (E - 1) 32 + (j - 1) Q + q (j = 1 .. E-1, lane < 32,
+// q < Q = 32 / E).
+struct WarpTw {
+  static constexpr int BASE = 4096, BLOCK = 1024, LOGM_MIN = 5, LOGM_MAX = 9;
+  static constexpr int TOTAL = BASE + BLOCK * (LOGM_MAX - LOGM_MIN + 1);
+  __host__ __device__ static constexpr int offset(int logm) { return BASE + BLOCK * (logm - LOGM_MIN); }
+};
+
 template <typename T> struct PlainArgs;
 template <typename T> struct ZvArgs;
 template <typename T> struct StageArgs;

@@ -278,7 +278,7 @@ template <typename T> struct Impl {
   }
 
   static int setup_tables(sc_handle* h) {
-    std::vector<C> t(4096);
+    std::vector<C> t(sc::WarpTw::TOTAL);
     for (int L = 2; L <= 2048; L *= 2)
       for (int m = 0; m < L; ++m) {
         const double a = 2.0 * M_PI * (double)m / (double)L;
@@ -286,7 +286,16 @@ template <typename T> struct Impl {
         t[L + m].y = (T)(-std::sin(a));
       }
     t[0].x = t[0].y = t[1].x = t[1].y = 0;
-    SC_CUDA(cudaMemcpy(h->tw, t.data(), sizeof(C) * 4096, cudaMemcpyHostToDevice));
+    // the warp FFT's lane-major tables: copies of entries of the M-point table
+    for (int logm = sc::WarpTw::LOGM_MIN; logm <= sc::WarpTw::LOGM_MAX; ++logm) {
+      const int M = 1 << logm, E = M / 32, Q = 32 / E;
+      C* b = t.data() + sc::WarpTw::offset(logm);
+      for (int j = 1; j < E; ++j) {
+        for (int lane = 0; lane < 32; ++lane) b[(j - 1) * 32 + lane] = t[M + (lane * j) % M];
+        for (int q = 0; q < Q; ++q) b[(E - 1) * 32 + (j - 1) * Q + q] = t[M + (q * E * j) % M];
+      }
+    }
+    SC_CUDA(cudaMemcpy(h->tw, t.data(), sizeof(C) * t.size(), cudaMemcpyHostToDevice));
     return set_dt(h, h->p.dt);
   }
 
@@ -411,6 +420,7 @@ template <typename T> struct Impl {
   }
   static sc::XArgs<T> xargs(sc_handle* h) {
     sc::XArgs<T> xa{};
+    xa.twx = reinterpret_cast<const C*>(h->tw);
     xa.scale = (T)(1.0 / ((double)h->g.nx * h->g.ny * h->g.nz));
     xa.c1 = h->dscal;
     xa.delta2 = h->p.delta * h->p.delta;
@@ -1758,7 +1768,7 @@ int sc_create(const sc_params* pin, sc_handle** out) {
   const size_t nfields = S_W + h->nwork;
   SC_CUDA(cudaMalloc(&h->fields, nfields * g.field * h->csize));
   SC_CUDA(cudaMemsetAsync(h->fields, 0, nfields * g.field * h->csize, h->stream));
-  SC_CUDA(cudaMalloc(&h->tw, 4096 * h->csize));
+  SC_CUDA(cudaMalloc(&h->tw, sc::WarpTw::TOTAL * h->csize));
   const size_t rsz = h->csize / 2;
   SC_CUDA(cudaMalloc(&h->ex, g.nxp * rsz));
   SC_CUDA(cudaMalloc(&h->ey, g.ny * rsz));

@@ -22,6 +22,7 @@
 #pragma once
 #include <utility>
 
+#include "sc_launch.h"
 #include "sc_passes.cuh"
 
 namespace sc {
@@ -113,6 +114,21 @@ template <typename T, int LOGM> struct WarpFFT {
     }
   }
 
+  // The same products from the lane-major tables of WarpTw (tx): x[j] *=
+  // W_M^{j lane} (first) or W_M^{j q E} (second level), one contiguous
+  // warp-wide load per power where the M-point table's entries lane j lie
+  // 8 j bytes apart.
+  template <bool INV>
+  __device__ static __forceinline__ void twiddle_first(C (&x)[E], const C* __restrict__ tx, int lane) {
+#pragma unroll
+    for (int j = 1; j < E; ++j) x[j] = cmul(x[j], twid(tx, (j - 1) * 32 + lane, INV));
+  }
+  template <bool INV>
+  __device__ static __forceinline__ void twiddle_second(C (&x)[E], const C* __restrict__ tx, int q) {
+#pragma unroll
+    for (int j = 1; j < E; ++j) x[j] = cmul(x[j], twid(tx, (E - 1) * 32 + (j - 1) * Q + q, INV));
+  }
+
   // all-to-all inside each group of Q2 lanes: afterwards lane q holds at
   // block p (registers p B .. p B + B-1) what lane p held at block q (q, p
   // the lane's index in its group).  One stage per lane bit h: the lane with
@@ -156,10 +172,14 @@ template <typename T, int LOGM> struct WarpFFT {
   // natural (x[r] = point lane + 32 r) -> a digit-scrambled order, the same
   // for every row and field (E >= Q: x[v B + i] = point k1 + E (q B + i) +
   // E^2 v, with k1 = lane / Q, q = lane % Q)
-  template <bool INV>
-  __device__ static __forceinline__ void nat_to_scr(C (&x)[E], C* sm, const C* __restrict__ tw, int lane) {
+  // TX: twiddles from the WarpTw tables tx of this M (else powers from the
+  // M-point table tw)
+  template <bool INV, bool TX = false>
+  __device__ static __forceinline__ void nat_to_scr(C (&x)[E], C* sm, const C* __restrict__ tw, int lane,
+                                                    const C* __restrict__ tx = nullptr) {
     dftE<E, INV>(x);
-    twiddle_powers<INV>(x, tw, lane);
+    if constexpr (TX) twiddle_first<INV>(x, tx, lane);
+    else twiddle_powers<INV>(x, tw, lane);
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) sm[k1 * ROW + lane] = x[k1];
     __syncwarp();
@@ -168,7 +188,8 @@ template <typename T, int LOGM> struct WarpFFT {
     for (int t = 0; t < E; ++t) x[t] = sm[k1 * ROW + q + Q * t];
     __syncwarp();
     dftE<E, INV>(x);
-    twiddle_powers<INV>(x, tw, q * E);
+    if constexpr (TX) twiddle_second<INV>(x, tx, q);
+    else twiddle_powers<INV>(x, tw, q * E);
 #pragma unroll
     for (int h = Q / 2; h >= HMIN; h >>= 1) {
       const C w = twid(tw, (q & (h - 1)) * (M / (2 * h)), INV);
@@ -188,8 +209,9 @@ template <typename T, int LOGM> struct WarpFFT {
   }
 
   // scrambled -> natural (the transposed network of nat_to_scr)
-  template <bool INV>
-  __device__ static __forceinline__ void scr_to_nat(C (&x)[E], C* sm, const C* __restrict__ tw, int lane) {
+  template <bool INV, bool TX = false>
+  __device__ static __forceinline__ void scr_to_nat(C (&x)[E], C* sm, const C* __restrict__ tw, int lane,
+                                                    const C* __restrict__ tx = nullptr) {
     const int k1 = lane / Q, q = lane % Q;
     if constexpr (XCH) {
       dft_cols<INV>(x);
@@ -207,7 +229,8 @@ template <typename T, int LOGM> struct WarpFFT {
         x[u] = up ? csub(p, cmul(w, x[u])) : cadd(x[u], cmul(w, p));
       }
     }
-    twiddle_powers<INV>(x, tw, q * E);
+    if constexpr (TX) twiddle_second<INV>(x, tx, q);
+    else twiddle_powers<INV>(x, tw, q * E);
     dftE<E, INV>(x);
 #pragma unroll
     for (int t = 0; t < E; ++t) sm[k1 * ROW + q + Q * t] = x[t];
@@ -215,7 +238,8 @@ template <typename T, int LOGM> struct WarpFFT {
 #pragma unroll
     for (int j = 0; j < E; ++j) x[j] = sm[j * ROW + lane];
     __syncwarp();
-    twiddle_powers<INV>(x, tw, lane);
+    if constexpr (TX) twiddle_first<INV>(x, tx, lane);
+    else twiddle_powers<INV>(x, tw, lane);
     dftE<E, INV>(x);
   }
 
@@ -259,6 +283,12 @@ template <typename T, int LOGM> struct XwRow {
   C* as;         // three rows a_c at [(c * E + i) * 32 + lane], scrambled order
   const C* twM;
   const C* twN;
+  const C* tx = nullptr;   // WarpTw tables of M (used when TX)
+#ifndef SC_XW_NO_TX
+  static constexpr bool TX = LOGM >= WarpTw::LOGM_MIN && LOGM <= WarpTw::LOGM_MAX;
+#else
+  static constexpr bool TX = false;
+#endif
   long long off;
   int lane;
   // Input rows staged through shared memory by cp.async: seq lists the
@@ -334,7 +364,7 @@ template <typename T, int LOGM> struct XwRow {
     for (int c = 0; c < 3; ++c) {
       C x[E];
       load_z(f[c], x);
-      WF::template nat_to_scr<true>(x, sm, twM, lane);
+      WF::template nat_to_scr<true, TX>(x, sm, twM, lane, tx);
 #pragma unroll
       for (int i = 0; i < E; ++i) as[(c * E + i) * 32 + lane] = x[i];
     }
@@ -375,7 +405,7 @@ template <typename T, int LOGM> struct XwRow {
     {
       C b[E];
       load_z(bf[0], b);   // b_x: L_y = a_z b_x - ..., L_z = ... - a_y b_x
-      WF::template nat_to_scr<true>(b, sm, twM, lane);
+      WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const C a1 = A(1, i), a2 = A(2, i);
@@ -383,7 +413,7 @@ template <typename T, int LOGM> struct XwRow {
         l[2][i] = mk<C>(-(a1.x * b[i].x), -(a1.y * b[i].y));
       }
       load_z(bf[1], b);   // b_y: L_x = ... - a_z b_y, L_z = a_x b_y - a_y b_x
-      WF::template nat_to_scr<true>(b, sm, twM, lane);
+      WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const C a0 = A(0, i), a2 = A(2, i);
@@ -391,7 +421,7 @@ template <typename T, int LOGM> struct XwRow {
         l[2][i] = mk<C>(a0.x * b[i].x + l[2][i].x, a0.y * b[i].y + l[2][i].y);
       }
       load_z(bf[2], b);   // b_z: L_x = a_y b_z - a_z b_y, L_y = a_z b_x - a_x b_z
-      WF::template nat_to_scr<true>(b, sm, twM, lane);
+      WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const C a0 = A(0, i), a1 = A(1, i);
@@ -404,7 +434,7 @@ template <typename T, int LOGM> struct XwRow {
       C x[E];
 #pragma unroll
       for (int i = 0; i < E; ++i) x[i] = cscale(l[c][i], sc);
-      WF::template scr_to_nat<false>(x, sm, twM, lane);
+      WF::template scr_to_nat<false, TX>(x, sm, twM, lane, tx);
       r2c_store(x, of[c] + off);
     }
   }
@@ -416,7 +446,7 @@ template <typename T, int LOGM> struct XwRow {
     for (int q = 0; q < 6; ++q) {
       C x[E];
       load_z(sf[q], x);
-      WF::template nat_to_scr<true>(x, sm, twM, lane);
+      WF::template nat_to_scr<true, TX>(x, sm, twM, lane, tx);
 #pragma unroll
       for (int i = 0; i < E; ++i) as[((3 + q) * E + i) * 32 + lane] = x[i];
     }
@@ -444,7 +474,7 @@ template <typename T, int LOGM> struct XwRow {
         const C s = S(q, i);
         x[i] = mk<C>(ar[i] * s.x, ai[i] * s.y);
       }
-      WF::template scr_to_nat<false>(x, sm, twM, lane);
+      WF::template scr_to_nat<false, TX>(x, sm, twM, lane, tx);
       r2c_store(x, of[q] + off);
     }
   }
@@ -473,6 +503,7 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
   R.as = R.sm + WarpFFT<T, LOGM>::SMEM;
   R.twM = twM;
   R.twN = twN;
+  if constexpr (XwRow<T, LOGM>::TX) R.tx = xa.twx + WarpTw::offset(LOGM);
   R.off = row * g.nxp;
   R.lane = lane;
   // the input fields in the order their rows are consumed
