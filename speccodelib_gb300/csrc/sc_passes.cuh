@@ -736,7 +736,8 @@ template <> struct XpIO<XP_R2C3> { static constexpr int fin = 3, fout = 3; };
 template <> struct XpIO<XP_ADJ> { static constexpr int fin = 9, fout = 6; };   // (u, w, phi) -> (w x phi, phi x u)
 
 template <typename T> struct XArgs {
-  const C2<T>* twx;        // the twiddle table base (WarpTw blocks after entry 4096), or nullptr
+  const C2<T>* twx;        // the twiddle table base (WarpTw blocks after entry 4096)
+  int* err;                // device error word of the bounded waits (may be nullptr)
   T scale;                 // 1/(nx ny nz)
   const double* c1;        // device scalar: Smagorinsky c1 (or dynamic cs2)
   double delta2;           // filter width squared

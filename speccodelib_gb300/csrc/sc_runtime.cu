@@ -421,6 +421,7 @@ template <typename T> struct Impl {
   static sc::XArgs<T> xargs(sc_handle* h) {
     sc::XArgs<T> xa{};
     xa.twx = reinterpret_cast<const C*>(h->tw);
+    xa.err = h->derr;
     xa.scale = (T)(1.0 / ((double)h->g.nx * h->g.ny * h->g.nz));
     xa.c1 = h->dscal;
     xa.delta2 = h->p.delta * h->p.delta;

@@ -24,6 +24,7 @@
 
 #include "sc_launch.h"
 #include "sc_passes.cuh"
+#include "sc_tma.cuh"
 
 namespace sc {
 
@@ -268,6 +269,10 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   static constexpr int STAGED = 2 * STG;
 #endif
   static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M + STAGED;
+  // the staging buffers are bulk-copy destinations: 16-byte aligned
+  static_assert((PER_WARP * sizeof(C2<T>)) % 16 == 0 &&
+                    ((WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M) * sizeof(C2<T>)) % 16 == 0,
+                "x-pass staging buffers must start on 16-byte boundaries");
   // 8 warps per CTA unless that passes 110 KB of shared memory
   static constexpr int WARPS = sizeof(C2<T>) * PER_WARP * 8 <= 110 * 1024 ? 8 : 4;
   static constexpr int NT = 32 * WARPS;
@@ -291,19 +296,28 @@ template <typename T, int LOGM> struct XwRow {
 #endif
   long long off;
   int lane;
-  // Input rows staged through shared memory by cp.async: seq lists the
-  // fields in the order load_z consumes their rows; while a row is
-  // transformed the next one streams into the other buffer (stg == nullptr:
-  // load_z reads global memory directly)
+  // Input rows staged through shared memory: seq lists the fields in the
+  // order load_z consumes their rows; while a row is transformed the next
+  // one streams into the other buffer (stg == nullptr: load_z reads global
+  // memory directly).  Each row arrives by one bulk copy issued by lane 0,
+  // completing on the buffer's mbarrier (sbar[0..1]), so the copies take no
+  // load/store-unit slots (SC_XW_CPASYNC: 16-byte cp.async by every lane).
+  // A wait that gives up records the timeout in *err and the warp waits on
+  // nothing after it (its results are then void; the host reports the
+  // error).
   C* stg = nullptr;
   int stg_elems = 0;
   const C* const* seq = nullptr;
   int nseq = 0;
   int used = 0;
+  uint64_t* sbar = nullptr;
+  int* err = nullptr;
+  bool ok = true;
 
   __device__ __forceinline__ void stage_issue(int i) {
     const char* src = reinterpret_cast<const char*>(seq[i] + off);
     char* dst = reinterpret_cast<char*>(stg + (i & 1) * stg_elems);
+#ifdef SC_XW_CPASYNC
     const int chunks = stg_elems * (int)sizeof(C) / 16;
     for (int c = lane; c < chunks; c += 32)
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
@@ -311,22 +325,44 @@ template <typename T, int LOGM> struct XwRow {
                    "l"(src + 16 * c)
                    : "memory");
     asm volatile("cp.async.commit_group;" ::: "memory");
+#else
+    if (lane == 0) {
+      // the buffer's earlier reads (generic proxy) before the copy's writes
+      fence_proxy_async();
+      const uint32_t bytes = (uint32_t)(stg_elems * sizeof(C));
+      mbar_arrive_expect_tx(&sbar[i & 1], bytes);
+      bulk_load(dst, src, bytes, &sbar[i & 1]);
+    }
+#endif
   }
   __device__ __forceinline__ void stage_start() {
+#ifndef SC_XW_CPASYNC
+    if (lane == 0) {
+      mbar_init(&sbar[0], 1);
+      mbar_init(&sbar[1], 1);
+      fence_mbar_init();
+    }
+    __syncwarp();
+#endif
     stage_issue(0);
     if (nseq > 1) stage_issue(1);
   }
   // the row of seq[used], staged and visible to the whole warp
   __device__ __forceinline__ const C* stage_acquire() {
+#ifdef SC_XW_CPASYNC
     if (used + 1 < nseq) asm volatile("cp.async.wait_group 1;" ::: "memory");
     else asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncwarp();
+#else
+    // buffer b's k-th fill (row index i = 2k + b) completes phase k
+    if (ok) ok = mbar_wait_bounded(&sbar[used & 1], (uint32_t)(used >> 1) & 1u, err);
+#endif
     return stg + (used & 1) * stg_elems;
   }
   // every lane is done with that row: its buffer takes the row after next
   __device__ __forceinline__ void stage_release() {
     __syncwarp();
-    if (used + 2 < nseq) stage_issue(used + 2);
+    if (used + 2 < nseq && ok) stage_issue(used + 2);
     ++used;
   }
 
@@ -495,6 +531,7 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
   using C = C2<T>;
   using Cfg = XwCfg<T, LOGM, MODE>;
   extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t sbar[2 * Cfg::WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long row = (long long)blockIdx.x * Cfg::WARPS + warp;
   if (row >= xa.rows) return;
@@ -524,6 +561,8 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
     R.stg_elems = Cfg::STG;
     R.seq = seq;
     R.nseq = (int)(sizeof(seq) / sizeof(seq[0]));
+    R.sbar = sbar + 2 * warp;
+    R.err = xa.err;
     R.stage_start();
   }
   if constexpr (MODE == XW_DNS) {
