@@ -6,7 +6,8 @@
 // of the warp (the 32x32b access shape), so two warps w and w + 4 share
 // lanes and must use different columns.  The z kernels keep the step-1 values
 // of a two-pass transform here while the tiles of shared memory are busy
-// with other transforms (sc_fused.cuh).
+// with other transforms (sc_fused.cuh); the warp x-pass keeps the rows it
+// transforms first there (sc_xwarp.cuh).
 //
 // The allocation does not poll: it completes when the columns are free.
 // The kernels that allocate hold 128 columns per CTA and run at most two
@@ -51,6 +52,21 @@ __device__ __forceinline__ void tmem_store32(uint32_t addr, const uint32_t (&r)[
       "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
       : "memory");
 }
+// Whole warp: 16 (8) words of each thread into its lane, columns addr ..
+// addr+15 (addr+7).
+__device__ __forceinline__ void tmem_store16(uint32_t addr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(addr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_store8(uint32_t addr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(addr),
+               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
 __device__ __forceinline__ void tmem_wait_store() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Whole warp: 32 words of each thread's lane, columns addr .. addr+31; the
@@ -65,6 +81,17 @@ __device__ __forceinline__ void tmem_load32(uint32_t addr, uint32_t (&r)[32]) {
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
         "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(addr)
+      : "memory");
+}
+
+// Whole warp: 8 words of each thread's lane, columns addr .. addr+7, with
+// the wait in the same statement.
+__device__ __forceinline__ void tmem_load8(uint32_t addr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
       : "r"(addr)
       : "memory");
 }

@@ -25,6 +25,7 @@
 #include "sc_launch.h"
 #include "sc_passes.cuh"
 #include "sc_tma.cuh"
+#include "sc_tmem.cuh"
 
 namespace sc {
 
@@ -260,6 +261,15 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   // per warp: the transpose buffer + the rows kept in scrambled order (u;
   // XW_SMAG also S_ij)
   static constexpr int KEPT = MODE == XW_SMAG ? 9 : 3;
+  // TM: the three kept rows in tensor memory instead (FP32, XW_DNS and
+  // XW_ADJ, 4 or 8 points per lane; SC_XW_NO_TMEM: shared memory): 6 E
+  // columns per warp, two warps per lane quarter, 128 columns per CTA
+#ifndef SC_XW_NO_TMEM
+  static constexpr bool TM = sizeof(T) == 4 && MODE != XW_SMAG && (LOGM == 7 || LOGM == 8);
+#else
+  static constexpr bool TM = false;
+#endif
+  static constexpr int KEPT_SM = TM ? 0 : KEPT;
   // two staging buffers for the warp's next input rows (points 0 .. M,
   // rounded up to 16 bytes)
   static constexpr int STG = (int)((((WarpFFT<T, LOGM>::M + 1) * sizeof(C2<T>) + 15) / 16 * 16) / sizeof(C2<T>));
@@ -268,10 +278,10 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
 #else
   static constexpr int STAGED = 2 * STG;
 #endif
-  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M + STAGED;
+  static constexpr int PER_WARP = WarpFFT<T, LOGM>::SMEM + KEPT_SM * WarpFFT<T, LOGM>::M + STAGED;
   // the staging buffers are bulk-copy destinations: 16-byte aligned
   static_assert((PER_WARP * sizeof(C2<T>)) % 16 == 0 &&
-                    ((WarpFFT<T, LOGM>::SMEM + KEPT * WarpFFT<T, LOGM>::M) * sizeof(C2<T>)) % 16 == 0,
+                    ((WarpFFT<T, LOGM>::SMEM + KEPT_SM * WarpFFT<T, LOGM>::M) * sizeof(C2<T>)) % 16 == 0,
                 "x-pass staging buffers must start on 16-byte boundaries");
   // 8 warps per CTA unless that passes 110 KB of shared memory
   static constexpr int WARPS = sizeof(C2<T>) * PER_WARP * 8 <= 110 * 1024 ? 8 : 4;
@@ -279,13 +289,16 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   static constexpr size_t SMEM = sizeof(C2<T>) * PER_WARP * WARPS;
 };
 
-// One warp's view of one grid row (y, z) at element offset `off` of every field.
-template <typename T, int LOGM> struct XwRow {
+// One warp's view of one grid row (y, z) at element offset `off` of every
+// field.  TM: the a rows in tensor memory.
+template <typename T, int LOGM, bool TM = false> struct XwRow {
   using WF = WarpFFT<T, LOGM>;
   using C = C2<T>;
   static constexpr int M = WF::M, E = WF::E;
+  static_assert(!TM || (sizeof(T) == 4 && (E == 4 || E == 8)), "tensor-memory rows: FP32, 4 or 8 points per lane");
   C* sm;         // transpose buffer
   C* as;         // three rows a_c at [(c * E + i) * 32 + lane], scrambled order
+  uint32_t ta = 0;   // TM: a_c at columns ta + 2 E c .. + 2 E - 1 of the warp's lanes
   const C* twM;
   const C* twN;
   const C* tx = nullptr;   // WarpTw tables of M (used when TX)
@@ -401,8 +414,33 @@ template <typename T, int LOGM> struct XwRow {
       C x[E];
       load_z(f[c], x);
       WF::template nat_to_scr<true, TX>(x, sm, twM, lane, tx);
+      if constexpr (TM) {
+        uint32_t w[2 * E];
 #pragma unroll
-      for (int i = 0; i < E; ++i) as[(c * E + i) * 32 + lane] = x[i];
+        for (int i = 0; i < E; ++i) {
+          w[2 * i] = __float_as_uint(x[i].x);
+          w[2 * i + 1] = __float_as_uint(x[i].y);
+        }
+        if constexpr (E == 8) tmem_store16(ta + 16u * c, w);
+        else tmem_store8(ta + 8u * c, w);
+      } else {
+#pragma unroll
+        for (int i = 0; i < E; ++i) as[(c * E + i) * 32 + lane] = x[i];
+      }
+    }
+    if constexpr (TM) tmem_wait_store();
+  }
+
+  // a_c at points i0 .. i0+3
+  __device__ __forceinline__ void a4(int c, int i0, C (&a)[4]) const {
+    if constexpr (TM) {
+      uint32_t w[8];
+      tmem_load8(ta + (uint32_t)(2 * E * c + 2 * i0), w);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = mk<C>(__uint_as_float(w[2 * i]), __uint_as_float(w[2 * i + 1]));
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = as[(c * E + i0 + i) * 32 + lane];
     }
   }
 
@@ -436,43 +474,74 @@ template <typename T, int LOGM> struct XwRow {
   // accumulated as the b components arrive (convec_dns.f90:30-38: even
   // points in .x, odd points in .y)
   __device__ __forceinline__ void cross_store(const C* const bf[3], C* const of[3], T sc) {
-    auto A = [&](int c, int i) { return as[(c * E + i) * 32 + lane]; };
-    C l[3][E];
+    static_assert(E % 4 == 0 || !TM, "a rows are read four points at a time");
+    constexpr int G = E < 4 ? E : 4;   // points per group of a reads
+    auto A = [&](int c, int i0, C (&a)[4]) {
+      if constexpr (TM) a4(c, i0, a);
+      else {
+#pragma unroll
+        for (int i = 0; i < G; ++i) a[i] = as[(c * E + i0 + i) * 32 + lane];
+      }
+    };
+    // L_z is complete after b_y and leaves before b_z is transformed, so
+    // only L_x and L_y stay in registers through the last transform
+    auto out = [&](C (&l)[E], int c) {
+      C x[E];
+#pragma unroll
+      for (int i = 0; i < E; ++i) x[i] = cscale(l[i], sc);
+      WF::template scr_to_nat<false, TX>(x, sm, twM, lane, tx);
+      r2c_store(x, of[c] + off);
+    };
+    C l0[E], l1[E];
+    C b[E];
     {
-      C b[E];
+      C l2[E];
       load_z(bf[0], b);   // b_x: L_y = a_z b_x - ..., L_z = ... - a_y b_x
       WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const C a1 = A(1, i), a2 = A(2, i);
-        l[1][i] = mk<C>(a2.x * b[i].x, a2.y * b[i].y);
-        l[2][i] = mk<C>(-(a1.x * b[i].x), -(a1.y * b[i].y));
+      for (int i0 = 0; i0 < E; i0 += G) {
+        C a1[4], a2[4];
+        A(1, i0, a1);
+        A(2, i0, a2);
+#pragma unroll
+        for (int ii = 0; ii < G; ++ii) {
+          const int i = i0 + ii;
+          l1[i] = mk<C>(a2[ii].x * b[i].x, a2[ii].y * b[i].y);
+          l2[i] = mk<C>(-(a1[ii].x * b[i].x), -(a1[ii].y * b[i].y));
+        }
       }
       load_z(bf[1], b);   // b_y: L_x = ... - a_z b_y, L_z = a_x b_y - a_y b_x
       WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const C a0 = A(0, i), a2 = A(2, i);
-        l[0][i] = mk<C>(-(a2.x * b[i].x), -(a2.y * b[i].y));
-        l[2][i] = mk<C>(a0.x * b[i].x + l[2][i].x, a0.y * b[i].y + l[2][i].y);
-      }
-      load_z(bf[2], b);   // b_z: L_x = a_y b_z - a_z b_y, L_y = a_z b_x - a_x b_z
-      WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
+      for (int i0 = 0; i0 < E; i0 += G) {
+        C a0[4], a2[4];
+        A(0, i0, a0);
+        A(2, i0, a2);
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const C a0 = A(0, i), a1 = A(1, i);
-        l[0][i] = mk<C>(a1.x * b[i].x + l[0][i].x, a1.y * b[i].y + l[0][i].y);
-        l[1][i] = mk<C>(l[1][i].x - a0.x * b[i].x, l[1][i].y - a0.y * b[i].y);
+        for (int ii = 0; ii < G; ++ii) {
+          const int i = i0 + ii;
+          l0[i] = mk<C>(-(a2[ii].x * b[i].x), -(a2[ii].y * b[i].y));
+          l2[i] = mk<C>(a0[ii].x * b[i].x + l2[i].x, a0[ii].y * b[i].y + l2[i].y);
+        }
+      }
+      out(l2, 2);
+    }
+    load_z(bf[2], b);   // b_z: L_x = a_y b_z - a_z b_y, L_y = a_z b_x - a_x b_z
+    WF::template nat_to_scr<true, TX>(b, sm, twM, lane, tx);
+#pragma unroll
+    for (int i0 = 0; i0 < E; i0 += G) {
+      C a0[4], a1[4];
+      A(0, i0, a0);
+      A(1, i0, a1);
+#pragma unroll
+      for (int ii = 0; ii < G; ++ii) {
+        const int i = i0 + ii;
+        l0[i] = mk<C>(a1[ii].x * b[i].x + l0[i].x, a1[ii].y * b[i].y + l0[i].y);
+        l1[i] = mk<C>(l1[i].x - a0[ii].x * b[i].x, l1[i].y - a0[ii].y * b[i].y);
       }
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      C x[E];
-#pragma unroll
-      for (int i = 0; i < E; ++i) x[i] = cscale(l[c][i], sc);
-      WF::template scr_to_nat<false, TX>(x, sm, twM, lane, tx);
-      r2c_store(x, of[c] + off);
-    }
+    out(l0, 0);
+    out(l1, 1);
   }
 
   // S_ij rows sf[0..5] (order 11 12 13 22 23 33) -> c2r, kept in shared
@@ -530,67 +599,89 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
                   const C2<T>* __restrict__ twN, XArgs<T> xa) {
   using C = C2<T>;
   using Cfg = XwCfg<T, LOGM, MODE>;
+  using Row = XwRow<T, LOGM, Cfg::TM>;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ __align__(8) uint64_t sbar[2 * Cfg::WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long row = (long long)blockIdx.x * Cfg::WARPS + warp;
-  if (row >= xa.rows) return;
-  XwRow<T, LOGM> R;
-  R.sm = reinterpret_cast<C*>(smraw) + warp * Cfg::PER_WARP;
-  R.as = R.sm + WarpFFT<T, LOGM>::SMEM;
-  R.twM = twM;
-  R.twN = twN;
-  if constexpr (XwRow<T, LOGM>::TX) R.tx = xa.twx + WarpTw::offset(LOGM);
-  R.off = row * g.nxp;
-  R.lane = lane;
-  // the input fields in the order their rows are consumed
-  const C* seq[Cfg::KEPT == 9 ? 12 : (MODE == XW_ADJ ? 9 : 6)];
-  if constexpr (MODE == XW_DNS) {
-    for (int f = 0; f < 6; ++f) seq[f] = fin.f[f];
-  } else if constexpr (MODE == XW_SMAG) {
-    for (int f = 0; f < 3; ++f) seq[f] = fin.f[f];          // u (load_a)
-    for (int f = 0; f < 6; ++f) seq[3 + f] = fin.f[6 + f];  // S_ij (load_s)
-    for (int f = 0; f < 3; ++f) seq[9 + f] = fin.f[3 + f];  // w (cross_store)
+  // TM: the CTA's 128 columns, warp w at lanes 32 (w % 4), columns 64 (w / 4)
+  __shared__ uint32_t s_tmem;
+  if constexpr (Cfg::TM) {
+    if (warp == 0) tmem_alloc(&s_tmem, 128);
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
   } else {
-    for (int f = 0; f < 3; ++f) seq[f] = fin.f[6 + f];      // phi (load_a)
-    for (int f = 0; f < 3; ++f) seq[3 + f] = fin.f[3 + f];  // w
-    for (int f = 0; f < 3; ++f) seq[6 + f] = fin.f[f];      // u
+    if (row >= xa.rows) return;
   }
-  if constexpr (Cfg::STAGED > 0) {
-    R.stg = R.sm + WarpFFT<T, LOGM>::SMEM + Cfg::KEPT * WarpFFT<T, LOGM>::M;
-    R.stg_elems = Cfg::STG;
-    R.seq = seq;
-    R.nseq = (int)(sizeof(seq) / sizeof(seq[0]));
-    R.sbar = sbar + 2 * warp;
-    R.err = xa.err;
-    R.stage_start();
+  if (row < xa.rows) {
+    Row R;
+    R.sm = reinterpret_cast<C*>(smraw) + warp * Cfg::PER_WARP;
+    R.as = R.sm + WarpFFT<T, LOGM>::SMEM;
+    if constexpr (Cfg::TM) R.ta = s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64u * (uint32_t)(warp >> 2);
+    R.twM = twM;
+    R.twN = twN;
+    if constexpr (Row::TX) R.tx = xa.twx + WarpTw::offset(LOGM);
+    R.off = row * g.nxp;
+    R.lane = lane;
+    // the input fields in the order their rows are consumed
+    const C* seq[Cfg::KEPT == 9 ? 12 : (MODE == XW_ADJ ? 9 : 6)];
+    if constexpr (MODE == XW_DNS) {
+      for (int f = 0; f < 6; ++f) seq[f] = fin.f[f];
+    } else if constexpr (MODE == XW_SMAG) {
+      for (int f = 0; f < 3; ++f) seq[f] = fin.f[f];          // u (load_a)
+      for (int f = 0; f < 6; ++f) seq[3 + f] = fin.f[6 + f];  // S_ij (load_s)
+      for (int f = 0; f < 3; ++f) seq[9 + f] = fin.f[3 + f];  // w (cross_store)
+    } else {
+      for (int f = 0; f < 3; ++f) seq[f] = fin.f[6 + f];      // phi (load_a)
+      for (int f = 0; f < 3; ++f) seq[3 + f] = fin.f[3 + f];  // w
+      for (int f = 0; f < 3; ++f) seq[6 + f] = fin.f[f];      // u
+    }
+    if constexpr (Cfg::STAGED > 0) {
+      R.stg = R.sm + WarpFFT<T, LOGM>::SMEM + Cfg::KEPT_SM * WarpFFT<T, LOGM>::M;
+      R.stg_elems = Cfg::STG;
+      R.seq = seq;
+      R.nseq = (int)(sizeof(seq) / sizeof(seq[0]));
+      R.sbar = sbar + 2 * warp;
+      R.err = xa.err;
+      R.stage_start();
+    }
+    if constexpr (MODE == XW_DNS) {
+      const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
+      const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
+      C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
+      R.load_a(a);
+      R.cross_store(b, o, xa.scale);
+    } else if constexpr (MODE == XW_SMAG) {
+      const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
+      const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
+      const C* s[6] = {fin.f[6], fin.f[7], fin.f[8], fin.f[9], fin.f[10], fin.f[11]};
+      C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
+      C* ot[6] = {fout.f[3], fout.f[4], fout.f[5], fout.f[6], fout.f[7], fout.f[8]};
+      const T tcoef = (T)(-2.0 * (*xa.c1) * xa.delta2) * xa.scale;
+      R.load_a(a);
+      R.load_s(s);
+      R.cross_store(b, o, xa.scale);
+      R.tau_store(ot, tcoef);
+    } else {
+      const C* phi[3] = {fin.f[6], fin.f[7], fin.f[8]};
+      const C* w[3] = {fin.f[3], fin.f[4], fin.f[5]};
+      const C* u[3] = {fin.f[0], fin.f[1], fin.f[2]};
+      C* o1[3] = {fout.f[0], fout.f[1], fout.f[2]};
+      C* o2[3] = {fout.f[3], fout.f[4], fout.f[5]};
+      R.load_a(phi);
+      R.cross_store(w, o1, T(-1));
+      R.cross_store(u, o2, T(1));
+    }
   }
-  if constexpr (MODE == XW_DNS) {
-    const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
-    const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
-    C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
-    R.load_a(a);
-    R.cross_store(b, o, xa.scale);
-  } else if constexpr (MODE == XW_SMAG) {
-    const C* a[3] = {fin.f[0], fin.f[1], fin.f[2]};
-    const C* b[3] = {fin.f[3], fin.f[4], fin.f[5]};
-    const C* s[6] = {fin.f[6], fin.f[7], fin.f[8], fin.f[9], fin.f[10], fin.f[11]};
-    C* o[3] = {fout.f[0], fout.f[1], fout.f[2]};
-    C* ot[6] = {fout.f[3], fout.f[4], fout.f[5], fout.f[6], fout.f[7], fout.f[8]};
-    const T tcoef = (T)(-2.0 * (*xa.c1) * xa.delta2) * xa.scale;
-    R.load_a(a);
-    R.load_s(s);
-    R.cross_store(b, o, xa.scale);
-    R.tau_store(ot, tcoef);
-  } else {
-    const C* phi[3] = {fin.f[6], fin.f[7], fin.f[8]};
-    const C* w[3] = {fin.f[3], fin.f[4], fin.f[5]};
-    const C* u[3] = {fin.f[0], fin.f[1], fin.f[2]};
-    C* o1[3] = {fout.f[0], fout.f[1], fout.f[2]};
-    C* o2[3] = {fout.f[3], fout.f[4], fout.f[5]};
-    R.load_a(phi);
-    R.cross_store(w, o1, T(-1));
-    R.cross_store(u, o2, T(1));
+  if constexpr (Cfg::TM) {
+    // every warp's tensor-memory reads are complete before the release
+    tmem_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+      tmem_fence_after_sync();
+      tmem_dealloc(s_tmem, 128);
+    }
   }
 }
 
