@@ -161,15 +161,10 @@ template <typename T> int select_variant(sc_ensemble* e, int vi) {
 template <typename T> int setup(sc_ensemble* e) {
   using C = sc::C2<T>;
   // twiddles
-  std::vector<C> t(4096);
-  for (int L = 2; L <= 2048; L *= 2)
-    for (int m = 0; m < L; ++m) {
-      const double a = 2.0 * M_PI * (double)m / (double)L;
-      t[L + m].x = (T)std::cos(a);
-      t[L + m].y = (T)(-std::sin(a));
-    }
-  EC(cudaMalloc(&e->tw, sizeof(C) * 4096));
-  EC(cudaMemcpy(e->tw, t.data(), sizeof(C) * 4096, cudaMemcpyHostToDevice));
+  std::vector<C> t(sc::WarpTw::TOTAL);
+  sc::WarpTw::fill(t.data(), [](double a) { return std::cos(a); }, [](double a) { return std::sin(a); });
+  EC(cudaMalloc(&e->tw, sizeof(C) * t.size()));
+  EC(cudaMemcpy(e->tw, t.data(), sizeof(C) * t.size(), cudaMemcpyHostToDevice));
   // fields: 6 per member (w, s, acc, work x3)
   size_t total = 0;
   e->field_off.resize(e->nm);

@@ -155,6 +155,9 @@ __device__ __forceinline__ void ens_xrow(const EnsMember<T>& mb, int row, C2<T>*
   const int lane = threadIdx.x & 31;
   const C* __restrict__ twM = tw + M;
   const C* __restrict__ twN = tw + 2 * M;
+  // twiddles from the lane-major tables after the power-of-two lengths
+  constexpr bool TX = WarpTw::covers(LOGM);
+  const C* __restrict__ tx = TX ? tw + WarpTw::offset(LOGM) : nullptr;
   const long long off = (long long)row * mb.nxp;
   auto load_z = [&](int f, C (&x)[E]) {
     const C* __restrict__ rp = mb.work + f * mb.field + off;
@@ -171,19 +174,19 @@ __device__ __forceinline__ void ens_xrow(const EnsMember<T>& mb, int row, C2<T>*
   C a[E];
   C* wsm = smw + WF::SMEM;   // w (scrambled order) at [i * 32 + lane]
   load_z(2, a);
-  WF::template nat_to_scr<true>(a, smw, twM, lane);
+  WF::template nat_to_scr<true, TX>(a, smw, twM, lane, tx);
 #pragma unroll
   for (int i = 0; i < E; ++i) wsm[i * 32 + lane] = a[i];
   const T sc = mb.scale;
   for (int f = 0; f < 2; ++f) {
     load_z(f, a);
-    WF::template nat_to_scr<true>(a, smw, twM, lane);
+    WF::template nat_to_scr<true, TX>(a, smw, twM, lane, tx);
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const C wv = wsm[i * 32 + lane];
       a[i] = mk<C>(a[i].x * wv.x * sc, a[i].y * wv.y * sc);
     }
-    WF::template scr_to_nat<false>(a, smw, twM, lane);
+    WF::template scr_to_nat<false, TX>(a, smw, twM, lane, tx);
     C* __restrict__ op = mb.work + f * mb.field + off;
     const int src = (32 - lane) & 31;
 #pragma unroll

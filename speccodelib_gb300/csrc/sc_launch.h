@@ -18,6 +18,28 @@ struct WarpTw {
   static constexpr int BASE = 4096, BLOCK = 1024, LOGM_MIN = 5, LOGM_MAX = 9;
   static constexpr int TOTAL = BASE + BLOCK * (LOGM_MAX - LOGM_MIN + 1);
   __host__ __device__ static constexpr int offset(int logm) { return BASE + BLOCK * (logm - LOGM_MIN); }
+  __host__ __device__ static constexpr bool covers(int logm) { return logm >= LOGM_MIN && logm <= LOGM_MAX; }
+  // The whole table (TOTAL entries, host side): entry L + m = e^{-2 pi i m/L}
+  // for L = 2 .. 2048 (computed in double precision, then rounded), then the
+  // lane-major blocks as copies of those entries.
+  template <typename C, typename FC, typename FS> static void fill(C* t, FC cosf_, FS sinf_) {
+    for (int i = 0; i < 4; ++i) t[i] = C{};
+    for (int L = 2; L <= 2048; L *= 2)
+      for (int m = 0; m < L; ++m) {
+        const double a = 2.0 * 3.14159265358979323846 * (double)m / (double)L;
+        t[L + m].x = (decltype(t[0].x))cosf_(a);
+        t[L + m].y = (decltype(t[0].x))(-sinf_(a));
+      }
+    t[0] = t[1] = C{};
+    for (int logm = LOGM_MIN; logm <= LOGM_MAX; ++logm) {
+      const int M = 1 << logm, E = M / 32, Q = 32 / E;
+      C* b = t + offset(logm);
+      for (int j = 1; j < E; ++j) {
+        for (int lane = 0; lane < 32; ++lane) b[(j - 1) * 32 + lane] = t[M + (lane * j) % M];
+        for (int q = 0; q < Q; ++q) b[(E - 1) * 32 + (j - 1) * Q + q] = t[M + (q * E * j) % M];
+      }
+    }
+  }
 };
 
 template <typename T> struct PlainArgs;

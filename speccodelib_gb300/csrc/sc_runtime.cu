@@ -279,22 +279,7 @@ template <typename T> struct Impl {
 
   static int setup_tables(sc_handle* h) {
     std::vector<C> t(sc::WarpTw::TOTAL);
-    for (int L = 2; L <= 2048; L *= 2)
-      for (int m = 0; m < L; ++m) {
-        const double a = 2.0 * M_PI * (double)m / (double)L;
-        t[L + m].x = (T)std::cos(a);
-        t[L + m].y = (T)(-std::sin(a));
-      }
-    t[0].x = t[0].y = t[1].x = t[1].y = 0;
-    // the warp FFT's lane-major tables: copies of entries of the M-point table
-    for (int logm = sc::WarpTw::LOGM_MIN; logm <= sc::WarpTw::LOGM_MAX; ++logm) {
-      const int M = 1 << logm, E = M / 32, Q = 32 / E;
-      C* b = t.data() + sc::WarpTw::offset(logm);
-      for (int j = 1; j < E; ++j) {
-        for (int lane = 0; lane < 32; ++lane) b[(j - 1) * 32 + lane] = t[M + (lane * j) % M];
-        for (int q = 0; q < Q; ++q) b[(E - 1) * 32 + (j - 1) * Q + q] = t[M + (q * E * j) % M];
-      }
-    }
+    sc::WarpTw::fill(t.data(), [](double a) { return std::cos(a); }, [](double a) { return std::sin(a); });
     SC_CUDA(cudaMemcpy(h->tw, t.data(), sizeof(C) * t.size(), cudaMemcpyHostToDevice));
     return set_dt(h, h->p.dt);
   }
