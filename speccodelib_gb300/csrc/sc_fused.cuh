@@ -50,7 +50,11 @@ template <typename T, int LOGN> struct ZiCfg {
   // ZI_MAX 256), or one job per thread up to 512 (ZI_DIV 8, ZI_MAX 512)
   static constexpr int NT_RAW = P * N / ZI_DIV;
   static constexpr int NT = NT_RAW > ZI_MAX ? ZI_MAX : (NT_RAW < 32 ? 32 : NT_RAW);
+#ifndef SC_ZI_EB
   static constexpr int EB = NT >= 512 ? 2 : 4;   // epilogue batch
+#else
+  static constexpr int EB = SC_ZI_EB;
+#endif
   using EngF = FFTEngine<T, LOGN, P, P, NT, true, 0, true>;           // whole tile, in place
   using EngH = FFTEngine<T, LOGN, P / 2, P / 2, NT, true, 0, true>;   // half tile
   static constexpr size_t TILE = sizeof(C2<T>) * (size_t)N * P;
