@@ -286,6 +286,14 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   // 8 warps per CTA unless that passes 110 KB of shared memory
   static constexpr int WARPS = sizeof(C2<T>) * PER_WARP * 8 <= 110 * 1024 ? 8 : 4;
   static constexpr int NT = 32 * WARPS;
+  // CTAs per SM the launch bounds ask for: three (80 registers) where the
+  // rows are in tensor memory and the transforms are 128 points long (no
+  // spills), else 16 warps per SM (SC_XW_MINB overrides)
+#ifndef SC_XW_MINB
+  static constexpr int MINB = (TM && LOGM <= 7 && WARPS == 8) ? 3 : 16 / WARPS;
+#else
+  static constexpr int MINB = SC_XW_MINB;
+#endif
   static constexpr size_t SMEM = sizeof(C2<T>) * PER_WARP * WARPS;
 };
 
@@ -594,7 +602,7 @@ template <typename T, int LOGM, bool TM = false> struct XwRow {
 //   fout must not alias u (read by the second product) -- the host passes
 //   the w and phi slots.
 template <typename T, int LOGM, int MODE>
-__global__ void __launch_bounds__(XwCfg<T, LOGM, MODE>::NT, 16 / XwCfg<T, LOGM, MODE>::WARPS)
+__global__ void __launch_bounds__(XwCfg<T, LOGM, MODE>::NT, XwCfg<T, LOGM, MODE>::MINB)
 xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __restrict__ twM,
                   const C2<T>* __restrict__ twN, XArgs<T> xa) {
   using C = C2<T>;
