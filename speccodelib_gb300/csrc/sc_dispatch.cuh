@@ -206,10 +206,10 @@ cudaError_t launch_xwarp(const FieldList<T>& fin, const FieldList<T>& fout, cons
                          const C2<T>* twN, const XArgs<T>& xa, cudaStream_t s) {
   using Cfg = XwCfg<T, LOGM, MODE>;
   auto k = xpass_warp_kernel<T, LOGM, MODE>;
-  static cudaError_t attr = smem_attr(k, Cfg::SMEM);
+  static cudaError_t attr = smem_attr(k, Cfg::SMEM_LAUNCH);
   if (attr != cudaSuccess) return attr;
   const long long nb = (xa.rows + Cfg::WARPS - 1) / Cfg::WARPS;
-  k<<<(unsigned)nb, Cfg::NT, Cfg::SMEM, s>>>(fin, fout, g, twM, twN, xa);
+  k<<<(unsigned)nb, Cfg::NT, Cfg::SMEM_LAUNCH, s>>>(fin, fout, g, twM, twN, xa);
   return cudaGetLastError();
 }
 

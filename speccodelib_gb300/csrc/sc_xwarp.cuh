@@ -261,14 +261,16 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   // per warp: the transpose buffer + the rows kept in scrambled order (u;
   // XW_SMAG also S_ij)
   static constexpr int KEPT = MODE == XW_SMAG ? 9 : 3;
-  // TM: the three kept rows in tensor memory instead (FP32, XW_DNS and
-  // XW_ADJ, 4 or 8 points per lane; SC_XW_NO_TMEM: shared memory): 6 E
-  // columns per warp, two warps per lane quarter, 128 columns per CTA
+  // TM: the kept rows in tensor memory instead (FP32; XW_DNS and XW_ADJ at
+  // 4 or 8 points per lane, XW_SMAG at 4; SC_XW_NO_TMEM: shared memory):
+  // 2 E KEPT columns per warp, two warps per lane quarter, TM_COLS columns
+  // per CTA (128, or 256 for the nine XW_SMAG rows)
 #ifndef SC_XW_NO_TMEM
-  static constexpr bool TM = sizeof(T) == 4 && MODE != XW_SMAG && (LOGM == 7 || LOGM == 8);
+  static constexpr bool TM = sizeof(T) == 4 && (MODE != XW_SMAG ? (LOGM == 7 || LOGM == 8) : LOGM == 7);
 #else
   static constexpr bool TM = false;
 #endif
+  static constexpr int TM_COLS = MODE == XW_SMAG ? 256 : 128;
   static constexpr int KEPT_SM = TM ? 0 : KEPT;
   // two staging buffers for the warp's next input rows (points 0 .. M,
   // rounded up to 16 bytes)
@@ -286,15 +288,19 @@ template <typename T, int LOGM, int MODE = XW_DNS> struct XwCfg {
   // 8 warps per CTA unless that passes 110 KB of shared memory
   static constexpr int WARPS = sizeof(C2<T>) * PER_WARP * 8 <= 110 * 1024 ? 8 : 4;
   static constexpr int NT = 32 * WARPS;
+  static_assert(!TM || WARPS == 8 || WARPS == 4, "two lane-quarter blocks of tensor-memory columns at most");
   // CTAs per SM the launch bounds ask for: three (80 registers) where the
-  // rows are in tensor memory and the transforms are 128 points long (no
-  // spills), else 16 warps per SM (SC_XW_MINB overrides)
+  // three rows are in tensor memory and the transforms are 128 points long
+  // (no spills), else 16 warps per SM (SC_XW_MINB overrides)
 #ifndef SC_XW_MINB
-  static constexpr int MINB = (TM && LOGM <= 7 && WARPS == 8) ? 3 : 16 / WARPS;
+  static constexpr int MINB = (TM && TM_COLS == 128 && LOGM <= 7 && WARPS == 8) ? 3 : 16 / WARPS;
 #else
   static constexpr int MINB = SC_XW_MINB;
 #endif
   static constexpr size_t SMEM = sizeof(C2<T>) * PER_WARP * WARPS;
+  // the launch's shared memory: with 256 tensor-memory columns per CTA, at
+  // least 77 KB, so that no more than two CTAs (512 columns) share an SM
+  static constexpr size_t SMEM_LAUNCH = (TM && TM_COLS > 128 && SMEM < 77 * 1024) ? 77 * 1024 : SMEM;
 };
 
 // One warp's view of one grid row (y, z) at element offset `off` of every
@@ -561,14 +567,62 @@ template <typename T, int LOGM, bool TM = false> struct XwRow {
       load_z(sf[q], x);
       WF::template nat_to_scr<true, TX>(x, sm, twM, lane, tx);
 #pragma unroll
-      for (int i = 0; i < E; ++i) as[((3 + q) * E + i) * 32 + lane] = x[i];
+      if constexpr (TM) {
+        uint32_t w[2 * E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          w[2 * i] = __float_as_uint(x[i].x);
+          w[2 * i + 1] = __float_as_uint(x[i].y);
+        }
+        if constexpr (E == 4) tmem_store8(ta + 8u * (3 + q), w);
+      } else {
+#pragma unroll
+        for (int i = 0; i < E; ++i) as[((3 + q) * E + i) * 32 + lane] = x[i];
+      }
     }
+    if constexpr (TM) tmem_wait_store();
   }
 
   // tau_ij = tcoef |S| S_ij on every real point (smag.f90:41-64: even points
   // in .x, odd in .y), |S| = sqrt(2 (S11^2 + S22^2 + S33^2 + 2 (S12^2 + S13^2
   // + S23^2))); r2c into of[0..5]
   __device__ __forceinline__ void tau_store(C* const of[6], T tcoef) const {
+    if constexpr (TM) {
+      // rows from tensor memory one at a time: the diagonal and off-diagonal
+      // sums in the order of the shared-memory form below
+      static_assert(E == 4, "tensor-memory S rows: 4 points per lane");
+      T dx[E], dy[E], ox[E], oy[E], ar[E], ai[E];
+      C r[4];
+      auto acc = [&](int q, T (&sx)[E], T (&sy)[E], bool first) {
+        a4(3 + q, 0, r);
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          sx[i] = first ? r[i].x * r[i].x : sx[i] + r[i].x * r[i].x;
+          sy[i] = first ? r[i].y * r[i].y : sy[i] + r[i].y * r[i].y;
+        }
+      };
+      acc(0, dx, dy, true);    // S11
+      acc(3, dx, dy, false);   // S22
+      acc(5, dx, dy, false);   // S33
+      acc(1, ox, oy, true);    // S12
+      acc(2, ox, oy, false);   // S13
+      acc(4, ox, oy, false);   // S23
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        ar[i] = tcoef * sqrt(T(2) * (dx[i] + T(2) * ox[i]));
+        ai[i] = tcoef * sqrt(T(2) * (dy[i] + T(2) * oy[i]));
+      }
+#pragma unroll 1
+      for (int q = 0; q < 6; ++q) {
+        a4(3 + q, 0, r);
+        C x[E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) x[i] = mk<C>(ar[i] * r[i].x, ai[i] * r[i].y);
+        WF::template scr_to_nat<false, TX>(x, sm, twM, lane, tx);
+        r2c_store(x, of[q] + off);
+      }
+      return;
+    }
     auto S = [&](int q, int i) { return as[((3 + q) * E + i) * 32 + lane]; };
     T ar[E], ai[E];
 #pragma unroll
@@ -612,10 +666,11 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
   __shared__ __align__(8) uint64_t sbar[2 * Cfg::WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long row = (long long)blockIdx.x * Cfg::WARPS + warp;
-  // TM: the CTA's 128 columns, warp w at lanes 32 (w % 4), columns 64 (w / 4)
+  // TM: the CTA's TM_COLS columns, warp w at lanes 32 (w % 4), columns
+  // TM_COLS / 2 * (w / 4)
   __shared__ uint32_t s_tmem;
   if constexpr (Cfg::TM) {
-    if (warp == 0) tmem_alloc(&s_tmem, 128);
+    if (warp == 0) tmem_alloc(&s_tmem, Cfg::TM_COLS);
     tmem_fence_before_sync();
     __syncthreads();
     tmem_fence_after_sync();
@@ -626,7 +681,8 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
     Row R;
     R.sm = reinterpret_cast<C*>(smraw) + warp * Cfg::PER_WARP;
     R.as = R.sm + WarpFFT<T, LOGM>::SMEM;
-    if constexpr (Cfg::TM) R.ta = s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64u * (uint32_t)(warp >> 2);
+    if constexpr (Cfg::TM)
+      R.ta = s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(Cfg::TM_COLS / 2) * (uint32_t)(warp >> 2);
     R.twM = twM;
     R.twN = twN;
     if constexpr (Row::TX) R.tx = xa.twx + WarpTw::offset(LOGM);
@@ -688,7 +744,7 @@ xpass_warp_kernel(FieldList<T> fin, FieldList<T> fout, Geom g, const C2<T>* __re
     __syncthreads();
     if (warp == 0) {
       tmem_fence_after_sync();
-      tmem_dealloc(s_tmem, 128);
+      tmem_dealloc(s_tmem, Cfg::TM_COLS);
     }
   }
 }
