@@ -159,9 +159,10 @@ def test_autograd_function_matches_adjoint_and_fd(specns_lib):
 
 
 def test_adjoint_schedules_agree(specns_lib):
-    """Pure checkpointing (budget 0: every segment recomputed), one kept
-    segment, and every segment kept from the forward sweep give the same J
-    and gradient; the state is left at v_0 each time."""
+    """Pure checkpointing (budget 0: the last segment recorded by the forward
+    sweep, every other one recomputed), one kept segment, and every segment
+    kept from the forward sweep give the same J and gradient; the state is
+    left at v_0 each time."""
     n, T, K = 16, 7, 3   # segments of 3, 3, 1 steps
     v = solenoidal_init(n)
     nxp = (n // 2 + 1 + 15) // 16 * 16
@@ -230,5 +231,27 @@ def test_adjoint_long_z_matches_oracle(specns_lib, prec, tol, nz):
             h.set_adjoint_budget(budget)
             h.set_state(*v)
             J, grad = h.adjoint(T, K, kmin=2, kmax=5)
+            assert abs(J - Jref) < tol * abs(Jref)
+            assert rel_l2(grad, ref) < tol, (budget, rel_l2(grad, ref))
+
+
+@pytest.mark.parametrize("prec,tol", [(S.SC_FP64, 1e-11), (S.SC_FP32, 1e-4)])
+@pytest.mark.parametrize("nx", [256, 512])
+def test_adjoint_long_rows_matches_oracle(specns_lib, prec, tol, nx):
+    """nx = 256 and 512 with a small (ny, nz): the adjoint's warp x-pass at
+    the row lengths whose FP32 form keeps phi's rows in tensor memory (three
+    CTAs per SM at 128-point rows); the gradient against the FP64 oracle
+    adjoint, both schedules."""
+    ny, nz, T, K = 16, 8, 3, 2
+    v = hermitian_fields((nx, ny, nz), 10, kcut=2 * (nz // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.02, fkmax=3.0))
+    ref, Jref = R.adjoint_gradient(v, g, T, kmin=1, kmax=3, checkpoint=K)
+    with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.02, fkmax=3.0)) as h:
+        for budget in (-1.0, 0.0):
+            h.set_adjoint_budget(budget)
+            h.set_state(*v)
+            J, grad = h.adjoint(T, K, kmin=1, kmax=3)
             assert abs(J - Jref) < tol * abs(Jref)
             assert rel_l2(grad, ref) < tol, (budget, rel_l2(grad, ref))

@@ -338,3 +338,22 @@ def test_fused_stage_passes_long_z(specns_lib, prec, nz, monkeypatch):
         assert rel_l2(o, ref) < TOL[prec]
     for o in outs[1:]:
         assert rel_l2(outs[0], o) < (1e-13 if prec == S.SC_FP64 else 2e-6)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("nx", [256, 512])
+def test_rk4_long_rows(specns_lib, prec, nx):
+    """nx = 256 and 512 with a small (ny, nz): the warp x-pass at the row
+    lengths whose FP32 form keeps u's rows in tensor memory (and runs three
+    CTAs per SM at 128-point rows), two forced RK4 steps against the oracle."""
+    ny, nz = 16, 8
+    v = hermitian_fields((nx, ny, nz), 12, kcut=2 * (nz // 2) / 3)
+    kx, ky, kz, _ = R.wavenumber(nx, ny, nz)
+    v = [R.symmetrize3d(a) for a in R.projection(*v, kx, ky, kz)]
+    g = R.Grid(R.Params(nx=nx, ny=ny, nz=nz, nu=0.02, fkmax=3.0))
+    ref = R.rk4_run(tuple(v), g, 2)
+    with S.SpectralNS(S.default_params(nx, prec, ny=ny, nz=nz, nu=0.02, fkmax=3.0)) as h:
+        h.set_state(*v)
+        h.rk4_steps(2)
+        out = h.get_state()
+    assert rel_l2(out, ref) < TOL[prec]
