@@ -169,8 +169,8 @@ cudaError_t launch_zfwd_zinv(const CUtensorMap& lmap, const CUtensorMap& fmap, c
 }
 
 template <typename T, int LOGN>
-cudaError_t launch_zinv_phi(const CUtensorMap& lmap, const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g,
-                            const C2<T>* tw, int* err, cudaStream_t s) {
+cudaError_t launch_zinv_phi(const CUtensorMap& lmap, const CUtensorMap& omap, const ZvArgs<T>& za,
+                            const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err, cudaStream_t s) {
   using Z = ZiCfg<T, LOGN>;
   if constexpr (!Z::SUPPORTED) {
     return cudaErrorNotSupported;
@@ -179,7 +179,7 @@ cudaError_t launch_zinv_phi(const CUtensorMap& lmap, const ZvArgs<T>& za, const 
     static cudaError_t attr = smem_attr(k, Z::SMEM);
     if (attr != cudaSuccess) return attr;
     dim3 grid((g.nxh + Z::P - 1) / Z::P, g.ny);
-    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, za, out, g, tw, err);
+    k<<<grid, Z::NT, Z::SMEM, s>>>(lmap, omap, za, out, g, tw, err);
     return cudaGetLastError();
   }
 }
@@ -541,8 +541,8 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
   case L:                                                                                          \
     return mode == sc::ZV_SMAG ? sc::launch_zinv5<double, L, sc::ZV_SMAG>(vmap, umap, za, out, g, tw, err, s) \
                                : sc::launch_zinv5<double, L, sc::ZV_DNS>(vmap, umap, za, out, g, tw, err, s);
-#define SC_ZPHI_CASE_float(L) case L: return sc::launch_zinv_phi<float, L>(lmap, za, out, g, tw, err, s);
-#define SC_ZPHI_CASE_double(L) case L: return sc::launch_zinv_phi<double, L>(lmap, za, out, g, tw, err, s);
+#define SC_ZPHI_CASE_float(L) case L: return sc::launch_zinv_phi<float, L>(lmap, omap, za, out, g, tw, err, s);
+#define SC_ZPHI_CASE_double(L) case L: return sc::launch_zinv_phi<double, L>(lmap, omap, za, out, g, tw, err, s);
 #define SC_ZI_P_CASE_float(L) case L: return sc::ZiCfg<float, L>::P;
 #define SC_ZI_P_CASE_double(L) case L: return sc::ZiCfg<double, L>::P;
 #define SC_ZI_OK_CASE_float(L) case L: return sc::ZiCfg<float, L>::SUPPORTED;
@@ -565,9 +565,9 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
     }                                                                                            \
   }                                                                                              \
   template <>                                                                                    \
-  cudaError_t sc::Launch<T>::zinv_phi_tma(int logn, const CUtensorMap& lmap, const ZvArgs<T>& za, \
-                                          const FieldList<T>& out, const Geom& g, const C2<T>* tw, \
-                                          int* err, cudaStream_t s) {                            \
+  cudaError_t sc::Launch<T>::zinv_phi_tma(int logn, const CUtensorMap& lmap, const CUtensorMap& omap, \
+                                          const ZvArgs<T>& za, const FieldList<T>& out, const Geom& g, \
+                                          const C2<T>* tw, int* err, cudaStream_t s) {           \
     switch (logn) {                                                                              \
       SC_LOGN_CASES(SC_ZPHI_CASE_##T)                                                            \
       default: return cudaErrorInvalidValue;                                                     \

@@ -380,8 +380,8 @@ zinv5_tma_kernel(const __grid_constant__ CUtensorMap vmap, const __grid_constant
 // in shared memory, three in-place transforms.  grid = (kx tiles, ny).
 template <typename T, int LOGN>
 __global__ void __launch_bounds__(ZiCfg<T, LOGN>::NT, ZiCfg<T, LOGN>::MINB)
-zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, FieldList<T> out, Geom g,
-                    const C2<T>* __restrict__ tw, int* err) {
+zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap omap, ZvArgs<T> za,
+                    FieldList<T> out, Geom g, const C2<T>* __restrict__ tw, int* err) {
   using Z = ZiCfg<T, LOGN>;
   using Cfg = TmaCfg<T, LOGN>;
   using EF = typename Z::EngF;
@@ -440,6 +440,25 @@ zinv_phi_tma_kernel(const __grid_constant__ CUtensorMap lmap, ZvArgs<T> za, Fiel
   if (fsum) {
     const double s2 = block_sum<NT>(q, red);
     if (threadIdx.x == 0) za.cpartial[(long long)blockIdx.x * g.ny + iy] = s2;
+  }
+  // 256- and 512-point pencils (two-pass in-place transforms): phi in place
+  // in the tiles, then out by bulk tensor stores (omap tiles the three
+  // outputs as lmap tiles lam; columns past nx/2+1 lie outside it and are
+  // not written).  Shorter pencils: element stores from the transform's
+  // registers (the bulk form gained nothing at 128^3).
+  if (EF::TWO_PASS && za.ustore) {
+    for (int c = 0; c < 3; ++c) EF::template run_inplace<true>(rt[c], tw);
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int c = 0; c < 3; ++c)
+        for (int h = 0; h < Cfg::NBOX; ++h)
+          tma_store_4d(&omap, reinterpret_cast<char*>(rt[c]) + (size_t)h * Cfg::BOX * P * sizeof(C), kx0 * Cfg::U,
+                       iy, h * Cfg::BOX, c);
+      tma_store_commit();
+      tma_store_wait_read<0>();
+    }
+    return;
   }
   for (int c = 0; c < 3; ++c) {
     C o[EF::JL][EF::RL];

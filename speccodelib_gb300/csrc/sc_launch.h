@@ -120,8 +120,11 @@ template <typename T> struct Launch {
                                const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                                cudaStream_t s, int mode = 0);
   // phi^ of the adjoint right-hand side from TMA-loaded lam tiles (za.lam is
-  // unused; the map covers lam), with the forcing-adjoint band sums
-  static cudaError_t zinv_phi_tma(int logn, const CUtensorMap& lmap, const ZvArgs<T>& za,
+  // unused; the map covers lam), with the forcing-adjoint band sums; with
+  // za.ustore, at 256- and 512-point pencils, phi leaves by bulk tensor
+  // stores through omap (out's three fields, tiles as lmap), else by element
+  // stores to out
+  static cudaError_t zinv_phi_tma(int logn, const CUtensorMap& lmap, const CUtensorMap& omap, const ZvArgs<T>& za,
                                   const FieldList<T>& out, const Geom& g, const C2<T>* tw, int* err,
                                   cudaStream_t s);
   // fmap: the whole field slab, tiles as lmap, for the L2 prefetch of the

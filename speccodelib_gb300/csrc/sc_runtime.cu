@@ -1115,7 +1115,12 @@ template <typename T> struct Impl {
       SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv5_tma(h->logz, smap, wmap, zu, w9, *g, tw(h, g->nz), h->derr, h->stream); }));
       sc::FieldList<T> phi{};
       for (int c = 0; c < 3; ++c) phi.f[c] = w9.f[6 + c];
-      SC_TRY(launch(h, "adj_zphi", [&] { return L::zinv_phi_tma(h->logz, lmap, za, phi, *g, tw(h, g->nz), h->derr, h->stream); }));
+      // phi (slots 6-8, equally spaced) leaves by bulk stores
+      CUtensorMap omap;
+      SC_TRY(encode_fields(h, w9.f[6], 3, 2, P, g->nz, &omap));
+      sc::ZvArgs<T> zp = za;
+      zp.ustore = 1;
+      SC_TRY(launch(h, "adj_zphi", [&] { return L::zinv_phi_tma(h->logz, lmap, omap, zp, phi, *g, tw(h, g->nz), h->derr, h->stream); }));
     } else {
       SC_TRY(launch(h, "adj_zinv", [&] { return L::zinv_vel(h->logz, sc::ZV_ADJ, za, w9, *g, tw(h, g->nz), h->stream); }));
     }
