@@ -253,14 +253,27 @@ zfwd_adj_kernel(FieldList<T> fin, AdjArgs<T> aa, Geom g, const C2<T>* __restrict
 // order (0-2: w x phi, 3-5: phi x u) to the tensor map's field index.
 template <typename T, int LOGN> struct AdjTmaCfg {
   using Cfg = TmaCfg<T, LOGN>;
-  static constexpr int P = Cfg::P;
-  static constexpr int NT = Cfg::NT;
+  // tiles half the pass tiles' width where their rows stay 64 bytes or more
+  // (128-byte pass rows): two CTAs of half the threads per SM (256^3 FP32
+  // adjoint step 8.67 -> 8.59 ms, 128^3 6% faster; SC_ADJ_WIDE: the pass
+  // tiles)
+#ifndef SC_ADJ_WIDE
+  static constexpr bool NARROW = Cfg::P * sizeof(C2<T>) >= 128;
+#else
+  static constexpr bool NARROW = false;
+#endif
+  static constexpr int P = NARROW ? Cfg::P / 2 : Cfg::P;
+  static constexpr int MINB = NARROW ? 2 : 1;
+  static constexpr int N = Cfg::N;
+  static constexpr int NT_RAW = P * N / 8;
+  static constexpr int NT = NT_RAW > 512 ? 512 : (NT_RAW < 32 ? 32 : NT_RAW);
   using Engine = FFTEngine<T, LOGN, P, P, NT, true>;
-  static constexpr size_t SMEM = 2 * Cfg::TILE_BYTES + kSmemAlignPad;
+  static constexpr size_t TILE_BYTES = sizeof(C2<T>) * N * P;
+  static constexpr size_t SMEM = 2 * TILE_BYTES + kSmemAlignPad;
 };
 
 template <typename T, int LOGN>
-__global__ void __launch_bounds__(AdjTmaCfg<T, LOGN>::NT, 1)
+__global__ void __launch_bounds__(AdjTmaCfg<T, LOGN>::NT, AdjTmaCfg<T, LOGN>::MINB)
 zfwd_adj_tma_kernel(const __grid_constant__ CUtensorMap pmap, int4 fidx_lo, int2 fidx_hi, AdjArgs<T> aa, Geom g,
                     const C2<T>* __restrict__ tw, int* err) {
   using AC = AdjTmaCfg<T, LOGN>;
@@ -270,7 +283,7 @@ zfwd_adj_tma_kernel(const __grid_constant__ CUtensorMap pmap, int4 fidx_lo, int2
   constexpr int P = AC::P;
   extern __shared__ __align__(128) unsigned char smdyn[];
   unsigned char* smraw = align128(smdyn);
-  C* buf[2] = {reinterpret_cast<C*>(smraw), reinterpret_cast<C*>(smraw + Cfg::TILE_BYTES)};
+  C* buf[2] = {reinterpret_cast<C*>(smraw), reinterpret_cast<C*>(smraw + AC::TILE_BYTES)};
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ double s_a, s_b;
   const int kx0 = blockIdx.x * P;
@@ -282,7 +295,7 @@ zfwd_adj_tma_kernel(const __grid_constant__ CUtensorMap pmap, int4 fidx_lo, int2
   const int fidx[6] = {fidx_lo.x, fidx_lo.y, fidx_lo.z, fidx_lo.w, fidx_hi.x, fidx_hi.y};
   if (launch_failed(err)) return;
   auto issue = [&](int f) {
-    mbar_arrive_expect_tx(&bars[f & 1], (uint32_t)Cfg::TILE_BYTES);
+    mbar_arrive_expect_tx(&bars[f & 1], (uint32_t)AC::TILE_BYTES);
     for (int h = 0; h < Cfg::NBOX; ++h)
       tma_load_4d(reinterpret_cast<char*>(buf[f & 1]) + (size_t)h * Cfg::BOX * P * sizeof(C), &pmap, &bars[f & 1],
                   kx0 * Cfg::U, iy, h * Cfg::BOX, fidx[f]);

@@ -242,8 +242,12 @@ cudaError_t launch_zfwd_adj_tma(const CUtensorMap& pmap, const int fidx[6], cons
 }  // namespace sc
 
 #define SC_ZFWDADJTMA_CASE(L) case L: return sc::launch_zfwd_adj_tma<ADJ_T, L>(pmap, fidx, aa, g, tw, err, s);
+#define SC_ADJTILE_CASE(L) case L: return sc::AdjTmaCfg<ADJ_T, L>::P;
 #define SC_ZFWDADJ_CASE(L) case L: return sc::launch_zfwd_adj<ADJ_T, L>(fin, aa, g, tw, s);
 #define SC_DEFINE_ADJ(T)                                                                         \
+  template <> int sc::Launch<T>::adj_tile(int logn) {                                            \
+    switch (logn) { SC_LOGN_CASES(SC_ADJTILE_CASE) default: return 0; }                           \
+  }                                                                                              \
   template <>                                                                                    \
   cudaError_t sc::Launch<T>::zfwd_adj_tma(int logn, const CUtensorMap& pmap, const int fidx[6],  \
                                           const AdjArgs<T>& aa, const Geom& g, const C2<T>* tw,  \

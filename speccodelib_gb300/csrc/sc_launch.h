@@ -137,6 +137,7 @@ template <typename T> struct Launch {
                               const C2<T>* tw, cudaStream_t s);
   // the same, the six product tiles by TMA (tma_tile width); fidx maps the
   // kernel's field order (w x phi, phi x u) to the tensor map's fields
+  static int adj_tile(int logn);       // zfwd_adj_tma tile width (its pmap's)
   static cudaError_t zfwd_adj_tma(int logn, const CUtensorMap& pmap, const int fidx[6], const AdjArgs<T>& aa,
                                   const Geom& g, const C2<T>* tw, int* err, cudaStream_t s);
   static cudaError_t adj_copyT(const FieldList<T>& lw, const Geom& g, cudaStream_t s);

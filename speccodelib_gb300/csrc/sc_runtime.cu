@@ -1160,7 +1160,7 @@ template <typename T> struct Impl {
     if (h->tma) {
       // products equally spaced from yf.f[0]; kernel field f lives at a6.f[f]
       CUtensorMap pmap;
-      SC_TRY(encode_fields(h, yf.f[0], 6, 2, L::tma_tile(h->logz), g->nz, &pmap));
+      SC_TRY(encode_fields(h, yf.f[0], 6, 2, L::adj_tile(h->logz), g->nz, &pmap));
       int fidx[6];
       for (int f = 0; f < 6; ++f) fidx[f] = (int)((a6.f[f] - yf.f[0]) / g->field);
       return launch(h, "adj_zfwd", [&] { return L::zfwd_adj_tma(h->logz, pmap, fidx, aa, *g, tw(h, g->nz), h->derr, h->stream); });
